@@ -1,0 +1,157 @@
+/*
+ * nekrs_gb300 — C ABI of the GB300-native pressure/Helmholtz elliptic solve.
+ *
+ * The entry points mirror nekRS's elliptic-solver boundary:
+ *   ellipticSolveSetup(elliptic_t*)          src/solvers/elliptic/elliptic.h:193
+ *   ellipticSolve(elliptic_t*, o_r, o_x)     src/solvers/elliptic/elliptic.h:191,
+ *                                            src/solvers/elliptic/ellipticSolve.cpp:32
+ *   ellipticOperator(elliptic, o_q, o_Aq, precision)
+ *                                            src/solvers/elliptic/elliptic.h:202-206
+ *   ellipticAx(...)                          src/solvers/elliptic/elliptic.h:208-213
+ * plus the per-kernel entry points the reference dispatches through OCCA
+ * (ellipticPartialAxCoeffHex3D, ellipticPartialAxTrilinearHex3D, oogs
+ * gather-scatter, mask, ellipticBlockUpdatePCG).
+ *
+ * Conventions.  All vectors are element-local "E-vectors" [E][Nq^3] with
+ * index i + Nq*(j + Nq*k) + Np*e (the reference's fieldOffset layout for one
+ * field).  Geometric factors are [E][7][Np] in the order G00, G01, G11, G12,
+ * G02, G22, GWJ (src/mesh/mesh3D.h:96-102).  Pointers named d_* are device
+ * pointers on the current CUDA device, h_* are host pointers.  Every entry
+ * point returns an int status (NRSG_OK = 0) and never aborts the process;
+ * nrsg_last_error() gives the message of the last failure on this thread.
+ * A CUDA stream of 0 means the legacy default stream.
+ */
+#ifndef NEKRS_GB300_H
+#define NEKRS_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NRSG_OK 0
+#define NRSG_ERR_MAXIT 1       /* iteration limit reached (ellipticSolve.cpp:161-162) */
+#define NRSG_ERR_BREAKDOWN 2   /* p.Ap <= 0 or H(k,k) == 0 */
+#define NRSG_ERR_NAN 3         /* NaN/Inf residual (PCG.cpp:193-195) */
+#define NRSG_ERR_OOM 4         /* device allocation failed */
+#define NRSG_ERR_BAD_CONFIG 5  /* invalid options or mesh description */
+#define NRSG_ERR_CUDA 6        /* CUDA runtime error */
+#define NRSG_ERR_NO_DEVICE 7   /* no CUDA device */
+#define NRSG_ERR_INVALID 8     /* invalid argument */
+
+/* Face boundary types (elliptic.h:46-49); lower id wins at shared nodes. */
+#define NRSG_BC_NONE 0
+#define NRSG_BC_DIRICHLET 1
+#define NRSG_BC_NEUMANN 4
+
+typedef struct nrsg_elliptic nrsg_elliptic;
+
+/* Mesh description filled by the caller before setup (the data
+ * ellipticSolveSetup reads from mesh_t / elliptic_t, setup.cpp:893-915). */
+typedef struct {
+  int N;                    /* polynomial order, 1..9 */
+  long long Nelements;
+  const double *h_VX;       /* [E][8][3] vertex coordinates, hypercube vertex order v = i + 2j + 4k */
+  const long long *h_EToV;  /* [E][8] global vertex ids (> 0), same order; drive the Nek5000 numbering */
+  const int *h_EToB;        /* [E][6] face BC per nekRS face order (t-, s-, r+, s+, r-, t+) */
+  const double *h_ggeo;     /* optional [E][7][Np]; NULL = computed on the device from the vertices */
+} nrsg_mesh_desc;
+
+typedef struct {
+  int iterations;      /* elliptic->Niter */
+  int status;          /* NRSG_* */
+  double res0;         /* elliptic->res0Norm: sqrt((r,r)_invDegree / volume) */
+  double res;          /* elliptic->resNorm at exit */
+  double solve_ms;     /* device time of the solve */
+} nrsg_solve_info;
+
+/* Library / device */
+const char *nrsg_last_error(void);
+int nrsg_version(void);
+/* Number of kernels this library has launched in the process so far. */
+long long nrsg_kernel_launches(void);
+
+/* Setup: mirrors ellipticSolveSetup.  `options` holds .par [PRESSURE]-section
+ * style "key = value" lines (or ';'-separated): solver (pcg | pcg+flexible |
+ * pfcg | pgmres+nVector=15 | pfgmres), residualTol (1e-8+relative),
+ * maxIterations, preconditioner (none | jacobi | multigrid), smootherType,
+ * pMGSchedule, coarseSolver, mgPrecision (fp64 | fp32 | mixed), lambda0,
+ * lambda1, poisson, elementMap (trilinear). */
+int nrsg_elliptic_create(const nrsg_mesh_desc *mesh, const char *options, nrsg_elliptic **out);
+int nrsg_elliptic_destroy(nrsg_elliptic *el);
+int nrsg_elliptic_set_stream(nrsg_elliptic *el, void *cuda_stream);
+
+/* Solve: mirrors ellipticSolve(elliptic, o_r, o_x).  d_r holds the RHS on
+ * entry and is overwritten with the final residual; d_x holds x0 on entry
+ * and the solution on exit.  Both are device E-vectors of E*Np doubles. */
+int nrsg_elliptic_solve(nrsg_elliptic *el, double *d_r, double *d_x, nrsg_solve_info *info);
+/* Same solve on host buffers: copies in, solves, copies back. */
+int nrsg_elliptic_solve_host(nrsg_elliptic *el, double *h_r, double *h_x, nrsg_solve_info *info);
+
+/* ellipticOperator(elliptic, q, Aq, dfloatString): Ax -> mask -> gs-sum. */
+int nrsg_elliptic_operator(nrsg_elliptic *el, const double *d_q, double *d_Aq);
+/* ellipticAx(elliptic, E, elementList, q, Aq, dfloatString): local Ax only. */
+int nrsg_elliptic_ax(nrsg_elliptic *el, const double *d_q, double *d_Aq);
+/* oogs::startFinish(q, ..., ogsDfloat, ogsAdd) on the masked handle. */
+int nrsg_elliptic_gs(nrsg_elliptic *el, double *d_q);
+/* ellipticApplyMask(elliptic, q, dfloatString). */
+int nrsg_elliptic_mask(nrsg_elliptic *el, double *d_q);
+/* ellipticPreconditioner(elliptic, r, z). */
+int nrsg_elliptic_precondition(nrsg_elliptic *el, const double *d_r, double *d_z);
+
+/* Setup data for parity checks, copied to host.  Names: "ids", "maskedIds"
+ * (int64), "gsOff", "gsIds", "maskIds" (int32), "invDegree", "ggeo",
+ * "invDiag", "x", "y", "z", "D" (float64), "history" (float64, last solve),
+ * "mg.levels" (int32).  With h_out == NULL only *count is set. */
+int nrsg_elliptic_get(nrsg_elliptic *el, const char *name, void *h_out, long long *count);
+
+/* Host-only setup (no device needed): Nek5000 global numbering (setvert3d,
+ * 3rd_party/nek5000/core/navier8.f:2004-2350), the Dirichlet mask
+ * (ellipticOgs.cpp:4-134) and the masked gather maps (ogsSetup.cpp:111-397).
+ * Output capacities: ids, maskedIds, invDegree, maskIds, gsIds: E*Np;
+ * gsOff: E*Np+1.  Any output pointer may be NULL. */
+int nrsg_host_setup_maps(int N, long long E, const long long *h_EToV, const int *h_EToB, long long *h_ids,
+                         long long *h_maskedIds, double *h_invDegree, int *h_maskIds, long long *nmask, int *h_gsOff,
+                         long long *ngroups, int *h_gsIds);
+
+/* ---- kernel-level entry points (one launch each, on `stream`) ---------- */
+
+/* ellipticPartialAxCoeffHex3D (kernels/elliptic/ellipticPartialAxCoeffHex3D.okl),
+ * all elements, scalar lambda (p_lambda = 0), poisson = 1 drops the GWJ term. */
+int nrsg_ax_stored_f64(int N, long long E, const double *d_ggeo, const double *d_D, double lambda0,
+                       double lambda1, int poisson, const double *d_q, double *d_Aq, void *stream);
+int nrsg_ax_stored_f32(int N, long long E, const float *d_ggeo, const float *d_D, float lambda0,
+                       float lambda1, int poisson, const float *d_q, float *d_Aq, void *stream);
+/* ellipticPartialAxTrilinearHex3D: geometry recomputed from d_VX [E][8][3]. */
+int nrsg_ax_trilinear_f64(int N, long long E, const double *d_VX, const double *d_gllz, const double *d_gllw,
+                          const double *d_D, double lambda0, double lambda1, int poisson, const double *d_q,
+                          double *d_Aq, void *stream);
+int nrsg_ax_trilinear_f32(int N, long long E, const float *d_VX, const float *d_gllz, const float *d_gllw,
+                          const float *d_D, float lambda0, float lambda1, int poisson, const float *d_q,
+                          float *d_Aq, void *stream);
+
+/* gatherScatterMany_doubleAdd (3rd_party/gslib/ogs/okl/gatherScatterMany.okl):
+ * q[ids[off[g]..off[g+1]]] = sum over the group, for every group g. */
+int nrsg_gs_add_f64(long long ngroups, const int *d_off, const int *d_ids, double *d_q, void *stream);
+int nrsg_gs_add_f32(long long ngroups, const int *d_off, const int *d_ids, float *d_q, void *stream);
+/* mask.okl: q[maskIds[n]] = 0. */
+int nrsg_mask_f64(long long n, const int *d_ids, double *d_q, void *stream);
+
+/* ellipticBlockUpdatePCG + axpbyMany (PCG.cpp:33-83), fused: r -= alpha Ap,
+ * x += alpha p, and *d_rdotr = sum invDegree r^2 (one launch, deterministic). */
+int nrsg_update_pcg_f64(long long n, const double *d_invDegree, const double *d_p, const double *d_Ap,
+                        double alpha, double *d_x, double *d_r, double *d_rdotr, void *stream);
+/* weightedInnerProdMany (kernels/linAlg/weightedInnerProdMany.okl), one field:
+ * *d_out = sum w a b (deterministic two-level reduction, one launch). */
+int nrsg_weighted_inner_prod_f64(long long n, const double *d_w, const double *d_a, const double *d_b,
+                                 double *d_out, void *stream);
+
+/* Geometric factors (kernels/mesh/geometricFactorsHex3D.okl) from trilinear
+ * vertices: writes ggeo [E][7][Np]. */
+int nrsg_geometric_factors_f64(int N, long long E, const double *d_VX, double *d_ggeo, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,252 @@
+"""nekrs_gb300 — GB300-native pressure/Helmholtz elliptic solve.
+
+Python front end of the C ABI declared in include/nekrs_gb300.h.  The compute
+path is the in-tree CUDA library nekrs_gb300/_lib/libnekrs_gb300.so (built for
+sm_103a by nekrs_gb300._build); there is no CPU fallback: if the library or a
+CUDA device is missing, every call raises.
+
+Device buffers are passed as objects exposing ``data_ptr()`` (e.g. torch CUDA
+tensors) or as raw integer device addresses.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import workloads  # noqa: F401
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libnekrs_gb300.so")
+
+NRSG_OK = 0
+STATUS = {0: "OK", 1: "MAXIT", 2: "BREAKDOWN", 3: "NAN", 4: "OOM", 5: "BAD_CONFIG", 6: "CUDA", 7: "NO_DEVICE",
+          8: "INVALID"}
+
+_lib = None
+vp = ctypes.c_void_p
+LL = ctypes.c_longlong
+
+
+class NrsgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"nekrs_gb300 error {code} ({STATUS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class MeshDesc(ctypes.Structure):
+    _fields_ = [("N", ctypes.c_int), ("Nelements", LL), ("h_VX", vp), ("h_EToV", vp), ("h_EToB", vp),
+                ("h_ggeo", vp)]
+
+
+class SolveInfo(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("status", ctypes.c_int), ("res0", ctypes.c_double),
+                ("res", ctypes.c_double), ("solve_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {"iterations": self.iterations, "status": self.status, "res0": self.res0, "res": self.res,
+                "solve_ms": self.solve_ms}
+
+
+def lib():
+    """Load the CUDA library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"nekrs_gb300 CUDA library not built ({LIB_PATH}); run nekrs_gb300._build.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        L.nrsg_last_error.restype = ctypes.c_char_p
+        L.nrsg_kernel_launches.restype = LL
+        L.nrsg_host_setup_maps.argtypes = [ctypes.c_int, LL] + [vp] * 10
+        L.nrsg_elliptic_create.argtypes = [ctypes.POINTER(MeshDesc), ctypes.c_char_p, ctypes.POINTER(vp)]
+        L.nrsg_elliptic_destroy.argtypes = [vp]
+        L.nrsg_elliptic_set_stream.argtypes = [vp, vp]
+        L.nrsg_elliptic_solve.argtypes = [vp, vp, vp, ctypes.POINTER(SolveInfo)]
+        L.nrsg_elliptic_solve_host.argtypes = [vp, vp, vp, ctypes.POINTER(SolveInfo)]
+        for f in ("nrsg_elliptic_operator", "nrsg_elliptic_ax", "nrsg_elliptic_precondition"):
+            getattr(L, f).argtypes = [vp, vp, vp]
+        L.nrsg_elliptic_gs.argtypes = [vp, vp]
+        L.nrsg_elliptic_mask.argtypes = [vp, vp]
+        L.nrsg_elliptic_get.argtypes = [vp, ctypes.c_char_p, vp, ctypes.POINTER(LL)]
+        d, f, i = ctypes.c_double, ctypes.c_float, ctypes.c_int
+        L.nrsg_ax_stored_f64.argtypes = [i, LL, vp, vp, d, d, i, vp, vp, vp]
+        L.nrsg_ax_stored_f32.argtypes = [i, LL, vp, vp, f, f, i, vp, vp, vp]
+        L.nrsg_ax_trilinear_f64.argtypes = [i, LL, vp, vp, vp, vp, d, d, i, vp, vp, vp]
+        L.nrsg_ax_trilinear_f32.argtypes = [i, LL, vp, vp, vp, vp, f, f, i, vp, vp, vp]
+        L.nrsg_gs_add_f64.argtypes = [LL, vp, vp, vp, vp]
+        L.nrsg_gs_add_f32.argtypes = [LL, vp, vp, vp, vp]
+        L.nrsg_mask_f64.argtypes = [LL, vp, vp, vp]
+        L.nrsg_update_pcg_f64.argtypes = [LL, vp, vp, vp, d, vp, vp, vp, vp]
+        L.nrsg_weighted_inner_prod_f64.argtypes = [LL, vp, vp, vp, vp, vp]
+        L.nrsg_geometric_factors_f64.argtypes = [i, LL, vp, vp, vp]
+        _lib = L
+    return _lib
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    raise TypeError("expected a device buffer with data_ptr() or an int address")
+
+
+def check(code):
+    if code != NRSG_OK:
+        raise NrsgError(code, lib().nrsg_last_error().decode(errors="replace"))
+    return code
+
+
+_DTYPES = {"ids": np.int64, "maskedIds": np.int64, "gsOff": np.int32, "gsIds": np.int32, "maskIds": np.int32,
+           "mg.levels": np.float64}
+
+
+class Elliptic:
+    """GB300 counterpart of one ``elliptic_t`` (ellipticSolveSetup + ellipticSolve).
+
+    ``options`` uses the .par [PRESSURE]-section keys, one ``key = value`` per
+    line or ';'-separated.
+    """
+
+    def __init__(self, N, VX, EToV, EToB, options="", ggeo=None):
+        self.N = int(N)
+        self._VX = np.ascontiguousarray(VX, dtype=np.float64)
+        self._EToV = np.ascontiguousarray(EToV, dtype=np.int64)
+        self._EToB = np.ascontiguousarray(EToB, dtype=np.int32)
+        self.E = self._VX.shape[0]
+        self.Np = (self.N + 1) ** 3
+        self.Nlocal = self.E * self.Np
+        self._ggeo = None if ggeo is None else np.ascontiguousarray(ggeo, dtype=np.float64)
+        desc = MeshDesc(self.N, self.E, self._VX.ctypes.data, self._EToV.ctypes.data, self._EToB.ctypes.data,
+                        None if self._ggeo is None else self._ggeo.ctypes.data)
+        h = vp()
+        check(lib().nrsg_elliptic_create(ctypes.byref(desc), options.encode(), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().nrsg_elliptic_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle):
+        check(lib().nrsg_elliptic_set_stream(self.h, stream_handle))
+
+    def solve(self, r, x):
+        """ellipticSolve(elliptic, r, x) on device E-vectors; r becomes the residual."""
+        info = SolveInfo()
+        code = lib().nrsg_elliptic_solve(self.h, _ptr(r), _ptr(x), ctypes.byref(info))
+        if code not in (NRSG_OK, 1):
+            check(code)
+        return info.as_dict()
+
+    def solve_host(self, r, x):
+        """Same solve on host numpy arrays (copied in and out)."""
+        assert r.dtype == np.float64 and x.dtype == np.float64 and r.flags.c_contiguous and x.flags.c_contiguous
+        info = SolveInfo()
+        code = lib().nrsg_elliptic_solve_host(self.h, r.ctypes.data, x.ctypes.data, ctypes.byref(info))
+        if code not in (NRSG_OK, 1):
+            check(code)
+        return info.as_dict()
+
+    def solve_host_ptr(self, r_ptr, x_ptr):
+        """Host solve on raw host addresses (e.g. pinned torch CPU tensors)."""
+        info = SolveInfo()
+        code = lib().nrsg_elliptic_solve_host(self.h, _ptr(r_ptr), _ptr(x_ptr), ctypes.byref(info))
+        if code not in (NRSG_OK, 1):
+            check(code)
+        return info.as_dict()
+
+    def operator(self, q, Aq):
+        check(lib().nrsg_elliptic_operator(self.h, _ptr(q), _ptr(Aq)))
+
+    def ax(self, q, Aq):
+        check(lib().nrsg_elliptic_ax(self.h, _ptr(q), _ptr(Aq)))
+
+    def gs(self, q):
+        check(lib().nrsg_elliptic_gs(self.h, _ptr(q)))
+
+    def mask(self, q):
+        check(lib().nrsg_elliptic_mask(self.h, _ptr(q)))
+
+    def precondition(self, r, z):
+        check(lib().nrsg_elliptic_precondition(self.h, _ptr(r), _ptr(z)))
+
+    def get(self, name):
+        n = LL(0)
+        check(lib().nrsg_elliptic_get(self.h, name.encode(), None, ctypes.byref(n)))
+        out = np.zeros(n.value, dtype=_DTYPES.get(name, np.float64))
+        if n.value:
+            check(lib().nrsg_elliptic_get(self.h, name.encode(), out.ctypes.data, ctypes.byref(n)))
+        return out
+
+
+def kernel_launches():
+    """Kernels launched by the library so far in this process."""
+    return lib().nrsg_kernel_launches()
+
+
+def host_setup_maps(N, EToV, EToB):
+    """Numbering, mask and masked gather maps computed by the library on the host."""
+    EToV = np.ascontiguousarray(EToV, dtype=np.int64)
+    EToB = np.ascontiguousarray(EToB, dtype=np.int32)
+    E = EToV.shape[0]
+    n = E * (N + 1) ** 3
+    ids = np.zeros(n, np.int64)
+    masked = np.zeros(n, np.int64)
+    inv = np.zeros(n)
+    mask = np.zeros(n, np.int32)
+    off = np.zeros(n + 1, np.int32)
+    gids = np.zeros(n, np.int32)
+    nm, ng = LL(0), LL(0)
+    check(lib().nrsg_host_setup_maps(N, E, EToV.ctypes.data, EToB.ctypes.data, ids.ctypes.data, masked.ctypes.data,
+                                     inv.ctypes.data, mask.ctypes.data, ctypes.byref(nm), off.ctypes.data,
+                                     ctypes.byref(ng), gids.ctypes.data))
+    off = off[: ng.value + 1]
+    return {"ids": ids, "maskedIds": masked, "invDegree": inv, "maskIds": mask[: nm.value], "gsOff": off,
+            "gsIds": gids[: off[-1]]}
+
+
+# ---- kernel-level entry points ---------------------------------------------
+def ax_stored_f64(N, E, ggeo, D, lambda0, lambda1, poisson, q, Aq, stream=0):
+    check(lib().nrsg_ax_stored_f64(N, E, _ptr(ggeo), _ptr(D), lambda0, lambda1, int(poisson), _ptr(q), _ptr(Aq), stream))
+
+
+def ax_stored_f32(N, E, ggeo, D, lambda0, lambda1, poisson, q, Aq, stream=0):
+    check(lib().nrsg_ax_stored_f32(N, E, _ptr(ggeo), _ptr(D), lambda0, lambda1, int(poisson), _ptr(q), _ptr(Aq), stream))
+
+
+def ax_trilinear_f64(N, E, VX, z, w, D, lambda0, lambda1, poisson, q, Aq, stream=0):
+    check(lib().nrsg_ax_trilinear_f64(N, E, _ptr(VX), _ptr(z), _ptr(w), _ptr(D), lambda0, lambda1, int(poisson),
+                                      _ptr(q), _ptr(Aq), stream))
+
+
+def ax_trilinear_f32(N, E, VX, z, w, D, lambda0, lambda1, poisson, q, Aq, stream=0):
+    check(lib().nrsg_ax_trilinear_f32(N, E, _ptr(VX), _ptr(z), _ptr(w), _ptr(D), lambda0, lambda1, int(poisson),
+                                      _ptr(q), _ptr(Aq), stream))
+
+
+def gs_add_f64(ngroups, off, ids, q, stream=0):
+    check(lib().nrsg_gs_add_f64(ngroups, _ptr(off), _ptr(ids), _ptr(q), stream))
+
+
+def mask_f64(n, ids, q, stream=0):
+    check(lib().nrsg_mask_f64(n, _ptr(ids), _ptr(q), stream))
+
+
+def update_pcg_f64(n, w, p, Ap, alpha, x, r, rdotr, stream=0):
+    check(lib().nrsg_update_pcg_f64(n, _ptr(w), _ptr(p), _ptr(Ap), alpha, _ptr(x), _ptr(r), _ptr(rdotr), stream))
+
+
+def weighted_inner_prod_f64(n, w, a, b, out, stream=0):
+    check(lib().nrsg_weighted_inner_prod_f64(n, _ptr(w), _ptr(a), _ptr(b), _ptr(out), stream))
+
+
+def geometric_factors_f64(N, E, VX, ggeo, stream=0):
+    check(lib().nrsg_geometric_factors_f64(N, E, _ptr(VX), _ptr(ggeo), stream))

@@ -1,0 +1,568 @@
+// Elliptic solver driver and C ABI.
+//
+// Mirrors (nekRS tree):
+//   ellipticSolveSetup   src/solvers/elliptic/ellipticSetup.cpp:116-327
+//   ellipticSolve        src/solvers/elliptic/ellipticSolve.cpp:32-190
+//   ellipticOperator     src/solvers/elliptic/ellipticOperator.cpp:117-172
+//   pcg (+ flexible)     src/solvers/elliptic/linearSolver/PCG.cpp:86-203
+//   pgmres (+ flexible)  src/solvers/elliptic/linearSolver/PGMRES.cpp:111-340
+//   Jacobi               src/solvers/elliptic/ellipticUpdateJacobi.cpp:32-89
+//
+// GB300 design: one CUDA stream per solver; Krylov scalars stay on the
+// device (alpha/beta are formed by the kernels that use them) and the only
+// host synchronisation per PCG iteration is an 8-byte read of the residual
+// norm for the convergence test.
+
+#include "elliptic.hpp"
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <atomic>
+#include <mutex>
+
+namespace nrsg {
+
+static thread_local std::string g_last_error;
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+// ---------------------------------------------------------------------------
+// Level setup
+// ---------------------------------------------------------------------------
+void FieldLevel::build(int N_, long long E_, const double *VX, const long long *EToV, const int *EToB,
+                       const double *h_ggeo, cudaStream_t s)
+{
+  N = N_;
+  Nq = N + 1;
+  Np = Nq * Nq * Nq;
+  E = E_;
+  Nlocal = E * Np;
+  gll_nodes(N, z, w);
+  diff_matrix(z, Dh);
+  d_D64.upload(Dh);
+  d_z64.upload(z);
+  d_w64.upload(w);
+  d_VX64.upload(VX, (size_t)E * 24);
+  // geometric factors: caller-provided or computed on the device
+  d_ggeo64.alloc((size_t)7 * Nlocal);
+  if (h_ggeo) {
+    NRSG_CUDA(cudaMemcpy(d_ggeo64.p, h_ggeo, sizeof(double) * 7 * Nlocal, cudaMemcpyHostToDevice));
+  } else {
+    launch_geofac(N, E, d_VX64.p, d_z64.p, d_w64.p, d_D64.p, d_ggeo64.p, s);
+  }
+  // numbering, gather maps, mask
+  nek_global_ids(N, E, EToV, ids);
+  GatherMap unmasked;
+  build_gather(ids, unmasked);
+  dirichlet_nodes(N, E, EToB, unmasked, maskIds);
+  maskedIds = ids;
+  for (int m : maskIds) maskedIds[m] = 0;
+  build_gather(maskedIds, gm);
+  d_gsOff.upload(gm.devOff);
+  d_gsIds.upload(gm.devIds);
+  d_mask.upload(maskIds);
+  d_invDegree64.upload(gm.invDegree);
+  ngroups = (long long)gm.devOff.size() - 1;
+  // volume = sum of JW over the E-vector (meshSetup.cpp:444)
+  DevBuf<double> tmp(1);
+  // reuse wdot with w = null on the GWJ slices would need a strided view; sum on host
+  std::vector<double> gg = d_ggeo64.download();
+  volume = 0;
+  for (long long e = 0; e < E; ++e)
+    for (int n = 0; n < Np; ++n) volume += gg[(size_t)e * 7 * Np + 6 * Np + n];
+  VXh.assign(VX, VX + E * 24);
+  EToBh.assign(EToB, EToB + E * 6);
+  EToVh.assign(EToV, EToV + E * 8);
+}
+
+void FieldLevel::make_fp32(cudaStream_t s)
+{
+  if (d_ggeo32.p) return;
+  d_ggeo32.alloc(d_ggeo64.n);
+  launch_copy_cast<double, float>((long long)d_ggeo64.n, d_ggeo64.p, d_ggeo32.p, s);
+  std::vector<float> D32(Dh.begin(), Dh.end()), z32(z.begin(), z.end()), w32(w.begin(), w.end()), v32(VXh.begin(), VXh.end());
+  d_D32.upload(D32);
+  d_z32.upload(z32);
+  d_w32.upload(w32);
+  d_VX32.upload(v32);
+  std::vector<float> inv32(gm.invDegree.begin(), gm.invDegree.end());
+  d_invDegree32.upload(inv32);
+}
+
+// ---------------------------------------------------------------------------
+// Elliptic
+// ---------------------------------------------------------------------------
+Elliptic::Elliptic(const nrsg_mesh_desc *m, const char *options)
+{
+  if (!m || !m->h_VX || !m->h_EToV || !m->h_EToB) throw Error(NRSG_ERR_INVALID, "mesh description incomplete");
+  if (m->N < 1 || m->N > 9) throw Error(NRSG_ERR_BAD_CONFIG, "polynomial order must be 1..9");
+  if (m->Nelements < 1) throw Error(NRSG_ERR_BAD_CONFIG, "Nelements must be positive");
+  if ((long long)m->Nelements * (m->N + 1) * (m->N + 1) * (m->N + 1) >= (1LL << 31))
+    throw Error(NRSG_ERR_BAD_CONFIG, "E*Np must stay below 2^31 (32-bit node indices)");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw Error(NRSG_ERR_NO_DEVICE, "no CUDA device");
+  opt = parse_options(options);
+  NRSG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  ownStream = true;
+  fine.build(m->N, m->Nelements, m->h_VX, m->h_EToV, m->h_EToB, m->h_ggeo, stream);
+  const long long n = fine.Nlocal;
+  p.alloc(n);
+  z.alloc(n);
+  Ap.alloc(n);
+  x0.alloc(n);
+  d_scal.alloc(1);
+  NRSG_CUDA(cudaMallocHost((void **)&h_scal, sizeof(PcgScalars)));
+  red_partials.alloc((size_t)kRedSlots * kRedBlocks);
+  red_counters.alloc(kRedSlots);
+  NRSG_CUDA(cudaMemsetAsync(red_counters.p, 0, sizeof(unsigned) * kRedSlots, stream));
+  NRSG_CUDA(cudaMemsetAsync(d_scal.p, 0, sizeof(PcgScalars), stream));
+  red.partials = red_partials.p;
+  red.counters = red_counters.p;
+  red.slots = kRedSlots;
+  NRSG_CUDA(cudaEventCreate(&ev0));
+  NRSG_CUDA(cudaEventCreate(&ev1));
+
+  if (opt.precon == "jacobi") {
+    invDiag.alloc(n);
+    launch_build_diag<double>(fine.N, fine.E, fine.d_ggeo64.p, fine.d_D64.p, opt.lambda0, opt.lambda1, opt.poisson,
+                              invDiag.p, stream);
+    launch_gs<double>(fine.ngroups, fine.d_gsOff.p, fine.d_gsIds.p, invDiag.p, stream);
+    launch_recip<double>(n, invDiag.p, stream);
+  } else if (opt.precon == "multigrid") {
+    mg_setup();
+  }
+  if (opt.solver == "pgmres" || opt.solver == "pfgmres") gmres_setup();
+  NRSG_CUDA(cudaStreamSynchronize(stream));
+}
+
+Elliptic::~Elliptic()
+{
+  if (stream) cudaStreamSynchronize(stream);
+  if (h_scal) cudaFreeHost(h_scal);
+  if (h_y) cudaFreeHost(h_y);
+  if (ev0) cudaEventDestroy(ev0);
+  if (ev1) cudaEventDestroy(ev1);
+  mg_release();
+  if (ownStream && stream) cudaStreamDestroy(stream);
+}
+
+void Elliptic::ax(const double *q, double *Aq)
+{
+  if (opt.trilinear)
+    launch_ax_trilinear<double>(fine.N, fine.E, fine.d_VX64.p, fine.d_z64.p, fine.d_w64.p, fine.d_D64.p, opt.lambda0,
+                                opt.lambda1, opt.poisson, q, Aq, stream);
+  else
+    launch_ax_stored<double>(fine.N, fine.E, fine.d_ggeo64.p, fine.d_D64.p, opt.lambda0, opt.lambda1, opt.poisson, q,
+                             Aq, stream);
+}
+
+void Elliptic::op(const double *q, double *Aq)
+{
+  ax(q, Aq);
+  launch_mask<double>((long long)fine.maskIds.size(), fine.d_mask.p, Aq, stream);
+  launch_gs<double>(fine.ngroups, fine.d_gsOff.p, fine.d_gsIds.p, Aq, stream);
+}
+
+void Elliptic::precondition(const double *r, double *zz)
+{
+  const long long n = fine.Nlocal;
+  if (opt.precon == "jacobi") {
+    launch_axmyz<double>(n, r, invDiag.p, zz, stream);
+  } else if (opt.precon == "multigrid") {
+    mg_apply(r, zz);
+  } else {
+    NRSG_CUDA(cudaMemcpyAsync(zz, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
+  }
+}
+
+double Elliptic::read_scalar(const double *d_src)
+{
+  NRSG_CUDA(cudaMemcpyAsync(&h_scal->pad, d_src, sizeof(double), cudaMemcpyDeviceToHost, stream));
+  NRSG_CUDA(cudaStreamSynchronize(stream));
+  return h_scal->pad;
+}
+
+// PCG / flexible PCG (PCG.cpp:86-203); scalars live in d_scal.
+int Elliptic::pcg(double *r, double *x, double tol, int maxit, double &rnorm)
+{
+  const long long n = fine.Nlocal;
+  const double *wt = fine.d_invDegree64.p;
+  const bool flexible = (opt.solver == "pfcg");
+  PcgScalars *sc = d_scal.p;
+  launch_fill<double>(n, 0.0, p.p, stream);
+  int it = 0;
+  const double sqrtFac = std::sqrt(1.0 / fine.volume);
+  do {
+    ++it;
+    if (opt.precon == "jacobi") {
+      launch_jacobi_rdotz(n, wt, invDiag.p, r, z.p, sc, red, 0, stream);
+    } else {
+      const double *zz = r;
+      if (opt.precon != "none") {
+        precondition(r, z.p);
+        zz = z.p;
+      } else {
+        NRSG_CUDA(cudaMemcpyAsync(z.p, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
+      }
+      launch_scalar_move(&sc->rdotz_old, &sc->rdotz, nullptr, stream);
+      launch_wdot<double>(n, wt, r, zz, &sc->rdotz, red, 0, stream);
+    }
+    if (flexible && it > 1) launch_wdot<double>(n, wt, z.p, Ap.p, &sc->zAp, red, 1, stream);
+    launch_update_p(n, z.p, p.p, sc, it == 1, flexible, stream);
+    op(p.p, Ap.p);
+    launch_wdot<double>(n, wt, p.p, Ap.p, &sc->pAp, red, 2, stream);
+    launch_update_xr(n, wt, p.p, Ap.p, x, r, sc, red, 3, stream);
+    const double rdotr = read_scalar(&sc->rdotr);
+    rnorm = std::sqrt(rdotr) * sqrtFac;
+    history.push_back(rnorm);
+    if (!std::isfinite(rnorm)) { status = NRSG_ERR_NAN; break; }
+  } while (rnorm > tol && it < maxit);
+  return it;
+}
+
+int Elliptic::solve(double *r, double *x, nrsg_solve_info *info)
+{
+  const long long n = fine.Nlocal;
+  history.clear();
+  status = NRSG_OK;
+  NRSG_CUDA(cudaEventRecord(ev0, stream));
+  // r = b - A x0 (local Ax, ellipticSolve.cpp:91-103), mask, gather-scatter
+  ax(x, Ap.p);
+  launch_axpby<double>(n, -1.0, Ap.p, 1.0, r, stream);
+  launch_mask<double>((long long)fine.maskIds.size(), fine.d_mask.p, r, stream);
+  launch_gs<double>(fine.ngroups, fine.d_gsOff.p, fine.d_gsIds.p, r, stream);
+  NRSG_CUDA(cudaMemcpyAsync(x0.p, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
+  launch_fill<double>(n, 0.0, x, stream);
+  launch_wdot<double>(n, fine.d_invDegree64.p, r, nullptr, &d_scal.p->rdotr, red, 0, stream);
+  const double res0 = std::sqrt(read_scalar(&d_scal.p->rdotr) / fine.volume);
+  if (!std::isfinite(res0)) throw Error(NRSG_ERR_NAN, "unreasonable res0Norm (NaN/Inf right-hand side)");
+  double tol = opt.tol;
+  if (opt.relative) tol *= res0;
+  double res = res0;
+  int iters = 0;
+  if (res0 > 0) {
+    if (opt.solver == "pcg" || opt.solver == "pfcg")
+      iters = pcg(r, x, tol, opt.maxIter, res);
+    else
+      iters = pgmres(r, x, tol, opt.maxIter, res);
+  }
+  launch_axpby<double>(n, 1.0, x0.p, 1.0, x, stream);
+  NRSG_CUDA(cudaEventRecord(ev1, stream));
+  NRSG_CUDA(cudaEventSynchronize(ev1));
+  float ms = 0;
+  NRSG_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+  if (status == NRSG_OK && iters >= opt.maxIter && res > tol) status = NRSG_ERR_MAXIT;
+  lastIters = iters;
+  if (info) {
+    info->iterations = iters;
+    info->status = status;
+    info->res0 = res0;
+    info->res = res;
+    info->solve_ms = ms;
+  }
+  return status;
+}
+
+} // namespace nrsg
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+using nrsg::Elliptic;
+using nrsg::Error;
+
+struct nrsg_elliptic {
+  std::unique_ptr<Elliptic> impl;
+};
+
+#define NRSG_TRY(...)                                                                                     \
+  try {                                                                                                    \
+    __VA_ARGS__;                                                                                           \
+    return NRSG_OK;                                                                                        \
+  } catch (const Error &e) {                                                                               \
+    nrsg::set_last_error(e.what());                                                                        \
+    return e.code;                                                                                         \
+  } catch (const std::bad_alloc &) {                                                                       \
+    nrsg::set_last_error("host allocation failed");                                                        \
+    return NRSG_ERR_OOM;                                                                                   \
+  } catch (const std::exception &e) {                                                                      \
+    nrsg::set_last_error(e.what());                                                                        \
+    return NRSG_ERR_INVALID;                                                                               \
+  }
+
+extern "C" {
+
+const char *nrsg_last_error(void) { return nrsg::g_last_error.c_str(); }
+int nrsg_version(void) { return 1; }
+long long nrsg_kernel_launches(void) { return nrsg::g_launches.load(); }
+
+int nrsg_elliptic_create(const nrsg_mesh_desc *mesh, const char *options, nrsg_elliptic **out)
+{
+  if (!out) return NRSG_ERR_INVALID;
+  *out = nullptr;
+  NRSG_TRY({
+    auto h = new nrsg_elliptic();
+    try {
+      h->impl.reset(new Elliptic(mesh, options));
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  })
+}
+
+int nrsg_elliptic_destroy(nrsg_elliptic *el)
+{
+  NRSG_TRY(delete el)
+}
+
+int nrsg_elliptic_set_stream(nrsg_elliptic *el, void *s)
+{
+  if (!el) return NRSG_ERR_INVALID;
+  NRSG_TRY({
+    auto &E = *el->impl;
+    NRSG_CUDA(cudaStreamSynchronize(E.stream));
+    if (E.ownStream) cudaStreamDestroy(E.stream);
+    E.stream = (cudaStream_t)s;
+    E.ownStream = false;
+  })
+}
+
+int nrsg_elliptic_solve(nrsg_elliptic *el, double *d_r, double *d_x, nrsg_solve_info *info)
+{
+  if (!el || !d_r || !d_x) return NRSG_ERR_INVALID;
+  try {
+    return el->impl->solve(d_r, d_x, info);
+  } catch (const Error &e) {
+    nrsg::set_last_error(e.what());
+    if (info) info->status = e.code;
+    return e.code;
+  } catch (const std::exception &e) {
+    nrsg::set_last_error(e.what());
+    return NRSG_ERR_INVALID;
+  }
+}
+
+int nrsg_elliptic_solve_host(nrsg_elliptic *el, double *h_r, double *h_x, nrsg_solve_info *info)
+{
+  if (!el || !h_r || !h_x) return NRSG_ERR_INVALID;
+  try {
+    auto &E = *el->impl;
+    const size_t bytes = sizeof(double) * E.fine.Nlocal;
+    if (!E.io_r.p) { E.io_r.alloc(E.fine.Nlocal); E.io_x.alloc(E.fine.Nlocal); }
+    NRSG_CUDA(cudaMemcpyAsync(E.io_r.p, h_r, bytes, cudaMemcpyHostToDevice, E.stream));
+    NRSG_CUDA(cudaMemcpyAsync(E.io_x.p, h_x, bytes, cudaMemcpyHostToDevice, E.stream));
+    const int st = E.solve(E.io_r.p, E.io_x.p, info);
+    NRSG_CUDA(cudaMemcpyAsync(h_r, E.io_r.p, bytes, cudaMemcpyDeviceToHost, E.stream));
+    NRSG_CUDA(cudaMemcpyAsync(h_x, E.io_x.p, bytes, cudaMemcpyDeviceToHost, E.stream));
+    NRSG_CUDA(cudaStreamSynchronize(E.stream));
+    return st;
+  } catch (const Error &e) {
+    nrsg::set_last_error(e.what());
+    return e.code;
+  } catch (const std::exception &e) {
+    nrsg::set_last_error(e.what());
+    return NRSG_ERR_INVALID;
+  }
+}
+
+int nrsg_elliptic_operator(nrsg_elliptic *el, const double *d_q, double *d_Aq)
+{
+  if (!el || !d_q || !d_Aq) return NRSG_ERR_INVALID;
+  NRSG_TRY({
+    el->impl->op(d_q, d_Aq);
+    NRSG_CUDA(cudaStreamSynchronize(el->impl->stream));
+  })
+}
+int nrsg_elliptic_ax(nrsg_elliptic *el, const double *d_q, double *d_Aq)
+{
+  if (!el || !d_q || !d_Aq) return NRSG_ERR_INVALID;
+  NRSG_TRY({
+    el->impl->ax(d_q, d_Aq);
+    NRSG_CUDA(cudaStreamSynchronize(el->impl->stream));
+  })
+}
+int nrsg_elliptic_gs(nrsg_elliptic *el, double *d_q)
+{
+  if (!el || !d_q) return NRSG_ERR_INVALID;
+  NRSG_TRY({
+    auto &E = *el->impl;
+    nrsg::launch_gs<double>(E.fine.ngroups, E.fine.d_gsOff.p, E.fine.d_gsIds.p, d_q, E.stream);
+    NRSG_CUDA(cudaStreamSynchronize(E.stream));
+  })
+}
+int nrsg_elliptic_mask(nrsg_elliptic *el, double *d_q)
+{
+  if (!el || !d_q) return NRSG_ERR_INVALID;
+  NRSG_TRY({
+    auto &E = *el->impl;
+    nrsg::launch_mask<double>((long long)E.fine.maskIds.size(), E.fine.d_mask.p, d_q, E.stream);
+    NRSG_CUDA(cudaStreamSynchronize(E.stream));
+  })
+}
+int nrsg_elliptic_precondition(nrsg_elliptic *el, const double *d_r, double *d_z)
+{
+  if (!el || !d_r || !d_z) return NRSG_ERR_INVALID;
+  NRSG_TRY({
+    el->impl->precondition(d_r, d_z);
+    NRSG_CUDA(cudaStreamSynchronize(el->impl->stream));
+  })
+}
+
+int nrsg_elliptic_get(nrsg_elliptic *el, const char *name, void *h_out, long long *count)
+{
+  if (!el || !name || !count) return NRSG_ERR_INVALID;
+  NRSG_TRY({
+    auto &E = *el->impl;
+    auto &L = E.fine;
+    const std::string s(name);
+    auto put = [&](const auto &v) {
+      *count = (long long)v.size();
+      if (h_out && !v.empty()) std::memcpy(h_out, v.data(), v.size() * sizeof(v[0]));
+    };
+    if (s == "ids") put(L.ids);
+    else if (s == "maskedIds") put(L.maskedIds);
+    else if (s == "gsOff") put(L.gm.off);
+    else if (s == "gsIds") put(L.gm.ids);
+    else if (s == "maskIds") put(L.maskIds);
+    else if (s == "invDegree") put(L.gm.invDegree);
+    else if (s == "D") put(L.Dh);
+    else if (s == "history") put(E.history);
+    else if (s == "ggeo") put(L.d_ggeo64.download());
+    else if (s == "invDiag") put(E.invDiag.download());
+    else if (s == "x" || s == "y" || s == "z") {
+      std::vector<double> X, Y, Z;
+      nrsg::trilinear_nodes(L.N, L.E, L.VXh.data(), L.z, X, Y, Z);
+      put(s == "x" ? X : (s == "y" ? Y : Z));
+    } else if (s.rfind("mg.", 0) == 0) {
+      put(E.mg_get(s));
+    } else
+      throw Error(NRSG_ERR_INVALID, "unknown array '" + s + "'");
+  })
+}
+
+// ---- host-only setup (no device needed) -----------------------------------
+int nrsg_host_setup_maps(int N, long long E, const long long *h_EToV, const int *h_EToB, long long *h_ids,
+                         long long *h_maskedIds, double *h_invDegree, int *h_maskIds, long long *nmask, int *h_gsOff,
+                         long long *ngroups, int *h_gsIds)
+{
+  if (N < 1 || E < 1 || !h_EToV || !h_EToB) return NRSG_ERR_INVALID;
+  NRSG_TRY({
+    std::vector<long long> ids;
+    nrsg::nek_global_ids(N, E, h_EToV, ids);
+    nrsg::GatherMap um, gm;
+    nrsg::build_gather(ids, um);
+    std::vector<int> mask;
+    nrsg::dirichlet_nodes(N, E, h_EToB, um, mask);
+    std::vector<long long> masked = ids;
+    for (int m : mask) masked[m] = 0;
+    nrsg::build_gather(masked, gm);
+    if (h_ids) std::memcpy(h_ids, ids.data(), ids.size() * sizeof(long long));
+    if (h_maskedIds) std::memcpy(h_maskedIds, masked.data(), masked.size() * sizeof(long long));
+    if (h_invDegree) std::memcpy(h_invDegree, gm.invDegree.data(), gm.invDegree.size() * sizeof(double));
+    if (h_maskIds) std::memcpy(h_maskIds, mask.data(), mask.size() * sizeof(int));
+    if (nmask) *nmask = (long long)mask.size();
+    if (h_gsOff) std::memcpy(h_gsOff, gm.off.data(), gm.off.size() * sizeof(int));
+    if (ngroups) *ngroups = (long long)gm.off.size() - 1;
+    if (h_gsIds) std::memcpy(h_gsIds, gm.ids.data(), gm.ids.size() * sizeof(int));
+  })
+}
+
+// ---- kernel-level entry points --------------------------------------------
+int nrsg_ax_stored_f64(int N, long long E, const double *ggeo, const double *D, double l0, double l1, int poisson,
+                       const double *q, double *Aq, void *s)
+{
+  NRSG_TRY(nrsg::launch_ax_stored<double>(N, E, ggeo, D, l0, l1, poisson != 0, q, Aq, (cudaStream_t)s))
+}
+int nrsg_ax_stored_f32(int N, long long E, const float *ggeo, const float *D, float l0, float l1, int poisson,
+                       const float *q, float *Aq, void *s)
+{
+  NRSG_TRY(nrsg::launch_ax_stored<float>(N, E, ggeo, D, l0, l1, poisson != 0, q, Aq, (cudaStream_t)s))
+}
+int nrsg_ax_trilinear_f64(int N, long long E, const double *VX, const double *z, const double *w, const double *D,
+                          double l0, double l1, int poisson, const double *q, double *Aq, void *s)
+{
+  NRSG_TRY(nrsg::launch_ax_trilinear<double>(N, E, VX, z, w, D, l0, l1, poisson != 0, q, Aq, (cudaStream_t)s))
+}
+int nrsg_ax_trilinear_f32(int N, long long E, const float *VX, const float *z, const float *w, const float *D,
+                          float l0, float l1, int poisson, const float *q, float *Aq, void *s)
+{
+  NRSG_TRY(nrsg::launch_ax_trilinear<float>(N, E, VX, z, w, D, l0, l1, poisson != 0, q, Aq, (cudaStream_t)s))
+}
+int nrsg_gs_add_f64(long long ng, const int *off, const int *ids, double *q, void *s)
+{
+  NRSG_TRY(nrsg::launch_gs<double>(ng, off, ids, q, (cudaStream_t)s))
+}
+int nrsg_gs_add_f32(long long ng, const int *off, const int *ids, float *q, void *s)
+{
+  NRSG_TRY(nrsg::launch_gs<float>(ng, off, ids, q, (cudaStream_t)s))
+}
+int nrsg_mask_f64(long long n, const int *ids, double *q, void *s)
+{
+  NRSG_TRY(nrsg::launch_mask<double>(n, ids, q, (cudaStream_t)s))
+}
+
+namespace {
+// scratch for the kernel-level reduction entry points (one per device)
+struct KernelScratch {
+  nrsg::DevBuf<double> partials;
+  nrsg::DevBuf<unsigned> counters;
+  nrsg::Reduce red;
+  int device = -1;
+};
+std::mutex g_ks_mutex;
+KernelScratch &kernel_scratch()
+{
+  static KernelScratch ks[16];
+  int dev = 0;
+  NRSG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 16) throw Error(NRSG_ERR_INVALID, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_ks_mutex);
+  KernelScratch &k = ks[dev];
+  if (k.device != dev) {
+    k.partials.alloc(nrsg::kRedBlocks);
+    k.counters.alloc(1);
+    NRSG_CUDA(cudaMemset(k.counters.p, 0, sizeof(unsigned)));
+    k.red.partials = k.partials.p;
+    k.red.counters = k.counters.p;
+    k.red.slots = 1;
+    k.device = dev;
+  }
+  return k;
+}
+} // namespace
+
+int nrsg_update_pcg_f64(long long n, const double *w, const double *p, const double *Ap, double alpha, double *x,
+                        double *r, double *rdotr, void *s)
+{
+  NRSG_TRY({
+    auto &k = kernel_scratch();
+    nrsg::launch_update_pcg_alpha(n, w, p, Ap, alpha, x, r, rdotr, k.red, 0, (cudaStream_t)s);
+  })
+}
+int nrsg_weighted_inner_prod_f64(long long n, const double *w, const double *a, const double *b, double *out, void *s)
+{
+  NRSG_TRY({
+    auto &k = kernel_scratch();
+    nrsg::launch_wdot<double>(n, w, a, b, out, k.red, 0, (cudaStream_t)s);
+  })
+}
+int nrsg_geometric_factors_f64(int N, long long E, const double *VX, double *ggeo, void *s)
+{
+  NRSG_TRY({
+    std::vector<double> z, w, D;
+    nrsg::gll_nodes(N, z, w);
+    nrsg::diff_matrix(z, D);
+    nrsg::DevBuf<double> dz, dw, dD;
+    dz.upload(z);
+    dw.upload(w);
+    dD.upload(D);
+    nrsg::launch_geofac(N, E, VX, dz.p, dw.p, dD.p, ggeo, (cudaStream_t)s);
+    NRSG_CUDA(cudaStreamSynchronize((cudaStream_t)s));
+  })
+}
+
+} // extern "C"

@@ -1,0 +1,92 @@
+// Solver state of one elliptic problem (the elliptic_t counterpart).
+#pragma once
+
+#include "nrsg_internal.hpp"
+
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace nrsg {
+
+// Mesh data of one polynomial order on the device (fine level or pMG level).
+struct FieldLevel {
+  int N = 0, Nq = 0, Np = 0;
+  long long E = 0, Nlocal = 0;
+  std::vector<double> z, w, Dh;
+  std::vector<long long> ids, maskedIds;
+  GatherMap gm;
+  std::vector<int> maskIds;
+  std::vector<double> VXh;
+  std::vector<int> EToBh;
+  std::vector<long long> EToVh;
+  double volume = 0;
+  long long ngroups = 0;
+  DevBuf<double> d_ggeo64, d_D64, d_z64, d_w64, d_VX64, d_invDegree64;
+  DevBuf<float> d_ggeo32, d_D32, d_z32, d_w32, d_VX32, d_invDegree32;
+  DevBuf<int> d_gsOff, d_gsIds, d_mask;
+
+  void build(int N, long long E, const double *VX, const long long *EToV, const int *EToB, const double *h_ggeo,
+             cudaStream_t s);
+  void make_fp32(cudaStream_t s);
+};
+
+struct MGState;   // p-multigrid hierarchy (mg.cu)
+struct MGDeleter {
+  void operator()(MGState *m) const;
+};
+
+struct Elliptic {
+  static constexpr int kRedSlots = 8;
+  Options opt;
+  cudaStream_t stream = nullptr;
+  bool ownStream = false;
+  FieldLevel fine;
+
+  // Krylov workspace (elliptic.h:240-262 slices)
+  DevBuf<double> p, z, Ap, x0, invDiag;
+  DevBuf<double> io_r, io_x;            // staging for the host-buffer solve
+  DevBuf<PcgScalars> d_scal;
+  PcgScalars *h_scal = nullptr;          // pinned
+  DevBuf<double> red_partials;
+  DevBuf<unsigned> red_counters;
+  Reduce red;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  // GMRES workspace
+  DevBuf<double> gV, gZ, gW, gB, gY;
+  double *h_y = nullptr;                  // pinned: y[0..nr] + nw
+
+  std::unique_ptr<MGState, MGDeleter> mg;
+  std::vector<double> history;
+  int status = NRSG_OK;
+  int lastIters = 0;
+
+  Elliptic(const nrsg_mesh_desc *mesh, const char *options);
+  ~Elliptic();
+
+  void ax(const double *q, double *Aq);
+  void op(const double *q, double *Aq);
+  void precondition(const double *r, double *z);
+  double read_scalar(const double *d_src);
+  int pcg(double *r, double *x, double tol, int maxit, double &rnorm);
+  void gmres_setup();
+  int pgmres(double *r, double *x, double tol, int maxit, double &rnorm);
+  int solve(double *r, double *x, nrsg_solve_info *info);
+
+  void mg_setup();
+  void mg_apply(const double *r, double *z);
+  void mg_release();
+  std::vector<double> mg_get(const std::string &name);
+};
+
+// GMRES kernels (kernels_vec.cu)
+void launch_multi_wdot(long long n, const double *w, const double *V, int nvec, const double *x, double *out,
+                       Reduce &red, int slot, cudaStream_t s);
+void launch_gram_schmidt(long long n, const double *w, const double *V, int nvec, const double *y, double *x,
+                         double *nrm2, Reduce &red, int slot, cudaStream_t s);
+void launch_gmres_update(long long n, const double *V, int nvec, const double *y, double *x, cudaStream_t s);
+void launch_residual_norm(long long n, const double *w, const double *b, const double *Ax, double *r, double *nrm2,
+                          Reduce &red, int slot, cudaStream_t s);
+
+} // namespace nrsg

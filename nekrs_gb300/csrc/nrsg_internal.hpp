@@ -1,0 +1,181 @@
+// Internal declarations of the nekrs_gb300 library (host + device).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/nekrs_gb300.h"
+
+namespace nrsg {
+
+struct Error : public std::runtime_error {
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+void set_last_error(const std::string &msg);
+
+#define NRSG_CUDA(call)                                                                                    \
+  do {                                                                                                     \
+    cudaError_t err__ = (call);                                                                            \
+    if (err__ != cudaSuccess)                                                                              \
+      throw ::nrsg::Error(err__ == cudaErrorMemoryAllocation ? NRSG_ERR_OOM : NRSG_ERR_CUDA,             \
+                          std::string(#call) + ": " + cudaGetErrorString(err__));                        \
+  } while (0)
+
+// Every launcher ends with NRSG_CHECK_LAUNCH(), which also counts the launch.
+void count_launch();
+#define NRSG_CHECK_LAUNCH()                                                                                \
+  do {                                                                                                     \
+    ::nrsg::count_launch();                                                                                \
+    NRSG_CUDA(cudaGetLastError());                                                                         \
+  } while (0)
+
+// Owning device buffer.
+template <typename T> struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  explicit DevBuf(size_t count) { alloc(count); }
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DevBuf &operator=(DevBuf &&o) noexcept
+  {
+    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void alloc(size_t count)
+  {
+    release();
+    if (count == 0) return;
+    NRSG_CUDA(cudaMalloc((void **)&p, count * sizeof(T)));
+    n = count;
+  }
+  void release()
+  {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void upload(const T *h, size_t count)
+  {
+    alloc(count);
+    if (count) NRSG_CUDA(cudaMemcpy(p, h, count * sizeof(T), cudaMemcpyHostToDevice));
+  }
+  void upload(const std::vector<T> &v) { upload(v.data(), v.size()); }
+  std::vector<T> download() const
+  {
+    std::vector<T> h(n);
+    if (n) NRSG_CUDA(cudaMemcpy(h.data(), p, n * sizeof(T), cudaMemcpyDeviceToHost));
+    return h;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+// ----------------------------------------------------------------------------
+// Options: the .par [PRESSURE]-section keys that reach the elliptic solve.
+// ----------------------------------------------------------------------------
+struct Options {
+  std::string solver = "pcg";   // pcg | pfcg | pgmres | pfgmres
+  int nVector = 15;
+  double tol = 1e-8;
+  bool relative = true;
+  int maxIter = 500;
+  std::string precon = "jacobi"; // none | jacobi | multigrid
+  std::string smoother = "cheby+jac";
+  int chebyDegree = 2;
+  double minEigFactor = 0.1, maxEigFactor = 1.1;
+  std::string schedule;
+  std::string coarse = "jpcg";
+  double coarseTol = 1e-4;
+  int coarseMaxIter = 200;
+  std::string mgPrecision = "fp64"; // fp64 | fp32 | mixed
+  bool poisson = true;
+  double lambda0 = 1.0, lambda1 = 0.0;
+  bool trilinear = false;
+  unsigned long long seed = 0x5eed;
+};
+Options parse_options(const char *text);
+
+// ----------------------------------------------------------------------------
+// Host-side setup (setup.cpp)
+// ----------------------------------------------------------------------------
+void gll_nodes(int N, std::vector<double> &z, std::vector<double> &w);
+void diff_matrix(const std::vector<double> &z, std::vector<double> &D);
+void lagrange_interp(const std::vector<double> &zin, const std::vector<double> &zout, std::vector<double> &I);
+void nek_global_ids(int N, long long E, const long long *EToV, std::vector<long long> &ids);
+struct GatherMap {
+  std::vector<int> off, ids;          // all groups (CSR), reference order
+  std::vector<int> devOff, devIds;    // groups with >= 2 members only (what the kernel visits)
+  std::vector<double> invDegree;
+};
+void build_gather(const std::vector<long long> &ids, GatherMap &gm);
+void dirichlet_nodes(int N, long long E, const int *EToB, const GatherMap &unmasked, std::vector<int> &maskIds);
+void trilinear_nodes(int N, long long E, const double *VX, const std::vector<double> &z1, std::vector<double> &x,
+                     std::vector<double> &y, std::vector<double> &zz);
+
+// ----------------------------------------------------------------------------
+// Device kernels (launchers)
+// ----------------------------------------------------------------------------
+struct Reduce {              // scratch for deterministic one-launch reductions
+  double *partials = nullptr; // [slots][kMaxBlocks]
+  unsigned *counters = nullptr;
+  int slots = 0;
+};
+constexpr int kRedBlocks = 1216;     // 152 SMs x 8
+constexpr int kRedThreads = 256;
+
+template <typename T>
+void launch_ax_stored(int N, long long E, const T *ggeo, const T *D, T lambda0, T lambda1, bool poisson, const T *q,
+                      T *Aq, cudaStream_t s);
+template <typename T>
+void launch_ax_trilinear(int N, long long E, const T *VX, const T *gllz, const T *gllw, const T *D, T lambda0,
+                         T lambda1, bool poisson, const T *q, T *Aq, cudaStream_t s);
+template <typename T> void launch_gs(long long ngroups, const int *off, const int *ids, T *q, cudaStream_t s);
+template <typename T> void launch_mask(long long n, const int *ids, T *q, cudaStream_t s);
+template <typename T>
+void launch_build_diag(int N, long long E, const T *ggeo, const T *D, T lambda0, T lambda1, bool poisson, T *diag,
+                       cudaStream_t s);
+void launch_geofac(int N, long long E, const double *VX, const double *gllz, const double *gllw, const double *D,
+                   double *ggeo, cudaStream_t s);
+
+// reductions: out = sum w*a*b (w may be null -> 1; b may be null -> a)
+template <typename T>
+void launch_wdot(long long n, const T *w, const T *a, const T *b, double *out, Reduce &red, int slot, cudaStream_t s);
+
+// vector ops
+template <typename T> void launch_fill(long long n, T v, T *x, cudaStream_t s);
+template <typename T> void launch_axpby(long long n, T a, const T *x, T b, T *y, cudaStream_t s); // y = a x + b y
+template <typename T> void launch_axmy(long long n, const T *w, T *x, cudaStream_t s);             // x = w .* x
+template <typename T> void launch_axmyz(long long n, const T *a, const T *b, T *z, cudaStream_t s);   // z = a .* b
+template <typename T> void launch_recip(long long n, T *x, cudaStream_t s);                           // x = 1/x
+template <typename T> void launch_scale_copy(long long n, T a, const T *x, T *y, cudaStream_t s);     // y = a x
+template <typename Ti, typename To> void launch_copy_cast(long long n, const Ti *x, To *y, cudaStream_t s);
+
+// PCG device scalars
+struct PcgScalars {
+  double rdotz, rdotz_old, pAp, rdotr, zAp, alpha, beta, pad;
+};
+// z = invDiag .* r; scal.rdotz = (r,z)_w   (rdotz_old <- rdotz first)
+void launch_jacobi_rdotz(long long n, const double *w, const double *invDiag, const double *r, double *z,
+                         PcgScalars *sc, Reduce &red, int slot, cudaStream_t s);
+// p = z + beta p, beta from scalars (first => 0; flexible => -alpha zAp / rdotz_old)
+void launch_update_p(long long n, const double *z, double *p, const PcgScalars *sc, bool first, bool flexible,
+                     cudaStream_t s);
+// alpha = rdotz/(pAp+1e-300); r -= alpha Ap; x += alpha p; rdotr = (r,r)_w
+void launch_update_xr(long long n, const double *w, const double *p, const double *Ap, double *x, double *r,
+                      PcgScalars *sc, Reduce &red, int slot, cudaStream_t s);
+// store a reduction result into a scalar field: dst = src (device), optionally save old
+void launch_scalar_move(double *dst, const double *src, double *save_old, cudaStream_t s);
+// fused update with explicit alpha (kernel-level entry point)
+void launch_update_pcg_alpha(long long n, const double *w, const double *p, const double *Ap, double alpha, double *x,
+                             double *r, double *rdotr, Reduce &red, int slot, cudaStream_t s);
+
+} // namespace nrsg

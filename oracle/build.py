@@ -1,0 +1,47 @@
+"""Build recipe for the oracle (test infrastructure only).
+
+Compiles the C++ restatement in oracle/*.cpp into oracle/_build/liboracle.so
+with the host compiler (portable flags, no -march), and, when the reference
+tree is present, the reference's serial kernels into oracle/_ref.
+"""
+import glob
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+
+
+def build_oracle(force=False):
+    os.makedirs(BUILD, exist_ok=True)
+    lib = os.path.join(BUILD, "liboracle.so")
+    srcs = sorted(glob.glob(os.path.join(HERE, "*.cpp")))
+    hdrs = sorted(glob.glob(os.path.join(HERE, "*.hpp")))
+    if not force and os.path.exists(lib):
+        t = os.path.getmtime(lib)
+        if all(os.path.getmtime(s) < t for s in srcs + hdrs):
+            return lib
+    objs, procs = [], []
+    for s in srcs:
+        o = os.path.join(BUILD, os.path.basename(s)[:-4] + ".o")
+        objs.append(o)
+        procs.append(subprocess.Popen(["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC", "-c", s, "-o", o]))
+    for p in procs:
+        if p.wait() != 0:
+            raise RuntimeError("oracle build failed")
+    subprocess.check_call(["g++", "-shared", "-fopenmp", "-o", lib] + objs)
+    return lib
+
+
+def build_all(reference_root="/root/reference"):
+    lib = build_oracle()
+    ref = None
+    if os.path.isdir(reference_root):
+        from . import build_ref  # noqa: E402
+
+        ref = build_ref.build(reference_root)
+    return lib, ref
+
+
+if __name__ == "__main__":
+    print(build_all())

@@ -1,0 +1,184 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+Imported by tests/, __graft_entry__.smoke() and the cpu-baseline leg of
+bench.py, never by the product package.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+_ref = None
+
+D = ctypes.POINTER(ctypes.c_double)
+F = ctypes.POINTER(ctypes.c_float)
+L = ctypes.POINTER(ctypes.c_longlong)
+I = ctypes.POINTER(ctypes.c_int)
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        _lib = ctypes.CDLL(path)
+        _lib.orc_create.restype = ctypes.c_void_p
+        _lib.orc_create.argtypes = [ctypes.c_int, ctypes.c_longlong, D, L, I, ctypes.c_char_p]
+        _lib.orc_destroy.argtypes = [ctypes.c_void_p]
+        _lib.orc_size.restype = ctypes.c_longlong
+        _lib.orc_size.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+        _lib.orc_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p]
+        _lib.orc_volume.restype = ctypes.c_double
+        _lib.orc_volume.argtypes = [ctypes.c_void_p]
+        for name in ("orc_ax", "orc_operator", "orc_precond"):
+            getattr(_lib, name).argtypes = [ctypes.c_void_p, D, D]
+        _lib.orc_ax_fp32.argtypes = [ctypes.c_void_p, F, F]
+        _lib.orc_gs.argtypes = [ctypes.c_void_p, D]
+        _lib.orc_mask.argtypes = [ctypes.c_void_p, D]
+        _lib.orc_solve.argtypes = [ctypes.c_void_p, D, D, D]
+        _lib.orc_box_mesh.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double, D, L, I, ctypes.c_int]
+        _lib.orc_box_rhs.argtypes = [ctypes.c_int] * 4 + [ctypes.c_ulonglong, D, D]
+        _lib.orc_global_ids.argtypes = [ctypes.c_int, ctypes.c_longlong, L, L]
+        _lib.orc_gll.argtypes = [ctypes.c_int, D, D]
+        _lib.orc_dmatrix.argtypes = [ctypes.c_int, D]
+        _lib.orc_interp.argtypes = [ctypes.c_int, ctypes.c_int, D]
+    return _lib
+
+
+def ref_lib():
+    """The reference's own serial kernels (oracle/_ref), or None where absent."""
+    global _ref
+    if _ref is None:
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_ref", "libnekref.so")
+        if not os.path.exists(path):
+            return None
+        _ref = ctypes.CDLL(path)
+    return _ref
+
+
+def gll(N):
+    z = np.zeros(N + 1)
+    w = np.zeros(N + 1)
+    lib().orc_gll(N, _p(z, D), _p(w, D))
+    return z, w
+
+
+def dmatrix(N):
+    Dm = np.zeros((N + 1) * (N + 1))
+    lib().orc_dmatrix(N, _p(Dm, D))
+    return Dm.reshape(N + 1, N + 1)
+
+
+def interp(Nin, Nout):
+    Im = np.zeros((Nout + 1) * (Nin + 1))
+    lib().orc_interp(Nin, Nout, _p(Im, D))
+    return Im.reshape(Nout + 1, Nin + 1)
+
+
+def box_mesh(nx, ny, nz, eps, all_dirichlet=True):
+    E = nx * ny * nz
+    VX = np.zeros((E, 8, 3))
+    EToV = np.zeros((E, 8), dtype=np.int64)
+    EToB = np.zeros((E, 6), dtype=np.int32)
+    lib().orc_box_mesh(nx, ny, nz, eps, _p(VX, D), _p(EToV, L), _p(EToB, I), 1 if all_dirichlet else 0)
+    return VX, EToV, EToB
+
+
+def global_ids(N, EToV):
+    E = EToV.shape[0]
+    ids = np.zeros(E * (N + 1) ** 3, dtype=np.int64)
+    EToV = np.ascontiguousarray(EToV, dtype=np.int64)
+    lib().orc_global_ids(N, E, _p(EToV, L), _p(ids, L))
+    return ids
+
+
+class Elliptic:
+    """Oracle solver for one mesh; options use the .par [PRESSURE] keys."""
+
+    def __init__(self, N, VX, EToV, EToB, options=""):
+        self.N = N
+        self.E = VX.shape[0]
+        self.Np = (N + 1) ** 3
+        self.Nlocal = self.E * self.Np
+        self._VX = np.ascontiguousarray(VX, dtype=np.float64)
+        self._EToV = np.ascontiguousarray(EToV, dtype=np.int64)
+        self._EToB = np.ascontiguousarray(EToB, dtype=np.int32)
+        self.h = lib().orc_create(N, self.E, _p(self._VX, D), _p(self._EToV, L), _p(self._EToB, I),
+                                  options.encode())
+        if not self.h:
+            raise RuntimeError("oracle setup failed")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def get(self, name):
+        n = lib().orc_size(self.h, name.encode())
+        if n < 0:
+            raise KeyError(name)
+        dt = {"ids": np.int64, "maskedIds": np.int64, "gsOff": np.int32, "gsIds": np.int32,
+              "maskIds": np.int32}.get(name, np.float64)
+        out = np.zeros(n, dtype=dt)
+        lib().orc_get(self.h, name.encode(), out.ctypes.data_as(ctypes.c_void_p))
+        return out
+
+    @property
+    def volume(self):
+        return lib().orc_volume(self.h)
+
+    def ax(self, q):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        out = np.zeros_like(q)
+        lib().orc_ax(self.h, _p(q, D), _p(out, D))
+        return out
+
+    def ax_fp32(self, q):
+        q = np.ascontiguousarray(q, dtype=np.float32)
+        out = np.zeros_like(q)
+        lib().orc_ax_fp32(self.h, _p(q, F), _p(out, F))
+        return out
+
+    def operator(self, q):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        out = np.zeros_like(q)
+        lib().orc_operator(self.h, _p(q, D), _p(out, D))
+        return out
+
+    def gs(self, q):
+        q = np.array(q, dtype=np.float64)
+        lib().orc_gs(self.h, _p(q, D))
+        return q
+
+    def mask(self, q):
+        q = np.array(q, dtype=np.float64)
+        lib().orc_mask(self.h, _p(q, D))
+        return q
+
+    def precond(self, r):
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        z = np.zeros_like(r)
+        lib().orc_precond(self.h, _p(r, D), _p(z, D))
+        return z
+
+    def solve(self, rhs, x0=None):
+        r = np.array(rhs, dtype=np.float64)
+        x = np.zeros_like(r) if x0 is None else np.array(x0, dtype=np.float64)
+        info = np.zeros(4)
+        lib().orc_solve(self.h, _p(r, D), _p(x, D), _p(info, D))
+        return x, {"iters": int(info[0]), "res0": info[1], "res": info[2], "status": int(info[3]),
+                   "history": self.get("history"), "r": r}
+
+
+def box_rhs(N, nx, ny, nz, seed, ggeo):
+    E = nx * ny * nz
+    rhs = np.zeros(E * (N + 1) ** 3)
+    g = np.ascontiguousarray(ggeo, dtype=np.float64)
+    lib().orc_box_rhs(N, nx, ny, nz, seed, _p(g, D), _p(rhs, D))
+    return rhs

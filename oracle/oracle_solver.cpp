@@ -1,0 +1,534 @@
+// ORACLE — test infrastructure only (see oracle_mesh.cpp header).
+//
+// CPU restatement of the elliptic operator and Krylov drivers:
+//   ellipticAx / ellipticOperator   src/solvers/elliptic/ellipticOperator.cpp:31-172
+//   Ax kernel (stored geometry)     kernels/elliptic/ellipticPartialAxCoeffHex3D.c:1-98
+//   Ax kernel (trilinear geometry)  kernels/elliptic/ellipticPartialAxTrilinearHex3D.okl:2-186
+//   Jacobi diagonal                 kernels/elliptic/ellipticBlockBuildDiagonalHex3D.okl:27-117,
+//                                   src/solvers/elliptic/ellipticUpdateJacobi.cpp:32-89
+//   local gather-scatter            3rd_party/gslib/ogs/okl/gatherScatterMany.okl
+//   ellipticSolve                   src/solvers/elliptic/ellipticSolve.cpp:32-190
+//   pcg / flexible pcg              src/solvers/elliptic/linearSolver/PCG.cpp:33-203
+//   pgmres / flexible pgmres        src/solvers/elliptic/linearSolver/PGMRES.cpp:31-340
+// The multigrid preconditioner lives in oracle_mg.cpp.
+
+#include "oracle_internal.hpp"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <sstream>
+#include <stdexcept>
+
+namespace orc {
+
+// ---------------------------------------------------------------------------
+// options: "key=value" pairs separated by ';' or newlines; keys follow the
+// .par [PRESSURE] section names (doc/parHelp.txt:80-120).
+// ---------------------------------------------------------------------------
+static std::string lower(std::string s)
+{
+  for (auto &c : s) c = (char)std::tolower((unsigned char)c);
+  return s;
+}
+static std::string trim(const std::string &s)
+{
+  size_t a = s.find_first_not_of(" \t\r\n"), b = s.find_last_not_of(" \t\r\n");
+  return a == std::string::npos ? "" : s.substr(a, b - a + 1);
+}
+
+Options parse_options(const std::string &text)
+{
+  Options o;
+  std::string t = text;
+  for (auto &c : t)
+    if (c == ';') c = '\n';
+  std::istringstream in(t);
+  std::string line;
+  while (std::getline(in, line)) {
+    const auto eq = line.find('=');
+    if (eq == std::string::npos) continue;
+    const std::string key = lower(trim(line.substr(0, eq)));
+    const std::string val = trim(line.substr(eq + 1));
+    const std::string lv = lower(val);
+    if (key == "solver") {
+      // pcg, pfcg (= pcg+flexible), pgmres+nvector=15, pfgmres
+      o.solver = lv.substr(0, lv.find('+'));
+      if (lv.find("flexible") != std::string::npos && o.solver == "pcg") o.solver = "pfcg";
+      const auto nv = lv.find("nvector=");
+      if (nv != std::string::npos) o.nVector = std::stoi(lv.substr(nv + 8));
+    } else if (key == "residualtol") {
+      o.tol = std::stod(lv.substr(0, lv.find('+')));
+      o.relative = lv.find("relative") != std::string::npos;
+    } else if (key == "relative") o.relative = std::stoi(lv) != 0;
+    else if (key == "maxiterations") o.maxIter = std::stoi(lv);
+    else if (key == "preconditioner") o.precon = lv;
+    else if (key == "smoothertype") o.smoother = lv;
+    else if (key == "chebyshevdegree") o.chebyDegree = std::stoi(lv);
+    else if (key == "mineigenvalueboundfactor") o.minEigFactor = std::stod(lv);
+    else if (key == "maxeigenvalueboundfactor") o.maxEigFactor = std::stod(lv);
+    else if (key == "pmgschedule") o.schedule = lv;
+    else if (key == "coarsesolver") o.coarse = lv;
+    else if (key == "coarsetol") o.coarseTol = std::stod(lv);
+    else if (key == "coarsemaxiterations") o.coarseMaxIter = std::stoi(lv);
+    else if (key == "mgprecision") o.mgPrecision = lv;
+    else if (key == "poisson") o.poisson = std::stoi(lv) != 0;
+    else if (key == "lambda0") o.lambda0 = std::stod(lv);
+    else if (key == "lambda1") o.lambda1 = std::stod(lv);
+    else if (key == "elementmap") o.trilinear = (lv == "trilinear");
+    else if (key == "seed") o.seed = std::stoull(lv);
+  }
+  return o;
+}
+
+// ---------------------------------------------------------------------------
+// Level construction (mesh data for one polynomial order)
+// ---------------------------------------------------------------------------
+void build_level(Level &L, int N, long long E, const double *VX, const long long *EToV, const int *EToB)
+{
+  L.N = N;
+  L.Nq = N + 1;
+  L.Np = L.Nq * L.Nq * L.Nq;
+  L.E = E;
+  L.Nlocal = E * L.Np;
+  L.z.resize(L.Nq);
+  L.w.resize(L.Nq);
+  gll(N, L.z.data(), L.w.data());
+  L.D.resize(L.Nq * L.Nq);
+  dmatrix(N, L.z.data(), L.D.data());
+  L.x.resize(L.Nlocal);
+  L.y.resize(L.Nlocal);
+  L.zc.resize(L.Nlocal);
+  trilinear_coords(N, E, VX, L.z.data(), L.x.data(), L.y.data(), L.zc.data());
+  L.ggeo.resize((size_t)7 * L.Nlocal);
+  geometric_factors(N, E, L.D.data(), L.w.data(), L.x.data(), L.y.data(), L.zc.data(), L.ggeo.data(), nullptr);
+  L.ids.resize(L.Nlocal);
+  global_ids(N, E, EToV, L.ids.data());
+  // unmasked handle (mesh->ogs) for the BC min-reduction, then the masked one
+  std::vector<int> off, gid;
+  std::vector<double> invd;
+  ogs_setup(L.Nlocal, L.ids.data(), off, gid, invd);
+  dirichlet_mask(N, E, EToB, off, gid, L.maskIds);
+  L.maskedIds = L.ids;
+  for (int m : L.maskIds) L.maskedIds[m] = 0;
+  ogs_setup(L.Nlocal, L.maskedIds.data(), L.gsOff, L.gsIds, L.invDegree);
+  L.volume = 0;
+  for (long long e = 0; e < E; ++e)
+    for (int n = 0; n < L.Np; ++n) L.volume += L.ggeo[(size_t)e * 7 * L.Np + 6 * L.Np + n];
+  L.VX.assign(VX, VX + E * 24);
+  L.EToB.assign(EToB, EToB + E * 6);
+  L.EToV.assign(EToV, EToV + E * 8);
+}
+
+// ---------------------------------------------------------------------------
+// Ax, stored geometric factors.  Same operation order as the serial kernel
+// ellipticPartialAxCoeffHex3D.c:27-96 (qr,qs,qt by DT; G*grad*lambda0; D^T).
+// ---------------------------------------------------------------------------
+template <typename T>
+void ax_stored(const Level &L, const T *ggeo, const T *D, T lambda0, T lambda1, bool poisson, const T *q, T *Aq)
+{
+  const int nq = L.Nq, np = L.Np;
+#pragma omp parallel for
+  for (long long e = 0; e < L.E; ++e) {
+    std::vector<T> Gr(np), Gs(np), Gt(np);
+    const T *qe = q + e * np;
+    const T *g = ggeo + (size_t)e * 7 * np;
+    for (int k = 0; k < nq; ++k)
+      for (int j = 0; j < nq; ++j)
+        for (int i = 0; i < nq; ++i) {
+          const int n = i + nq * (j + nq * k);
+          T qr = 0, qs = 0, qt = 0;
+          for (int m = 0; m < nq; ++m) {
+            qr += D[i * nq + m] * qe[m + nq * (j + nq * k)];
+            qs += D[j * nq + m] * qe[i + nq * (m + nq * k)];
+            qt += D[k * nq + m] * qe[i + nq * (j + nq * m)];
+          }
+          const T G00 = g[0 * np + n], G01 = g[1 * np + n], G11 = g[2 * np + n];
+          const T G12 = g[3 * np + n], G02 = g[4 * np + n], G22 = g[5 * np + n];
+          T a = G00 * qr; a += G01 * qs; a += G02 * qt;
+          T b = G01 * qr; b += G11 * qs; b += G12 * qt;
+          T c = G02 * qr; c += G12 * qs; c += G22 * qt;
+          Gr[n] = lambda0 * a;
+          Gs[n] = lambda0 * b;
+          Gt[n] = lambda0 * c;
+        }
+    for (int k = 0; k < nq; ++k)
+      for (int j = 0; j < nq; ++j)
+        for (int i = 0; i < nq; ++i) {
+          const int n = i + nq * (j + nq * k);
+          T r0 = 0;
+          if (!poisson) r0 = g[6 * np + n] * lambda1 * qe[n];
+          T ar = 0, as = 0, at = 0;
+          for (int m = 0; m < nq; ++m) {
+            ar += D[m * nq + i] * Gr[m + nq * (j + nq * k)];
+            as += D[m * nq + j] * Gs[i + nq * (m + nq * k)];
+            at += D[m * nq + k] * Gt[i + nq * (j + nq * m)];
+          }
+          Aq[e * np + n] = ar + as + at + r0;
+        }
+  }
+}
+
+// Ax with geometric factors rebuilt from the 8 trilinear vertices
+// (ellipticPartialAxTrilinearHex3D.okl:50-120).  Vertex input is in
+// hypercube order; lambda0 scales all three fluxes (the reference applies it
+// to the t-flux only, which is identical for the constant lambda0 = 1 case).
+void ax_trilinear(const Level &L, double lambda0, double lambda1, bool poisson, const double *q, double *Aq)
+{
+  const int nq = L.Nq, np = L.Np;
+  const double *D = L.D.data();
+#pragma omp parallel for
+  for (long long e = 0; e < L.E; ++e) {
+    std::vector<double> Gr(np), Gs(np), Gt(np), G6(np);
+    // CCW vertex order used by the reference kernel: 0:(-,-,-) 1:(+,-,-) 2:(+,+,-) 3:(-,+,-), 4..7 at t=+1
+    static const int ccw[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+    double xe[8], ye[8], ze[8];
+    for (int v = 0; v < 8; ++v) {
+      xe[v] = L.VX[(e * 8 + ccw[v]) * 3 + 0];
+      ye[v] = L.VX[(e * 8 + ccw[v]) * 3 + 1];
+      ze[v] = L.VX[(e * 8 + ccw[v]) * 3 + 2];
+    }
+    const double *qe = q + e * np;
+    for (int k = 0; k < nq; ++k)
+      for (int j = 0; j < nq; ++j)
+        for (int i = 0; i < nq; ++i) {
+          const double rn = L.z[i], sn = L.z[j], tn = L.z[k];
+          auto dr = [&](const double *X) {
+            return 0.125 * ((1 - tn) * (1 - sn) * (X[1] - X[0]) + (1 - tn) * (1 + sn) * (X[2] - X[3]) +
+                            (1 + tn) * (1 - sn) * (X[5] - X[4]) + (1 + tn) * (1 + sn) * (X[6] - X[7]));
+          };
+          auto ds = [&](const double *X) {
+            return 0.125 * ((1 - tn) * (1 - rn) * (X[3] - X[0]) + (1 - tn) * (1 + rn) * (X[2] - X[1]) +
+                            (1 + tn) * (1 - rn) * (X[7] - X[4]) + (1 + tn) * (1 + rn) * (X[6] - X[5]));
+          };
+          auto dt = [&](const double *X) {
+            return 0.125 * ((1 - rn) * (1 - sn) * (X[4] - X[0]) + (1 + rn) * (1 - sn) * (X[5] - X[1]) +
+                            (1 + rn) * (1 + sn) * (X[6] - X[2]) + (1 - rn) * (1 + sn) * (X[7] - X[3]));
+          };
+          const double xr = dr(xe), xs = ds(xe), xt = dt(xe);
+          const double yr = dr(ye), ys = ds(ye), yt = dt(ye);
+          const double zr = dr(ze), zs = ds(ze), zt = dt(ze);
+          const double J = xr * (ys * zt - zs * yt) - yr * (xs * zt - zs * xt) + zr * (xs * yt - ys * xt);
+          const double rx = (ys * zt - zs * yt), ry = -(xs * zt - zs * xt), rz = (xs * yt - ys * xt);
+          const double sx = -(yr * zt - zr * yt), sy = (xr * zt - zr * xt), sz = -(xr * yt - yr * xt);
+          const double tx = (yr * zs - zr * ys), ty = -(xr * zs - zr * xs), tz = (xr * ys - yr * xs);
+          const double W = L.w[i] * L.w[j] * L.w[k];
+          const double sc = W / J;
+          const double G00 = sc * (rx * rx + ry * ry + rz * rz), G01 = sc * (rx * sx + ry * sy + rz * sz);
+          const double G02 = sc * (rx * tx + ry * ty + rz * tz), G11 = sc * (sx * sx + sy * sy + sz * sz);
+          const double G12 = sc * (sx * tx + sy * ty + sz * tz), G22 = sc * (tx * tx + ty * ty + tz * tz);
+          double qr = 0, qs = 0, qt = 0;
+          for (int m = 0; m < nq; ++m) {
+            qr += D[i * nq + m] * qe[m + nq * (j + nq * k)];
+            qs += D[j * nq + m] * qe[i + nq * (m + nq * k)];
+            qt += D[k * nq + m] * qe[i + nq * (j + nq * m)];
+          }
+          const int n = i + nq * (j + nq * k);
+          Gr[n] = lambda0 * (G00 * qr + G01 * qs + G02 * qt);
+          Gs[n] = lambda0 * (G01 * qr + G11 * qs + G12 * qt);
+          Gt[n] = lambda0 * (G02 * qr + G12 * qs + G22 * qt);
+          G6[n] = poisson ? 0.0 : W * J * lambda1 * qe[n];
+        }
+    for (int k = 0; k < nq; ++k)
+      for (int j = 0; j < nq; ++j)
+        for (int i = 0; i < nq; ++i) {
+          const int n = i + nq * (j + nq * k);
+          double ar = 0, as = 0, at = 0;
+          for (int m = 0; m < nq; ++m) {
+            ar += D[m * nq + i] * Gr[m + nq * (j + nq * k)];
+            as += D[m * nq + j] * Gs[i + nq * (m + nq * k)];
+            at += D[m * nq + k] * Gt[i + nq * (j + nq * m)];
+          }
+          Aq[e * np + n] = ar + as + at + G6[n];
+        }
+  }
+}
+
+// diag(A_L) per element (ellipticBlockBuildDiagonalHex3D.okl:61-107), single field.
+template <typename T>
+void build_diag(const Level &L, const T *ggeo, const T *D, T lambda0, T lambda1, bool poisson, T *diag)
+{
+  const int nq = L.Nq, np = L.Np;
+#pragma omp parallel for
+  for (long long e = 0; e < L.E; ++e) {
+    const T *g = ggeo + (size_t)e * 7 * np;
+    for (int k = 0; k < nq; ++k)
+      for (int j = 0; j < nq; ++j)
+        for (int i = 0; i < nq; ++i) {
+          const int n = i + nq * (j + nq * k);
+          T r = 0;
+          const T grs = g[1 * np + n], grt = g[4 * np + n], gst = g[3 * np + n];
+          r += (T)2.0 * grs * lambda0 * D[i * nq + i] * D[j * nq + j];
+          r += (T)2.0 * grt * lambda0 * D[i * nq + i] * D[k * nq + k];
+          r += (T)2.0 * gst * lambda0 * D[j * nq + j] * D[k * nq + k];
+          for (int m = 0; m < nq; ++m) {
+            r += g[0 * np + m + nq * (j + nq * k)] * lambda0 * D[m * nq + i] * D[m * nq + i];
+            r += g[2 * np + i + nq * (m + nq * k)] * lambda0 * D[m * nq + j] * D[m * nq + j];
+            r += g[5 * np + i + nq * (j + nq * m)] * lambda0 * D[m * nq + k] * D[m * nq + k];
+          }
+          if (!poisson) r += g[6 * np + n] * lambda1;
+          diag[e * np + n] = r;
+        }
+  }
+}
+
+template <typename T> void gs_add(const Level &L, T *q)
+{
+  const long long ng = (long long)L.gsOff.size() - 1;
+#pragma omp parallel for
+  for (long long g = 0; g < ng; ++g) {
+    const int s = L.gsOff[g], t = L.gsOff[g + 1];
+    if (s + 1 == t) continue;
+    T v = 0;
+    for (int m = s; m < t; ++m) v += q[L.gsIds[m]];
+    for (int m = s; m < t; ++m) q[L.gsIds[m]] = v;
+  }
+}
+
+template <typename T> void apply_mask(const Level &L, T *q)
+{
+  for (int m : L.maskIds) q[m] = 0;
+}
+
+template <typename T> T wdot(long long n, const T *w, const T *a, const T *b)
+{
+  double s = 0;
+#pragma omp parallel for reduction(+ : s)
+  for (long long i = 0; i < n; ++i) s += (double)w[i] * (double)a[i] * (double)b[i];
+  return (T)s;
+}
+
+// explicit instantiations used by the MG code
+template void ax_stored<double>(const Level &, const double *, const double *, double, double, bool, const double *, double *);
+template void ax_stored<float>(const Level &, const float *, const float *, float, float, bool, const float *, float *);
+template void build_diag<double>(const Level &, const double *, const double *, double, double, bool, double *);
+template void build_diag<float>(const Level &, const float *, const float *, float, float, bool, float *);
+template void gs_add<double>(const Level &, double *);
+template void gs_add<float>(const Level &, float *);
+template void apply_mask<double>(const Level &, double *);
+template void apply_mask<float>(const Level &, float *);
+template double wdot<double>(long long, const double *, const double *, const double *);
+template float wdot<float>(long long, const float *, const float *, const float *);
+
+// ---------------------------------------------------------------------------
+// Elliptic solver state
+// ---------------------------------------------------------------------------
+void Elliptic::setup(int N, long long E, const double *VX, const long long *EToV, const int *EToB, const std::string &opt)
+{
+  o = parse_options(opt);
+  build_level(fine, N, E, VX, EToV, EToB);
+  if (o.precon == "jacobi") {
+    invDiag.resize(fine.Nlocal);
+    build_diag<double>(fine, fine.ggeo.data(), fine.D.data(), o.lambda0, o.lambda1, o.poisson, invDiag.data());
+    gs_add(fine, invDiag.data());
+    for (auto &v : invDiag) v = 1.0 / v;
+  } else if (o.precon == "multigrid") {
+    mg_setup(*this);
+  }
+}
+
+void Elliptic::ax(const double *q, double *Aq) const
+{
+  if (o.trilinear)
+    ax_trilinear(fine, o.lambda0, o.lambda1, o.poisson, q, Aq);
+  else
+    ax_stored<double>(fine, fine.ggeo.data(), fine.D.data(), o.lambda0, o.lambda1, o.poisson, q, Aq);
+}
+
+void Elliptic::op(const double *q, double *Aq) const
+{
+  ax(q, Aq);
+  apply_mask(fine, Aq);
+  gs_add(fine, Aq);
+}
+
+void Elliptic::precond(const double *r, double *z)
+{
+  const long long n = fine.Nlocal;
+  if (o.precon == "jacobi") {
+    for (long long i = 0; i < n; ++i) z[i] = r[i] * invDiag[i];
+  } else if (o.precon == "multigrid") {
+    mg_apply(*this, r, z);
+  } else {
+    std::memcpy(z, r, sizeof(double) * n);
+  }
+}
+
+double Elliptic::norm(const double *r) const
+{
+  return std::sqrt(wdot<double>(fine.Nlocal, fine.invDegree.data(), r, r) / fine.volume);
+}
+
+// PCG / flexible PCG (PCG.cpp:86-203)
+int Elliptic::pcg(double *r, double *x, double tol, int maxit, double &rnorm)
+{
+  const long long n = fine.Nlocal;
+  const double *w = fine.invDegree.data();
+  const bool flexible = (o.solver == "pfcg");
+  std::vector<double> p(n, 0.0), z(n), Ap(n);
+  double rdotz1 = 0, alpha = 0;
+  int it = 0;
+  do {
+    ++it;
+    const double rdotz2 = rdotz1;
+    if (o.precon != "none") {
+      precond(r, z.data());
+      rdotz1 = wdot<double>(n, w, r, z.data());
+    } else {
+      std::memcpy(z.data(), r, sizeof(double) * n);
+      // (PCG.cpp:129 reuses the scaled residual norm here; the restatement
+      // uses (r,r)_w, which is what unpreconditioned CG needs)
+      rdotz1 = wdot<double>(n, w, r, r);
+    }
+    double beta = 0;
+    if (it > 1) {
+      beta = rdotz1 / rdotz2;
+      if (flexible) {
+        const double zdotAp = wdot<double>(n, w, z.data(), Ap.data());
+        beta = -alpha * zdotAp / rdotz2;
+      }
+    }
+    for (long long i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+    op(p.data(), Ap.data());
+    const double pAp = wdot<double>(n, w, p.data(), Ap.data());
+    alpha = rdotz1 / (pAp + 1e-300);
+    double rdotr = 0;
+    for (long long i = 0; i < n; ++i) {
+      r[i] -= alpha * Ap[i];
+      rdotr += r[i] * r[i] * w[i];
+    }
+    for (long long i = 0; i < n; ++i) x[i] += alpha * p[i];
+    rnorm = std::sqrt(rdotr / fine.volume);
+    history.push_back(rnorm);
+    if (std::isnan(rnorm)) { status = 3; break; }
+  } while (rnorm > tol && it < maxit);
+  return it;
+}
+
+// ellipticSolve (ellipticSolve.cpp:32-190), x0 taken from x on input.
+int Elliptic::solve(double *r, double *x, double &res0, double &res)
+{
+  const long long n = fine.Nlocal;
+  std::vector<double> Ax0(n), x0(x, x + n);
+  ax(x, Ax0.data());
+  for (long long i = 0; i < n; ++i) r[i] = -Ax0[i] + r[i];
+  apply_mask(fine, r);
+  gs_add(fine, r);
+  for (long long i = 0; i < n; ++i) x[i] = 0;
+  res0 = norm(r);
+  double tol = o.tol;
+  if (o.relative) tol *= res0;
+  res = res0;
+  history.clear();
+  status = 0;
+  int iters = 0;
+  if (o.solver == "pcg" || o.solver == "pfcg")
+    iters = pcg(r, x, tol, o.maxIter, res);
+  else
+    iters = pgmres(r, x, tol, o.maxIter, res);
+  for (long long i = 0; i < n; ++i) x[i] += x0[i];
+  if (std::isnan(res)) status = 3;
+  else if (iters >= o.maxIter && res > tol) status = 1;
+  return iters;
+}
+
+// Restarted (flexible) GMRES restated from PGMRES.cpp:111-340 and the
+// gmresUpdate helper (PGMRES.cpp:70-107): classical Gram-Schmidt through one
+// weighted multi-dot per step, Givens rotations on the host, right
+// preconditioning (flexible keeps every Z_i), true residual at each restart.
+int Elliptic::pgmres(double *r, double *x, double tol, int maxit, double &rdotr)
+{
+  const long long n = fine.Nlocal;
+  const double *wt = fine.invDegree.data();
+  const int nr = o.nVector;
+  const bool flexible = (o.solver == "pfgmres");
+  const int ld = nr + 1;
+  std::vector<std::vector<double>> V(nr, std::vector<double>(n)), Z(flexible ? nr : 1, std::vector<double>(n));
+  std::vector<double> H(ld * ld, 0.0), sn(nr), cs(nr), s(nr + 1), y(nr);
+  std::vector<double> w(n), b(r, r + n), Ax(n), ztmp(n), tmp(n);
+  const double sqrtFac = std::sqrt(1.0 / fine.volume);
+  double nrm = rdotr / sqrtFac;
+  double error = rdotr;
+  auto update = [&](int m) {
+    for (int k = m - 1; k >= 0; --k) {
+      y[k] = s[k];
+      for (int j = k + 1; j < m; ++j) y[k] -= H[k + j * ld] * y[j];
+      y[k] /= H[k + k * ld];
+    }
+    if (flexible) {
+      for (long long q = 0; q < n; ++q) {
+        double v = x[q];
+        for (int k = 0; k < m; ++k) v += y[k] * Z[k][q];
+        x[q] = v;
+      }
+    } else {
+      for (long long q = 0; q < n; ++q) {
+        double v = 0;
+        for (int k = 0; k < m; ++k) v += y[k] * V[k][q];
+        ztmp[q] = v;
+      }
+      precond(ztmp.data(), tmp.data());
+      for (long long q = 0; q < n; ++q) x[q] = tmp[q] + x[q];
+    }
+  };
+  int iter = 0;
+  for (iter = 0; iter < maxit;) {
+    s[0] = nrm;
+    for (long long q = 0; q < n; ++q) V[0][q] = r[q] / nrm;
+    for (int i = 0; i < nr; ++i) {
+      std::vector<double> &Mv = flexible ? Z[i] : Z[0];
+      precond(V[i].data(), Mv.data());
+      op(Mv.data(), w.data());
+      for (int k = 0; k <= i; ++k) y[k] = wdot<double>(n, wt, V[k].data(), w.data());
+      double nw2 = 0;
+      for (long long q = 0; q < n; ++q) {
+        double v = w[q];
+        for (int k = 0; k <= i; ++k) v -= y[k] * V[k][q];
+        w[q] = v;
+        nw2 += wt[q] * v * v;
+      }
+      const double nw = std::sqrt(nw2);
+      H[i + 1 + i * ld] = nw;
+      if (i < nr - 1)
+        for (long long q = 0; q < n; ++q) V[i + 1][q] = w[q] / nw;
+      for (int k = 0; k <= i; ++k) H[k + i * ld] = y[k];
+      for (int k = 0; k < i; ++k) {
+        const double h1 = H[k + i * ld], h2 = H[k + 1 + i * ld];
+        H[k + i * ld] = cs[k] * h1 + sn[k] * h2;
+        H[k + 1 + i * ld] = -sn[k] * h1 + cs[k] * h2;
+      }
+      const double h1 = H[i + i * ld], h2 = H[i + 1 + i * ld];
+      const double hr = std::sqrt(h1 * h1 + h2 * h2);
+      cs[i] = h1 / hr;
+      sn[i] = h2 / hr;
+      H[i + i * ld] = cs[i] * h1 + sn[i] * h2;
+      H[i + 1 + i * ld] = 0;
+      s[i + 1] = -sn[i] * s[i];
+      s[i] = cs[i] * s[i];
+      ++iter;
+      error = std::fabs(s[i + 1]) * sqrtFac;
+      rdotr = error;
+      history.push_back(error);
+      if (std::isnan(error)) { status = 3; return iter; }
+      if (error < tol || iter == maxit) {
+        update(i + 1);
+        break;
+      }
+    }
+    if (error < tol || iter == maxit) break;
+    update(nr);
+    op(x, Ax.data());
+    double nr2 = 0;
+    for (long long q = 0; q < n; ++q) {
+      r[q] = b[q] - Ax[q];
+      nr2 += wt[q] * r[q] * r[q];
+    }
+    nrm = std::sqrt(nr2);
+    error = nrm * sqrtFac;
+    rdotr = error;
+    if (error <= tol) return iter;
+  }
+  return iter;
+}
+
+} // namespace orc

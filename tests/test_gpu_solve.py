@@ -1,0 +1,128 @@
+"""End-to-end solve parity: the GPU ellipticSolve against the CPU oracle on the
+same Kershaw boxes and seeded right-hand sides.  Bar (FP64 plain form):
+identical iteration counts and solutions within 1e-10 relative."""
+import numpy as np
+import pytest
+
+import nekrs_gb300 as G
+from nekrs_gb300 import workloads as W
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def run_pair(torch, N, n, opts, eps=0.3, seed=11, x0=None):
+    VX, EToV, EToB = W.kershaw_box(n, eps=eps)
+    orc = O.Elliptic(N, VX, EToV, EToB, opts)
+    rhs = W.box_rhs(N, n, n, n, seed, orc.get("ggeo"))
+    xo, io = orc.solve(rhs, x0)
+    el = G.Elliptic(N, VX, EToV, EToB, opts)
+    r = torch.from_numpy(rhs.copy()).cuda()
+    x = torch.zeros_like(r) if x0 is None else torch.from_numpy(x0.copy()).cuda()
+    ig = el.solve(r, x)
+    torch.cuda.synchronize()
+    return xo, io, x.cpu().numpy(), ig, el, orc
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("N,n", [(1, 4), (3, 3), (5, 3), (7, 3), (9, 2)])
+def test_jacobi_pcg_parity(product_lib, oracle_mod, torch_cuda, N, n):
+    opts = "preconditioner=jacobi;solver=pcg;residualTol=1e-8+relative;maxIterations=3000"
+    xo, io, xg, ig, el, orc = run_pair(torch_cuda, N, n, opts)
+    assert ig["status"] == 0 and io["status"] == 0
+    assert ig["iterations"] == io["iterations"]
+    assert abs(ig["res0"] - io["res0"]) <= 1e-12 * io["res0"]
+    assert rel(xg, xo) < 1e-10
+    hist = el.get("history")
+    assert np.allclose(hist, io["history"], rtol=1e-6, atol=0)
+
+
+@pytest.mark.parametrize("solver", ["pfcg", "pgmres+nVector=10", "pfgmres"])
+def test_krylov_variants_parity(product_lib, oracle_mod, torch_cuda, solver):
+    opts = f"preconditioner=jacobi;solver={solver};residualTol=1e-8+relative;maxIterations=3000"
+    xo, io, xg, ig, el, orc = run_pair(torch_cuda, 4, 3, opts)
+    assert ig["status"] == 0
+    assert ig["iterations"] == io["iterations"]
+    assert rel(xg, xo) < 1e-10
+
+
+def test_nonzero_initial_guess_and_helmholtz(product_lib, oracle_mod, torch_cuda):
+    N, n = 4, 3
+    opts = "preconditioner=jacobi;solver=pcg;residualTol=1e-9+relative;poisson=0;lambda0=1.0;lambda1=2.5"
+    rng = np.random.default_rng(5)
+    x0 = rng.uniform(-1, 1, n ** 3 * (N + 1) ** 3)
+    xo, io, xg, ig, el, orc = run_pair(torch_cuda, N, n, opts, x0=x0)
+    assert ig["iterations"] == io["iterations"]
+    assert rel(xg, xo) < 1e-10
+
+
+def test_trilinear_operator_solve(product_lib, oracle_mod, torch_cuda):
+    opts = "preconditioner=jacobi;solver=pcg;residualTol=1e-8+relative;elementMap=trilinear"
+    xo, io, xg, ig, el, orc = run_pair(torch_cuda, 5, 3, opts, eps=1.0)
+    assert ig["iterations"] == io["iterations"]
+    assert rel(xg, xo) < 1e-10
+
+
+def test_operator_gs_mask_entry_points(product_lib, oracle_mod, torch_cuda):
+    torch = torch_cuda
+    N, n = 6, 3
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    opts = "preconditioner=jacobi"
+    orc = O.Elliptic(N, VX, EToV, EToB, opts)
+    el = G.Elliptic(N, VX, EToV, EToB, opts)
+    q = np.random.default_rng(2).uniform(-1, 1, orc.Nlocal)
+    qd = torch.from_numpy(q).cuda()
+    out = torch.zeros_like(qd)
+    el.operator(qd, out)
+    ref = orc.operator(q)
+    assert np.max(np.abs(out.cpu().numpy() - ref)) < 1e-13 * np.max(np.abs(ref))
+    for k in ("ids", "gsOff", "gsIds", "maskIds", "invDegree"):
+        assert np.array_equal(el.get(k), orc.get(k)), k
+    assert np.max(np.abs(el.get("ggeo") - orc.get("ggeo"))) < 1e-13 * np.max(np.abs(orc.get("ggeo")))
+    assert np.max(np.abs(el.get("invDiag") - orc.get("invDiag"))) < 1e-13 * np.max(np.abs(orc.get("invDiag")))
+
+
+def test_host_buffer_solve_matches_device_solve(product_lib, torch_cuda):
+    torch = torch_cuda
+    N, n = 5, 3
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    opts = "preconditioner=jacobi;residualTol=1e-8+relative"
+    el = G.Elliptic(N, VX, EToV, EToB, opts)
+    g = el.get("ggeo")
+    rhs = W.box_rhs(N, n, n, n, 3, g)
+    r1, x1 = rhs.copy(), np.zeros_like(rhs)
+    i1 = el.solve_host(r1, x1)
+    r2 = torch.from_numpy(rhs.copy()).cuda()
+    x2 = torch.zeros_like(r2)
+    i2 = el.solve(r2, x2)
+    assert i1["iterations"] == i2["iterations"]
+    assert np.array_equal(x1, x2.cpu().numpy())  # deterministic reductions
+
+
+def test_status_codes(product_lib, torch_cuda):
+    torch = torch_cuda
+    N, n = 3, 2
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    el = G.Elliptic(N, VX, EToV, EToB, "preconditioner=jacobi;maxIterations=3;residualTol=1e-12+relative")
+    rhs = W.box_rhs(N, n, n, n, 1, el.get("ggeo"))
+    r = torch.from_numpy(rhs).cuda()
+    x = torch.zeros_like(r)
+    info = el.solve(r, x)
+    assert info["status"] == 1 and info["iterations"] == 3  # MAXIT, not an abort
+    bad = rhs.copy()
+    bad[7] = np.nan
+    r = torch.from_numpy(bad).cuda()
+    with pytest.raises(G.NrsgError) as e:
+        el.solve(r, torch.zeros_like(r))
+    assert e.value.code == 3
+    # zero right-hand side: nothing to do
+    r = torch.zeros(el.Nlocal, dtype=torch.float64, device="cuda")
+    x = torch.zeros_like(r)
+    info = el.solve(r, x)
+    assert info["iterations"] == 0 and float(x.abs().max()) == 0.0
+    with pytest.raises(G.NrsgError) as e:
+        G.Elliptic(N, VX, EToV, EToB, "preconditioner=bogus")
+    assert e.value.code == 5

@@ -1,0 +1,110 @@
+"""CPU oracle checks: pinned against the reference's own serial kernels
+(oracle/_ref, when built here) and against the committed golden fixtures."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "ref_kernels.npz")
+
+
+def test_gll_and_derivative(oracle_mod):
+    for N in range(1, 10):
+        z, w = O.gll(N)
+        # exactness of GLL quadrature for degree 2N-1
+        for p in range(2 * N):
+            exact = (1 - (-1) ** (p + 1)) / (p + 1)
+            assert abs(np.dot(w, z ** p) - exact) < 1e-13
+        D = O.dmatrix(N)
+        for p in range(N + 1):
+            assert np.allclose(D @ z ** p, p * z ** max(p - 1, 0) if p else 0 * z, atol=1e-12)
+
+
+def test_interp_reproduces_polynomials(oracle_mod):
+    for (Nf, Nc) in [(7, 3), (3, 1), (9, 5), (5, 3)]:
+        Im = O.interp(Nc, Nf)  # coarse -> fine
+        zc, _ = O.gll(Nc)
+        zf, _ = O.gll(Nf)
+        for p in range(Nc + 1):
+            assert np.allclose(Im @ zc ** p, zf ** p, atol=1e-13)
+
+
+@pytest.mark.parametrize("N,n", [(1, 3), (2, 3), (4, 2), (7, 2), (9, 2)])
+def test_global_ids_match_coordinates(oracle_mod, N, n):
+    VX, EToV, EToB = O.box_mesh(n, n, n, 0.3)
+    el = O.Elliptic(N, VX, EToV, EToB, "preconditioner=jacobi")
+    ids = el.get("ids")
+    x, y, z = el.get("x"), el.get("y"), el.get("z")
+    key = np.round(np.stack([x, y, z], 1) * 1e9).astype(np.int64)
+    nz = ids != 0
+    # same id <=> same physical node; interiors (id 0) are exactly the element interiors
+    _, inv_p = np.unique(key[nz], axis=0, return_inverse=True)
+    _, inv_i = np.unique(ids[nz], return_inverse=True)
+    assert np.array_equal(inv_p.ravel(), inv_i.ravel()[np.argsort(np.argsort(inv_i.ravel()))]) or \
+        len(np.unique(np.stack([inv_p.ravel(), inv_i.ravel()], 1), axis=0)) == len(np.unique(inv_i))
+    assert (ids == 0).sum() == n ** 3 * max(N - 1, 0) ** 3
+    # unique non-interior nodes of the box lattice
+    L = n * N + 1
+    assert ids.max() == L ** 3 - n ** 3 * max(N - 1, 0) ** 3
+
+
+def test_gather_sanity(oracle_mod):
+    # ogs sum test of meshParallelGatherScatterSetup.cpp:136-165 on the unmasked maps
+    VX, EToV, EToB = O.box_mesh(3, 2, 2, 0.3)
+    N = 5
+    el = O.Elliptic(N, VX, EToV, np.zeros_like(EToB), "preconditioner=jacobi")
+    one = np.ones(el.Nlocal)
+    s = el.gs(one) * el.get("invDegree")
+    assert abs(s.sum() - el.Nlocal) / el.Nlocal < 1e-15
+
+
+def test_oracle_ax_matches_golden(oracle_mod):
+    g = np.load(GOLD)
+    for N in (3, 7):
+        VX = g[f"N{N}_VX"]
+        E = VX.shape[0]
+        n = E
+        _, EToV, EToB = O.box_mesh(n, 1, 1, 0.3)
+        el = O.Elliptic(N, VX, EToV, EToB, "preconditioner=jacobi")
+        assert np.allclose(el.get("ggeo"), g[f"N{N}_ggeo"], rtol=1e-13, atol=1e-13)
+        q = g[f"N{N}_q"]
+        ref = g[f"N{N}_Aq_poisson"]
+        assert np.max(np.abs(el.ax(q) - ref)) <= 1e-13 * np.max(np.abs(ref))
+        el2 = O.Elliptic(N, VX, EToV, EToB, "preconditioner=jacobi;poisson=0;lambda0=1.3;lambda1=0.7")
+        refh = g[f"N{N}_Aq_helmholtz"]
+        assert np.max(np.abs(el2.ax(q) - refh)) <= 1e-13 * np.max(np.abs(refh))
+        ref32 = g[f"N{N}_Aq_poisson_f32"]
+        assert np.max(np.abs(el.ax_fp32(q) - ref32)) <= 1e-6 * np.max(np.abs(ref32))
+
+
+@pytest.mark.skipif(O.ref_lib() is None, reason="reference kernels (oracle/_ref) not built on this host")
+@pytest.mark.parametrize("N", [1, 2, 3, 5, 7, 9])
+def test_oracle_ax_bitexact_vs_reference(oracle_mod, N):
+    import ctypes
+
+    from tests.golden.make_golden import ref_ax
+
+    VX, EToV, EToB = O.box_mesh(2, 2, 1, 0.5)
+    el = O.Elliptic(N, VX, EToV, EToB, "preconditioner=jacobi")
+    rng = np.random.default_rng(N)
+    q = rng.uniform(-1, 1, el.Nlocal)
+    ref = ref_ax(O.ref_lib(), N, el.E, el.get("ggeo"), el.get("D"), q, True)
+    assert np.array_equal(el.ax(q), ref)
+
+
+@pytest.mark.parametrize("solver", ["pcg", "pfcg", "pgmres", "pfgmres"])
+def test_oracle_krylov_converges(oracle_mod, solver):
+    VX, EToV, EToB = O.box_mesh(3, 3, 3, 0.3)
+    N = 4
+    el = O.Elliptic(N, VX, EToV, EToB, f"preconditioner=jacobi;solver={solver};residualTol=1e-8+relative;maxIterations=2000")
+    rhs = O.box_rhs(N, 3, 3, 3, 7, el.get("ggeo"))
+    x, info = el.solve(rhs)
+    assert info["status"] == 0
+    assert info["res"] <= 1e-8 * info["res0"]
+    # true residual of the assembled system
+    b = el.gs(el.mask(rhs))
+    r = b - el.operator(x)
+    w = el.get("invDegree")
+    assert np.sqrt((w * r * r).sum() / el.volume) <= 2e-8 * info["res0"]
