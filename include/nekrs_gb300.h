@@ -103,8 +103,15 @@ int nrsg_elliptic_precondition(nrsg_elliptic *el, const double *d_r, double *d_z
 /* Setup data for parity checks, copied to host.  Names: "ids", "maskedIds"
  * (int64), "gsOff", "gsIds", "maskIds" (int32), "invDegree", "ggeo",
  * "invDiag", "x", "y", "z", "D" (float64), "history" (float64, last solve),
- * "mg.levels" (int32).  With h_out == NULL only *count is set. */
+ * "mg.levels", "mg.rho", "mg.degrees", "mg.coarseIters" (float64).  With h_out == NULL only *count is set. */
 int nrsg_elliptic_get(nrsg_elliptic *el, const char *name, void *h_out, long long *count);
+
+/* Schwarz smoother of pMG level `level` (pMGLevel::smoothSchwarz,
+ * ellipticMultiGridSchwarz.cpp:1056-1156) applied once: Su = S u, FP64 in
+ * and out (computed in the multigrid precision).  For parity checks. */
+int nrsg_elliptic_mg_smoother(nrsg_elliptic *el, int level, const double *d_u, double *d_Su);
+/* Number of E-vector nodes of pMG level `level` (-1 on error). */
+long long nrsg_elliptic_mg_level_size(nrsg_elliptic *el, int level);
 
 /* Host-only setup (no device needed): Nek5000 global numbering (setvert3d,
  * 3rd_party/nek5000/core/navier8.f:2004-2350), the Dirichlet mask

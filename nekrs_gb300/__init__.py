@@ -67,6 +67,9 @@ def lib():
         L.nrsg_elliptic_gs.argtypes = [vp, vp]
         L.nrsg_elliptic_mask.argtypes = [vp, vp]
         L.nrsg_elliptic_get.argtypes = [vp, ctypes.c_char_p, vp, ctypes.POINTER(LL)]
+        L.nrsg_elliptic_mg_smoother.argtypes = [vp, ctypes.c_int, vp, vp]
+        L.nrsg_elliptic_mg_level_size.restype = LL
+        L.nrsg_elliptic_mg_level_size.argtypes = [vp, ctypes.c_int]
         d, f, i = ctypes.c_double, ctypes.c_float, ctypes.c_int
         L.nrsg_ax_stored_f64.argtypes = [i, LL, vp, vp, d, d, i, vp, vp, vp]
         L.nrsg_ax_stored_f32.argtypes = [i, LL, vp, vp, f, f, i, vp, vp, vp]
@@ -98,8 +101,7 @@ def check(code):
     return code
 
 
-_DTYPES = {"ids": np.int64, "maskedIds": np.int64, "gsOff": np.int32, "gsIds": np.int32, "maskIds": np.int32,
-           "mg.levels": np.float64}
+_DTYPES = {"ids": np.int64, "maskedIds": np.int64, "gsOff": np.int32, "gsIds": np.int32, "maskIds": np.int32}
 
 
 class Elliptic:
@@ -177,6 +179,12 @@ class Elliptic:
 
     def precondition(self, r, z):
         check(lib().nrsg_elliptic_precondition(self.h, _ptr(r), _ptr(z)))
+
+    def mg_smoother(self, level, u, Su):
+        check(lib().nrsg_elliptic_mg_smoother(self.h, level, _ptr(u), _ptr(Su)))
+
+    def mg_level_size(self, level):
+        return lib().nrsg_elliptic_mg_level_size(self.h, level)
 
     def get(self, name):
         n = LL(0)

@@ -54,9 +54,8 @@ void FieldLevel::build(int N_, long long E_, const double *VX, const long long *
   }
   // numbering, gather maps, mask
   nek_global_ids(N, E, EToV, ids);
-  GatherMap unmasked;
-  build_gather(ids, unmasked);
-  dirichlet_nodes(N, E, EToB, unmasked, maskIds);
+  build_gather(ids, um);
+  dirichlet_nodes(N, E, EToB, um, maskIds);
   maskedIds = ids;
   for (int m : maskIds) maskedIds[m] = 0;
   build_gather(maskedIds, gm);
@@ -66,8 +65,6 @@ void FieldLevel::build(int N_, long long E_, const double *VX, const long long *
   d_invDegree64.upload(gm.invDegree);
   ngroups = (long long)gm.devOff.size() - 1;
   // volume = sum of JW over the E-vector (meshSetup.cpp:444)
-  DevBuf<double> tmp(1);
-  // reuse wdot with w = null on the GWJ slices would need a strided view; sum on host
   std::vector<double> gg = d_ggeo64.download();
   volume = 0;
   for (long long e = 0; e < E; ++e)
@@ -442,6 +439,22 @@ int nrsg_elliptic_get(nrsg_elliptic *el, const char *name, void *h_out, long lon
     } else
       throw Error(NRSG_ERR_INVALID, "unknown array '" + s + "'");
   })
+}
+
+int nrsg_elliptic_mg_smoother(nrsg_elliptic *el, int level, const double *d_u, double *d_Su)
+{
+  if (!el || !d_u || !d_Su) return NRSG_ERR_INVALID;
+  NRSG_TRY(el->impl->mg_schwarz(level, d_u, d_Su))
+}
+long long nrsg_elliptic_mg_level_size(nrsg_elliptic *el, int level)
+{
+  if (!el) return -1;
+  try {
+    return el->impl->mg_level_size(level);
+  } catch (const std::exception &e) {
+    nrsg::set_last_error(e.what());
+    return -1;
+  }
 }
 
 // ---- host-only setup (no device needed) -----------------------------------

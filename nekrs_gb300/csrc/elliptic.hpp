@@ -15,7 +15,8 @@ struct FieldLevel {
   long long E = 0, Nlocal = 0;
   std::vector<double> z, w, Dh;
   std::vector<long long> ids, maskedIds;
-  GatherMap gm;
+  GatherMap gm;  // masked (the solver's gather-scatter)
+  GatherMap um;  // unmasked (mesh->ogs)
   std::vector<int> maskIds;
   std::vector<double> VXh;
   std::vector<int> EToBh;
@@ -78,6 +79,8 @@ struct Elliptic {
   void mg_apply(const double *r, double *z);
   void mg_release();
   std::vector<double> mg_get(const std::string &name);
+  long long mg_level_size(int level);
+  void mg_schwarz(int level, const double *u, double *Su);
 };
 
 // GMRES kernels (kernels_vec.cu)

@@ -1,0 +1,419 @@
+// p-multigrid kernels (sm_103a): restriction / prolongation, Chebyshev
+// updates, the fused FDM (Schwarz) local solve with direct neighbour-halo
+// gather, the ASM overlap combine, and templated Jacobi-PCG kernels for the
+// coarse level.
+//
+// Reference kernels (nekRS tree):
+//   ellipticPreconCoarsenHex3D / ellipticPreconProlongateHex3D (kernels/elliptic/*.okl, *.c)
+//   updateChebyshev.okl, updateFourthKindChebyshev.okl
+//   preFDM / fusedFDM / postFDM (kernels/elliptic/*.okl, *.c)
+//
+// FDM on GB300: the reference scatters every element into an (N+3)^3
+// extended array in HBM, gather-scatters the extended arrays to exchange
+// the one-node overlap, solves, and (ASM) gather-scatters the extended result
+// again.  Here one CTA per element builds the extended tile in shared memory
+// straight from the element's own nodes plus a precomputed neighbour-halo map
+// (src index of the neighbour node each halo point stands for), runs the six
+// tensor contractions in shared memory, and writes only the element's own
+// nodes (RAS) or its own nodes plus the 6 N_q^2 halo results (ASM).  The
+// extended arrays never touch HBM.
+
+#include "mg_kernels.hpp"
+
+namespace nrsg {
+
+namespace {
+constexpr int kT = 256;
+inline unsigned grid_for(long long n)
+{
+  long long b = (n + kT - 1) / kT;
+  if (b < 1) b = 1;
+  const long long cap = 152LL * 16;
+  return (unsigned)(b < cap ? b : cap);
+}
+#define MG_LOOP(i, n)                                                                                      \
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (n); i += (long long)gridDim.x * blockDim.x)
+} // namespace
+
+#define NRSG_DISPATCH_NQ_MG(N, MACRO)                                                                      \
+  switch (N) {                                                                                             \
+  case 1: MACRO(2); break;                                                                                 \
+  case 2: MACRO(3); break;                                                                                 \
+  case 3: MACRO(4); break;                                                                                 \
+  case 4: MACRO(5); break;                                                                                 \
+  case 5: MACRO(6); break;                                                                                 \
+  case 6: MACRO(7); break;                                                                                 \
+  case 7: MACRO(8); break;                                                                                 \
+  case 8: MACRO(9); break;                                                                                 \
+  case 9: MACRO(10); break;                                                                                \
+  default: throw Error(NRSG_ERR_BAD_CONFIG, "polynomial order must be 1..9");                              \
+  }
+
+// ---------------------------------------------------------------------------
+// restriction qc = (R x R x R) qf, R[c][f]  (NQF fine points per direction)
+// ---------------------------------------------------------------------------
+template <typename T, int NQF>
+__global__ void __launch_bounds__(NQF *NQF) coarsen_kernel(long long E, int NQC, const T *__restrict__ R,
+                                                             const T *__restrict__ qf, T *__restrict__ qc)
+{
+  __shared__ T s_R[NQF][NQF];
+  __shared__ T s_a[NQF][NQF][NQF]; // [c or k][j][i]
+  __shared__ T s_b[NQF][NQF][NQF];
+  const long long e = blockIdx.x;
+  const int t = threadIdx.x, i = t % NQF, j = t / NQF;
+  if (j < NQC) s_R[j][i] = R[j * NQF + i];
+  const T *f = qf + e * NQF * NQF * NQF;
+  T r[NQF];
+#pragma unroll
+  for (int k = 0; k < NQF; ++k) r[k] = f[i + NQF * (j + NQF * k)];
+  __syncthreads();
+  // along k (thread owns column (i,j))
+  for (int c = 0; c < NQC; ++c) {
+    T v = 0;
+#pragma unroll
+    for (int k = 0; k < NQF; ++k) v += s_R[c][k] * r[k];
+    s_a[c][j][i] = v;
+  }
+  __syncthreads();
+  // along j: thread (i, b) for b < NQC, all c
+  if (j < NQC) {
+    for (int c = 0; c < NQC; ++c) {
+      T v = 0;
+#pragma unroll
+      for (int m = 0; m < NQF; ++m) v += s_R[j][m] * s_a[c][m][i];
+      s_b[c][j][i] = v;
+    }
+  }
+  __syncthreads();
+  // along i: thread (a, b) for a, b < NQC
+  if (i < NQC && j < NQC) {
+    for (int c = 0; c < NQC; ++c) {
+      T v = 0;
+#pragma unroll
+      for (int m = 0; m < NQF; ++m) v += s_R[i][m] * s_b[c][j][m];
+      qc[e * NQC * NQC * NQC + i + NQC * (j + NQC * c)] = v;
+    }
+  }
+}
+
+// prolongation qf += (P x P x P) qc, P = R^T
+template <typename T, int NQF>
+__global__ void __launch_bounds__(NQF *NQF) prolong_kernel(long long E, int NQC, const T *__restrict__ R,
+                                                             const T *__restrict__ qc, T *__restrict__ qf)
+{
+  __shared__ T s_R[NQF][NQF];
+  __shared__ T s_c[NQF][NQF][NQF]; // coarse [c][b][a]
+  __shared__ T s_a[NQF][NQF][NQF]; // [c][b][i]
+  __shared__ T s_b[NQF][NQF][NQF]; // [c][j][i]
+  const long long e = blockIdx.x;
+  const int t = threadIdx.x, i = t % NQF, j = t / NQF;
+  if (j < NQC) s_R[j][i] = R[j * NQF + i];
+  const int npc = NQC * NQC * NQC;
+  for (int q = t; q < npc; q += NQF * NQF) s_c[q / (NQC * NQC)][(q / NQC) % NQC][q % NQC] = qc[e * npc + q];
+  __syncthreads();
+  // along a -> i: thread (i, b)
+  if (j < NQC)
+    for (int c = 0; c < NQC; ++c) {
+      T v = 0;
+      for (int a = 0; a < NQC; ++a) v += s_R[a][i] * s_c[c][j][a];
+      s_a[c][j][i] = v;
+    }
+  __syncthreads();
+  // along b -> j: thread (i, j)
+  for (int c = 0; c < NQC; ++c) {
+    T v = 0;
+    for (int b = 0; b < NQC; ++b) v += s_R[b][j] * s_a[c][b][i];
+    s_b[c][j][i] = v;
+  }
+  __syncthreads();
+  // along c -> k, accumulate
+  T *f = qf + e * NQF * NQF * NQF;
+#pragma unroll
+  for (int k = 0; k < NQF; ++k) {
+    T v = 0;
+    for (int c = 0; c < NQC; ++c) v += s_R[c][k] * s_b[c][j][i];
+    f[i + NQF * (j + NQF * k)] += v;
+  }
+}
+
+template <typename T> void launch_coarsen(int Nf, int Nc, long long E, const T *R, const T *qf, T *qc, cudaStream_t s)
+{
+  if (E <= 0) return;
+#define NRSG_CO(NQ) coarsen_kernel<T, NQ><<<(unsigned)E, NQ * NQ, 0, s>>>(E, Nc + 1, R, qf, qc)
+  NRSG_DISPATCH_NQ_MG(Nf, NRSG_CO)
+#undef NRSG_CO
+  NRSG_CHECK_LAUNCH();
+}
+template <typename T> void launch_prolong(int Nf, int Nc, long long E, const T *R, const T *qc, T *qf, cudaStream_t s)
+{
+  if (E <= 0) return;
+#define NRSG_PR(NQ) prolong_kernel<T, NQ><<<(unsigned)E, NQ * NQ, 0, s>>>(E, Nc + 1, R, qc, qf)
+  NRSG_DISPATCH_NQ_MG(Nf, NRSG_PR)
+#undef NRSG_PR
+  NRSG_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// Chebyshev updates
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void cheby1_kernel(long long n, T dc, T rc, const T *__restrict__ SAd, T *__restrict__ d, T *__restrict__ r,
+                              T *__restrict__ x)
+{
+  MG_LOOP(i, n)
+  {
+    const T xn = x[i], dn = d[i], rn = r[i], sa = SAd[i];
+    const T r1 = rn - sa;
+    x[i] = xn + dn;
+    r[i] = r1;
+    d[i] = dc * dn + rc * r1;
+  }
+}
+template <typename T>
+__global__ void cheby4_kernel(long long n, T beta, const T *__restrict__ Ad, const T *__restrict__ d, T *__restrict__ r,
+                              T *__restrict__ x)
+{
+  MG_LOOP(i, n)
+  {
+    x[i] = x[i] + beta * d[i];
+    r[i] = r[i] - Ad[i];
+  }
+}
+template <typename T>
+void launch_cheby1_update(long long n, T dc, T rc, const T *SAd, T *d, T *r, T *x, cudaStream_t s)
+{
+  cheby1_kernel<T><<<grid_for(n), kT, 0, s>>>(n, dc, rc, SAd, d, r, x);
+  NRSG_CHECK_LAUNCH();
+}
+template <typename T> void launch_cheby4_update(long long n, T beta, const T *Ad, const T *d, T *r, T *x, cudaStream_t s)
+{
+  cheby4_kernel<T><<<grid_for(n), kT, 0, s>>>(n, beta, Ad, d, r, x);
+  NRSG_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// fused FDM local solve.  Halo point h = (e*6 + f)*NQ^2 + a + NQ*b for face
+// f in {x-, x+, y-, y+, z-, z+}; haloSrc[h] is the E-vector index of the
+// neighbour node the halo point stands for (-1: none).
+// S*_e[r + nl*c] = S(r, c) (column c = eigenvector c); invL[e][Npe].
+// ---------------------------------------------------------------------------
+template <int NQ> __device__ __forceinline__ int halo_ext_index(int f, int a, int b)
+{
+  constexpr int NL = NQ + 2;
+  switch (f) {
+  case 0: return 0 + NL * ((a + 1) + NL * (b + 1));
+  case 1: return (NL - 1) + NL * ((a + 1) + NL * (b + 1));
+  case 2: return (a + 1) + NL * (0 + NL * (b + 1));
+  case 3: return (a + 1) + NL * ((NL - 1) + NL * (b + 1));
+  case 4: return (a + 1) + NL * ((b + 1) + NL * 0);
+  default: return (a + 1) + NL * ((b + 1) + NL * (NL - 1));
+  }
+}
+
+template <typename T, int NQ, bool RAS>
+__global__ void __launch_bounds__((NQ + 2) * (NQ + 2))
+    fdm_kernel(long long E, const T *__restrict__ u, const int *__restrict__ haloSrc, const T *__restrict__ Sx,
+               const T *__restrict__ Sy, const T *__restrict__ Sz, const T *__restrict__ invL,
+               const T *__restrict__ wts, T *__restrict__ Su, T *__restrict__ haloOut)
+{
+  constexpr int NL = NQ + 2, NPE = NL * NL * NL, NP = NQ * NQ * NQ, NF = NQ * NQ;
+  __shared__ T s_w[NPE];
+  __shared__ T s_Sx[NL * NL], s_Sy[NL * NL], s_Sz[NL * NL];
+  const long long e = blockIdx.x;
+  const int t = threadIdx.x;
+  for (int q = t; q < NL * NL; q += NL * NL) {
+    s_Sx[q] = Sx[e * NL * NL + q];
+    s_Sy[q] = Sy[e * NL * NL + q];
+    s_Sz[q] = Sz[e * NL * NL + q];
+  }
+  for (int q = t; q < NPE; q += NL * NL) s_w[q] = T(0);
+  __syncthreads();
+  const T *ue = u + e * NP;
+  for (int q = t; q < NP; q += NL * NL) {
+    const int i = q % NQ, j = (q / NQ) % NQ, k = q / NF;
+    s_w[(i + 1) + NL * ((j + 1) + NL * (k + 1))] = ue[q];
+  }
+  const int *hs = haloSrc + e * 6 * NF;
+  for (int q = t; q < 6 * NF; q += NL * NL) {
+    const int f = q / NF, p = q % NF;
+    const int src = hs[q];
+    s_w[halo_ext_index<NQ>(f, p % NQ, p / NQ)] = src >= 0 ? u[src] : T(0);
+  }
+  __syncthreads();
+  // thread (p, q) owns one line per direction
+  const int p = t % NL, q = t / NL;
+  T line[NL];
+  // forward: x (S^T), y, z
+#pragma unroll
+  for (int l = 0; l < NL; ++l) line[l] = s_w[l + NL * (p + NL * q)];
+#pragma unroll
+  for (int i = 0; i < NL; ++i) {
+    T v = 0;
+#pragma unroll
+    for (int l = 0; l < NL; ++l) v += s_Sx[l + NL * i] * line[l];
+    s_w[i + NL * (p + NL * q)] = v;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int l = 0; l < NL; ++l) line[l] = s_w[p + NL * (l + NL * q)];
+#pragma unroll
+  for (int j = 0; j < NL; ++j) {
+    T v = 0;
+#pragma unroll
+    for (int l = 0; l < NL; ++l) v += s_Sy[l + NL * j] * line[l];
+    s_w[p + NL * (j + NL * q)] = v;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int l = 0; l < NL; ++l) line[l] = s_w[p + NL * (q + NL * l)];
+  const T *iL = invL + e * NPE;
+#pragma unroll
+  for (int k = 0; k < NL; ++k) {
+    T v = 0;
+#pragma unroll
+    for (int l = 0; l < NL; ++l) v += s_Sz[l + NL * k] * line[l];
+    s_w[p + NL * (q + NL * k)] = v * iL[p + NL * (q + NL * k)];
+  }
+  __syncthreads();
+  // backward: x (S), y, z
+#pragma unroll
+  for (int l = 0; l < NL; ++l) line[l] = s_w[l + NL * (p + NL * q)];
+#pragma unroll
+  for (int i = 0; i < NL; ++i) {
+    T v = 0;
+#pragma unroll
+    for (int l = 0; l < NL; ++l) v += s_Sx[i + NL * l] * line[l];
+    s_w[i + NL * (p + NL * q)] = v;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int l = 0; l < NL; ++l) line[l] = s_w[p + NL * (l + NL * q)];
+#pragma unroll
+  for (int j = 0; j < NL; ++j) {
+    T v = 0;
+#pragma unroll
+    for (int l = 0; l < NL; ++l) v += s_Sy[j + NL * l] * line[l];
+    s_w[p + NL * (j + NL * q)] = v;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int l = 0; l < NL; ++l) line[l] = s_w[p + NL * (q + NL * l)];
+#pragma unroll
+  for (int k = 0; k < NL; ++k) {
+    T v = 0;
+#pragma unroll
+    for (int l = 0; l < NL; ++l) v += s_Sz[k + NL * l] * line[l];
+    s_w[p + NL * (q + NL * k)] = v;
+  }
+  __syncthreads();
+  T *se = Su + e * NP;
+  for (int qq = t; qq < NP; qq += NL * NL) {
+    const int i = qq % NQ, j = (qq / NQ) % NQ, k = qq / NF;
+    const T v = s_w[(i + 1) + NL * ((j + 1) + NL * (k + 1))];
+    se[qq] = RAS ? v * wts[e * NP + qq] : v;
+  }
+  if (!RAS) {
+    T *ho = haloOut + e * 6 * NF;
+    for (int qq = t; qq < 6 * NF; qq += NL * NL) {
+      const int f = qq / NF, pp = qq % NF;
+      ho[qq] = s_w[halo_ext_index<NQ>(f, pp % NQ, pp / NQ)];
+    }
+  }
+}
+
+// ASM: add the neighbours' overlap results onto the nodes next to each face,
+// face by face in the order x-, x+, y-, y+, z-, z+, then weight.
+// haloPartner[h] is the halo index of the neighbour's halo point that maps
+// onto the node next to face point h (-1: none).
+template <typename T, int NQ>
+__global__ void asm_combine_kernel(long long E, const int *__restrict__ haloPartner, const T *__restrict__ haloOut,
+                                   const T *__restrict__ wts, T *__restrict__ Su)
+{
+  constexpr int NP = NQ * NQ * NQ, NF = NQ * NQ, N = NQ - 1;
+  __shared__ T s_u[NP];
+  const long long e = blockIdx.x;
+  for (int q = threadIdx.x; q < NP; q += blockDim.x) s_u[q] = Su[e * NP + q];
+  __syncthreads();
+  for (int f = 0; f < 6; ++f) {
+    for (int p = threadIdx.x; p < NF; p += blockDim.x) {
+      const int hp = haloPartner[(e * 6 + f) * NF + p];
+      if (hp < 0) continue;
+      const int a = p % NQ, b = p / NQ;
+      int n;
+      switch (f) {
+      case 0: n = 1 + NQ * (a + NQ * b); break;
+      case 1: n = (N - 1) + NQ * (a + NQ * b); break;
+      case 2: n = a + NQ * (1 + NQ * b); break;
+      case 3: n = a + NQ * ((N - 1) + NQ * b); break;
+      case 4: n = a + NQ * (b + NQ * 1); break;
+      default: n = a + NQ * (b + NQ * (N - 1)); break;
+      }
+      s_u[n] += haloOut[hp];
+    }
+    __syncthreads();
+  }
+  for (int q = threadIdx.x; q < NP; q += blockDim.x) Su[e * NP + q] = s_u[q] * wts[e * NP + q];
+}
+
+template <typename T>
+void launch_fdm(int N, long long E, bool ras, const T *u, const int *haloSrc, const T *Sx, const T *Sy, const T *Sz,
+                const T *invL, const T *wts, T *Su, T *haloOut, cudaStream_t s)
+{
+  if (E <= 0) return;
+#define NRSG_FDM(NQ)                                                                                       \
+  {                                                                                                        \
+    const int thr = (NQ + 2) * (NQ + 2);                                                                   \
+    if (ras)                                                                                               \
+      fdm_kernel<T, NQ, true><<<(unsigned)E, thr, 0, s>>>(E, u, haloSrc, Sx, Sy, Sz, invL, wts, Su, haloOut); \
+    else                                                                                                   \
+      fdm_kernel<T, NQ, false><<<(unsigned)E, thr, 0, s>>>(E, u, haloSrc, Sx, Sy, Sz, invL, wts, Su, haloOut); \
+  }
+  NRSG_DISPATCH_NQ_MG(N, NRSG_FDM)
+#undef NRSG_FDM
+  NRSG_CHECK_LAUNCH();
+}
+template <typename T>
+void launch_asm_combine(int N, long long E, const int *haloPartner, const T *haloOut, const T *wts, T *Su,
+                        cudaStream_t s)
+{
+  if (E <= 0) return;
+#define NRSG_ASMC(NQ) asm_combine_kernel<T, NQ><<<(unsigned)E, 128, 0, s>>>(E, haloPartner, haloOut, wts, Su)
+  NRSG_DISPATCH_NQ_MG(N, NRSG_ASMC)
+#undef NRSG_ASMC
+  NRSG_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// seeded start vector for the Arnoldi lambda_max estimate: U[0,1) per index
+// (splitmix64 of seed and the index)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long smix64(unsigned long long x)
+{
+  x += 0x9E3779B97F4A7C15ull;
+  unsigned long long z = x;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__global__ void random_fill_kernel(long long n, unsigned long long seed, double *v)
+{
+  MG_LOOP(i, n) v[i] = (double)(smix64(seed ^ smix64((unsigned long long)i)) >> 11) * (1.0 / 9007199254740992.0);
+}
+void launch_random_fill(long long n, unsigned long long seed, double *v, cudaStream_t s)
+{
+  random_fill_kernel<<<grid_for(n), kT, 0, s>>>(n, seed, v);
+  NRSG_CHECK_LAUNCH();
+}
+
+#define NRSG_INST_MG(T)                                                                                    \
+  template void launch_coarsen<T>(int, int, long long, const T *, const T *, T *, cudaStream_t);           \
+  template void launch_prolong<T>(int, int, long long, const T *, const T *, T *, cudaStream_t);           \
+  template void launch_cheby1_update<T>(long long, T, T, const T *, T *, T *, T *, cudaStream_t);          \
+  template void launch_cheby4_update<T>(long long, T, const T *, const T *, T *, T *, cudaStream_t);       \
+  template void launch_fdm<T>(int, long long, bool, const T *, const int *, const T *, const T *, const T *, \
+                              const T *, const T *, T *, T *, cudaStream_t);                               \
+  template void launch_asm_combine<T>(int, long long, const int *, const T *, const T *, T *, cudaStream_t);
+NRSG_INST_MG(double)
+NRSG_INST_MG(float)
+
+} // namespace nrsg

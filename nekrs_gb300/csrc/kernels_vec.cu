@@ -462,3 +462,81 @@ template void launch_scale_copy<double>(long long, double, const double *, doubl
 template void launch_scale_copy<float>(long long, float, const float *, float *, cudaStream_t);
 
 } // namespace nrsg
+
+// ===========================================================================
+// Jacobi-PCG kernels in precision T with double scalars (coarse-level solve)
+// ===========================================================================
+#include "mg_kernels.hpp"
+
+namespace nrsg {
+
+template <typename T>
+__global__ void pcgT_rdotz_kernel(long long n, const T *__restrict__ w, const T *__restrict__ invDiag,
+                                  const T *__restrict__ r, T *__restrict__ z, PcgScalars *sc, double *partials,
+                                  unsigned *counter)
+{
+  double acc = 0;
+  for (long long i = blockIdx.x * (long long)kThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kThreads) {
+    const T ri = r[i];
+    const T zi = invDiag[i] * ri;
+    z[i] = zi;
+    acc += (double)w[i] * (double)ri * (double)zi;
+  }
+  __shared__ double s_old;
+  if (threadIdx.x == 0) s_old = sc->rdotz;
+  __syncthreads();
+  if (finish_reduction(block_sum(acc), partials, counter, &sc->rdotz)) sc->rdotz_old = s_old;
+}
+template <typename T>
+__global__ void pcgT_p_kernel(long long n, const T *__restrict__ z, T *__restrict__ p, const PcgScalars *sc, bool first)
+{
+  const T beta = first ? T(0) : (T)(sc->rdotz / sc->rdotz_old);
+  NRSG_GRID_LOOP(i, n) p[i] = z[i] + beta * p[i];
+}
+template <typename T>
+__global__ void pcgT_xr_kernel(long long n, const T *__restrict__ w, const T *__restrict__ p, const T *__restrict__ Ap,
+                               T *__restrict__ x, T *__restrict__ r, PcgScalars *sc, double *partials,
+                               unsigned *counter)
+{
+  const T alpha = (T)(sc->rdotz / (sc->pAp + 1e-300));
+  double acc = 0;
+  for (long long i = blockIdx.x * (long long)kThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kThreads) {
+    x[i] += alpha * p[i];
+    const T ri = r[i] - alpha * Ap[i];
+    r[i] = ri;
+    acc += (double)w[i] * (double)ri * (double)ri;
+  }
+  finish_reduction(block_sum(acc), partials, counter, &sc->rdotr);
+}
+
+template <typename T>
+void launch_pcg_rdotz(long long n, const T *w, const T *invDiag, const T *r, T *z, PcgScalars *sc, Reduce &red, int slot,
+                      cudaStream_t s)
+{
+  pcgT_rdotz_kernel<T><<<red_grid(n), kThreads, 0, s>>>(n, w, invDiag, r, z, sc, red.partials + (size_t)slot * kRedBlocks,
+                                                        red.counters + slot);
+  NRSG_CHECK_LAUNCH();
+}
+template <typename T> void launch_pcg_p(long long n, const T *z, T *p, const PcgScalars *sc, bool first, cudaStream_t s)
+{
+  pcgT_p_kernel<T><<<vec_grid(n), kThreads, 0, s>>>(n, z, p, sc, first);
+  NRSG_CHECK_LAUNCH();
+}
+template <typename T>
+void launch_pcg_xr(long long n, const T *w, const T *p, const T *Ap, T *x, T *r, PcgScalars *sc, Reduce &red, int slot,
+                   cudaStream_t s)
+{
+  pcgT_xr_kernel<T><<<red_grid(n), kThreads, 0, s>>>(n, w, p, Ap, x, r, sc, red.partials + (size_t)slot * kRedBlocks,
+                                                     red.counters + slot);
+  NRSG_CHECK_LAUNCH();
+}
+#define NRSG_INST_PCGT(T)                                                                                  \
+  template void launch_pcg_rdotz<T>(long long, const T *, const T *, const T *, T *, PcgScalars *, Reduce &, int, \
+                                    cudaStream_t);                                                         \
+  template void launch_pcg_p<T>(long long, const T *, T *, const PcgScalars *, bool, cudaStream_t);        \
+  template void launch_pcg_xr<T>(long long, const T *, const T *, const T *, T *, T *, PcgScalars *, Reduce &, int, \
+                                 cudaStream_t);
+NRSG_INST_PCGT(double)
+NRSG_INST_PCGT(float)
+
+} // namespace nrsg

@@ -1,17 +1,482 @@
-// p-multigrid preconditioner (filled in with the pMG rows).
-#include "elliptic.hpp"
+// p-multigrid preconditioner on the device.
+//
+// Mirrors (nekRS tree):
+//   MGSolver_t::Run / runVcycle             src/solvers/elliptic/MG/MGSolver.cpp:150-193
+//   pMGLevel smoothers / residual / transfers  src/solvers/elliptic/MG/ellipticMultiGridLevel.cpp:31-277
+//   pMGLevel::setupSmoother, maxEigSmoothAx  src/solvers/elliptic/MG/ellipticMultiGridLevelSetup.cpp:109-453
+//   ellipticMultiGridSetup                   src/solvers/elliptic/MG/ellipticMultiGridSetup.cpp:60-343
+//   ellipticPreconditioner (MG branch)       src/solvers/elliptic/ellipticPreconditioner.cpp:55-62
+// The whole hierarchy lives in HBM for the lifetime of the solver (meshes,
+// geometric factors, FDM operators, halo maps).  The multigrid arithmetic
+// runs in the precision T of `mgPrecision` (fp64 or fp32); the coarsest level
+// is solved by Jacobi-PCG in T to `coarseTol` (default 1e-4) or smoothed.
+
+#include "mg_host.hpp"
+#include "mg_kernels.hpp"
+
+#include <cmath>
+#include <cstring>
 
 namespace nrsg {
 
-struct MGState {};
+struct MGState {
+  virtual ~MGState() = default;
+  virtual void apply(const double *r, double *z) = 0;
+  virtual std::vector<double> info(const std::string &what) = 0;
+  virtual void schwarz(int level, const double *u, double *Su) = 0;
+  virtual long long level_size(int level) = 0;
+};
 void MGDeleter::operator()(MGState *m) const { delete m; }
 
-void Elliptic::mg_setup() { throw Error(NRSG_ERR_BAD_CONFIG, "preconditioner = multigrid is not available yet"); }
-void Elliptic::mg_apply(const double *, double *) { throw Error(NRSG_ERR_BAD_CONFIG, "multigrid not set up"); }
+template <typename T> struct MGLevelDev {
+  FieldLevel *L = nullptr;
+  std::unique_ptr<FieldLevel> own;
+  DevBuf<T> ggeo, D, invDegree;
+  DevBuf<T> R, invDegreeFine;
+  int Nf = 0;
+  bool smoothed = true;
+  DevBuf<T> invDiag;
+  double rho = 0, lambda0 = 0, lambda1 = 0;
+  int up = 2, down = 2;
+  std::vector<double> upBetas, downBetas;
+  DevBuf<T> Sx, Sy, Sz, invL, wts, haloOut;
+  DevBuf<int> haloSrc, haloPartner;
+  DevBuf<T> x, rhs, res;
+};
+
+template <typename T> struct MGImpl : public MGState {
+  Elliptic &el;
+  cudaStream_t s;
+  MGPlan plan;
+  std::vector<MGLevelDev<T>> lv;
+  DevBuf<T> sRes, sRes2, sUpd, sTmp, rP, zP;
+  DevBuf<T> cp, cz, cAp, cr;
+  DevBuf<PcgScalars> csc;
+  std::vector<int> coarseIters;
+  T l0, l1;
+  bool poisson;
+
+  explicit MGImpl(Elliptic &e) : el(e), s(e.stream)
+  {
+    const Options &o = el.opt;
+    plan = plan_levels(o, el.fine.N);
+    l0 = (T)o.lambda0;
+    l1 = (T)o.lambda1;
+    poisson = o.poisson;
+    const int nlev = (int)plan.orders.size();
+    lv.resize(nlev);
+    size_t nmax = 0;
+    for (int l = 0; l < nlev; ++l) {
+      auto &v = lv[l];
+      if (l == 0) {
+        v.L = &el.fine;
+      } else {
+        v.own.reset(new FieldLevel());
+        v.own->build(plan.orders[l], el.fine.E, el.fine.VXh.data(), el.fine.EToVh.data(), el.fine.EToBh.data(),
+                     nullptr, s);
+        v.L = v.own.get();
+        const FieldLevel &Lf = *lv[l - 1].L;
+        v.Nf = Lf.N;
+        std::vector<double> I; // I[f*Ncq + c] = l_c(z_f)
+        lagrange_interp(v.L->z, Lf.z, I);
+        const int Ncq = v.L->Nq, Nfq = Lf.Nq;
+        std::vector<T> R((size_t)Ncq * Nfq);
+        for (int c = 0; c < Ncq; ++c)
+          for (int f = 0; f < Nfq; ++f) R[c * Nfq + f] = (T)I[f * Ncq + c];
+        v.R.upload(R);
+        std::vector<T> idf(Lf.gm.invDegree.begin(), Lf.gm.invDegree.end());
+        v.invDegreeFine.upload(idf);
+      }
+      FieldLevel &L = *v.L;
+      nmax = std::max(nmax, (size_t)L.Nlocal);
+      v.ggeo.alloc(L.d_ggeo64.n);
+      launch_copy_cast<double, T>((long long)L.d_ggeo64.n, L.d_ggeo64.p, v.ggeo.p, s);
+      std::vector<T> D(L.Dh.begin(), L.Dh.end()), inv(L.gm.invDegree.begin(), L.gm.invDegree.end());
+      v.D.upload(D);
+      v.invDegree.upload(inv);
+      v.x.alloc(L.Nlocal);
+      v.rhs.alloc(L.Nlocal);
+      v.res.alloc(L.Nlocal);
+      const bool coarsest = (l == nlev - 1);
+      v.smoothed = !coarsest || o.coarse == "smooth";
+      if (plan.base == 0 || coarsest) {
+        v.invDiag.alloc(L.Nlocal);
+        launch_build_diag<T>(L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, v.invDiag.p, s);
+        launch_gs<T>(L.ngroups, L.d_gsOff.p, L.d_gsIds.p, v.invDiag.p, s);
+        launch_recip<T>(L.Nlocal, v.invDiag.p, s);
+      }
+    }
+    sRes.alloc(nmax);
+    sRes2.alloc(nmax);
+    sUpd.alloc(nmax);
+    sTmp.alloc(nmax);
+    const FieldLevel &C = *lv.back().L;
+    cp.alloc(C.Nlocal);
+    cz.alloc(C.Nlocal);
+    cAp.alloc(C.Nlocal);
+    cr.alloc(C.Nlocal);
+    csc.alloc(1);
+    NRSG_CUDA(cudaMemsetAsync(csc.p, 0, sizeof(PcgScalars), s));
+    if (!std::is_same<T, double>::value) {
+      rP.alloc(el.fine.Nlocal);
+      zP.alloc(el.fine.Nlocal);
+    }
+    // smoothers: FDM operators, lambda_max, Chebyshev degrees
+    for (int l = 0; l < nlev; ++l) {
+      auto &v = lv[l];
+      if (!v.smoothed) continue;
+      if (plan.base != 0) build_fdm(v);
+      v.rho = max_eig(v, o.seed + (unsigned long long)l);
+      v.lambda1 = o.maxEigFactor * v.rho;
+      v.lambda0 = o.minEigFactor * v.rho;
+      const int ord = plan.orders[l];
+      const bool coarsest = (l == nlev - 1);
+      v.up = v.down = coarsest ? 3 : o.chebyDegree;
+      auto itd = plan.down.find(ord), itu = plan.up.find(ord);
+      if (!o.schedule.empty()) {
+        if (itd != plan.down.end() && itd->second > -1) v.down = itd->second;
+        if (itu != plan.up.end() && itu->second > -1) v.up = itu->second;
+      }
+      if (plan.kind == 2) {
+        v.upBetas = opt4_betas(v.up);
+        v.downBetas = opt4_betas(v.down);
+      } else {
+        v.upBetas.assign(std::max(v.up, 1), 1.0);
+        v.downBetas.assign(std::max(v.down, 1), 1.0);
+      }
+    }
+    NRSG_CUDA(cudaStreamSynchronize(s));
+  }
+
+  // --------------------------------------------------------------- setup
+  void build_fdm(MGLevelDev<T> &v)
+  {
+    const FieldLevel &L = *v.L;
+    const int nl = L.N + 3, npe = nl * nl * nl;
+    const long long E = L.E;
+    const FdmLengths len = fdm_lengths(el.fine, el.fine.um);
+    std::vector<T> Sx((size_t)E * nl * nl), Sy((size_t)E * nl * nl), Sz((size_t)E * nl * nl), iL((size_t)E * npe);
+#pragma omp parallel for
+    for (long long e = 0; e < E; ++e) {
+      const int *bc = &L.EToBh[e * 6];
+      // (left, right) faces per direction in nekRS face order: r: 4,2  s: 1,3  t: 0,5
+      const int lb[3] = {bc[4], bc[1], bc[0]}, rb[3] = {bc[2], bc[3], bc[5]};
+      std::vector<double> S[3], lam[3];
+      for (int d = 0; d < 3; ++d)
+        fdm_1d_operator(L, lb[d], rb[d], len.left[3 * e + d], len.mid[3 * e + d], len.right[3 * e + d], S[d], lam[d]);
+      for (int q = 0; q < nl * nl; ++q) {
+        Sx[e * nl * nl + q] = (T)S[0][q];
+        Sy[e * nl * nl + q] = (T)S[1][q];
+        Sz[e * nl * nl + q] = (T)S[2][q];
+      }
+      for (int k = 0; k < nl; ++k)
+        for (int j = 0; j < nl; ++j)
+          for (int i = 0; i < nl; ++i) {
+            const double dsum = lam[0][i] + lam[1][j] + lam[2][k];
+            iL[e * npe + i + nl * (j + nl * k)] = (T)(dsum > 1e-5 ? 1.0 / dsum : 0.0);
+          }
+    }
+    v.Sx.upload(Sx);
+    v.Sy.upload(Sy);
+    v.Sz.upload(Sz);
+    v.invL.upload(iL);
+    std::vector<int> src, partner;
+    std::vector<double> w;
+    fdm_halo_maps(L, src, partner, w);
+    v.haloSrc.upload(src);
+    v.haloPartner.upload(partner);
+    std::vector<T> wt(w.begin(), w.end());
+    v.wts.upload(wt);
+    if (plan.base == 1) v.haloOut.alloc(src.size());
+  }
+
+  double read(const double *d)
+  {
+    double h = 0;
+    NRSG_CUDA(cudaMemcpyAsync(&h, d, sizeof(double), cudaMemcpyDeviceToHost, s));
+    NRSG_CUDA(cudaStreamSynchronize(s));
+    return h;
+  }
+
+  // rho(S A) by 10 Arnoldi steps with a seeded start vector (maxEigSmoothAx)
+  double max_eig(MGLevelDev<T> &v, unsigned long long seed)
+  {
+    FieldLevel &L = *v.L;
+    const long long n = L.Nlocal;
+    const int k = (int)std::min<long long>(10, n);
+    DevBuf<double> V((size_t)(k + 1) * n), vx(n);
+    DevBuf<T> tq(n), ta(n);
+    DevBuf<int> uoff, uids;
+    uoff.upload(L.um.devOff);
+    uids.upload(L.um.devIds);
+    launch_random_fill(n, seed, vx.p, s);
+    launch_gs<double>((long long)L.um.devOff.size() - 1, uoff.p, uids.p, vx.p, s);
+    launch_mask<double>((long long)L.maskIds.size(), L.d_mask.p, vx.p, s);
+    double *out = &el.d_scal.p->pad;
+    const double *w = L.d_invDegree64.p;
+    launch_wdot<double>(n, w, vx.p, nullptr, out, el.red, 4, s);
+    const double nv = std::sqrt(read(out));
+    auto Vj = [&](int j) { return V.p + (size_t)j * n; };
+    launch_scale_copy<double>(n, 1.0 / nv, vx.p, Vj(0), s);
+    std::vector<double> H((size_t)k * k, 0.0);
+    for (int j = 0; j < k; ++j) {
+      launch_copy_cast<double, T>(n, Vj(j), tq.p, s);
+      level_op(v, tq.p, ta.p);
+      apply_S(v, ta.p, tq.p);
+      launch_copy_cast<T, double>(n, tq.p, Vj(j + 1), s);
+      for (int i = 0; i <= j; ++i) {
+        launch_wdot<double>(n, w, Vj(i), Vj(j + 1), out, el.red, 4, s);
+        const double hij = read(out);
+        launch_axpby<double>(n, -hij, Vj(i), 1.0, Vj(j + 1), s);
+        H[i + (size_t)j * k] = hij;
+      }
+      if (j + 1 < k) {
+        launch_wdot<double>(n, w, Vj(j + 1), nullptr, out, el.red, 4, s);
+        const double nj = std::sqrt(read(out));
+        launch_scale_copy<double>(n, 1.0 / nj, Vj(j + 1), Vj(j + 1), s);
+        H[j + 1 + (size_t)j * k] = nj;
+      }
+    }
+    NRSG_CUDA(cudaStreamSynchronize(s));
+    return hessenberg_spectral_radius(k, H);
+  }
+
+  // --------------------------------------------------------------- operators
+  void level_op(MGLevelDev<T> &v, const T *q, T *Aq)
+  {
+    FieldLevel &L = *v.L;
+    launch_ax_stored<T>(L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, q, Aq, s);
+    launch_mask<T>((long long)L.maskIds.size(), L.d_mask.p, Aq, s);
+    launch_gs<T>(L.ngroups, L.d_gsOff.p, L.d_gsIds.p, Aq, s);
+  }
+
+  // Schwarz: FDM (+ ASM combine) -> gs -> mask; u and Su must not alias
+  void schwarz_apply(MGLevelDev<T> &v, const T *u, T *Su)
+  {
+    FieldLevel &L = *v.L;
+    const bool ras = plan.base == 2;
+    launch_fdm<T>(L.N, L.E, ras, u, v.haloSrc.p, v.Sx.p, v.Sy.p, v.Sz.p, v.invL.p, v.wts.p, Su, v.haloOut.p, s);
+    if (!ras) launch_asm_combine<T>(L.N, L.E, v.haloPartner.p, v.haloOut.p, v.wts.p, Su, s);
+    launch_gs<T>(L.ngroups, L.d_gsOff.p, L.d_gsIds.p, Su, s);
+    launch_mask<T>((long long)L.maskIds.size(), L.d_mask.p, Su, s);
+  }
+
+  void apply_S(MGLevelDev<T> &v, const T *r, T *Sr)
+  {
+    const long long n = v.L->Nlocal;
+    if (plan.base == 0) {
+      launch_axmyz<T>(n, v.invDiag.p, r, Sr, s);
+    } else if (r == Sr) {
+      NRSG_CUDA(cudaMemcpyAsync(sTmp.p, r, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
+      schwarz_apply(v, sTmp.p, Sr);
+    } else {
+      schwarz_apply(v, r, Sr);
+    }
+  }
+
+  void smooth_cheby1(MGLevelDev<T> &v, const T *r, T *x, bool xIsZero)
+  {
+    const int degree = xIsZero ? v.down : v.up;
+    if (degree == 0) return;
+    const long long n = v.L->Nlocal;
+    const T theta = (T)(0.5 * (v.lambda1 + v.lambda0));
+    const T delta = (T)(0.5 * (v.lambda1 - v.lambda0));
+    const T invTheta = (T)1.0 / theta;
+    const T sigma = theta / delta;
+    T rho_n = (T)1.0 / sigma;
+    T *res = sRes.p, *Ad = sRes2.p, *d = sUpd.p;
+    if (xIsZero) launch_fill<T>(n, T(0), x, s);
+    if (!xIsZero) {
+      level_op(v, x, res);
+      launch_axpby<T>(n, T(1), r, T(-1), res, s);
+    } else {
+      NRSG_CUDA(cudaMemcpyAsync(res, r, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
+    }
+    apply_S(v, res, res);
+    launch_scale_copy<T>(n, invTheta, res, d, s);
+    for (int k = 1; k < degree; ++k) {
+      level_op(v, d, Ad);
+      apply_S(v, Ad, Ad);
+      const T rhoSave = rho_n;
+      rho_n = (T)1.0 / ((T)2.0 * sigma - rho_n);
+      const T rCoeff = (T)2.0 * rho_n / delta;
+      const T dCoeff = rho_n * rhoSave;
+      launch_cheby1_update<T>(n, dCoeff, rCoeff, Ad, d, res, x, s);
+    }
+    launch_axpby<T>(n, T(1), d, T(1), x, s);
+    launch_mask<T>((long long)v.L->maskIds.size(), v.L->d_mask.p, x, s);
+  }
+
+  void smooth_cheby4(MGLevelDev<T> &v, const T *r, T *x, bool xIsZero)
+  {
+    const int degree = xIsZero ? v.down : v.up;
+    if (degree == 0) return;
+    const auto &betas = xIsZero ? v.downBetas : v.upBetas;
+    const long long n = v.L->Nlocal;
+    T *res = sRes.p, *Ad = sRes2.p, *d = sUpd.p;
+    const double rho = v.lambda1;
+    if (xIsZero) {
+      launch_fill<T>(n, T(0), x, s);
+      NRSG_CUDA(cudaMemcpyAsync(res, r, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
+    } else {
+      level_op(v, x, res);
+      launch_axpby<T>(n, T(1), r, T(-1), res, s);
+    }
+    apply_S(v, res, Ad);
+    launch_scale_copy<T>(n, (T)(4.0 / (3.0 * rho)), Ad, d, s);
+    for (int k = 1; k < degree; ++k) {
+      level_op(v, d, Ad);
+      launch_cheby4_update<T>(n, (T)betas[k - 1], Ad, d, res, x, s);
+      apply_S(v, res, Ad);
+      const T dCoeff = (T)((2.0 * k - 1.0) / (2.0 * k + 3.0));
+      const T rCoeff = (T)((8.0 * k + 4.0) / ((2.0 * k + 3.0) * rho));
+      launch_axpby<T>(n, rCoeff, Ad, dCoeff, d, s);
+    }
+    launch_axpby<T>(n, (T)betas.back(), d, T(1), x, s);
+    launch_mask<T>((long long)v.L->maskIds.size(), v.L->d_mask.p, x, s);
+  }
+
+  void smooth(MGLevelDev<T> &v, const T *r, T *x, bool xIsZero)
+  {
+    if (plan.kind == 0)
+      smooth_cheby1(v, r, x, xIsZero);
+    else
+      smooth_cheby4(v, r, x, xIsZero);
+  }
+
+  int coarse_pcg(MGLevelDev<T> &v, const T *b, T *x)
+  {
+    FieldLevel &L = *v.L;
+    const long long n = L.Nlocal;
+    const Options &o = el.opt;
+    const T *w = v.invDegree.p;
+    PcgScalars *sc = csc.p;
+    launch_fill<T>(n, T(0), x, s);
+    NRSG_CUDA(cudaMemcpyAsync(cr.p, b, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
+    launch_fill<T>(n, T(0), cp.p, s);
+    launch_wdot<T>(n, w, cr.p, nullptr, &sc->rdotr, el.red, 5, s);
+    const double r0 = std::sqrt(read(&sc->rdotr));
+    if (r0 == 0) return 0;
+    const double tol = o.coarseTol * r0;
+    double rn = r0;
+    int it = 0;
+    while (rn > tol && it < o.coarseMaxIter) {
+      ++it;
+      launch_pcg_rdotz<T>(n, w, v.invDiag.p, cr.p, cz.p, sc, el.red, 5, s);
+      launch_pcg_p<T>(n, cz.p, cp.p, sc, it == 1, s);
+      level_op(v, cp.p, cAp.p);
+      launch_wdot<T>(n, w, cp.p, cAp.p, &sc->pAp, el.red, 6, s);
+      launch_pcg_xr<T>(n, w, cp.p, cAp.p, x, cr.p, sc, el.red, 7, s);
+      rn = std::sqrt(read(&sc->rdotr));
+    }
+    coarseIters.push_back(it);
+    return it;
+  }
+
+  void vcycle(int k)
+  {
+    auto &v = lv[k];
+    const int base = (int)lv.size() - 1;
+    if (k == base) {
+      if (el.opt.coarse == "smooth")
+        smooth(v, v.rhs.p, v.x.p, true);
+      else
+        coarse_pcg(v, v.rhs.p, v.x.p);
+      return;
+    }
+    auto &c = lv[k + 1];
+    const long long n = v.L->Nlocal;
+    smooth(v, v.rhs.p, v.x.p, true);
+    level_op(v, v.x.p, v.res.p);
+    launch_axpby<T>(n, T(1), v.rhs.p, T(-1), v.res.p, s);
+    // coarsen: res *= invDegree(fine), restrict, gs, mask
+    launch_axmy<T>(n, c.invDegreeFine.p, v.res.p, s);
+    launch_coarsen<T>(v.L->N, c.L->N, c.L->E, c.R.p, v.res.p, c.rhs.p, s);
+    launch_gs<T>(c.L->ngroups, c.L->d_gsOff.p, c.L->d_gsIds.p, c.rhs.p, s);
+    launch_mask<T>((long long)c.L->maskIds.size(), c.L->d_mask.p, c.rhs.p, s);
+    vcycle(k + 1);
+    launch_prolong<T>(v.L->N, c.L->N, c.L->E, c.R.p, c.x.p, v.x.p, s);
+    smooth(v, v.rhs.p, v.x.p, false);
+  }
+
+  // --------------------------------------------------------------- interface
+  void apply(const double *r, double *z) override
+  {
+    auto &v0 = lv[0];
+    const long long n = el.fine.Nlocal;
+    if (std::is_same<T, double>::value) {
+      NRSG_CUDA(cudaMemcpyAsync(v0.rhs.p, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+      vcycle(0);
+      NRSG_CUDA(cudaMemcpyAsync(z, v0.x.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    } else {
+      launch_copy_cast<double, T>(n, r, v0.rhs.p, s);
+      vcycle(0);
+      launch_copy_cast<T, double>(n, v0.x.p, z, s);
+    }
+  }
+
+  std::vector<double> info(const std::string &what) override
+  {
+    std::vector<double> out;
+    if (what == "mg.levels")
+      for (auto &v : lv) out.push_back(v.L->N);
+    else if (what == "mg.rho")
+      for (auto &v : lv) {
+        if (v.smoothed) out.push_back(v.rho);
+      }
+    else if (what == "mg.coarseIters")
+      out.assign(coarseIters.begin(), coarseIters.end());
+    else if (what == "mg.degrees")
+      for (auto &v : lv) {
+        if (v.smoothed) { out.push_back(v.down); out.push_back(v.up); }
+      }
+    else
+      throw Error(NRSG_ERR_INVALID, "unknown array '" + what + "'");
+    return out;
+  }
+
+  long long level_size(int level) override { return lv.at(level).L->Nlocal; }
+
+  void schwarz(int level, const double *u, double *Su) override
+  {
+    auto &v = lv.at(level);
+    const long long n = v.L->Nlocal;
+    launch_copy_cast<double, T>(n, u, sRes.p, s);
+    apply_S(v, sRes.p, sRes2.p);
+    launch_copy_cast<T, double>(n, sRes2.p, Su, s);
+    NRSG_CUDA(cudaStreamSynchronize(s));
+  }
+};
+
+void Elliptic::mg_setup()
+{
+  if (opt.mgPrecision == "fp32" || opt.mgPrecision == "mixed")
+    mg.reset(new MGImpl<float>(*this));
+  else if (opt.mgPrecision == "fp64")
+    mg.reset(new MGImpl<double>(*this));
+  else
+    throw Error(NRSG_ERR_BAD_CONFIG, "mgPrecision must be fp64, fp32 or mixed");
+}
+void Elliptic::mg_apply(const double *r, double *zz)
+{
+  if (!mg) throw Error(NRSG_ERR_BAD_CONFIG, "multigrid not set up");
+  mg->apply(r, zz);
+}
 void Elliptic::mg_release() { mg.reset(); }
 std::vector<double> Elliptic::mg_get(const std::string &name)
 {
-  throw Error(NRSG_ERR_INVALID, "unknown array '" + name + "'");
+  if (!mg) throw Error(NRSG_ERR_INVALID, "no multigrid preconditioner");
+  return mg->info(name);
+}
+long long Elliptic::mg_level_size(int level)
+{
+  if (!mg) throw Error(NRSG_ERR_INVALID, "no multigrid preconditioner");
+  return mg->level_size(level);
+}
+void Elliptic::mg_schwarz(int level, const double *u, double *Su)
+{
+  if (!mg) throw Error(NRSG_ERR_INVALID, "no multigrid preconditioner");
+  mg->schwarz(level, u, Su);
 }
 
 } // namespace nrsg

@@ -1,0 +1,30 @@
+// Host-side p-multigrid setup helpers (mg_setup.cpp).
+#pragma once
+
+#include "elliptic.hpp"
+
+#include <map>
+#include <vector>
+
+namespace nrsg {
+
+struct MGPlan {
+  std::vector<int> orders;     // down-leg polynomial orders, finest first
+  std::map<int, int> down, up; // Chebyshev degree per order (-1 / absent: default)
+  int base = 0;                // 0 Jacobi, 1 ASM, 2 RAS
+  int kind = 0;                // 0 1st-kind, 1 4th-kind, 2 optimal 4th-kind Chebyshev
+};
+MGPlan plan_levels(const Options &o, int N);
+const std::vector<double> &opt4_betas(int degree);
+
+struct FdmLengths {
+  std::vector<double> left, mid, right; // [E][3] (x, y, z)
+};
+FdmLengths fdm_lengths(const FieldLevel &fine, const GatherMap &unmaskedFine);
+void fdm_1d_operator(const FieldLevel &L, int lbc, int rbc, double ll, double lm, double lr, std::vector<double> &S,
+                     std::vector<double> &lam);
+void fdm_halo_maps(const FieldLevel &L, std::vector<int> &haloSrc, std::vector<int> &haloPartner,
+                   std::vector<double> &wts);
+double hessenberg_spectral_radius(int n, const std::vector<double> &Hcol);
+
+} // namespace nrsg

@@ -1,0 +1,30 @@
+// Launchers of the p-multigrid kernels (kernels_mg.cu, kernels_vec.cu).
+#pragma once
+
+#include "nrsg_internal.hpp"
+
+namespace nrsg {
+
+template <typename T> void launch_coarsen(int Nf, int Nc, long long E, const T *R, const T *qf, T *qc, cudaStream_t s);
+template <typename T> void launch_prolong(int Nf, int Nc, long long E, const T *R, const T *qc, T *qf, cudaStream_t s);
+template <typename T>
+void launch_cheby1_update(long long n, T dc, T rc, const T *SAd, T *d, T *r, T *x, cudaStream_t s);
+template <typename T> void launch_cheby4_update(long long n, T beta, const T *Ad, const T *d, T *r, T *x, cudaStream_t s);
+template <typename T>
+void launch_fdm(int N, long long E, bool ras, const T *u, const int *haloSrc, const T *Sx, const T *Sy, const T *Sz,
+                const T *invL, const T *wts, T *Su, T *haloOut, cudaStream_t s);
+template <typename T>
+void launch_asm_combine(int N, long long E, const int *haloPartner, const T *haloOut, const T *wts, T *Su,
+                        cudaStream_t s);
+void launch_random_fill(long long n, unsigned long long seed, double *v, cudaStream_t s);
+
+// Jacobi-PCG in precision T with double scalars (coarse-level solve)
+template <typename T>
+void launch_pcg_rdotz(long long n, const T *w, const T *invDiag, const T *r, T *z, PcgScalars *sc, Reduce &red, int slot,
+                      cudaStream_t s);
+template <typename T> void launch_pcg_p(long long n, const T *z, T *p, const PcgScalars *sc, bool first, cudaStream_t s);
+template <typename T>
+void launch_pcg_xr(long long n, const T *w, const T *p, const T *Ap, T *x, T *r, PcgScalars *sc, Reduce &red, int slot,
+                   cudaStream_t s);
+
+} // namespace nrsg

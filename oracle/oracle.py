@@ -44,6 +44,11 @@ def lib():
         _lib.orc_solve.argtypes = [ctypes.c_void_p, D, D, D]
         _lib.orc_box_mesh.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double, D, L, I, ctypes.c_int]
         _lib.orc_box_rhs.argtypes = [ctypes.c_int] * 4 + [ctypes.c_ulonglong, D, D]
+        _lib.orc_mg_info.restype = ctypes.c_longlong
+        _lib.orc_mg_info.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p]
+        _lib.orc_mg_level_size.restype = ctypes.c_longlong
+        _lib.orc_mg_level_size.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        _lib.orc_mg_schwarz.argtypes = [ctypes.c_void_p, ctypes.c_int, D, D]
         _lib.orc_global_ids.argtypes = [ctypes.c_int, ctypes.c_longlong, L, L]
         _lib.orc_gll.argtypes = [ctypes.c_int, D, D]
         _lib.orc_dmatrix.argtypes = [ctypes.c_int, D]
@@ -167,12 +172,27 @@ class Elliptic:
         lib().orc_precond(self.h, _p(r, D), _p(z, D))
         return z
 
+    def mg_info(self, what):
+        n = lib().orc_mg_info(self.h, what.encode(), None)
+        out = np.zeros(n)
+        if n:
+            lib().orc_mg_info(self.h, what.encode(), out.ctypes.data_as(ctypes.c_void_p))
+        return out
+
+    def mg_schwarz(self, level, u):
+        n = lib().orc_mg_level_size(self.h, level)
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        assert u.size == n
+        out = np.zeros(n)
+        lib().orc_mg_schwarz(self.h, level, _p(u, D), _p(out, D))
+        return out
+
     def solve(self, rhs, x0=None):
         r = np.array(rhs, dtype=np.float64)
         x = np.zeros_like(r) if x0 is None else np.array(x0, dtype=np.float64)
         info = np.zeros(4)
         lib().orc_solve(self.h, _p(r, D), _p(x, D), _p(info, D))
-        return x, {"iters": int(info[0]), "res0": info[1], "res": info[2], "status": int(info[3]),
+        return x, {"iterations": int(info[0]), "res0": info[1], "res": info[2], "status": int(info[3]),
                    "history": self.get("history"), "r": r}
 
 

@@ -143,4 +143,13 @@ int orc_solve(void *h, double *r, double *x, double *info)
   return 0;
 }
 
+long long orc_mg_info(void *h, const char *what, double *out)
+{
+  auto v = mg_info(*(Elliptic *)h, what);
+  if (out) std::memcpy(out, v.data(), v.size() * sizeof(double));
+  return (long long)v.size();
+}
+long long orc_mg_level_size(void *h, int level) { return mg_level_size(*(Elliptic *)h, level); }
+void orc_mg_schwarz(void *h, int level, const double *u, double *Su) { mg_level_smooth_schwarz(*(Elliptic *)h, level, u, Su); }
+
 } // extern "C"

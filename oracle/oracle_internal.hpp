@@ -57,5 +57,8 @@ struct Elliptic {
 
 void mg_setup(Elliptic &el);
 void mg_apply(Elliptic &el, const double *r, double *z);
+std::vector<double> mg_info(const Elliptic &el, const std::string &what);
+void mg_level_smooth_schwarz(Elliptic &el, int level, const double *u, double *Su);
+long long mg_level_size(Elliptic &el, int level);
 
 } // namespace orc

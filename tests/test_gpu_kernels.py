@@ -129,8 +129,9 @@ def test_fused_pcg_update_and_dot(product_lib, torch_cuda):
     G.update_pcg_f64(n, dev(torch, w), dev(torch, p), dev(torch, Ap), alpha, xd, rd, out)
     torch.cuda.synchronize()
     r2 = r - alpha * Ap
-    assert np.allclose(rd.cpu().numpy(), r2, rtol=0, atol=0)
-    assert np.allclose(xd.cpu().numpy(), x + alpha * p, rtol=1e-16, atol=0)
+    # the device contracts r - alpha*Ap into one FMA: one rounding instead of two
+    assert np.max(np.abs(rd.cpu().numpy() - r2)) <= 2.3e-16 * np.max(np.abs(r2)) * 2
+    assert np.max(np.abs(xd.cpu().numpy() - (x + alpha * p))) <= 4.5e-16 * np.max(np.abs(x + alpha * p))
     assert abs(out.item() - np.sum(w * r2 * r2)) < 1e-12 * abs(np.sum(w * r2 * r2))
     G.weighted_inner_prod_f64(n, dev(torch, w), dev(torch, p), dev(torch, Ap), out)
     torch.cuda.synchronize()

@@ -1,0 +1,94 @@
+"""p-multigrid parity on the GPU against the CPU oracle.
+
+FP64 multigrid (mgPrecision=fp64, the plain form): same lambda_max estimates
+(1e-9 relative), same iteration counts, solutions within 1e-10 relative.
+FP32 multigrid (the reference's pfloat default): iteration counts within one,
+converged to the tolerance, solution within 1e-7 of the FP64 oracle solve."""
+import numpy as np
+import pytest
+
+import nekrs_gb300 as G
+from nekrs_gb300 import workloads as W
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+SCHED = {7: "p=7+degree=2,p=3+degree=2,p=1,p=3+degree=2,p=7+degree=2",
+         5: "p=5+degree=2,p=3+degree=2,p=1,p=3+degree=2,p=5+degree=2",
+         3: "p=3+degree=2,p=1,p=3+degree=2"}
+
+
+def solve_both(torch, N, n, opts, eps=0.3, seed=3):
+    VX, EToV, EToB = W.kershaw_box(n, eps=eps)
+    orc = O.Elliptic(N, VX, EToV, EToB, opts)
+    rhs = W.box_rhs(N, n, n, n, seed, orc.get("ggeo"))
+    xo, io = orc.solve(rhs)
+    el = G.Elliptic(N, VX, EToV, EToB, opts)
+    r = torch.from_numpy(rhs.copy()).cuda()
+    x = torch.zeros_like(r)
+    ig = el.solve(r, x)
+    torch.cuda.synchronize()
+    return orc, el, xo, io, x.cpu().numpy(), ig, rhs
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("smoother,solver", [("cheby+jac", "pcg"), ("cheby+asm", "pcg"), ("fourthcheby+asm", "pcg"),
+                                             ("fourthoptcheby+asm", "pcg"), ("cheby+ras", "pfcg"),
+                                             ("fourthoptcheby+ras", "pfgmres")])
+@pytest.mark.parametrize("N", [3, 7])
+def test_mg_fp64_parity(product_lib, oracle_mod, torch_cuda, smoother, solver, N):
+    opts = (f"solver={solver};preconditioner=multigrid;smootherType={smoother};mgPrecision=fp64;"
+            f"residualTol=1e-8+relative;maxIterations=200;pMGSchedule={SCHED[N]}")
+    orc, el, xo, io, xg, ig, _ = solve_both(torch_cuda, N, 3, opts)
+    assert np.allclose(el.get("mg.rho"), orc.mg_info("rho"), rtol=1e-9, atol=0)
+    assert list(el.get("mg.levels")) == list(orc.mg_info("levels"))
+    assert ig["status"] == 0 and io["status"] == 0
+    assert ig["iterations"] == io["iterations"]
+    assert rel(xg, xo) < 1e-10
+
+
+@pytest.mark.parametrize("smoother,solver", [("cheby+asm", "pcg"), ("fourthoptcheby+ras", "pfcg")])
+def test_mg_fp32_matches_fp64_oracle(product_lib, oracle_mod, torch_cuda, smoother, solver):
+    N, n = 7, 3
+    base = (f"solver={solver};preconditioner=multigrid;smootherType={smoother};residualTol=1e-8+relative;"
+            f"maxIterations=200;pMGSchedule={SCHED[N]}")
+    orc32, el, xo32, io32, xg, ig, rhs = solve_both(torch_cuda, N, n, base + ";mgPrecision=fp32")
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    orc64 = O.Elliptic(N, VX, EToV, EToB, base + ";mgPrecision=fp64")
+    xo64, io64 = orc64.solve(rhs)
+    assert np.allclose(el.get("mg.rho"), orc32.mg_info("rho"), rtol=1e-4)
+    assert abs(ig["iterations"] - io32["iterations"]) <= 1
+    assert ig["res"] <= 1e-8 * ig["res0"]
+    assert rel(xg, xo64) < 1e-7
+
+
+def test_default_levels_and_smoothed_coarse(product_lib, oracle_mod, torch_cuda):
+    # Chebyshev+Jacobi default levels for N=7 are 7,5,3,1 (determineMGLevels.cpp:81-96)
+    opts = ("solver=pcg;preconditioner=multigrid;smootherType=cheby+jac;mgPrecision=fp64;coarseSolver=smooth;"
+            "residualTol=1e-8+relative;maxIterations=300")
+    orc, el, xo, io, xg, ig, _ = solve_both(torch_cuda, 7, 2, opts)
+    assert list(el.get("mg.levels")) == [7, 5, 3, 1]
+    assert ig["iterations"] == io["iterations"]
+    assert rel(xg, xo) < 1e-10
+
+
+@pytest.mark.parametrize("smoother", ["cheby+asm", "cheby+ras"])
+@pytest.mark.parametrize("N", [2, 5, 7])
+def test_schwarz_smoother_parity(product_lib, oracle_mod, torch_cuda, smoother, N):
+    torch = torch_cuda
+    n = 3
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.5)
+    sched = f"p={N}+degree=2,p=1,p={N}+degree=2"
+    opts = (f"solver=pfcg;preconditioner=multigrid;smootherType={smoother};mgPrecision=fp64;pMGSchedule={sched}")
+    orc = O.Elliptic(N, VX, EToV, EToB, opts)
+    el = G.Elliptic(N, VX, EToV, EToB, opts)
+    u = np.random.default_rng(N).uniform(-1, 1, orc.Nlocal)
+    u = orc.mask(orc.gs(u) * orc.get("invDegree"))  # a continuous, masked field
+    ref = orc.mg_schwarz(0, u)
+    ud = torch.from_numpy(u).cuda()
+    out = torch.zeros_like(ud)
+    el.mg_smoother(0, ud, out)
+    assert np.max(np.abs(out.cpu().numpy() - ref)) < 1e-12 * np.max(np.abs(ref))
