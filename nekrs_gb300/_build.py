@@ -50,7 +50,20 @@ def build(force=False, verbose=False):
         raise RuntimeError("nvcc failed for: " + ", ".join(bad))
     if force or procs or not os.path.exists(LIB):
         subprocess.check_call([nvcc] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-o", LIB] + objs + ["-lcudart"])
+        _check_unresolved()
     return LIB
+
+
+def _check_unresolved():
+    """Fail the build if the library references a library-internal symbol it does not define."""
+    try:
+        out = subprocess.run(["nm", "-D", "--undefined-only", LIB], capture_output=True, text=True, check=True).stdout
+    except (OSError, subprocess.CalledProcessError):
+        return
+    missing = [ln.split()[-1] for ln in out.splitlines() if "nrsg" in ln]
+    if missing:
+        os.remove(LIB)
+        raise RuntimeError("unresolved library symbols: " + ", ".join(missing))
 
 
 if __name__ == "__main__":

@@ -219,6 +219,8 @@ NRSG_INST_BLAS(double)
 NRSG_INST_BLAS(float)
 template void launch_copy_cast<double, float>(long long, const double *, float *, cudaStream_t);
 template void launch_copy_cast<float, double>(long long, const float *, double *, cudaStream_t);
+template void launch_copy_cast<double, double>(long long, const double *, double *, cudaStream_t);
+template void launch_copy_cast<float, float>(long long, const float *, float *, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // PCG kernels with device-resident scalars
