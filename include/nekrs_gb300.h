@@ -122,6 +122,11 @@ int nrsg_host_setup_maps(int N, long long E, const long long *h_EToV, const int 
                          long long *h_maskedIds, double *h_invDegree, int *h_maskIds, long long *nmask, int *h_gsOff,
                          long long *ngroups, int *h_gsIds);
 
+/* Spectral radius of an n x n upper-Hessenberg matrix (column-major), the
+ * eigenvalue step of the Arnoldi lambda_max estimate
+ * (ellipticMultiGridLevelSetup.cpp:415-438, LAPACK dgeev there).  -1 on error. */
+double nrsg_host_hessenberg_rho(int n, const double *h_H);
+
 /* ---- kernel-level entry points (one launch each, on `stream`) ---------- */
 
 /* ellipticPartialAxCoeffHex3D (kernels/elliptic/ellipticPartialAxCoeffHex3D.okl),

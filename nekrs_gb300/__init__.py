@@ -56,6 +56,8 @@ def lib():
         L = ctypes.CDLL(LIB_PATH)
         L.nrsg_last_error.restype = ctypes.c_char_p
         L.nrsg_kernel_launches.restype = LL
+        L.nrsg_host_hessenberg_rho.restype = ctypes.c_double
+        L.nrsg_host_hessenberg_rho.argtypes = [ctypes.c_int, vp]
         L.nrsg_host_setup_maps.argtypes = [ctypes.c_int, LL] + [vp] * 10
         L.nrsg_elliptic_create.argtypes = [ctypes.POINTER(MeshDesc), ctypes.c_char_p, ctypes.POINTER(vp)]
         L.nrsg_elliptic_destroy.argtypes = [vp]
@@ -198,6 +200,12 @@ class Elliptic:
 def kernel_launches():
     """Kernels launched by the library so far in this process."""
     return lib().nrsg_kernel_launches()
+
+
+def host_hessenberg_rho(n, Hcol):
+    """Spectral radius of a column-major upper-Hessenberg matrix (host code of the library)."""
+    H = np.ascontiguousarray(Hcol, dtype=np.float64)
+    return lib().nrsg_host_hessenberg_rho(n, H.ctypes.data)
 
 
 def host_setup_maps(N, EToV, EToB):

@@ -14,6 +14,7 @@
 // norm for the convergence test.
 
 #include "elliptic.hpp"
+#include "mg_host.hpp"
 
 #include <chrono>
 #include <cmath>
@@ -458,6 +459,17 @@ long long nrsg_elliptic_mg_level_size(nrsg_elliptic *el, int level)
 }
 
 // ---- host-only setup (no device needed) -----------------------------------
+double nrsg_host_hessenberg_rho(int n, const double *h_H)
+{
+  if (n < 1 || !h_H) return -1.0;
+  try {
+    return nrsg::hessenberg_spectral_radius(n, std::vector<double>(h_H, h_H + (size_t)n * n));
+  } catch (const std::exception &e) {
+    nrsg::set_last_error(e.what());
+    return -1.0;
+  }
+}
+
 int nrsg_host_setup_maps(int N, long long E, const long long *h_EToV, const int *h_EToB, long long *h_ids,
                          long long *h_maskedIds, double *h_invDegree, int *h_maskIds, long long *nmask, int *h_gsOff,
                          long long *ngroups, int *h_gsIds)

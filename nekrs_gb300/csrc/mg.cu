@@ -219,6 +219,7 @@ template <typename T> struct MGImpl : public MGState {
     auto Vj = [&](int j) { return V.p + (size_t)j * n; };
     launch_scale_copy<double>(n, 1.0 / nv, vx.p, Vj(0), s);
     std::vector<double> H((size_t)k * k, 0.0);
+    int keff = k;
     for (int j = 0; j < k; ++j) {
       launch_copy_cast<double, T>(n, Vj(j), tq.p, s);
       level_op(v, tq.p, ta.p);
@@ -233,12 +234,21 @@ template <typename T> struct MGImpl : public MGState {
       if (j + 1 < k) {
         launch_wdot<double>(n, w, Vj(j + 1), nullptr, out, el.red, 4, s);
         const double nj = std::sqrt(read(out));
+        // invariant subspace (e.g. a level with a single free node): the
+        // leading (j+1) x (j+1) block already holds the exact eigenvalues
+        if (!(nj > 1e-13 * std::fabs(H[j + (size_t)j * k]))) {
+          keff = j + 1;
+          break;
+        }
         launch_scale_copy<double>(n, 1.0 / nj, Vj(j + 1), Vj(j + 1), s);
         H[j + 1 + (size_t)j * k] = nj;
       }
     }
     NRSG_CUDA(cudaStreamSynchronize(s));
-    return hessenberg_spectral_radius(k, H);
+    std::vector<double> Hk((size_t)keff * keff);
+    for (int c = 0; c < keff; ++c)
+      for (int r = 0; r < keff; ++r) Hk[r + (size_t)keff * c] = H[r + (size_t)k * c];
+    return hessenberg_spectral_radius(keff, Hk);
   }
 
   // --------------------------------------------------------------- operators

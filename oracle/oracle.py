@@ -49,6 +49,11 @@ def lib():
         _lib.orc_mg_level_size.restype = ctypes.c_longlong
         _lib.orc_mg_level_size.argtypes = [ctypes.c_void_p, ctypes.c_int]
         _lib.orc_mg_schwarz.argtypes = [ctypes.c_void_p, ctypes.c_int, D, D]
+        _lib.orc_mg_get.restype = ctypes.c_longlong
+        _lib.orc_mg_get.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_void_p]
+        _lib.orc_mg_transfer.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, D, D]
+        _lib.orc_hessenberg_rho.restype = ctypes.c_double
+        _lib.orc_hessenberg_rho.argtypes = [ctypes.c_int, D]
         _lib.orc_global_ids.argtypes = [ctypes.c_int, ctypes.c_longlong, L, L]
         _lib.orc_gll.argtypes = [ctypes.c_int, D, D]
         _lib.orc_dmatrix.argtypes = [ctypes.c_int, D]
@@ -187,6 +192,19 @@ class Elliptic:
         lib().orc_mg_schwarz(self.h, level, _p(u, D), _p(out, D))
         return out
 
+    def mg_get(self, level, name):
+        n = lib().orc_mg_get(self.h, level, name.encode(), None)
+        out = np.zeros(n)
+        if n:
+            lib().orc_mg_get(self.h, level, name.encode(), out.ctypes.data_as(ctypes.c_void_p))
+        return out
+
+    def mg_transfer(self, level, restrict, v, nout):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        out = np.zeros(nout)
+        lib().orc_mg_transfer(self.h, level, 1 if restrict else 0, _p(v, D), _p(out, D))
+        return out
+
     def solve(self, rhs, x0=None):
         r = np.array(rhs, dtype=np.float64)
         x = np.zeros_like(r) if x0 is None else np.array(x0, dtype=np.float64)
@@ -202,3 +220,8 @@ def box_rhs(N, nx, ny, nz, seed, ggeo):
     g = np.ascontiguousarray(ggeo, dtype=np.float64)
     lib().orc_box_rhs(N, nx, ny, nz, seed, _p(g, D), _p(rhs, D))
     return rhs
+
+
+def hessenberg_rho(n, Hcol):
+    Hcol = np.ascontiguousarray(Hcol, dtype=np.float64)
+    return lib().orc_hessenberg_rho(n, _p(Hcol, D))

@@ -152,4 +152,17 @@ long long orc_mg_info(void *h, const char *what, double *out)
 long long orc_mg_level_size(void *h, int level) { return mg_level_size(*(Elliptic *)h, level); }
 void orc_mg_schwarz(void *h, int level, const double *u, double *Su) { mg_level_smooth_schwarz(*(Elliptic *)h, level, u, Su); }
 
+long long orc_mg_get(void *h, int level, const char *name, double *out)
+{
+  auto v = mg_level_array(*(Elliptic *)h, level, name);
+  if (out) std::memcpy(out, v.data(), v.size() * sizeof(double));
+  return (long long)v.size();
+}
+void orc_mg_transfer(void *h, int level, int restrict_, const double *in, double *out)
+{
+  mg_level_transfer(*(Elliptic *)h, level, restrict_ != 0, in, out);
+}
+
+double orc_hessenberg_rho(int n, const double *H) { return hessenberg_rho_public(n, H); }
+
 } // extern "C"

@@ -60,5 +60,8 @@ void mg_apply(Elliptic &el, const double *r, double *z);
 std::vector<double> mg_info(const Elliptic &el, const std::string &what);
 void mg_level_smooth_schwarz(Elliptic &el, int level, const double *u, double *Su);
 long long mg_level_size(Elliptic &el, int level);
+std::vector<double> mg_level_array(Elliptic &el, int level, const std::string &name);
+double hessenberg_rho_public(int n, const double *Hcol);
+void mg_level_transfer(Elliptic &el, int level, bool restrict_, const double *in, double *out);
 
 } // namespace orc

@@ -998,6 +998,7 @@ template <typename T> static double max_eig(MGT<T> &M, MGLevel<T> &lv, unsigned 
   const double nv = std::sqrt(wdot<double>(n, w, v.data(), v.data()));
   for (long long i = 0; i < n; ++i) V[0][i] = 1.0 / nv * v[i];
   std::vector<T> vp(n), avp(n);
+  int keff = k;
   for (int j = 0; j < k; ++j) {
     for (long long i = 0; i < n; ++i) vp[i] = (T)V[j][i];
     level_op(M, lv, vp.data(), avp.data());
@@ -1010,12 +1011,21 @@ template <typename T> static double max_eig(MGT<T> &M, MGLevel<T> &lv, unsigned 
     }
     if (j + 1 < k) {
       const double nj = std::sqrt(wdot<double>(n, w, V[j + 1].data(), V[j + 1].data()));
+      // breakdown: invariant subspace reached, keep the leading block (the
+      // reference would hand NaN entries to dgeev and abort)
+      if (!(nj > 1e-13 * std::fabs(H[j + j * k]))) {
+        keff = j + 1;
+        break;
+      }
       for (long long q = 0; q < n; ++q) V[j + 1][q] *= 1.0 / nj;
       H[j + 1 + j * k] = nj;
     }
   }
+  std::vector<double> Hk((size_t)keff * keff);
+  for (int c = 0; c < keff; ++c)
+    for (int r = 0; r < keff; ++r) Hk[r + keff * c] = H[r + k * c];
   double rho = 0;
-  for (auto &ev : hessenberg_eigs(k, H)) rho = std::max(rho, std::abs(ev));
+  for (auto &ev : hessenberg_eigs(keff, Hk)) rho = std::max(rho, std::abs(ev));
   return rho;
 }
 
@@ -1191,4 +1201,68 @@ long long mg_level_size(Elliptic &el, int level)
   return el.mg->d.levels.at(level).L->Nlocal;
 }
 
+} // namespace orc
+
+namespace orc {
+// ---------------------------------------------------------------------------
+// accessors for parity tests
+// ---------------------------------------------------------------------------
+std::vector<double> mg_level_array(Elliptic &el, int level, const std::string &name)
+{
+  std::vector<double> out;
+  auto go = [&](auto &M) {
+    auto &lv = M.levels.at(level);
+    auto put = [&](const auto &v) { out.assign(v.begin(), v.end()); };
+    if (name == "R") put(lv.R);
+    else if (name == "Sx") put(lv.fdm.Sx);
+    else if (name == "Sy") put(lv.fdm.Sy);
+    else if (name == "Sz") put(lv.fdm.Sz);
+    else if (name == "invL") put(lv.fdm.invL);
+    else if (name == "wts") put(lv.fdm.wts);
+    else if (name == "extOff") put(lv.fdm.extOff);
+    else if (name == "extIds") put(lv.fdm.extIds);
+    else if (name == "ids") put(lv.L->ids);
+    else if (name == "gsOff") put(lv.L->gsOff);
+    else if (name == "gsIds") put(lv.L->gsIds);
+    else if (name == "maskIds") put(lv.L->maskIds);
+    else if (name == "invDegree") put(lv.L->invDegree);
+    else if (name == "invDiag") put(lv.invDiag);
+    else if (name == "ggeo") put(lv.L->ggeo);
+    else throw std::runtime_error("unknown MG array " + name);
+  };
+  if (el.mg->fp32) go(el.mg->f);
+  else go(el.mg->d);
+  return out;
+}
+
+void mg_level_transfer(Elliptic &el, int level, bool restrict_, const double *in, double *out)
+{
+  auto go = [&](auto &M) {
+    using T = typename std::decay<decltype(M.sRes)>::type::value_type;
+    auto &lc = M.levels.at(level);
+    const int Nfq = lc.Nf + 1, Ncq = lc.L->Nq;
+    const long long nf = lc.L->E * Nfq * Nfq * Nfq, nc = lc.L->E * Ncq * Ncq * Ncq;
+    if (restrict_) {
+      std::vector<T> a(in, in + nf), b(nc);
+      coarsen_apply(lc, a.data(), b.data());
+      for (long long i = 0; i < nc; ++i) out[i] = b[i];
+    } else {
+      std::vector<T> a(in, in + nc), b(out, out + nf);
+      prolong_apply(lc, a.data(), b.data());
+      for (long long i = 0; i < nf; ++i) out[i] = b[i];
+    }
+  };
+  if (el.mg->fp32) go(el.mg->f);
+  else go(el.mg->d);
+}
+} // namespace orc
+
+namespace orc {
+double hessenberg_rho_public(int n, const double *Hcol)
+{
+  std::vector<double> H(Hcol, Hcol + (size_t)n * n);
+  double r = 0;
+  for (auto &ev : hessenberg_eigs(n, H)) r = std::max(r, std::abs(ev));
+  return r;
+}
 } // namespace orc
