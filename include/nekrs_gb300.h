@@ -76,7 +76,8 @@ long long nrsg_kernel_launches(void);
  * style "key = value" lines (or ';'-separated): solver (pcg | pcg+flexible |
  * pfcg | pgmres+nVector=15 | pfgmres), residualTol (1e-8+relative),
  * maxIterations, preconditioner (none | jacobi | multigrid), smootherType,
- * pMGSchedule, coarseSolver, mgPrecision (fp64 | fp32 | mixed), lambda0,
+ * pMGSchedule, coarseSolver, mgPrecision (fp64 | fp32 | mixed), axPrecision
+ * (fp64 | fp32x2), lambda0,
  * lambda1, poisson, elementMap (trilinear). */
 int nrsg_elliptic_create(const nrsg_mesh_desc *mesh, const char *options, nrsg_elliptic **out);
 int nrsg_elliptic_destroy(nrsg_elliptic *el);
@@ -142,6 +143,16 @@ int nrsg_ax_trilinear_f64(int N, long long E, const double *d_VX, const double *
 int nrsg_ax_trilinear_f32(int N, long long E, const float *d_VX, const float *d_gllz, const float *d_gllw,
                           const float *d_D, float lambda0, float lambda1, int poisson, const float *d_q,
                           float *d_Aq, void *stream);
+
+/* FP64-accurate axhelm computed in FP32-pair arithmetic (about 48
+ * significant bits; GB300 runs FP32 at 64x its FP64 rate).  ggeo_pairs /
+ * D_pairs hold each FP64 value v as the float pair (hi, lo) with
+ * hi = (float)v, lo = (float)(v - hi) (see nrsg_split_pairs); q and Aq are
+ * FP64.  Same operator as nrsg_ax_stored_f64. */
+int nrsg_ax_fp32x2(int N, long long E, const void *d_ggeo_pairs, const void *d_D_pairs, double lambda0,
+                   double lambda1, int poisson, const double *d_q, double *d_Aq, void *stream);
+/* (hi, lo) float-pair split of n doubles (8 bytes per pair). */
+int nrsg_split_pairs(long long n, const double *d_x, void *d_pairs, void *stream);
 
 /* gatherScatterMany_doubleAdd (3rd_party/gslib/ogs/okl/gatherScatterMany.okl):
  * q[ids[off[g]..off[g+1]]] = sum over the group, for every group g. */

@@ -77,6 +77,8 @@ def lib():
         L.nrsg_ax_stored_f32.argtypes = [i, LL, vp, vp, f, f, i, vp, vp, vp]
         L.nrsg_ax_trilinear_f64.argtypes = [i, LL, vp, vp, vp, vp, d, d, i, vp, vp, vp]
         L.nrsg_ax_trilinear_f32.argtypes = [i, LL, vp, vp, vp, vp, f, f, i, vp, vp, vp]
+        L.nrsg_ax_fp32x2.argtypes = [i, LL, vp, vp, d, d, i, vp, vp, vp]
+        L.nrsg_split_pairs.argtypes = [LL, vp, vp, vp]
         L.nrsg_gs_add_f64.argtypes = [LL, vp, vp, vp, vp]
         L.nrsg_gs_add_f32.argtypes = [LL, vp, vp, vp, vp]
         L.nrsg_mask_f64.argtypes = [LL, vp, vp, vp]
@@ -246,6 +248,15 @@ def ax_trilinear_f64(N, E, VX, z, w, D, lambda0, lambda1, poisson, q, Aq, stream
 def ax_trilinear_f32(N, E, VX, z, w, D, lambda0, lambda1, poisson, q, Aq, stream=0):
     check(lib().nrsg_ax_trilinear_f32(N, E, _ptr(VX), _ptr(z), _ptr(w), _ptr(D), lambda0, lambda1, int(poisson),
                                       _ptr(q), _ptr(Aq), stream))
+
+
+def ax_fp32x2(N, E, ggeo_pairs, D_pairs, lambda0, lambda1, poisson, q, Aq, stream=0):
+    check(lib().nrsg_ax_fp32x2(N, E, _ptr(ggeo_pairs), _ptr(D_pairs), lambda0, lambda1, int(poisson), _ptr(q),
+                               _ptr(Aq), stream))
+
+
+def split_pairs(n, x, pairs, stream=0):
+    check(lib().nrsg_split_pairs(n, _ptr(x), _ptr(pairs), stream))
 
 
 def gs_add_f64(ngroups, off, ids, q, stream=0):

@@ -122,6 +122,17 @@ Elliptic::Elliptic(const nrsg_mesh_desc *m, const char *options)
   NRSG_CUDA(cudaEventCreate(&ev0));
   NRSG_CUDA(cudaEventCreate(&ev1));
 
+  if (opt.axPrecision == "fp32x2") {
+    if (opt.trilinear) throw Error(NRSG_ERR_BAD_CONFIG, "axPrecision = fp32x2 needs stored geometric factors");
+    ggeoPairs.alloc(fine.d_ggeo64.n);
+    launch_split_pairs((long long)fine.d_ggeo64.n, fine.d_ggeo64.p, ggeoPairs.p, stream);
+    std::vector<float2> dp(fine.Dh.size());
+    for (size_t q = 0; q < dp.size(); ++q) {
+      dp[q].x = (float)fine.Dh[q];
+      dp[q].y = (float)(fine.Dh[q] - (double)dp[q].x);
+    }
+    DPairs.upload(dp);
+  }
   if (opt.precon == "jacobi") {
     invDiag.alloc(n);
     launch_build_diag<double>(fine.N, fine.E, fine.d_ggeo64.p, fine.d_D64.p, opt.lambda0, opt.lambda1, opt.poisson,
@@ -148,7 +159,9 @@ Elliptic::~Elliptic()
 
 void Elliptic::ax(const double *q, double *Aq)
 {
-  if (opt.trilinear)
+  if (ggeoPairs.p)
+    launch_ax_fp32x2(fine.N, fine.E, ggeoPairs.p, DPairs.p, opt.lambda0, opt.lambda1, opt.poisson, q, Aq, stream);
+  else if (opt.trilinear)
     launch_ax_trilinear<double>(fine.N, fine.E, fine.d_VX64.p, fine.d_z64.p, fine.d_w64.p, fine.d_D64.p, opt.lambda0,
                                 opt.lambda1, opt.poisson, q, Aq, stream);
   else
@@ -516,6 +529,16 @@ int nrsg_ax_trilinear_f32(int N, long long E, const float *VX, const float *z, c
                           float l0, float l1, int poisson, const float *q, float *Aq, void *s)
 {
   NRSG_TRY(nrsg::launch_ax_trilinear<float>(N, E, VX, z, w, D, l0, l1, poisson != 0, q, Aq, (cudaStream_t)s))
+}
+int nrsg_ax_fp32x2(int N, long long E, const void *ggeo_pairs, const void *D_pairs, double l0, double l1, int poisson,
+                   const double *q, double *Aq, void *s)
+{
+  NRSG_TRY(nrsg::launch_ax_fp32x2(N, E, (const float2 *)ggeo_pairs, (const float2 *)D_pairs, l0, l1, poisson != 0, q,
+                                  Aq, (cudaStream_t)s))
+}
+int nrsg_split_pairs(long long n, const double *x, void *pairs, void *s)
+{
+  NRSG_TRY(nrsg::launch_split_pairs(n, x, (float2 *)pairs, (cudaStream_t)s))
 }
 int nrsg_gs_add_f64(long long ng, const int *off, const int *ids, double *q, void *s)
 {

@@ -46,6 +46,7 @@ struct Elliptic {
 
   // Krylov workspace (elliptic.h:240-262 slices)
   DevBuf<double> p, z, Ap, x0, invDiag;
+  DevBuf<float2> ggeoPairs, DPairs;     // axPrecision = fp32x2
   DevBuf<double> io_r, io_x;            // staging for the host-buffer solve
   DevBuf<PcgScalars> d_scal;
   PcgScalars *h_scal = nullptr;          // pinned

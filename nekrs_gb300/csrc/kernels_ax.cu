@@ -380,3 +380,208 @@ void launch_geofac(int N, long long E, const double *VX, const double *gllz, con
 }
 
 } // namespace nrsg
+
+namespace nrsg {
+
+// ===========================================================================
+// FP64-accurate axhelm in FP32-pair arithmetic (for the FP64 outer operator).
+//
+// GB300 executes FP32 at 64x the FP64 rate.  This kernel computes the same
+// A q as ax_stored_kernel<double> with every value carried as an unevaluated
+// sum hi + lo of two floats (about 48 significant bits): products are formed
+// exactly with fmaf (TwoProduct), sums are accumulated with Knuth's TwoSum
+// and the rounding errors are carried in a second float.  D and the geometric
+// factors are split once at setup; q is split on load and A q is returned as
+// the double hi + lo.  Accuracy is about 2^-47 relative per term (FP64: 2^-53),
+// i.e. ~1e-14 on the operator; see the parity tests for the measured error.
+// ===========================================================================
+namespace {
+struct F2 {
+  float s, t; // running sum (s) and carried error (t)
+};
+__device__ __forceinline__ void acc_prod(F2 &a, float xh, float xl, float yh, float yl)
+{
+  const float p = xh * yh;
+  float e = fmaf(xh, yh, -p);
+  e = fmaf(xh, yl, e);
+  e = fmaf(xl, yh, e);
+  const float u = a.s + p;
+  const float bb = u - a.s;
+  const float err = (a.s - (u - bb)) + (p - bb);
+  a.s = u;
+  a.t += err + e;
+}
+__device__ __forceinline__ void norm2(F2 a, float &hi, float &lo)
+{
+  hi = a.s + a.t;
+  lo = a.t - (hi - a.s);
+}
+__device__ __forceinline__ void split_d(double x, float &hi, float &lo)
+{
+  hi = __double2float_rn(x);
+  lo = __double2float_rn(x - (double)hi);
+}
+} // namespace
+
+template <int NQ, bool POISSON>
+__global__ void __launch_bounds__(NQ *NQ *AxShape<NQ>::epb)
+    ax_fp32x2_kernel(long long E, const float2 *__restrict__ ggeo, const float2 *__restrict__ D, float2 lam0,
+                     float2 lam1, const double *__restrict__ q, double *__restrict__ Aq)
+{
+  constexpr int EPB = AxShape<NQ>::epb;
+  constexpr int NP = NQ * NQ * NQ;
+  __shared__ float s_Dh[NQ][NQ + 1], s_Dl[NQ][NQ + 1];
+  __shared__ float s_qh[EPB][NQ][NQ], s_ql[EPB][NQ][NQ];
+  __shared__ float s_Grh[EPB][NQ][NQ], s_Grl[EPB][NQ][NQ];
+  __shared__ float s_Gsh[EPB][NQ][NQ], s_Gsl[EPB][NQ][NQ];
+
+  const int t = threadIdx.x;
+  const int i = t % NQ, j = t / NQ;
+  const int el = threadIdx.y;
+  const long long e = (long long)blockIdx.x * EPB + el;
+  const bool active = e < E;
+  if (el == 0) {
+    const float2 d = D[j * NQ + i];
+    s_Dh[j][i] = d.x;
+    s_Dl[j][i] = d.y;
+  }
+  float qh[NQ], ql[NQ];
+  F2 aq[NQ];
+  const long long base = e * NP + t;
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    split_d(active ? q[base + k * NQ * NQ] : 0.0, qh[k], ql[k]);
+    aq[k].s = 0.f;
+    aq[k].t = 0.f;
+  }
+  __syncthreads();
+  const float2 *g = ggeo + e * 7 * NP + t;
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    float2 G00 = {0, 0}, G01 = {0, 0}, G11 = {0, 0}, G12 = {0, 0}, G02 = {0, 0}, G22 = {0, 0}, GWJ = {0, 0};
+    if (active) {
+      const int o = k * NQ * NQ;
+      G00 = g[0 * NP + o];
+      G01 = g[1 * NP + o];
+      G11 = g[2 * NP + o];
+      G12 = g[3 * NP + o];
+      G02 = g[4 * NP + o];
+      G22 = g[5 * NP + o];
+      if (!POISSON) GWJ = g[6 * NP + o];
+    }
+    s_qh[el][j][i] = qh[k];
+    s_ql[el][j][i] = ql[k];
+    F2 at = {0.f, 0.f};
+#pragma unroll
+    for (int m = 0; m < NQ; ++m) acc_prod(at, s_Dh[k][m], s_Dl[k][m], qh[m], ql[m]);
+    __syncthreads();
+    F2 ar = {0.f, 0.f}, as = {0.f, 0.f};
+#pragma unroll
+    for (int m = 0; m < NQ; ++m) {
+      acc_prod(ar, s_Dh[i][m], s_Dl[i][m], s_qh[el][j][m], s_ql[el][j][m]);
+      acc_prod(as, s_Dh[j][m], s_Dl[j][m], s_qh[el][m][i], s_ql[el][m][i]);
+    }
+    float rh, rl, sh, sl, th, tl;
+    norm2(ar, rh, rl);
+    norm2(as, sh, sl);
+    norm2(at, th, tl);
+    F2 gr = {0.f, 0.f}, gs = {0.f, 0.f}, gt = {0.f, 0.f};
+    acc_prod(gr, G00.x, G00.y, rh, rl);
+    acc_prod(gr, G01.x, G01.y, sh, sl);
+    acc_prod(gr, G02.x, G02.y, th, tl);
+    acc_prod(gs, G01.x, G01.y, rh, rl);
+    acc_prod(gs, G11.x, G11.y, sh, sl);
+    acc_prod(gs, G12.x, G12.y, th, tl);
+    acc_prod(gt, G02.x, G02.y, rh, rl);
+    acc_prod(gt, G12.x, G12.y, sh, sl);
+    acc_prod(gt, G22.x, G22.y, th, tl);
+    float grh, grl, gsh, gsl, gth, gtl;
+    norm2(gr, grh, grl);
+    norm2(gs, gsh, gsl);
+    norm2(gt, gth, gtl);
+    if (lam0.x != 1.f || lam0.y != 0.f) {
+      F2 a = {0.f, 0.f}, b = {0.f, 0.f}, c = {0.f, 0.f};
+      acc_prod(a, lam0.x, lam0.y, grh, grl);
+      acc_prod(b, lam0.x, lam0.y, gsh, gsl);
+      acc_prod(c, lam0.x, lam0.y, gth, gtl);
+      norm2(a, grh, grl);
+      norm2(b, gsh, gsl);
+      norm2(c, gth, gtl);
+    }
+    s_Grh[el][j][i] = grh;
+    s_Grl[el][j][i] = grl;
+    s_Gsh[el][j][i] = gsh;
+    s_Gsl[el][j][i] = gsl;
+    F2 auk = {0.f, 0.f};
+    if (!POISSON) {
+      F2 w = {0.f, 0.f};
+      acc_prod(w, GWJ.x, GWJ.y, lam1.x, lam1.y);
+      float wh, wl;
+      norm2(w, wh, wl);
+      acc_prod(auk, wh, wl, qh[k], ql[k]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < NQ; ++m) {
+      acc_prod(auk, s_Dh[m][j], s_Dl[m][j], s_Gsh[el][m][i], s_Gsl[el][m][i]);
+      acc_prod(aq[m], s_Dh[k][m], s_Dl[k][m], gth, gtl);
+      acc_prod(auk, s_Dh[m][i], s_Dl[m][i], s_Grh[el][j][m], s_Grl[el][j][m]);
+    }
+    float uh, ul;
+    norm2(auk, uh, ul);
+    acc_prod(aq[k], uh, ul, 1.f, 0.f);
+    __syncthreads();
+  }
+  if (active) {
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      float h, l;
+      norm2(aq[k], h, l);
+      Aq[base + k * NQ * NQ] = (double)h + (double)l;
+    }
+  }
+}
+
+void launch_ax_fp32x2(int N, long long E, const float2 *ggeo, const float2 *D, double lambda0, double lambda1,
+                      bool poisson, const double *q, double *Aq, cudaStream_t s)
+{
+  if (E <= 0) return;
+  float2 l0, l1;
+  l0.x = (float)lambda0;
+  l0.y = (float)(lambda0 - (double)l0.x);
+  l1.x = (float)lambda1;
+  l1.y = (float)(lambda1 - (double)l1.x);
+#define NRSG_AXD(NQ)                                                                                       \
+  {                                                                                                        \
+    constexpr int EPB = AxShape<NQ>::epb;                                                                  \
+    dim3 blk(NQ * NQ, EPB);                                                                                \
+    const unsigned grid = (unsigned)((E + EPB - 1) / EPB);                                                 \
+    if (poisson)                                                                                           \
+      ax_fp32x2_kernel<NQ, true><<<grid, blk, 0, s>>>(E, ggeo, D, l0, l1, q, Aq);                          \
+    else                                                                                                   \
+      ax_fp32x2_kernel<NQ, false><<<grid, blk, 0, s>>>(E, ggeo, D, l0, l1, q, Aq);                         \
+  }
+  NRSG_DISPATCH_NQ(N, NRSG_AXD)
+#undef NRSG_AXD
+  NRSG_CHECK_LAUNCH();
+}
+
+// split doubles into (hi, lo) float pairs
+__global__ void split_pairs_kernel(long long n, const double *__restrict__ x, float2 *__restrict__ y)
+{
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    float h, l;
+    split_d(x[i], h, l);
+    y[i] = make_float2(h, l);
+  }
+}
+void launch_split_pairs(long long n, const double *x, float2 *y, cudaStream_t s)
+{
+  if (n <= 0) return;
+  long long b = (n + 255) / 256;
+  if (b > 152 * 16) b = 152 * 16;
+  split_pairs_kernel<<<(unsigned)b, 256, 0, s>>>(n, x, y);
+  NRSG_CHECK_LAUNCH();
+}
+
+} // namespace nrsg

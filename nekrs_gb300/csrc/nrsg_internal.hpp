@@ -97,6 +97,7 @@ struct Options {
   double coarseTol = 1e-4;
   int coarseMaxIter = 200;
   std::string mgPrecision = "fp64"; // fp64 | fp32 | mixed
+  std::string axPrecision = "fp64"; // fine-level operator: fp64 | fp32x2 (FP64-accurate FP32-pair arithmetic)
   bool poisson = true;
   double lambda0 = 1.0, lambda1 = 0.0;
   bool trilinear = false;
@@ -143,6 +144,10 @@ template <typename T> void launch_mask(long long n, const int *ids, T *q, cudaSt
 template <typename T>
 void launch_build_diag(int N, long long E, const T *ggeo, const T *D, T lambda0, T lambda1, bool poisson, T *diag,
                        cudaStream_t s);
+// FP64-accurate Ax in FP32-pair arithmetic: ggeo/D as (hi, lo) float pairs, q and Aq FP64
+void launch_ax_fp32x2(int N, long long E, const float2 *ggeo, const float2 *D, double lambda0, double lambda1,
+                      bool poisson, const double *q, double *Aq, cudaStream_t s);
+void launch_split_pairs(long long n, const double *x, float2 *y, cudaStream_t s);
 void launch_geofac(int N, long long E, const double *VX, const double *gllz, const double *gllw, const double *D,
                    double *ggeo, cudaStream_t s);
 

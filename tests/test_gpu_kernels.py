@@ -140,3 +140,25 @@ def test_fused_pcg_update_and_dot(product_lib, torch_cuda):
     torch.cuda.synchronize()
     assert out.item() == v1  # deterministic
     assert abs(v1 - np.sum(w * p * Ap)) < 1e-12 * abs(v1)
+
+
+@pytest.mark.parametrize("N", [1, 3, 5, 7, 9])
+@pytest.mark.parametrize("poisson", [True, False])
+def test_ax_fp32x2_is_fp64_accurate(product_lib, oracle_mod, torch_cuda, N, poisson):
+    """FP32-pair axhelm against the FP64 oracle: within 2e-13 of max |Aq| (FP64 kernel: 1e-13)."""
+    torch = torch_cuda
+    VX, EToV, EToB = W.kershaw_box(3, 2, 2, eps=0.3)
+    l0, l1 = (1.0, 0.0) if poisson else (1.3, 0.7)
+    el = O.Elliptic(N, VX, EToV, EToB, f"preconditioner=jacobi;poisson={int(poisson)};lambda0={l0};lambda1={l1}")
+    q = np.random.default_rng(N + 100).uniform(-1, 1, el.Nlocal)
+    ref = el.ax(q)
+    g = dev(torch, el.get("ggeo"))
+    D = dev(torch, el.get("D"))
+    gp = torch.zeros(2 * g.numel(), dtype=torch.float32, device="cuda")
+    Dp = torch.zeros(2 * D.numel(), dtype=torch.float32, device="cuda")
+    G.split_pairs(g.numel(), g, gp)
+    G.split_pairs(D.numel(), D, Dp)
+    out = torch.zeros(el.Nlocal, dtype=torch.float64, device="cuda")
+    G.ax_fp32x2(N, el.E, gp, Dp, l0, l1, poisson, dev(torch, q), out)
+    torch.cuda.synchronize()
+    assert relerr(out.cpu().numpy(), ref) < 2e-13

@@ -126,3 +126,24 @@ def test_status_codes(product_lib, torch_cuda):
     with pytest.raises(G.NrsgError) as e:
         G.Elliptic(N, VX, EToV, EToB, "preconditioner=bogus")
     assert e.value.code == 5
+
+
+@pytest.mark.parametrize("precon", ["jacobi", "multigrid"])
+def test_fp32x2_operator_solve_parity(product_lib, oracle_mod, torch_cuda, precon):
+    """Solve with the FP32-pair fine operator against the FP64 oracle: same iterations, 1e-10."""
+    extra = ";smootherType=cheby+asm;mgPrecision=fp64;pMGSchedule=p=5+degree=2,p=3+degree=2,p=1,p=3+degree=2,p=5+degree=2" \
+        if precon == "multigrid" else ""
+    base = f"preconditioner={precon};solver=pcg;residualTol=1e-8+relative;maxIterations=3000" + extra
+    N, n = 5, 3
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    orc = O.Elliptic(N, VX, EToV, EToB, base)
+    rhs = W.box_rhs(N, n, n, n, 21, orc.get("ggeo"))
+    xo, io = orc.solve(rhs)
+    el = G.Elliptic(N, VX, EToV, EToB, base + ";axPrecision=fp32x2")
+    torch = torch_cuda
+    r = torch.from_numpy(rhs.copy()).cuda()
+    x = torch.zeros_like(r)
+    ig = el.solve(r, x)
+    assert ig["status"] == 0
+    assert abs(ig["iterations"] - io["iterations"]) <= 1
+    assert rel(x.cpu().numpy(), xo) < 1e-10
