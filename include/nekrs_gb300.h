@@ -170,6 +170,18 @@ int nrsg_update_pcg_f64(long long n, const double *d_invDegree, const double *d_
 int nrsg_weighted_inner_prod_f64(long long n, const double *d_w, const double *d_a, const double *d_b,
                                  double *d_out, void *stream);
 
+/* Allocation-free variant of nrsg_weighted_inner_prod_f64 for callers that
+ * cannot call cudaMalloc (their device memory is owned by another allocator,
+ * or they must not take an allocation's implicit device synchronisation).
+ * This entry point has no counterpart in the reference.  Its scratch (8192
+ * partial sums + a counter, 64 KiB per GPU, held until exit) is a fixed
+ * array inside this library; n is limited to 67,108,864 and larger n returns
+ * NRSG_ERR_INVALID.  The first call on a device looks up the array's device
+ * address and should come before any stream capture.  Calls share the array:
+ * calls that overlap on the GPU race. */
+int nrsg_weighted_inner_prod_f64_noalloc(long long n, const double *d_w, const double *d_a, const double *d_b,
+                                         double *d_out, void *stream);
+
 /* Geometric factors (kernels/mesh/geometricFactorsHex3D.okl) from trilinear
  * vertices: writes ggeo [E][7][Np]. */
 int nrsg_geometric_factors_f64(int N, long long E, const double *d_VX, double *d_ggeo, void *stream);
