@@ -1,16 +1,19 @@
-"""Benchmark of the GB300 elliptic solve (Poisson DOFs/s, time-to-tolerance).
+"""Benchmark of the GB300 elliptic solve (Poisson DOFs/s and time-to-tolerance).
 
 One "step" is one complete ellipticSolve of the workload's Kershaw-box Poisson
-problem to the relative tolerance, starting from the seeded right-hand side
-already resident in HBM (`value`), and the same solve through the host-buffer
-C ABI call with the host<->device copies inside the timed region (`e2e`).
-DOF = E*N^3 per solve (the reference's convention, examples/kershaw/kershaw.udf).
+problem to its relative tolerance, starting from the seeded right-hand side
+already resident in HBM (`value`); `e2e` is the same solve through the
+host-buffer C ABI call (nrsg_elliptic_solve_host) with the host<->device copies
+of the right-hand side, initial guess, residual and solution inside the timed
+region.  DOF = E*N^3 per solve (the reference's convention,
+examples/kershaw/kershaw.udf).  For the mixed-precision workload the line also
+carries the plain FP64 form of the same problem ("fp64_plain": FP64
+multigrid and FP64 operator) and the mixed solution's error against it.
 
     python bench.py [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
 
-Under torchrun (N>1) every rank solves its own replica (no data-path
-collective: independent problems), `value` sums the ranks' DOFs and the time
-is the max over ranks.
+Under torchrun (N>1) every rank solves its own replica (independent problems,
+no data-path collective); `value` sums the ranks' DOFs over the max time.
 """
 import argparse
 import json
@@ -25,17 +28,37 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+SCHED7 = "p=7+degree=2,p=3+degree=2,p=1,p=3+degree=2,p=7+degree=2"
+PMG = "preconditioner=multigrid;smootherType=cheby+asm;pMGSchedule=" + SCHED7 + ";coarseSolver=jpcg;coarseTol=1e-4"
+
+# name: (elements per side, N, eps, options, description)
 WORKLOADS = {
-    # name: (elements per side, N, eps, options, description)
-    "kershaw16-n7-jacobi": (16, 7, 0.3, "preconditioner=jacobi;solver=pcg;residualTol=1e-8+relative;maxIterations=20000",
-                            "Kershaw box E=16^3 N=7 eps=0.3, Jacobi-PCG FP64 to 1e-8 relative"),
-    "kershaw32-n7-jacobi": (32, 7, 0.3, "preconditioner=jacobi;solver=pcg;residualTol=1e-8+relative;maxIterations=20000",
-                            "Kershaw box E=32^3 N=7 eps=0.3, Jacobi-PCG FP64 to 1e-8 relative"),
-    "kershaw8-n7-jacobi": (8, 7, 0.3, "preconditioner=jacobi;solver=pcg;residualTol=1e-8+relative;maxIterations=20000",
-                           "Kershaw box E=8^3 N=7 eps=0.3, Jacobi-PCG FP64 to 1e-8 relative"),
+    "kershaw48-n7-mixed": (48, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG +
+                           ";mgPrecision=mixed",
+                           "Kershaw box E=48^3 N=7 eps=0.3: FP64 flexible PCG, FP32 pMG 7/3/1 (Chebyshev(2)+ASM "
+                           "FDM, coarse Jacobi-PCG 1e-4), FP64-accurate FP32-pair fine operator, to 1e-8 relative"),
+    "kershaw32-n7-fp64": (32, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG +
+                          ";mgPrecision=fp64;axPrecision=fp64",
+                          "Kershaw box E=32^3 N=7 eps=0.3: plain FP64 pMG-PCG (flexible), Chebyshev(2)+ASM, "
+                          "coarse Jacobi-PCG 1e-4, to 1e-8 relative"),
+    "kershaw16-n7-jacobi": (16, 7, 0.3, "preconditioner=jacobi;solver=pcg;residualTol=1e-8+relative;"
+                            "maxIterations=20000", "Kershaw box E=16^3 N=7 eps=0.3, Jacobi-PCG FP64 to 1e-8"),
+    "kershaw8-n7-jacobi": (8, 7, 0.3, "preconditioner=jacobi;solver=pcg;residualTol=1e-8+relative;"
+                           "maxIterations=20000", "Kershaw box E=8^3 N=7 eps=0.3, Jacobi-PCG FP64 to 1e-8"),
 }
-DEFAULT_WORKLOAD = "kershaw16-n7-jacobi"
+DEFAULT_WORKLOAD = "kershaw48-n7-mixed"
+# iterations to tolerance of each workload (measured on the GPU; the solvers are parity-tested against the
+# oracle), used by the reference arm to project its per-iteration CPU time to a full solve
+EXPECTED_ITERS = {"kershaw48-n7-mixed": 76, "kershaw32-n7-fp64": 70, "kershaw16-n7-jacobi": 1632,
+                  "kershaw8-n7-jacobi": 800}
 METRIC = "Poisson DOFs/s (E*N^3 / time-to-tolerance)"
+FP64_PLAIN = {"mgPrecision=mixed": "mgPrecision=fp64;axPrecision=fp64"}
+
+
+def plain_fp64_options(opts):
+    for k, v in FP64_PLAIN.items():
+        opts = opts.replace(k, v)
+    return opts
 
 
 def load_peaks():
@@ -81,7 +104,7 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, smax, reasons = [], None, set()
+        sm, smax, reasons, power = [], None, set(), []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for r in self.rows:
             if len(r) < 9:
@@ -89,86 +112,131 @@ class ClockSampler:
             try:
                 sm.append(float(r[1]))
                 smax = float(r[2])
+                power.append(float(r[3]))
             except ValueError:
                 continue
             for k, nm in enumerate(names):
                 if r[5 + k].lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "power_w_max": max(power) if power else None}
 
 
 def dist_info():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
-def cpu_baseline(nel, N, eps, opts, gpu_iters, budget_s=20.0):
-    """Oracle (CPU port, all host threads) on the same workload: time a bounded
-    number of PCG iterations and project the solve time with the GPU's
-    iteration count."""
+def cpu_sample(nel, N, eps, opts, gpu_iters, budget_s=20.0, probe_iters=2):
+    """CPU oracle (all host threads) on the same workload: it is timed on a box
+    small enough to set up in seconds (same N, options, element deformation),
+    per Krylov iteration, scaled by the element count to the workload and
+    projected to the GPU's iteration count."""
     from oracle import oracle as O
     from nekrs_gb300 import workloads as W
 
-    VX, EToV, EToB = W.kershaw_box(nel, eps=eps)
-    probe = 3
-    o = O.Elliptic(N, VX, EToV, EToB, opts.replace("maxIterations=20000", f"maxIterations={probe}"))
-    rhs = W.box_rhs(N, nel, nel, nel, 1234, o.get("ggeo"))
+    E = nel ** 3
+    nel_c = nel
+    while nel_c ** 3 * (N + 1) ** 3 > 2_500_000 and nel_c > 2:
+        nel_c //= 2
+    VX, EToV, EToB = W.kershaw_box(nel_c, eps=eps)
+    mx = "maxIterations=%d"
+    base = opts.split("maxIterations=")[0]
+    tail = opts.split("maxIterations=")[1].split(";", 1)
+    tail = ";" + tail[1] if len(tail) > 1 else ""
+    o = O.Elliptic(N, VX, EToV, EToB, base + (mx % probe_iters) + tail)
+    rhs = W.box_rhs(N, nel_c, nel_c, nel_c, 1234, o.get("ggeo"))
     t = time.perf_counter()
-    o.solve(rhs)
-    per_it = (time.perf_counter() - t) / probe
-    k = int(max(probe, min(gpu_iters, budget_s / max(per_it, 1e-9))))
-    o2 = O.Elliptic(N, VX, EToV, EToB, opts.replace("maxIterations=20000", f"maxIterations={k}"))
+    _, info = o.solve(rhs)
+    per_it = (time.perf_counter() - t) / max(info["iterations"], 1)
+    k = int(max(probe_iters, min(gpu_iters, budget_s / max(per_it, 1e-9))))
+    o2 = O.Elliptic(N, VX, EToV, EToB, base + (mx % k) + tail)
     t = time.perf_counter()
     _, info = o2.solve(rhs)
     dt = time.perf_counter() - t
-    per_it = dt / max(info["iterations"], 1)
+    per_it = dt / max(info["iterations"], 1) * (E / nel_c ** 3)
     solve_s = per_it * gpu_iters
-    dofs = nel ** 3 * N ** 3
-    return {"value": dofs / solve_s, "unit": "DOF/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": f"{info['iterations']} PCG iterations of the same solve on the CPU oracle "
-                      f"({dt:.1f} s), projected to the GPU's {gpu_iters} iterations",
+    return {"value": E * N ** 3 / solve_s, "unit": "DOF/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": (f"{info['iterations']} Krylov iterations of the same solver on a {nel_c}^3-element Kershaw box "
+                       f"({dt:.1f} s on the CPU oracle), scaled per iteration by the element count to {nel}^3 and "
+                       f"projected to the GPU's {gpu_iters} iterations"),
             "seconds_per_iteration": per_it}
 
 
 def run_reference(args, nel, N, eps, opts, desc):
-    rank, world, _ = dist_info()
+    rank, _, _ = dist_info()
     if rank != 0:
         return
-    # iterations of the full solve are needed to project; run the oracle for a bounded sample each step
-    from oracle import oracle as O
-    from nekrs_gb300 import workloads as W
-
-    VX, EToV, EToB = W.kershaw_box(nel, eps=eps)
-    sample_iters = 10
-    o = O.Elliptic(N, VX, EToV, EToB, opts.replace("maxIterations=20000", f"maxIterations={sample_iters}"))
-    rhs = W.box_rhs(N, nel, nel, nel, 1234, o.get("ggeo"))
-    # iteration count to tolerance from a converged oracle run is too slow for big boxes; use the
-    # product's recorded count when available, else the sample count
-    iters_env = int(os.environ.get("NRSG_REF_ITERS", "0"))
-    times = []
+    iters = int(os.environ.get("NRSG_REF_ITERS", "0")) or EXPECTED_ITERS.get(args.workload, 1)
+    vals = []
+    sample = None
     for s in range(args.warmup + args.steps):
-        t = time.perf_counter()
-        _, info = o.solve(rhs)
-        dt = time.perf_counter() - t
+        cb = cpu_sample(nel, N, eps, opts, iters, budget_s=8.0)
         if s >= args.warmup:
-            times.append(dt / max(info["iterations"], 1))
-    per_it = float(np.mean(times))
-    iters = iters_env if iters_env > 0 else sample_iters
-    dofs = nel ** 3 * N ** 3
-    value = dofs / (per_it * iters)
+            vals.append(cb["value"])
+            sample = cb
+    value = float(np.mean(vals))
     line = {"metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": per_it * sample_iters * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "impl": "reference",
+            "warmup": args.warmup, "ms_per_step": nel ** 3 * N ** 3 / value * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": {"workload": args.workload, "description": desc, "elements": nel ** 3, "N": N},
-            "cpu_baseline": {"value": value, "unit": "DOF/s", "cores": os.cpu_count(), "kind": "port",
-                             "sample": f"{sample_iters} PCG iterations per step on the CPU oracle, projected to "
-                                       f"{iters} iterations"},
+            "cpu_baseline": {"value": value, "unit": "DOF/s", "cores": sample["cores"], "kind": "port",
+                             "sample": sample["sample"] + " (iteration count of the GPU solve of this workload)"},
             "e2e": {"value": value, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def time_kernel(fn, stream, reps=10):
+    import torch
+
+    for _ in range(3):
+        fn()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(reps):
+        fn()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) / 1e3 / reps
+
+
+def kernel_rooflines(G, el, N, E):
+    """Achieved algorithmic GB/s of the fine-level operator kernels, CUDA events on their stream."""
+    import torch
+
+    Np = (N + 1) ** 3
+    n = E * Np
+    peak, src = load_peaks()
+    stream = torch.cuda.current_stream()
+    cs = stream.cuda_stream
+    g64 = torch.from_numpy(el.get("ggeo")).cuda()
+    D64 = torch.from_numpy(el.get("D")).cuda()
+    q64 = torch.rand(n, dtype=torch.float64, device="cuda")
+    a64 = torch.empty_like(q64)
+    out = {}
+    flops = float(E) * (12 * (N + 1) * Np + 15 * Np + Np)
+    t = time_kernel(lambda: G.ax_stored_f64(N, E, g64, D64, 1.0, 0.0, True, q64, a64, cs), stream)
+    out["ax_stored_f64"] = {"launch_ms": t * 1e3, "achieved": 64.0 * n / t / 1e9, "unit": "GB/s",
+                            "algorithmic_bytes": 64.0 * n, "fp64_tflops": flops / t / 1e12}
+    gp = torch.empty(2 * g64.numel(), dtype=torch.float32, device="cuda")
+    Dp = torch.empty(2 * D64.numel(), dtype=torch.float32, device="cuda")
+    G.split_pairs(g64.numel(), g64, gp, cs)
+    G.split_pairs(D64.numel(), D64, Dp, cs)
+    t = time_kernel(lambda: G.ax_fp32x2(N, E, gp, Dp, 1.0, 0.0, True, q64, a64, cs), stream)
+    out["ax_fp32x2"] = {"launch_ms": t * 1e3, "achieved": 64.0 * n / t / 1e9, "unit": "GB/s",
+                        "algorithmic_bytes": 64.0 * n, "fp64_equiv_tflops": flops / t / 1e12}
+    del gp
+    g32 = g64.float()
+    del g64
+    D32 = D64.float()
+    q32 = q64.float()
+    a32 = torch.empty_like(q32)
+    t = time_kernel(lambda: G.ax_stored_f32(N, E, g32, D32, 1.0, 0.0, True, q32, a32, cs), stream)
+    out["ax_stored_f32"] = {"launch_ms": t * 1e3, "achieved": 32.0 * n / t / 1e9, "unit": "GB/s",
+                            "algorithmic_bytes": 32.0 * n}
+    for v in out.values():
+        v["frac_of_hbm"] = v["achieved"] / peak
+    return out, peak, src
 
 
 def main():
@@ -179,6 +247,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-plain", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     nel, N, eps, opts, desc = WORKLOADS[args.workload]
@@ -199,11 +268,13 @@ def main():
     import nekrs_gb300 as G
     from nekrs_gb300 import workloads as W
 
+    E = nel ** 3
+    dofs = E * N ** 3
     VX, EToV, EToB = W.kershaw_box(nel, eps=eps)
+    t0 = time.perf_counter()
     el = G.Elliptic(N, VX, EToV, EToB, opts)
-    ggeo = el.get("ggeo")
-    rhs = W.box_rhs(N, nel, nel, nel, 1234 + rank, ggeo)
-    del ggeo
+    setup_s = time.perf_counter() - t0
+    rhs = W.box_rhs(N, nel, nel, nel, 1234 + rank, el.get("ggeo"))
     rhs_d = torch.from_numpy(rhs).cuda()
     r = torch.empty_like(rhs_d)
     x = torch.zeros_like(rhs_d)
@@ -221,23 +292,20 @@ def main():
     clocks = ClockSampler(local)
     clocks.start()
     l0 = G.kernel_launches()
-    ms = []
     infos = []
     torch.cuda.synchronize()
     for _ in range(args.steps):
-        info = step()
-        ms.append(info["solve_ms"])
-        infos.append(info)
+        infos.append(step())
     torch.cuda.synchronize()
     launches = G.kernel_launches() - l0
     clk = clocks.stop()
-    t_step = float(np.mean(ms)) / 1e3
+    t_step = float(np.mean([i["solve_ms"] for i in infos])) / 1e3
     if world > 1:
         tt = torch.tensor([t_step], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         t_step = tt.item()
-    dofs = nel ** 3 * N ** 3
     value = dofs * world / t_step
+    x_mixed = x.cpu().numpy().copy()
 
     # ---- end to end through the host-buffer C ABI call (pinned host memory)
     rh = torch.from_numpy(rhs.copy()).pin_memory()
@@ -251,51 +319,55 @@ def main():
         if s >= args.warmup:
             e2e_t.append(time.perf_counter() - t)
     e2e_s = float(np.mean(e2e_t))
-    nbytes = rhs.nbytes
+    del rh, xh
 
-    # ---- roofline of the dominant kernel (fp64 stored-geometry Ax), CUDA events on its stream
-    E = nel ** 3
-    Np = (N + 1) ** 3
-    g_d = torch.from_numpy(el.get("ggeo")).cuda()
-    D_d = torch.from_numpy(el.get("D")).cuda()
-    q_d = torch.rand(E * Np, dtype=torch.float64, device="cuda")
-    a_d = torch.empty_like(q_d)
-    stream = torch.cuda.current_stream()
-    for _ in range(3):
-        G.ax_stored_f64(N, E, g_d, D_d, 1.0, 0.0, True, q_d, a_d, stream.cuda_stream)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = 10
-    torch.cuda.synchronize()
-    ev0.record(stream)
-    for _ in range(reps):
-        G.ax_stored_f64(N, E, g_d, D_d, 1.0, 0.0, True, q_d, a_d, stream.cuda_stream)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    ax_s = ev0.elapsed_time(ev1) / 1e3 / reps
-    bytes_per_launch = 64.0 * E * Np  # q 8 + Aq 8 + 6 G x 8 per point (Poisson, stored geometry)
-    flops_per_launch = float(E) * (12 * (N + 1) * Np + 15 * Np + Np)
-    peak, peak_kind = load_peaks()
-    achieved = bytes_per_launch / ax_s / 1e9
-    roof = {"bound": "hbm", "kernel": "ax_stored_kernel<double,%d,poisson>" % (N + 1), "achieved": achieved,
-            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-            "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-            "fp64_pipe": {"achieved_tflops": flops_per_launch / ax_s / 1e12, "nominal_peak_tflops": 1.25,
-                          "frac_of_nominal": flops_per_launch / ax_s / 1e12 / 1.25},
-            "launch_ms": ax_s * 1e3}
-    del g_d, q_d, a_d
+    extra = {}
+    if "mgPrecision=mixed" in opts and not args.no_fp64_plain:
+        del el
+        torch.cuda.empty_cache()
+        elp = G.Elliptic(N, VX, EToV, EToB, plain_fp64_options(opts))
+        for _ in range(1):
+            r.copy_(rhs_d)
+            x.zero_()
+            elp.solve(r, x)
+        r.copy_(rhs_d)
+        x.zero_()
+        ip = elp.solve(r, x)
+        xp = x.cpu().numpy()
+        extra["fp64_plain"] = {"value": dofs / (ip["solve_ms"] / 1e3), "unit": "DOF/s", "iterations": ip["iterations"],
+                               "time_to_tolerance_s": ip["solve_ms"] / 1e3,
+                               "options": plain_fp64_options(opts)}
+        extra["speedup_mixed_vs_fp64_plain"] = value / world / extra["fp64_plain"]["value"]
+        extra["error_vs_fp64"] = float(np.linalg.norm(x_mixed - xp) / np.linalg.norm(xp))
+        del elp
+        torch.cuda.empty_cache()
+        el = None
+    # ---- kernel rooflines (fine-level operator kernels)
+    if el is None:
+        el = G.Elliptic(N, VX, EToV, EToB, "preconditioner=jacobi")
+    kr, peak, psrc = kernel_rooflines(G, el, N, E)
+    dominant = "ax_fp32x2" if "mixed" in opts else ("ax_stored_f64")
+    d = kr[dominant]
+    roof = {"bound": "hbm", "kernel": dominant, "achieved": d["achieved"], "peak": peak, "unit": "GB/s",
+            "frac": d["achieved"] / peak, "traffic": None, "peak_source": psrc + " (MEASURED_PEAKS.json hbm_gbs)",
+            "launch_ms": d["launch_ms"], "kernels": kr,
+            "note": "FP64 axhelm is FP64-pipe bound on GB300 (1.25 TF/s nominal); ax_fp32x2 is its FP64-accurate "
+                    "FP32-pair form (FP32-pipe bound); ax_stored_f32 is the HBM-bound multigrid operator"}
 
     line = {"metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Kershaw box, U[-1,1] mass-weighted RHS)",
             "config": {"workload": args.workload, "description": desc, "elements": E, "N": N,
                        "dofs_per_solve": dofs, "iterations": infos[-1]["iterations"],
-                       "time_to_tolerance_s": t_step, "l2": "inputs larger than L2 (vectors 8*E*Np B, ggeo 56*E*Np B)",
+                       "time_to_tolerance_s": t_step, "setup_s": setup_s,
+                       "l2": "inputs larger than L2 (E-vectors 8*E*Np B, geometric factors 56*E*Np B)",
                        "parallelism": "replicas" if world > 1 else "single"},
-            "e2e": {"value": dofs / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": 2 * nbytes,
-                    "d2h_bytes_per_step": 2 * nbytes},
+            "e2e": {"value": dofs / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": 2 * rhs.nbytes,
+                    "d2h_bytes_per_step": 2 * rhs.nbytes},
             "roofline": roof, "gpu_launches": int(launches), "clocks": clk}
+    line.update(extra)
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(nel, N, eps, opts, infos[-1]["iterations"])
+        line["cpu_baseline"] = cpu_sample(nel, N, eps, opts, infos[-1]["iterations"])
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -265,6 +265,10 @@ int Elliptic::solve(double *r, double *x, nrsg_solve_info *info)
   float ms = 0;
   NRSG_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
   if (status == NRSG_OK && iters >= opt.maxIter && res > tol) status = NRSG_ERR_MAXIT;
+  if (mg_error()) {
+    status = NRSG_ERR_CUDA;
+    set_last_error("coarse-level solver: grid barrier wait exceeded its limit");
+  }
   lastIters = iters;
   if (info) {
     info->iterations = iters;

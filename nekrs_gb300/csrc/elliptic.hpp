@@ -79,6 +79,7 @@ struct Elliptic {
   void mg_setup();
   void mg_apply(const double *r, double *z);
   void mg_release();
+  int mg_error();
   std::vector<double> mg_get(const std::string &name);
   long long mg_level_size(int level);
   void mg_schwarz(int level, const double *u, double *Su);

@@ -25,6 +25,7 @@ struct MGState {
   virtual std::vector<double> info(const std::string &what) = 0;
   virtual void schwarz(int level, const double *u, double *Su) = 0;
   virtual long long level_size(int level) = 0;
+  virtual int error() = 0;
 };
 void MGDeleter::operator()(MGState *m) const { delete m; }
 
@@ -52,6 +53,11 @@ template <typename T> struct MGImpl : public MGState {
   DevBuf<T> sRes, sRes2, sUpd, sTmp, rP, zP;
   DevBuf<T> cp, cz, cAp, cr;
   DevBuf<PcgScalars> csc;
+  // persistent coarse solve (order-1 coarsest level)
+  bool persistentCoarse = false;
+  static constexpr int kCoarseGridMax = 4096;
+  DevBuf<double> cPartials;
+  DevBuf<unsigned char> cState;
   std::vector<int> coarseIters;
   T l0, l1;
   bool poisson;
@@ -117,6 +123,12 @@ template <typename T> struct MGImpl : public MGState {
     cr.alloc(C.Nlocal);
     csc.alloc(1);
     NRSG_CUDA(cudaMemsetAsync(csc.p, 0, sizeof(PcgScalars), s));
+    persistentCoarse = (C.N == 1) && o.coarse != "smooth" && o.coarsePersistent;
+    if (persistentCoarse) {
+      cPartials.alloc(3 * kCoarseGridMax);
+      cState.alloc(coarse_state_bytes());
+      NRSG_CUDA(cudaMemsetAsync(cState.p, 0, coarse_state_bytes(), s));
+    }
     if (!std::is_same<T, double>::value) {
       rP.alloc(el.fine.Nlocal);
       zP.alloc(el.fine.Nlocal);
@@ -357,6 +369,13 @@ template <typename T> struct MGImpl : public MGState {
   int coarse_pcg(MGLevelDev<T> &v, const T *b, T *x)
   {
     FieldLevel &L = *v.L;
+    if (persistentCoarse) {
+      coarse_pcg_persistent<T>(L.E, v.ggeo.p, l0, l1, poisson, L.ngroups, L.d_gsOff.p, L.d_gsIds.p,
+                               (long long)L.maskIds.size(), L.d_mask.p, v.invDiag.p, v.invDegree.p, b, x, cr.p, cp.p,
+                               cz.p, cAp.p, cPartials.p, cState.p, kCoarseGridMax, el.opt.coarseTol,
+                               el.opt.coarseMaxIter, s);
+      return 0;
+    }
     const long long n = L.Nlocal;
     const Options &o = el.opt;
     const T *w = v.invDegree.p;
@@ -434,8 +453,27 @@ template <typename T> struct MGImpl : public MGState {
       for (auto &v : lv) {
         if (v.smoothed) out.push_back(v.rho);
       }
-    else if (what == "mg.coarseIters")
-      out.assign(coarseIters.begin(), coarseIters.end());
+    else if (what == "mg.coarseIters") {
+      if (persistentCoarse) {
+        std::vector<unsigned char> h(coarse_state_bytes());
+        NRSG_CUDA(cudaStreamSynchronize(s));
+        NRSG_CUDA(cudaMemcpy(h.data(), cState.p, h.size(), cudaMemcpyDeviceToHost));
+        int it = 0;
+        coarse_state_read(h.data(), &it, nullptr, nullptr);
+        out.push_back(it);
+      } else {
+        out.assign(coarseIters.begin(), coarseIters.end());
+      }
+    } else if (what == "mg.coarseError") {
+      double e = 0;
+      if (persistentCoarse) {
+        std::vector<unsigned char> h(coarse_state_bytes());
+        NRSG_CUDA(cudaStreamSynchronize(s));
+        NRSG_CUDA(cudaMemcpy(h.data(), cState.p, h.size(), cudaMemcpyDeviceToHost));
+        e = coarse_state_read(h.data(), nullptr, nullptr, nullptr);
+      }
+      out.push_back(e);
+    }
     else if (what == "mg.degrees")
       for (auto &v : lv) {
         if (v.smoothed) { out.push_back(v.down); out.push_back(v.up); }
@@ -446,6 +484,15 @@ template <typename T> struct MGImpl : public MGState {
   }
 
   long long level_size(int level) override { return lv.at(level).L->Nlocal; }
+
+  int error() override
+  {
+    if (!persistentCoarse) return 0;
+    std::vector<unsigned char> h(coarse_state_bytes());
+    NRSG_CUDA(cudaMemcpyAsync(h.data(), cState.p, h.size(), cudaMemcpyDeviceToHost, s));
+    NRSG_CUDA(cudaStreamSynchronize(s));
+    return coarse_state_read(h.data(), nullptr, nullptr, nullptr);
+  }
 
   void schwarz(int level, const double *u, double *Su) override
   {
@@ -473,6 +520,7 @@ void Elliptic::mg_apply(const double *r, double *zz)
   mg->apply(r, zz);
 }
 void Elliptic::mg_release() { mg.reset(); }
+int Elliptic::mg_error() { return mg ? mg->error() : 0; }
 std::vector<double> Elliptic::mg_get(const std::string &name)
 {
   if (!mg) throw Error(NRSG_ERR_INVALID, "no multigrid preconditioner");

@@ -27,4 +27,15 @@ template <typename T>
 void launch_pcg_xr(long long n, const T *w, const T *p, const T *Ap, T *x, T *r, PcgScalars *sc, Reduce &red, int slot,
                    cudaStream_t s);
 
+// persistent cooperative Jacobi-PCG on an order-1 level (kernels_coarse.cu);
+// returns the grid size used.  `state` holds coarse_state_bytes() bytes.
+template <typename T>
+int coarse_pcg_persistent(long long E, const T *ggeo, T lam0, T lam1, bool poisson, long long ngroups,
+                          const int *gsOff, const int *gsIds, long long nmask, const int *mask, const T *invDiag,
+                          const T *w, const T *b, T *x, T *r, T *p, T *z, T *Ap, double *partials, void *state,
+                          int gridMax, double tol, int maxit, cudaStream_t s);
+size_t coarse_state_bytes();
+// decode a host copy of the state; returns the error flag (0 = ok)
+int coarse_state_read(const void *state_host, int *iters, double *res0, double *res);
+
 } // namespace nrsg

@@ -96,6 +96,7 @@ struct Options {
   std::string coarse = "jpcg";
   double coarseTol = 1e-4;
   int coarseMaxIter = 200;
+  bool coarsePersistent = true;     // order-1 coarse Jacobi-PCG as one cooperative kernel
   std::string mgPrecision = "fp64"; // fp64 | fp32 | mixed
   std::string axPrecision = "fp64"; // fine-level operator: fp64 | fp32x2 (FP64-accurate FP32-pair arithmetic)
   bool poisson = true;

@@ -358,6 +358,7 @@ static std::string strip(const std::string &s)
 Options parse_options(const char *text)
 {
   Options o;
+  bool axSet = false;
   std::string t = text ? text : "";
   std::replace(t.begin(), t.end(), ';', '\n');
   std::istringstream in(t);
@@ -396,10 +397,12 @@ Options parse_options(const char *text)
       else if (key == "coarsesolver") o.coarse = v;
       else if (key == "coarsetol") o.coarseTol = std::stod(v);
       else if (key == "coarsemaxiterations") o.coarseMaxIter = std::stoi(v);
+      else if (key == "coarsepersistent") o.coarsePersistent = std::stoi(v) != 0;
       else if (key == "mgprecision") o.mgPrecision = v;
       else if (key == "axprecision") {
         if (v != "fp64" && v != "fp32x2") throw Error(NRSG_ERR_BAD_CONFIG, "axPrecision must be fp64 or fp32x2");
         o.axPrecision = v;
+        axSet = true;
       }
       else if (key == "poisson") o.poisson = std::stoi(v) != 0;
       else if (key == "lambda0") o.lambda0 = std::stod(v);
@@ -413,6 +416,10 @@ Options parse_options(const char *text)
       throw Error(NRSG_ERR_BAD_CONFIG, "bad value for '" + key + "': " + v);
     }
   }
+  // mixed precision: FP32 multigrid under an FP64-accurate FP32-pair fine operator
+  if (o.mgPrecision == "mixed" && !axSet && !o.trilinear) o.axPrecision = "fp32x2";
+  if (o.mgPrecision != "fp64" && o.mgPrecision != "fp32" && o.mgPrecision != "mixed")
+    throw Error(NRSG_ERR_BAD_CONFIG, "mgPrecision must be fp64, fp32 or mixed");
   if (o.tol <= 0 || o.maxIter < 1) throw Error(NRSG_ERR_BAD_CONFIG, "residualTol and maxIterations must be positive");
   if (!o.poisson && o.precon == "multigrid" && o.smoother.find("jac") == std::string::npos)
     throw Error(NRSG_ERR_BAD_CONFIG, "Non-Poisson type equations require Jacobi multigrid smoother");

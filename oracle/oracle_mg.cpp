@@ -1135,7 +1135,9 @@ template <typename T> static void build_mg(Elliptic &el, MGT<T> &M, MG &mg)
 void mg_setup(Elliptic &el)
 {
   el.mg = std::make_shared<MG>();
-  el.mg->fp32 = (el.o.mgPrecision == "fp32");
+  // "mixed" keeps the FP32 multigrid of the reference's pfloat build (the FP32-pair fine operator is a GPU
+  // implementation detail of the FP64 operator)
+  el.mg->fp32 = (el.o.mgPrecision == "fp32" || el.o.mgPrecision == "mixed");
   if (el.mg->fp32)
     build_mg<float>(el, el.mg->f, *el.mg);
   else

@@ -92,3 +92,46 @@ def test_schwarz_smoother_parity(product_lib, oracle_mod, torch_cuda, smoother, 
     out = torch.zeros_like(ud)
     el.mg_smoother(0, ud, out)
     assert np.max(np.abs(out.cpu().numpy() - ref)) < 1e-12 * np.max(np.abs(ref))
+
+
+def test_persistent_coarse_matches_host_driven(product_lib, torch_cuda):
+    """The cooperative coarse Jacobi-PCG gives the same preconditioner as the host-driven loop."""
+    torch = torch_cuda
+    N, n = 5, 4
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    base = (f"solver=pfcg;preconditioner=multigrid;smootherType=cheby+asm;mgPrecision=fp64;"
+            f"residualTol=1e-9+relative;maxIterations=200;pMGSchedule={SCHED[5]}")
+    sols, its = [], []
+    for pers in (1, 0):
+        el = G.Elliptic(N, VX, EToV, EToB, base + f";coarsePersistent={pers}")
+        rhs = W.box_rhs(N, n, n, n, 8, el.get("ggeo"))
+        r = torch.from_numpy(rhs).cuda()
+        x = torch.zeros_like(r)
+        info = el.solve(r, x)
+        assert info["status"] == 0
+        its.append(info["iterations"])
+        sols.append(x.cpu().numpy())
+        assert el.get("mg.coarseError")[0] == 0
+    assert its[0] == its[1]
+    assert rel(sols[0], sols[1]) < 1e-10
+
+
+def test_mixed_precision_error_vs_fp64_oracle(product_lib, oracle_mod, torch_cuda):
+    """mgPrecision=mixed: FP32 multigrid under the FP64-accurate FP32-pair fine operator; the error
+    against the FP64-throughout oracle solve is at the level the tolerance allows (1e-8 here)."""
+    N, n = 7, 3
+    base = (f"solver=pfcg;preconditioner=multigrid;smootherType=cheby+asm;residualTol=1e-10+relative;"
+            f"maxIterations=200;pMGSchedule={SCHED[7]}")
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    orc = O.Elliptic(N, VX, EToV, EToB, base + ";mgPrecision=fp64")
+    rhs = W.box_rhs(N, n, n, n, 5, orc.get("ggeo"))
+    xo, io = orc.solve(rhs)
+    el = G.Elliptic(N, VX, EToV, EToB, base + ";mgPrecision=mixed")
+    torch = torch_cuda
+    r = torch.from_numpy(rhs.copy()).cuda()
+    x = torch.zeros_like(r)
+    ig = el.solve(r, x)
+    assert ig["status"] == 0
+    assert ig["res"] <= 1e-10 * ig["res0"]
+    assert abs(ig["iterations"] - io["iterations"]) <= 2
+    assert rel(x.cpu().numpy(), xo) < 1e-8
