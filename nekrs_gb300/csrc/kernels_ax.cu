@@ -50,10 +50,30 @@ __global__ void __launch_bounds__(NQ *NQ *AxShape<NQ>::epb)
   __syncthreads();
 
   const T *g = ggeo + e * 7 * NP + t;
+  // FP32 (HBM-bound): issue every plane's geometric-factor loads up front so
+  // that enough bytes are in flight per SM; FP64 (FP64-pipe bound) loads per
+  // plane to keep register pressure down.
+  constexpr bool PRELOAD = (sizeof(T) == 4);
+  constexpr int NG = POISSON ? 6 : 7;
+  T gpre[PRELOAD ? NG * NQ : 1];
+  if (PRELOAD) {
+#pragma unroll
+    for (int k = 0; k < NQ; ++k)
+#pragma unroll
+      for (int c = 0; c < NG; ++c) gpre[c * NQ + k] = active ? __ldg(g + c * NP + k * NQ * NQ) : T(0);
+  }
 #pragma unroll
   for (int k = 0; k < NQ; ++k) {
     T G00 = 0, G01 = 0, G11 = 0, G12 = 0, G02 = 0, G22 = 0, GWJ = 0;
-    if (active) {
+    if (PRELOAD) {
+      G00 = gpre[0 * NQ + k];
+      G01 = gpre[1 * NQ + k];
+      G11 = gpre[2 * NQ + k];
+      G12 = gpre[3 * NQ + k];
+      G02 = gpre[4 * NQ + k];
+      G22 = gpre[5 * NQ + k];
+      if (!POISSON) GWJ = gpre[(NG - 1) * NQ + k];
+    } else if (active) {
       const int o = k * NQ * NQ;
       G00 = __ldg(g + 0 * NP + o);
       G01 = __ldg(g + 1 * NP + o);

@@ -76,7 +76,7 @@ __device__ bool grid_barrier(CoarseState *st)
           ok = 0;
           break;
         }
-        __nanosleep(64);
+        if (spins > 256) __nanosleep(32);
       }
     }
     __threadfence();
@@ -140,6 +140,7 @@ template <typename T> struct CoarseArgs {
   long long nmask;
   const int *mask;
   const T *invDiag, *w, *b;
+  const unsigned char *gathered; // 1 where the node belongs to a gather group
   T *x, *r, *p, *z, *Ap;
   double *partials; // [3][gridDim]
   CoarseState *st;
@@ -182,7 +183,8 @@ template <typename T> __global__ void __launch_bounds__(kCT) coarse_pcg_kernel(C
   while (rn > tol && it < a.maxit && r0 > 0) {
     ++it;
     const T beta = (it == 1) ? T(0) : (T)(rdotz / rdotz_old);
-    // A: p = z + beta p and A p, one element per thread
+    // A: p = z + beta p and A p, one element per thread; (p, Ap)_w over nodes outside gather groups
+    double pap = 0;
     for (long long e = tid; e < a.E; e += nth) {
       T q[8], out[8];
 #pragma unroll
@@ -193,21 +195,24 @@ template <typename T> __global__ void __launch_bounds__(kCT) coarse_pcg_kernel(C
       }
       ax_n1<T>(a.ggeo + e * 56, a.lam0, a.lam1, a.poisson, q, out);
 #pragma unroll
-      for (int m = 0; m < 8; ++m) a.Ap[e * 8 + m] = out[m];
+      for (int m = 0; m < 8; ++m) {
+        a.Ap[e * 8 + m] = out[m];
+        if (!a.gathered[e * 8 + m]) pap += (double)a.w[e * 8 + m] * (double)q[m] * (double)out[m];
+      }
     }
     if (!grid_barrier(a.st)) return;
-    // B: mask and gather-scatter (disjoint node sets)
+    // B: mask and gather-scatter (disjoint node sets); (p, Ap)_w over the gathered nodes
     for (long long m = tid; m < a.nmask; m += nth) a.Ap[a.mask[m]] = T(0);
     for (long long g = tid; g < a.ngroups; g += nth) {
-      const int s = a.gsOff[g], t = a.gsOff[g + 1];
+      const int s0 = a.gsOff[g], t0 = a.gsOff[g + 1];
       T v = 0;
-      for (int q = s; q < t; ++q) v += a.Ap[a.gsIds[q]];
-      for (int q = s; q < t; ++q) a.Ap[a.gsIds[q]] = v;
+      for (int q = s0; q < t0; ++q) v += a.Ap[a.gsIds[q]];
+      for (int q = s0; q < t0; ++q) {
+        const int id = a.gsIds[q];
+        a.Ap[id] = v;
+        pap += (double)a.w[id] * (double)a.p[id] * (double)v;
+      }
     }
-    if (!grid_barrier(a.st)) return;
-    // C: (p, A p)_w
-    double pap = 0;
-    for (long long i = tid; i < n; i += nth) pap += (double)a.w[i] * (double)a.p[i] * (double)a.Ap[i];
     pap = cblock(pap, sh);
     if (threadIdx.x == 0) a.partials[2 * gridDim.x + blockIdx.x] = pap;
     if (!grid_barrier(a.st)) return;
@@ -250,14 +255,14 @@ template <typename T> struct CoarseSolverImpl;
 template <typename T>
 int coarse_pcg_persistent(long long E, const T *ggeo, T lam0, T lam1, bool poisson, long long ngroups,
                           const int *gsOff, const int *gsIds, long long nmask, const int *mask, const T *invDiag,
-                          const T *w, const T *b, T *x, T *r, T *p, T *z, T *Ap, double *partials, void *state,
-                          int gridMax, double tol, int maxit, cudaStream_t s)
+                          const T *w, const unsigned char *gathered, const T *b, T *x, T *r, T *p, T *z, T *Ap,
+                          double *partials, void *state, int gridMax, double tol, int maxit, cudaStream_t s)
 {
   int dev = 0, sms = 0, perSM = 0;
   NRSG_CUDA(cudaGetDevice(&dev));
   NRSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   NRSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, coarse_pcg_kernel<T>, kCT, 0));
-  int grid = sms * (perSM < 2 ? perSM : 2);
+  int grid = sms * (perSM < 1 ? perSM : 1);
   const long long need = (E * 8 + kCT - 1) / kCT;
   if (grid > need) grid = (int)(need > 0 ? need : 1);
   if (grid > gridMax) grid = gridMax;
@@ -276,6 +281,7 @@ int coarse_pcg_persistent(long long E, const T *ggeo, T lam0, T lam1, bool poiss
   a.mask = mask;
   a.invDiag = invDiag;
   a.w = w;
+  a.gathered = gathered;
   a.b = b;
   a.x = x;
   a.r = r;
@@ -304,11 +310,11 @@ int coarse_state_read(const void *state_host, int *iters, double *res0, double *
 
 template int coarse_pcg_persistent<double>(long long, const double *, double, double, bool, long long, const int *,
                                            const int *, long long, const int *, const double *, const double *,
-                                           const double *, double *, double *, double *, double *, double *, double *,
-                                           void *, int, double, int, cudaStream_t);
+                                           const unsigned char *, const double *, double *, double *, double *,
+                                           double *, double *, double *, void *, int, double, int, cudaStream_t);
 template int coarse_pcg_persistent<float>(long long, const float *, float, float, bool, long long, const int *,
                                           const int *, long long, const int *, const float *, const float *,
-                                          const float *, float *, float *, float *, float *, float *, double *, void *,
-                                          int, double, int, cudaStream_t);
+                                          const unsigned char *, const float *, float *, float *, float *, float *,
+                                          float *, double *, void *, int, double, int, cudaStream_t);
 
 } // namespace nrsg

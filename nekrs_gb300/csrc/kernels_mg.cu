@@ -210,113 +210,136 @@ template <int NQ> __device__ __forceinline__ int halo_ext_index(int f, int a, in
   }
 }
 
-template <typename T, int NQ, bool RAS>
-__global__ void __launch_bounds__((NQ + 2) * (NQ + 2))
+template <int NQ> struct FdmShape {
+  static constexpr int NL = NQ + 2;
+  static constexpr int line = NL * NL;
+  static constexpr int epb = line >= 256 ? 1 : 256 / line;
+};
+
+// EPB elements per CTA, (N+3)^2 threads per element (one line per thread and
+// direction).  With RECIP the 1/(lx+ly+lz) scaling is rebuilt from the three
+// 1-D eigenvalue sets (3 (N+3) values per element instead of (N+3)^3).
+template <typename T, int NQ, bool RAS, bool RECIP>
+__global__ void __launch_bounds__(FdmShape<NQ>::line *FdmShape<NQ>::epb)
     fdm_kernel(long long E, const T *__restrict__ u, const int *__restrict__ haloSrc, const T *__restrict__ Sx,
                const T *__restrict__ Sy, const T *__restrict__ Sz, const T *__restrict__ invL,
-               const T *__restrict__ wts, T *__restrict__ Su, T *__restrict__ haloOut)
+               const T *__restrict__ lam, const T *__restrict__ wts, T *__restrict__ Su, T *__restrict__ haloOut)
 {
-  constexpr int NL = NQ + 2, NPE = NL * NL * NL, NP = NQ * NQ * NQ, NF = NQ * NQ;
-  __shared__ T s_w[NPE];
-  __shared__ T s_Sx[NL * NL], s_Sy[NL * NL], s_Sz[NL * NL];
-  const long long e = blockIdx.x;
-  const int t = threadIdx.x;
-  for (int q = t; q < NL * NL; q += NL * NL) {
-    s_Sx[q] = Sx[e * NL * NL + q];
-    s_Sy[q] = Sy[e * NL * NL + q];
-    s_Sz[q] = Sz[e * NL * NL + q];
+  constexpr int NL = NQ + 2, NPE = NL * NL * NL, NP = NQ * NQ * NQ, NF = NQ * NQ, LINE = NL * NL;
+  constexpr int EPB = FdmShape<NQ>::epb;
+  __shared__ T s_w[EPB][NPE];
+  __shared__ T s_S[EPB][3][LINE];
+  __shared__ T s_l[EPB][3][NL];
+  const int t = threadIdx.x, el = threadIdx.y;
+  const long long e = (long long)blockIdx.x * EPB + el;
+  const bool active = e < E;
+  const long long ee = active ? e : 0;
+  for (int q = t; q < LINE; q += LINE) {
+    s_S[el][0][q] = Sx[ee * LINE + q];
+    s_S[el][1][q] = Sy[ee * LINE + q];
+    s_S[el][2][q] = Sz[ee * LINE + q];
   }
-  for (int q = t; q < NPE; q += NL * NL) s_w[q] = T(0);
+  if (RECIP && t < 3 * NL) s_l[el][t / NL][t % NL] = lam[ee * 3 * NL + t];
+  for (int q = t; q < NPE; q += LINE) s_w[el][q] = T(0);
   __syncthreads();
-  const T *ue = u + e * NP;
-  for (int q = t; q < NP; q += NL * NL) {
+  const T *ue = u + ee * NP;
+  for (int q = t; q < NP; q += LINE) {
     const int i = q % NQ, j = (q / NQ) % NQ, k = q / NF;
-    s_w[(i + 1) + NL * ((j + 1) + NL * (k + 1))] = ue[q];
+    s_w[el][(i + 1) + NL * ((j + 1) + NL * (k + 1))] = active ? ue[q] : T(0);
   }
-  const int *hs = haloSrc + e * 6 * NF;
-  for (int q = t; q < 6 * NF; q += NL * NL) {
-    const int f = q / NF, p = q % NF;
-    const int src = hs[q];
-    s_w[halo_ext_index<NQ>(f, p % NQ, p / NQ)] = src >= 0 ? u[src] : T(0);
+  const int *hs = haloSrc + ee * 6 * NF;
+  for (int q = t; q < 6 * NF; q += LINE) {
+    const int f = q / NF, pp = q % NF;
+    const int src = active ? hs[q] : -1;
+    s_w[el][halo_ext_index<NQ>(f, pp % NQ, pp / NQ)] = src >= 0 ? u[src] : T(0);
   }
   __syncthreads();
-  // thread (p, q) owns one line per direction
   const int p = t % NL, q = t / NL;
   T line[NL];
-  // forward: x (S^T), y, z
+  T *w = s_w[el];
+  const T *SX = s_S[el][0], *SY = s_S[el][1], *SZ = s_S[el][2];
+  // forward: S^T along x, y, z
 #pragma unroll
-  for (int l = 0; l < NL; ++l) line[l] = s_w[l + NL * (p + NL * q)];
-#pragma unroll
-  for (int i = 0; i < NL; ++i) {
-    T v = 0;
-#pragma unroll
-    for (int l = 0; l < NL; ++l) v += s_Sx[l + NL * i] * line[l];
-    s_w[i + NL * (p + NL * q)] = v;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int l = 0; l < NL; ++l) line[l] = s_w[p + NL * (l + NL * q)];
-#pragma unroll
-  for (int j = 0; j < NL; ++j) {
-    T v = 0;
-#pragma unroll
-    for (int l = 0; l < NL; ++l) v += s_Sy[l + NL * j] * line[l];
-    s_w[p + NL * (j + NL * q)] = v;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int l = 0; l < NL; ++l) line[l] = s_w[p + NL * (q + NL * l)];
-  const T *iL = invL + e * NPE;
-#pragma unroll
-  for (int k = 0; k < NL; ++k) {
-    T v = 0;
-#pragma unroll
-    for (int l = 0; l < NL; ++l) v += s_Sz[l + NL * k] * line[l];
-    s_w[p + NL * (q + NL * k)] = v * iL[p + NL * (q + NL * k)];
-  }
-  __syncthreads();
-  // backward: x (S), y, z
-#pragma unroll
-  for (int l = 0; l < NL; ++l) line[l] = s_w[l + NL * (p + NL * q)];
+  for (int l = 0; l < NL; ++l) line[l] = w[l + NL * (p + NL * q)];
 #pragma unroll
   for (int i = 0; i < NL; ++i) {
     T v = 0;
 #pragma unroll
-    for (int l = 0; l < NL; ++l) v += s_Sx[i + NL * l] * line[l];
-    s_w[i + NL * (p + NL * q)] = v;
+    for (int l = 0; l < NL; ++l) v += SX[l + NL * i] * line[l];
+    w[i + NL * (p + NL * q)] = v;
   }
   __syncthreads();
 #pragma unroll
-  for (int l = 0; l < NL; ++l) line[l] = s_w[p + NL * (l + NL * q)];
+  for (int l = 0; l < NL; ++l) line[l] = w[p + NL * (l + NL * q)];
 #pragma unroll
   for (int j = 0; j < NL; ++j) {
     T v = 0;
 #pragma unroll
-    for (int l = 0; l < NL; ++l) v += s_Sy[j + NL * l] * line[l];
-    s_w[p + NL * (j + NL * q)] = v;
+    for (int l = 0; l < NL; ++l) v += SY[l + NL * j] * line[l];
+    w[p + NL * (j + NL * q)] = v;
   }
   __syncthreads();
 #pragma unroll
-  for (int l = 0; l < NL; ++l) line[l] = s_w[p + NL * (q + NL * l)];
+  for (int l = 0; l < NL; ++l) line[l] = w[p + NL * (q + NL * l)];
+  const T *iL = invL + ee * NPE;
 #pragma unroll
   for (int k = 0; k < NL; ++k) {
     T v = 0;
 #pragma unroll
-    for (int l = 0; l < NL; ++l) v += s_Sz[k + NL * l] * line[l];
-    s_w[p + NL * (q + NL * k)] = v;
+    for (int l = 0; l < NL; ++l) v += SZ[l + NL * k] * line[l];
+    T sc;
+    if (RECIP) {
+      const T d = s_l[el][0][p] + s_l[el][1][q] + s_l[el][2][k];
+      sc = d > T(1e-5) ? T(1) / d : T(0);
+    } else {
+      sc = iL[p + NL * (q + NL * k)];
+    }
+    w[p + NL * (q + NL * k)] = v * sc;
   }
   __syncthreads();
+  // backward: S along x, y, z
+#pragma unroll
+  for (int l = 0; l < NL; ++l) line[l] = w[l + NL * (p + NL * q)];
+#pragma unroll
+  for (int i = 0; i < NL; ++i) {
+    T v = 0;
+#pragma unroll
+    for (int l = 0; l < NL; ++l) v += SX[i + NL * l] * line[l];
+    w[i + NL * (p + NL * q)] = v;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int l = 0; l < NL; ++l) line[l] = w[p + NL * (l + NL * q)];
+#pragma unroll
+  for (int j = 0; j < NL; ++j) {
+    T v = 0;
+#pragma unroll
+    for (int l = 0; l < NL; ++l) v += SY[j + NL * l] * line[l];
+    w[p + NL * (j + NL * q)] = v;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int l = 0; l < NL; ++l) line[l] = w[p + NL * (q + NL * l)];
+#pragma unroll
+  for (int k = 0; k < NL; ++k) {
+    T v = 0;
+#pragma unroll
+    for (int l = 0; l < NL; ++l) v += SZ[k + NL * l] * line[l];
+    w[p + NL * (q + NL * k)] = v;
+  }
+  __syncthreads();
+  if (!active) return;
   T *se = Su + e * NP;
-  for (int qq = t; qq < NP; qq += NL * NL) {
+  for (int qq = t; qq < NP; qq += LINE) {
     const int i = qq % NQ, j = (qq / NQ) % NQ, k = qq / NF;
-    const T v = s_w[(i + 1) + NL * ((j + 1) + NL * (k + 1))];
+    const T v = w[(i + 1) + NL * ((j + 1) + NL * (k + 1))];
     se[qq] = RAS ? v * wts[e * NP + qq] : v;
   }
   if (!RAS) {
     T *ho = haloOut + e * 6 * NF;
-    for (int qq = t; qq < 6 * NF; qq += NL * NL) {
+    for (int qq = t; qq < 6 * NF; qq += LINE) {
       const int f = qq / NF, pp = qq % NF;
-      ho[qq] = s_w[halo_ext_index<NQ>(f, pp % NQ, pp / NQ)];
+      ho[qq] = w[halo_ext_index<NQ>(f, pp % NQ, pp / NQ)];
     }
   }
 }
@@ -357,16 +380,23 @@ __global__ void asm_combine_kernel(long long E, const int *__restrict__ haloPart
 
 template <typename T>
 void launch_fdm(int N, long long E, bool ras, const T *u, const int *haloSrc, const T *Sx, const T *Sy, const T *Sz,
-                const T *invL, const T *wts, T *Su, T *haloOut, cudaStream_t s)
+                const T *invL, const T *lam, const T *wts, T *Su, T *haloOut, cudaStream_t s)
 {
   if (E <= 0) return;
+  const bool recip = (lam != nullptr);
 #define NRSG_FDM(NQ)                                                                                       \
   {                                                                                                        \
-    const int thr = (NQ + 2) * (NQ + 2);                                                                   \
-    if (ras)                                                                                               \
-      fdm_kernel<T, NQ, true><<<(unsigned)E, thr, 0, s>>>(E, u, haloSrc, Sx, Sy, Sz, invL, wts, Su, haloOut); \
+    constexpr int EPB = FdmShape<NQ>::epb;                                                                 \
+    const dim3 blk(FdmShape<NQ>::line, EPB);                                                               \
+    const unsigned grid = (unsigned)((E + EPB - 1) / EPB);                                                 \
+    if (ras && recip)                                                                                      \
+      fdm_kernel<T, NQ, true, true><<<grid, blk, 0, s>>>(E, u, haloSrc, Sx, Sy, Sz, invL, lam, wts, Su, haloOut);   \
+    else if (ras)                                                                                          \
+      fdm_kernel<T, NQ, true, false><<<grid, blk, 0, s>>>(E, u, haloSrc, Sx, Sy, Sz, invL, lam, wts, Su, haloOut);  \
+    else if (recip)                                                                                        \
+      fdm_kernel<T, NQ, false, true><<<grid, blk, 0, s>>>(E, u, haloSrc, Sx, Sy, Sz, invL, lam, wts, Su, haloOut);  \
     else                                                                                                   \
-      fdm_kernel<T, NQ, false><<<(unsigned)E, thr, 0, s>>>(E, u, haloSrc, Sx, Sy, Sz, invL, wts, Su, haloOut); \
+      fdm_kernel<T, NQ, false, false><<<grid, blk, 0, s>>>(E, u, haloSrc, Sx, Sy, Sz, invL, lam, wts, Su, haloOut); \
   }
   NRSG_DISPATCH_NQ_MG(N, NRSG_FDM)
 #undef NRSG_FDM
@@ -411,7 +441,7 @@ void launch_random_fill(long long n, unsigned long long seed, double *v, cudaStr
   template void launch_cheby1_update<T>(long long, T, T, const T *, T *, T *, T *, cudaStream_t);          \
   template void launch_cheby4_update<T>(long long, T, const T *, const T *, T *, T *, cudaStream_t);       \
   template void launch_fdm<T>(int, long long, bool, const T *, const int *, const T *, const T *, const T *, \
-                              const T *, const T *, T *, T *, cudaStream_t);                               \
+                              const T *, const T *, const T *, T *, T *, cudaStream_t);                    \
   template void launch_asm_combine<T>(int, long long, const int *, const T *, const T *, T *, cudaStream_t);
 NRSG_INST_MG(double)
 NRSG_INST_MG(float)

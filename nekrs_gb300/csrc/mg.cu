@@ -40,7 +40,7 @@ template <typename T> struct MGLevelDev {
   double rho = 0, lambda0 = 0, lambda1 = 0;
   int up = 2, down = 2;
   std::vector<double> upBetas, downBetas;
-  DevBuf<T> Sx, Sy, Sz, invL, wts, haloOut;
+  DevBuf<T> Sx, Sy, Sz, invL, lam, wts, haloOut;  // invL (FP64 multigrid) or lam (FP32: 1/(lx+ly+lz) rebuilt)
   DevBuf<int> haloSrc, haloPartner;
   DevBuf<T> x, rhs, res;
 };
@@ -57,7 +57,7 @@ template <typename T> struct MGImpl : public MGState {
   bool persistentCoarse = false;
   static constexpr int kCoarseGridMax = 4096;
   DevBuf<double> cPartials;
-  DevBuf<unsigned char> cState;
+  DevBuf<unsigned char> cState, cGathered;
   std::vector<int> coarseIters;
   T l0, l1;
   bool poisson;
@@ -128,6 +128,9 @@ template <typename T> struct MGImpl : public MGState {
       cPartials.alloc(3 * kCoarseGridMax);
       cState.alloc(coarse_state_bytes());
       NRSG_CUDA(cudaMemsetAsync(cState.p, 0, coarse_state_bytes(), s));
+      std::vector<unsigned char> flag(C.Nlocal, 0);
+      for (int id : C.gm.devIds) flag[id] = 1;
+      cGathered.upload(flag);
     }
     if (!std::is_same<T, double>::value) {
       rP.alloc(el.fine.Nlocal);
@@ -167,7 +170,9 @@ template <typename T> struct MGImpl : public MGState {
     const int nl = L.N + 3, npe = nl * nl * nl;
     const long long E = L.E;
     const FdmLengths len = fdm_lengths(el.fine, el.fine.um);
-    std::vector<T> Sx((size_t)E * nl * nl), Sy((size_t)E * nl * nl), Sz((size_t)E * nl * nl), iL((size_t)E * npe);
+    const bool recip = !std::is_same<T, double>::value;
+    std::vector<T> Sx((size_t)E * nl * nl), Sy((size_t)E * nl * nl), Sz((size_t)E * nl * nl);
+    std::vector<T> iL(recip ? 0 : (size_t)E * npe), lm(recip ? (size_t)E * 3 * nl : 0);
 #pragma omp parallel for
     for (long long e = 0; e < E; ++e) {
       const int *bc = &L.EToBh[e * 6];
@@ -181,17 +186,23 @@ template <typename T> struct MGImpl : public MGState {
         Sy[e * nl * nl + q] = (T)S[1][q];
         Sz[e * nl * nl + q] = (T)S[2][q];
       }
-      for (int k = 0; k < nl; ++k)
-        for (int j = 0; j < nl; ++j)
-          for (int i = 0; i < nl; ++i) {
-            const double dsum = lam[0][i] + lam[1][j] + lam[2][k];
-            iL[e * npe + i + nl * (j + nl * k)] = (T)(dsum > 1e-5 ? 1.0 / dsum : 0.0);
-          }
+      if (recip) {
+        for (int d = 0; d < 3; ++d)
+          for (int i = 0; i < nl; ++i) lm[(e * 3 + d) * nl + i] = (T)lam[d][i];
+      } else {
+        for (int k = 0; k < nl; ++k)
+          for (int j = 0; j < nl; ++j)
+            for (int i = 0; i < nl; ++i) {
+              const double dsum = lam[0][i] + lam[1][j] + lam[2][k];
+              iL[e * npe + i + nl * (j + nl * k)] = (T)(dsum > 1e-5 ? 1.0 / dsum : 0.0);
+            }
+      }
     }
     v.Sx.upload(Sx);
     v.Sy.upload(Sy);
     v.Sz.upload(Sz);
-    v.invL.upload(iL);
+    if (recip) v.lam.upload(lm);
+    else v.invL.upload(iL);
     std::vector<int> src, partner;
     std::vector<double> w;
     fdm_halo_maps(L, src, partner, w);
@@ -277,7 +288,8 @@ template <typename T> struct MGImpl : public MGState {
   {
     FieldLevel &L = *v.L;
     const bool ras = plan.base == 2;
-    launch_fdm<T>(L.N, L.E, ras, u, v.haloSrc.p, v.Sx.p, v.Sy.p, v.Sz.p, v.invL.p, v.wts.p, Su, v.haloOut.p, s);
+    launch_fdm<T>(L.N, L.E, ras, u, v.haloSrc.p, v.Sx.p, v.Sy.p, v.Sz.p, v.invL.p, v.lam.p, v.wts.p, Su, v.haloOut.p,
+                  s);
     if (!ras) launch_asm_combine<T>(L.N, L.E, v.haloPartner.p, v.haloOut.p, v.wts.p, Su, s);
     launch_gs<T>(L.ngroups, L.d_gsOff.p, L.d_gsIds.p, Su, s);
     launch_mask<T>((long long)L.maskIds.size(), L.d_mask.p, Su, s);
@@ -371,8 +383,8 @@ template <typename T> struct MGImpl : public MGState {
     FieldLevel &L = *v.L;
     if (persistentCoarse) {
       coarse_pcg_persistent<T>(L.E, v.ggeo.p, l0, l1, poisson, L.ngroups, L.d_gsOff.p, L.d_gsIds.p,
-                               (long long)L.maskIds.size(), L.d_mask.p, v.invDiag.p, v.invDegree.p, b, x, cr.p, cp.p,
-                               cz.p, cAp.p, cPartials.p, cState.p, kCoarseGridMax, el.opt.coarseTol,
+                               (long long)L.maskIds.size(), L.d_mask.p, v.invDiag.p, v.invDegree.p, cGathered.p, b, x,
+                               cr.p, cp.p, cz.p, cAp.p, cPartials.p, cState.p, kCoarseGridMax, el.opt.coarseTol,
                                el.opt.coarseMaxIter, s);
       return 0;
     }

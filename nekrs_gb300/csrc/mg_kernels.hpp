@@ -12,7 +12,7 @@ void launch_cheby1_update(long long n, T dc, T rc, const T *SAd, T *d, T *r, T *
 template <typename T> void launch_cheby4_update(long long n, T beta, const T *Ad, const T *d, T *r, T *x, cudaStream_t s);
 template <typename T>
 void launch_fdm(int N, long long E, bool ras, const T *u, const int *haloSrc, const T *Sx, const T *Sy, const T *Sz,
-                const T *invL, const T *wts, T *Su, T *haloOut, cudaStream_t s);
+                const T *invL, const T *lam, const T *wts, T *Su, T *haloOut, cudaStream_t s);
 template <typename T>
 void launch_asm_combine(int N, long long E, const int *haloPartner, const T *haloOut, const T *wts, T *Su,
                         cudaStream_t s);
@@ -32,8 +32,8 @@ void launch_pcg_xr(long long n, const T *w, const T *p, const T *Ap, T *x, T *r,
 template <typename T>
 int coarse_pcg_persistent(long long E, const T *ggeo, T lam0, T lam1, bool poisson, long long ngroups,
                           const int *gsOff, const int *gsIds, long long nmask, const int *mask, const T *invDiag,
-                          const T *w, const T *b, T *x, T *r, T *p, T *z, T *Ap, double *partials, void *state,
-                          int gridMax, double tol, int maxit, cudaStream_t s);
+                          const T *w, const unsigned char *gathered, const T *b, T *x, T *r, T *p, T *z, T *Ap,
+                          double *partials, void *state, int gridMax, double tol, int maxit, cudaStream_t s);
 size_t coarse_state_bytes();
 // decode a host copy of the state; returns the error flag (0 = ok)
 int coarse_state_read(const void *state_host, int *iters, double *res0, double *res);
