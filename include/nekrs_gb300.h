@@ -81,6 +81,10 @@ long long nrsg_kernel_launches(void);
  * lambda1, poisson, elementMap (trilinear). */
 int nrsg_elliptic_create(const nrsg_mesh_desc *mesh, const char *options, nrsg_elliptic **out);
 int nrsg_elliptic_destroy(nrsg_elliptic *el);
+/* Run all later work of `el` on `cuda_stream` (a cudaStream_t; NULL = the
+ * legacy default stream) instead of the library's own non-blocking stream,
+ * which does not wait for work the caller queued elsewhere.  Waits for the
+ * previous stream to drain.  No reference counterpart (OCCA's device stream). */
 int nrsg_elliptic_set_stream(nrsg_elliptic *el, void *cuda_stream);
 
 /* Solve: mirrors ellipticSolve(elliptic, o_r, o_x).  d_r holds the RHS on
@@ -127,6 +131,20 @@ int nrsg_host_setup_maps(int N, long long E, const long long *h_EToV, const int 
  * eigenvalue step of the Arnoldi lambda_max estimate
  * (ellipticMultiGridLevelSetup.cpp:415-438, LAPACK dgeev there).  -1 on error. */
 double nrsg_host_hessenberg_rho(int n, const double *h_H);
+
+/* Host-only: the assembled matrix of the level operator
+ * lambda0 * (stiffness) + lambda1 * JW (lambda1 ignored when poisson != 0)
+ * over the unmasked unique nodes, the matrix the reference hands to its
+ * coarse solver (ellipticBuildFEMHex3D, src/solvers/elliptic/MG/
+ * ellipticBuildFEM.cpp:73-230; coarseLevel_t::setupSolver,
+ * src/solvers/elliptic/MG/coarseLevel.cpp:47).  Row r is the r-th masked
+ * gather group, CSR with columns ascending.  h_ggeo is [E][7][Np].  Call with
+ * h_rowPtr == NULL to get *nrow and *nnz; then capacities are nrow+1
+ * (h_rowPtr), nnz (h_cols, h_vals) and E*Np (h_rowOfNode: row of each E-vector
+ * node, -1 where masked).  The solver uses it on an order-1 coarsest level. */
+int nrsg_host_assemble_operator(int N, long long E, const long long *h_EToV, const int *h_EToB, const double *h_ggeo,
+                                double lambda0, double lambda1, int poisson, long long *nrow, long long *nnz,
+                                long long *h_rowPtr, long long *h_cols, double *h_vals, long long *h_rowOfNode);
 
 /* ---- kernel-level entry points (one launch each, on `stream`) ---------- */
 

@@ -59,6 +59,8 @@ def lib():
         L.nrsg_host_hessenberg_rho.restype = ctypes.c_double
         L.nrsg_host_hessenberg_rho.argtypes = [ctypes.c_int, vp]
         L.nrsg_host_setup_maps.argtypes = [ctypes.c_int, LL] + [vp] * 10
+        L.nrsg_host_assemble_operator.argtypes = ([ctypes.c_int, LL, vp, vp, vp, ctypes.c_double, ctypes.c_double,
+                                                   ctypes.c_int] + [vp] * 6)
         L.nrsg_elliptic_create.argtypes = [ctypes.POINTER(MeshDesc), ctypes.c_char_p, ctypes.POINTER(vp)]
         L.nrsg_elliptic_destroy.argtypes = [vp]
         L.nrsg_elliptic_set_stream.argtypes = [vp, vp]
@@ -129,6 +131,7 @@ class Elliptic:
         h = vp()
         check(lib().nrsg_elliptic_create(ctypes.byref(desc), options.encode(), ctypes.byref(h)))
         self.h = h
+        self._stream = None  # None: the library's own stream
 
     def close(self):
         if getattr(self, "h", None):
@@ -143,9 +146,24 @@ class Elliptic:
 
     def set_stream(self, stream_handle):
         check(lib().nrsg_elliptic_set_stream(self.h, stream_handle))
+        self._stream = stream_handle
+
+    def _order_with(self, *bufs):
+        """Given torch CUDA tensors, run the library on the caller's current torch stream, so that the
+        caller's earlier writes to the buffers and later reads of them are ordered with its kernels (the
+        library's own stream is non-blocking and would not wait for them)."""
+        for b in bufs:
+            if getattr(b, "is_cuda", False):
+                import torch
+
+                s = torch.cuda.current_stream(b.device).cuda_stream
+                if s != self._stream:
+                    self.set_stream(s)
+                return
 
     def solve(self, r, x):
         """ellipticSolve(elliptic, r, x) on device E-vectors; r becomes the residual."""
+        self._order_with(r, x)
         info = SolveInfo()
         code = lib().nrsg_elliptic_solve(self.h, _ptr(r), _ptr(x), ctypes.byref(info))
         if code not in (NRSG_OK, 1):
@@ -170,21 +188,27 @@ class Elliptic:
         return info.as_dict()
 
     def operator(self, q, Aq):
+        self._order_with(q, Aq)
         check(lib().nrsg_elliptic_operator(self.h, _ptr(q), _ptr(Aq)))
 
     def ax(self, q, Aq):
+        self._order_with(q, Aq)
         check(lib().nrsg_elliptic_ax(self.h, _ptr(q), _ptr(Aq)))
 
     def gs(self, q):
+        self._order_with(q)
         check(lib().nrsg_elliptic_gs(self.h, _ptr(q)))
 
     def mask(self, q):
+        self._order_with(q)
         check(lib().nrsg_elliptic_mask(self.h, _ptr(q)))
 
     def precondition(self, r, z):
+        self._order_with(r, z)
         check(lib().nrsg_elliptic_precondition(self.h, _ptr(r), _ptr(z)))
 
     def mg_smoother(self, level, u, Su):
+        self._order_with(u, Su)
         check(lib().nrsg_elliptic_mg_smoother(self.h, level, _ptr(u), _ptr(Su)))
 
     def mg_level_size(self, level):
@@ -229,6 +253,25 @@ def host_setup_maps(N, EToV, EToB):
     off = off[: ng.value + 1]
     return {"ids": ids, "maskedIds": masked, "invDegree": inv, "maskIds": mask[: nm.value], "gsOff": off,
             "gsIds": gids[: off[-1]]}
+
+
+def host_assemble_operator(N, EToV, EToB, ggeo, lambda0=1.0, lambda1=0.0, poisson=True):
+    """Assembled level operator on the unmasked unique nodes (CSR) computed by the library on the host:
+    (rowPtr, cols, vals, rowOfNode)."""
+    EToV = np.ascontiguousarray(EToV, dtype=np.int64)
+    EToB = np.ascontiguousarray(EToB, dtype=np.int32)
+    ggeo = np.ascontiguousarray(ggeo, dtype=np.float64)
+    E = EToV.shape[0]
+    nrow, nnz = LL(0), LL(0)
+    args = (N, E, EToV.ctypes.data, EToB.ctypes.data, ggeo.ctypes.data, float(lambda0), float(lambda1), int(poisson))
+    check(lib().nrsg_host_assemble_operator(*args, ctypes.byref(nrow), ctypes.byref(nnz), None, None, None, None))
+    rp = np.zeros(nrow.value + 1, np.int64)
+    cols = np.zeros(nnz.value, np.int64)
+    vals = np.zeros(nnz.value)
+    rown = np.zeros(E * (N + 1) ** 3, np.int64)
+    check(lib().nrsg_host_assemble_operator(*args, ctypes.byref(nrow), ctypes.byref(nnz), rp.ctypes.data,
+                                            cols.ctypes.data, vals.ctypes.data, rown.ctypes.data))
+    return rp, cols, vals, rown
 
 
 # ---- kernel-level entry points ---------------------------------------------

@@ -1,246 +1,311 @@
-// Coarse-level Jacobi-PCG as one persistent cooperative kernel (sm_103a).
+// Coarse-level Jacobi-PCG on the assembled operator as one persistent
+// cooperative kernel (sm_103a).
 //
 // The coarsest pMG level (order 1 in the configurations here) is solved by
 // Jacobi-preconditioned CG to a relative tolerance (1e-4 by default), the
 // build's stand-in for the reference's AMG coarse solve (coarseLevel_t::solve,
-// src/solvers/elliptic/MG/coarseLevel.cpp:182-222).  That solve takes on the
-// order of a hundred iterations on a few hundred thousand nodes: launch- and
-// latency-bound as separate kernels with a host convergence test per
-// iteration.  Here every iteration runs inside one kernel whose CTAs are all
-// co-resident (cooperative launch): element-parallel p = z + beta p and
-// A p (order-1 hexahedra, one thread per element), then mask + gather-
-// scatter, then the fused update x += alpha p, r -= alpha A p, z = invDiag r
-// with both dot products.  Grid-wide dependencies use a generation barrier
-// whose waits are bounded: on timeout the kernel records an error and every
-// CTA returns.  Dot products are deterministic: each CTA writes a partial,
-// every CTA sums all partials in index order after the barrier.  The whole
-// working set (about 40 B per node) stays in the 129 MB L2.
+// src/solvers/elliptic/MG/coarseLevel.cpp:182-222).  Like the reference, the
+// solve works on the assembled matrix of the level operator over the unmasked
+// unique nodes (ellipticBuildFEMHex3D, src/solvers/elliptic/MG/
+// ellipticBuildFEM.cpp:73-230).  That removes the gather-scatter, the mask
+// and the E-vector redundancy (8 copies per node of an order-1 hexahedral
+// mesh) from every iteration.
+//
+// The solve is a distributed SpMV inside one launch.  Rows are split into
+// contiguous blocks, one per CTA (one CTA per SM).  Everything a CTA owns
+// stays in shared memory for the whole solve: its rows of x, r, p, A p, z and
+// 1/diag, the list of other blocks' rows it reads (its halo) and, when it
+// fits, its block of the matrix in ELL form with local 16-bit column indices
+// (own rows first, then the halo).  Per iteration a CTA reads only the halo
+// values of z from L2 and writes only its own z back.  A p is carried by the
+// recurrence A p_new = A z + beta A p_old, so z is the only vector that
+// crosses CTAs.  One iteration is two phases separated by grid barriers:
+//   A  halo of z into shared memory; w = A z; p = z + beta p;
+//      Ap = w + beta Ap; partial (p, Ap)
+//   B  x += alpha p, r -= alpha Ap, z = invDiag r; partials (r, r), (r, z)
+// Per-thread products and warp sums run in the solve's precision (FP32 in
+// the mixed and FP32 multigrid; FP64 pipes are a small fraction of the FP32
+// ones on this part); sums across warps and CTAs are FP64.  Thread 0 forms
+// the scalars (alpha, beta, the convergence test) and shares them through
+// shared memory.
+// The grid barrier is one arrival counter per launch: each CTA adds 1 with a
+// release, then waits with acquire loads until the counter reaches its next
+// multiple of the grid size, then fences.  Every wait is bounded: on timeout
+// the kernel records an error flag and every CTA returns.  Values other CTAs
+// wrote during the launch (z, the solution, the partial sums) are read with
+// ld.global.cg from L2: an SM's L1 is not coherent with other SMs' stores.
+// Dot products are deterministic: each CTA writes a partial and every CTA
+// sums all partials in the same fixed order.
 
 #include "mg_kernels.hpp"
+
+#include <algorithm>
 
 namespace nrsg {
 
 namespace {
-constexpr int kCT = 256;              // threads per CTA
+constexpr int kCT = 1024;              // threads per CTA (one CTA per SM)
 constexpr long long kSpinLimit = 1LL << 22;
+constexpr int kMinRowsPerCta = 128;
 
 struct CoarseState {
-  unsigned count;
-  unsigned gen;
+  unsigned arrive;
   int err;
   int iters;
+  int pad;
   double res0, res;
 };
 
-__device__ __forceinline__ double cwarp(double v)
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p)
 {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ double cblock(double v, double *sh)
+__device__ __forceinline__ void red_release_add_u32(unsigned *p, unsigned v)
 {
-  v = cwarp(v);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) sh[wid] = v;
-  __syncthreads();
-  double r = 0;
-  if (wid == 0) r = cwarp(lane < kCT / 32 ? sh[lane] : 0.0);
-  __syncthreads();
-  return r; // valid in thread 0
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Grid barrier with bounded waiting.  Returns false (in every thread) if the
-// wait timed out or another CTA reported an error.
-__device__ bool grid_barrier(CoarseState *st)
+template <typename T> __device__ __forceinline__ T wsum(T v)
+{
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// CTA sums of one or two per-thread values (warp sums in T, then FP64 across
+// warps in warp 0); thread 0 stores them to dst0 / dst1.  `sh` holds 64 doubles.
+template <typename T> __device__ __forceinline__ void cta_partial(T a, double *sh, double *dst0)
+{
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  a = wsum(a);
+  if (lane == 0) sh[wid] = (double)a;
+  __syncthreads();
+  if (wid == 0) {
+    const double x = wsum(sh[lane]); // kCT / 32 == 32 warps
+    if (lane == 0) *dst0 = x;
+  }
+}
+template <typename T> __device__ __forceinline__ void cta_partial2(T a, T b, double *sh, double *dst0, double *dst1)
+{
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  a = wsum(a);
+  b = wsum(b);
+  if (lane == 0) {
+    sh[wid] = (double)a;
+    sh[32 + wid] = (double)b;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    const double x = wsum(sh[lane]), y = wsum(sh[32 + lane]);
+    if (lane == 0) {
+      *dst0 = x;
+      *dst1 = y;
+    }
+  }
+}
+
+// Sum of the per-CTA partials of one slot, in warp 0 (valid in its lanes).
+__device__ __forceinline__ double grid_sum(const double *part)
+{
+  double v = 0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) v += __ldcg(part + b);
+  return wsum(v);
+}
+
+// Grid barrier number `nb` (1, 2, ...).  Returns false in every thread of the
+// CTA if the wait timed out or another CTA reported an error.
+__device__ __forceinline__ bool grid_barrier(CoarseState *st, unsigned nb)
 {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    volatile unsigned *vgen = &st->gen;
-    volatile int *verr = &st->err;
-    const unsigned g = *vgen;
-    __threadfence();
-    const unsigned arrived = atomicAdd(&st->count, 1u);
+    red_release_add_u32(&st->arrive, 1u);
+    const unsigned target = nb * gridDim.x;
     int ok = 1;
-    if (arrived == gridDim.x - 1) {
-      st->count = 0;
-      __threadfence();
-      atomicAdd(&st->gen, 1u);
-    } else {
-      long long spins = 0;
-      while (*vgen == g) {
-        if (*verr) { ok = 0; break; }
-        if (++spins > kSpinLimit) {
+    long long spins = 0;
+    while ((int)(ld_acquire_u32(&st->arrive) - target) < 0) {
+      ++spins;
+      if ((spins & 63) == 0) {
+        if (*(volatile int *)&st->err) { ok = 0; break; }
+        if (spins > kSpinLimit) {
           atomicExch(&st->err, 1);
           ok = 0;
           break;
         }
-        if (spins > 256) __nanosleep(32);
       }
+      if (spins > 2048) __nanosleep(64);
     }
     __threadfence();
-    if (*verr) ok = 0;
     s_ok = ok;
   }
   __syncthreads();
   return s_ok != 0;
 }
 
-// sum of the per-CTA partials of `nslot` quantities (identical in every CTA)
-__device__ void grid_sums(const double *partials, int nslot, double *out, double *sh)
-{
-  for (int q = 0; q < nslot; ++q) {
-    double v = 0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += kCT) v += ((volatile const double *)partials)[q * gridDim.x + b];
-    v = cblock(v, sh);
-    if (threadIdx.x == 0) sh[32 + q] = v;
-    __syncthreads();
-    out[q] = sh[32 + q];
-    __syncthreads();
-  }
-}
+template <typename T> __device__ __forceinline__ T fma_t(T a, T b, T c);
+template <> __device__ __forceinline__ float fma_t<float>(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+template <> __device__ __forceinline__ double fma_t<double>(double a, double b, double c) { return __fma_rn(a, b, c); }
 
-// A q on one order-1 hexahedron (D = [[-1/2, 1/2], [-1/2, 1/2]])
-template <typename T>
-__device__ __forceinline__ void ax_n1(const T *__restrict__ g, T lam0, T lam1, bool poisson, const T q[8], T out[8])
+__host__ __device__ __forceinline__ size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
+
+// dynamic shared memory: z (own rows, then halo), x, r, p, Ap, 1/diag of the
+// own rows, the halo row list; then the matrix block when it is kept there
+template <typename T> __host__ __device__ __forceinline__ size_t vec_bytes(int chunk, int maxHalo)
 {
-  T Gr[8], Gs[8], Gt[8];
-#pragma unroll
-  for (int n = 0; n < 8; ++n) {
-    const int i = n & 1, j = (n >> 1) & 1, k = n >> 2;
-    const T qr = T(0.5) * (q[1 + 2 * j + 4 * k] - q[0 + 2 * j + 4 * k]);
-    const T qs = T(0.5) * (q[i + 2 + 4 * k] - q[i + 0 + 4 * k]);
-    const T qt = T(0.5) * (q[i + 2 * j + 4] - q[i + 2 * j + 0]);
-    const T G00 = g[0 * 8 + n], G01 = g[1 * 8 + n], G11 = g[2 * 8 + n];
-    const T G12 = g[3 * 8 + n], G02 = g[4 * 8 + n], G22 = g[5 * 8 + n];
-    Gr[n] = lam0 * (G00 * qr + G01 * qs + G02 * qt);
-    Gs[n] = lam0 * (G01 * qr + G11 * qs + G12 * qt);
-    Gt[n] = lam0 * (G02 * qr + G12 * qs + G22 * qt);
-  }
-#pragma unroll
-  for (int n = 0; n < 8; ++n) {
-    const int i = n & 1, j = (n >> 1) & 1, k = n >> 2;
-    const T si = i ? T(0.5) : T(-0.5), sj = j ? T(0.5) : T(-0.5), sk = k ? T(0.5) : T(-0.5);
-    T v = si * (Gr[0 + 2 * j + 4 * k] + Gr[1 + 2 * j + 4 * k]) + sj * (Gs[i + 0 + 4 * k] + Gs[i + 2 + 4 * k]) +
-          sk * (Gt[i + 2 * j + 0] + Gt[i + 2 * j + 4]);
-    if (!poisson) v += g[6 * 8 + n] * lam1 * q[n];
-    out[n] = v;
-  }
+  return align16(sizeof(T) * (6 * (size_t)chunk + maxHalo) + sizeof(int) * (size_t)maxHalo);
+}
+template <typename T> __host__ __device__ __forceinline__ size_t mat_bytes(int chunk, int width)
+{
+  return align16((size_t)width * chunk * (sizeof(T) + sizeof(unsigned short)));
 }
 } // namespace
 
 template <typename T> struct CoarseArgs {
-  long long E;
-  const T *ggeo;
-  T lam0, lam1;
-  bool poisson;
-  long long ngroups;
-  const int *gsOff, *gsIds;
-  long long nmask;
-  const int *mask;
-  const T *invDiag, *w, *b;
-  const unsigned char *gathered; // 1 where the node belongs to a gather group
-  T *x, *r, *p, *z, *Ap;
-  double *partials; // [3][gridDim]
+  long long nrow, nE;
+  int width, chunk, maxHalo, matInSmem;
+  const unsigned short *lcol; // [grid][width][chunk]
+  const T *val;               // [grid][width][chunk]
+  const int *haloOff, *haloIds;
+  const T *invDiag;           // [nrow]
+  const int *rep;             // [nrow] an E-vector node of each row
+  const int *rowOf;           // [nE] row of each E-vector node, -1 where masked
+  const T *b;                 // E-vector right-hand side (continuous, masked)
+  T *xE;                      // E-vector solution
+  T *x, *z;                   // [nrow]: the solution rows (for the scatter), z (for the halos)
+  double *partials;           // [3][gridDim]
   CoarseState *st;
-  double tol;       // relative
+  double tol;                 // relative
   int maxit;
 };
 
-template <typename T> __global__ void __launch_bounds__(kCT) coarse_pcg_kernel(CoarseArgs<T> a)
+template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_pcg_kernel(CoarseArgs<T> a)
 {
   __shared__ double sh[64];
-  const long long n = a.E * 8;
-  const long long tid = blockIdx.x * (long long)kCT + threadIdx.x;
-  const long long nth = (long long)gridDim.x * kCT;
-  double sums[2];
-  // x = 0, p = 0, r = b, z = invDiag r; partials: (r,r)_w and (r,z)_w
-  double rr = 0, rz = 0;
-  for (long long i = tid; i < n; i += nth) {
-    const T ri = a.b[i];
-    const T zi = a.invDiag[i] * ri;
-    a.x[i] = T(0);
-    a.p[i] = T(0);
-    a.r[i] = ri;
-    a.z[i] = zi;
-    rr += (double)a.w[i] * (double)ri * (double)ri;
-    rz += (double)a.w[i] * (double)ri * (double)zi;
+  __shared__ T s_alpha, s_beta;
+  __shared__ int s_cont;
+  extern __shared__ __align__(16) unsigned char dsm[];
+  const int chunk = a.chunk, W = a.width, mh = a.maxHalo;
+  const long long start = (long long)blockIdx.x * chunk;
+  const int cnt = (int)min((long long)chunk, a.nrow - start);
+  const int h0 = __ldg(a.haloOff + blockIdx.x), nh = __ldg(a.haloOff + blockIdx.x + 1) - h0;
+  T *zs = (T *)dsm; // [chunk + maxHalo]: own z, then the halo
+  T *xs = zs + chunk + mh, *rs = xs + chunk, *ps = rs + chunk, *aps = ps + chunk, *ids = aps + chunk;
+  int *hs = (int *)(ids + chunk);
+  const T *V;
+  const unsigned short *Lc;
+  {
+    const size_t off = (size_t)blockIdx.x * W * chunk;
+    if (a.matInSmem) {
+      T *sv = (T *)(dsm + vec_bytes<T>(chunk, mh));
+      unsigned short *sl = (unsigned short *)(sv + (size_t)W * chunk);
+      for (int i = threadIdx.x; i < W * chunk; i += kCT) {
+        sv[i] = __ldg(a.val + off + i);
+        sl[i] = __ldg(a.lcol + off + i);
+      }
+      V = sv;
+      Lc = sl;
+    } else {
+      V = a.val + off;
+      Lc = a.lcol + off;
+    }
   }
-  rr = cblock(rr, sh);
-  rz = cblock(rz, sh);
-  if (threadIdx.x == 0) {
-    a.partials[0 * gridDim.x + blockIdx.x] = rr;
-    a.partials[1 * gridDim.x + blockIdx.x] = rz;
+  for (int i = threadIdx.x; i < nh; i += kCT) hs[i] = __ldg(a.haloIds + h0 + i);
+  T *zg = a.z + start;
+  T rr = T(0), rz = T(0);
+  for (int t = threadIdx.x; t < cnt; t += kCT) {
+    const T ru = __ldg(a.b + __ldg(a.rep + start + t));
+    const T iv = __ldg(a.invDiag + start + t);
+    const T zu = iv * ru;
+    xs[t] = T(0);
+    ps[t] = T(0);
+    aps[t] = T(0);
+    rs[t] = ru;
+    ids[t] = iv;
+    zs[t] = zu;
+    zg[t] = zu;
+    rr = fma_t<T>(ru, ru, rr);
+    rz = fma_t<T>(ru, zu, rz);
   }
-  if (!grid_barrier(a.st)) return;
-  grid_sums(a.partials, 2, sums, sh);
-  const double r0 = sqrt(sums[0]);
-  double rdotz = sums[1], rdotz_old = 0;
-  double rn = r0;
-  const double tol = a.tol * r0;
+  cta_partial2<T>(rr, rz, sh, a.partials + blockIdx.x, a.partials + gridDim.x + blockIdx.x);
+  if (!grid_barrier(a.st, 1)) return;
+  unsigned nb = 1;
+  // scalars, kept by thread 0 of each CTA (identical in every CTA)
+  double r0 = 0, rn = 0, tol = 0, rdotz = 0;
   int it = 0;
-  while (rn > tol && it < a.maxit && r0 > 0) {
-    ++it;
-    const T beta = (it == 1) ? T(0) : (T)(rdotz / rdotz_old);
-    // A: p = z + beta p and A p, one element per thread; (p, Ap)_w over nodes outside gather groups
-    double pap = 0;
-    for (long long e = tid; e < a.E; e += nth) {
-      T q[8], out[8];
-#pragma unroll
-      for (int m = 0; m < 8; ++m) {
-        const T v = a.z[e * 8 + m] + beta * a.p[e * 8 + m];
-        a.p[e * 8 + m] = v;
-        q[m] = v;
-      }
-      ax_n1<T>(a.ggeo + e * 56, a.lam0, a.lam1, a.poisson, q, out);
-#pragma unroll
-      for (int m = 0; m < 8; ++m) {
-        a.Ap[e * 8 + m] = out[m];
-        if (!a.gathered[e * 8 + m]) pap += (double)a.w[e * 8 + m] * (double)q[m] * (double)out[m];
-      }
-    }
-    if (!grid_barrier(a.st)) return;
-    // B: mask and gather-scatter (disjoint node sets); (p, Ap)_w over the gathered nodes
-    for (long long m = tid; m < a.nmask; m += nth) a.Ap[a.mask[m]] = T(0);
-    for (long long g = tid; g < a.ngroups; g += nth) {
-      const int s0 = a.gsOff[g], t0 = a.gsOff[g + 1];
-      T v = 0;
-      for (int q = s0; q < t0; ++q) v += a.Ap[a.gsIds[q]];
-      for (int q = s0; q < t0; ++q) {
-        const int id = a.gsIds[q];
-        a.Ap[id] = v;
-        pap += (double)a.w[id] * (double)a.p[id] * (double)v;
-      }
-    }
-    pap = cblock(pap, sh);
-    if (threadIdx.x == 0) a.partials[2 * gridDim.x + blockIdx.x] = pap;
-    if (!grid_barrier(a.st)) return;
-    grid_sums(a.partials + 2 * gridDim.x, 1, sums, sh);
-    const T alpha = (T)(rdotz / (sums[0] + 1e-300));
-    // D: x += alpha p, r -= alpha Ap, z = invDiag r, partial (r,r)_w, (r,z)_w
-    rr = 0;
-    rz = 0;
-    for (long long i = tid; i < n; i += nth) {
-      a.x[i] += alpha * a.p[i];
-      const T ri = a.r[i] - alpha * a.Ap[i];
-      a.r[i] = ri;
-      const T zi = a.invDiag[i] * ri;
-      a.z[i] = zi;
-      rr += (double)a.w[i] * (double)ri * (double)ri;
-      rz += (double)a.w[i] * (double)ri * (double)zi;
-    }
-    rr = cblock(rr, sh);
-    rz = cblock(rz, sh);
+  if (threadIdx.x < 32) {
+    const double srr = grid_sum(a.partials), srz = grid_sum(a.partials + gridDim.x);
     if (threadIdx.x == 0) {
-      a.partials[0 * gridDim.x + blockIdx.x] = rr;
-      a.partials[1 * gridDim.x + blockIdx.x] = rz;
+      r0 = sqrt(srr);
+      rn = r0;
+      rdotz = srz;
+      tol = a.tol * r0;
+      s_beta = T(0);
+      s_cont = (rn > tol && a.maxit > 0 && r0 > 0) ? 1 : 0;
     }
-    if (!grid_barrier(a.st)) return;
-    grid_sums(a.partials, 2, sums, sh);
-    rn = sqrt(sums[0]);
-    rdotz_old = rdotz;
-    rdotz = sums[1];
+  }
+  __syncthreads();
+  while (s_cont) {
+    const T beta = s_beta;
+    // A: halo of z, then w = A z, p, Ap, (p, Ap)
+#pragma unroll 4
+    for (int i = threadIdx.x; i < nh; i += kCT) zs[chunk + i] = __ldcg(a.z + hs[i]);
+    __syncthreads();
+    T pap = T(0);
+    for (int t = threadIdx.x; t < cnt; t += kCT) {
+      T w = T(0);
+#pragma unroll 9
+      for (int k = 0; k < W; ++k) w = fma_t<T>(V[k * chunk + t], zs[Lc[k * chunk + t]], w);
+      const T pu = fma_t<T>(beta, ps[t], zs[t]);
+      const T apu = fma_t<T>(beta, aps[t], w);
+      ps[t] = pu;
+      aps[t] = apu;
+      pap = fma_t<T>(pu, apu, pap);
+    }
+    cta_partial<T>(pap, sh, a.partials + 2 * gridDim.x + blockIdx.x);
+    if (!grid_barrier(a.st, ++nb)) return;
+    if (threadIdx.x < 32) {
+      const double spap = grid_sum(a.partials + 2 * gridDim.x);
+      if (threadIdx.x == 0) s_alpha = (T)(rdotz / (spap + 1e-300));
+    }
+    __syncthreads();
+    const T alpha = s_alpha;
+    // B: x += alpha p, r -= alpha Ap, z = invDiag r, (r, r), (r, z)
+    rr = T(0);
+    rz = T(0);
+    for (int t = threadIdx.x; t < cnt; t += kCT) {
+      xs[t] = fma_t<T>(alpha, ps[t], xs[t]);
+      const T ru = fma_t<T>(-alpha, aps[t], rs[t]);
+      rs[t] = ru;
+      const T zu = ids[t] * ru;
+      zs[t] = zu;
+      zg[t] = zu;
+      rr = fma_t<T>(ru, ru, rr);
+      rz = fma_t<T>(ru, zu, rz);
+    }
+    cta_partial2<T>(rr, rz, sh, a.partials + blockIdx.x, a.partials + gridDim.x + blockIdx.x);
+    if (!grid_barrier(a.st, ++nb)) return;
+    if (threadIdx.x < 32) {
+      const double srr = grid_sum(a.partials), srz = grid_sum(a.partials + gridDim.x);
+      if (threadIdx.x == 0) {
+        ++it;
+        rn = sqrt(srr);
+        const double rdotz_old = rdotz;
+        rdotz = srz;
+        s_beta = (T)(rdotz / rdotz_old);
+        s_cont = (rn > tol && it < a.maxit) ? 1 : 0;
+      }
+    }
+    __syncthreads();
+  }
+  // E-vector solution: every copy of a row takes its value, masked nodes 0
+  for (int t = threadIdx.x; t < cnt; t += kCT) a.x[start + t] = xs[t];
+  if (!grid_barrier(a.st, ++nb)) return;
+  const long long tid = blockIdx.x * (long long)kCT + threadIdx.x, nth = (long long)gridDim.x * kCT;
+  for (long long i = tid; i < a.nE; i += nth) {
+    const int u = __ldg(a.rowOf + i);
+    a.xE[i] = u >= 0 ? __ldcg(a.x + u) : T(0);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     a.st->iters = it;
@@ -249,53 +314,124 @@ template <typename T> __global__ void __launch_bounds__(kCT) coarse_pcg_kernel(C
   }
 }
 
-template <typename T> struct CoarseSolverImpl;
-
-// Host side: grid sizing, scratch, launch.
+// Host: partition the rows over one CTA per SM, build each CTA's ELL block
+// (local columns: own rows 0..chunk-1, halo rows chunk..), its halo list and
+// the shared-memory plan.
 template <typename T>
-int coarse_pcg_persistent(long long E, const T *ggeo, T lam0, T lam1, bool poisson, long long ngroups,
-                          const int *gsOff, const int *gsIds, long long nmask, const int *mask, const T *invDiag,
-                          const T *w, const unsigned char *gathered, const T *b, T *x, T *r, T *p, T *z, T *Ap,
-                          double *partials, void *state, int gridMax, double tol, int maxit, cudaStream_t s)
+void coarse_matrix_setup(long long n, const long long *rowPtr, const long long *col, const double *val, long long nE,
+                         const long long *rowOfNode, const int *rep, CoarseMatrix<T> &M)
 {
-  int dev = 0, sms = 0, perSM = 0;
+  int dev = 0, sms = 0, optin = 0;
   NRSG_CUDA(cudaGetDevice(&dev));
   NRSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  NRSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, coarse_pcg_kernel<T>, kCT, 0));
-  int grid = sms * (perSM < 1 ? perSM : 1);
-  const long long need = (E * 8 + kCT - 1) / kCT;
-  if (grid > need) grid = (int)(need > 0 ? need : 1);
-  if (grid > gridMax) grid = gridMax;
-  if (grid < 1) throw Error(NRSG_ERR_CUDA, "coarse solver: no co-resident CTAs");
+  NRSG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (nE >= (1LL << 31) || n >= (1LL << 31)) throw Error(NRSG_ERR_BAD_CONFIG, "coarse level too large for 32-bit indices");
+  int width = 1;
+  for (long long r = 0; r < n; ++r) width = std::max(width, (int)(rowPtr[r + 1] - rowPtr[r]));
+  long long grid = std::min<long long>(sms, std::max<long long>(1, (n + kMinRowsPerCta - 1) / kMinRowsPerCta));
+  const long long chunk = std::max<long long>(1, (n + grid - 1) / grid);
+  grid = std::max<long long>(1, (n + chunk - 1) / chunk);
+  std::vector<int> haloOff(grid + 1, 0), haloIds;
+  std::vector<unsigned short> lcol((size_t)grid * width * chunk, 0);
+  std::vector<T> v((size_t)grid * width * chunk, T(0));
+  std::vector<long long> loc(n > 0 ? n : 1, -1);
+  int maxHalo = 0;
+  for (long long b = 0; b < grid; ++b) {
+    const long long s0 = b * chunk, s1 = std::min(n, s0 + chunk);
+    std::vector<long long> halo;
+    for (long long r = s0; r < s1; ++r)
+      for (long long q = rowPtr[r]; q < rowPtr[r + 1]; ++q)
+        if (col[q] < s0 || col[q] >= s1) halo.push_back(col[q]);
+    std::sort(halo.begin(), halo.end());
+    halo.erase(std::unique(halo.begin(), halo.end()), halo.end());
+    if (chunk + (long long)halo.size() > 65535)
+      throw Error(NRSG_ERR_BAD_CONFIG, "coarse level: row block and halo exceed 16-bit local indices");
+    for (size_t h = 0; h < halo.size(); ++h) loc[halo[h]] = chunk + (long long)h;
+    const size_t base = (size_t)b * width * chunk;
+    for (long long r = s0; r < s1; ++r) {
+      const long long t = r - s0, len = rowPtr[r + 1] - rowPtr[r];
+      for (int k = 0; k < width; ++k) {
+        const size_t at = base + (size_t)k * chunk + t;
+        if (k < len) {
+          const long long c = col[rowPtr[r] + k];
+          lcol[at] = (unsigned short)((c >= s0 && c < s1) ? c - s0 : loc[c]);
+          v[at] = (T)val[rowPtr[r] + k];
+        } else {
+          lcol[at] = (unsigned short)t; // padding: zero entry on the row itself
+        }
+      }
+    }
+    for (long long c : halo) haloIds.push_back((int)c);
+    haloOff[b + 1] = (int)haloIds.size();
+    maxHalo = std::max(maxHalo, (int)halo.size());
+  }
+  std::vector<T> invD(n > 0 ? n : 1, T(0));
+  for (long long r = 0; r < n; ++r)
+    for (long long q = rowPtr[r]; q < rowPtr[r + 1]; ++q)
+      if (col[q] == r && val[q] != 0.0) invD[r] = (T)(1.0 / val[q]);
+  std::vector<int> rowOf(nE);
+  for (long long i = 0; i < nE; ++i) rowOf[i] = (int)rowOfNode[i];
+  // shared memory: the row vectors and the halo list always; the matrix block when it fits
+  const size_t vBytes = vec_bytes<T>((int)chunk, maxHalo), mBytes = mat_bytes<T>((int)chunk, width);
+  const size_t limit = (size_t)optin > 2048 ? (size_t)optin - 2048 : 0; // static shared memory of the kernel
+  if (vBytes > limit) throw Error(NRSG_ERR_BAD_CONFIG, "coarse level: row block too large for shared memory");
+  M.matInSmem = vBytes + mBytes <= limit;
+  M.smem = vBytes + (M.matInSmem ? mBytes : 0);
+  NRSG_CUDA(cudaFuncSetAttribute(coarse_pcg_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)M.smem));
+  int perSM = 0;
+  NRSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, coarse_pcg_kernel<T>, kCT, M.smem));
+  if (perSM < 1) throw Error(NRSG_ERR_CUDA, "coarse solver: kernel cannot be resident");
+  M.nrow = n;
+  M.nE = nE;
+  M.width = width;
+  M.grid = (int)grid;
+  M.chunk = (int)chunk;
+  M.maxHalo = maxHalo;
+  M.nnz = n > 0 ? rowPtr[n] : 0;
+  M.lcol.upload(lcol);
+  M.val.upload(v);
+  M.haloOff.upload(haloOff);
+  if (haloIds.empty()) haloIds.push_back(0);
+  M.haloIds.upload(haloIds);
+  M.invDiag.upload(invD);
+  std::vector<int> repv(rep, rep + n);
+  if (repv.empty()) repv.push_back(0);
+  M.rep.upload(repv);
+  M.rowOf.upload(rowOf);
+}
+
+template <typename T>
+int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *z, double *partials, void *state,
+                          int gridMax, double tol, int maxit, cudaStream_t s)
+{
+  if (A.grid > gridMax) throw Error(NRSG_ERR_CUDA, "coarse solver: partial-sum buffer too small");
   NRSG_CUDA(cudaMemsetAsync(state, 0, sizeof(CoarseState), s));
   CoarseArgs<T> a;
-  a.E = E;
-  a.ggeo = ggeo;
-  a.lam0 = lam0;
-  a.lam1 = lam1;
-  a.poisson = poisson;
-  a.ngroups = ngroups;
-  a.gsOff = gsOff;
-  a.gsIds = gsIds;
-  a.nmask = nmask;
-  a.mask = mask;
-  a.invDiag = invDiag;
-  a.w = w;
-  a.gathered = gathered;
+  a.nrow = A.nrow;
+  a.nE = A.nE;
+  a.width = A.width;
+  a.chunk = A.chunk;
+  a.maxHalo = A.maxHalo;
+  a.matInSmem = A.matInSmem ? 1 : 0;
+  a.lcol = A.lcol.p;
+  a.val = A.val.p;
+  a.haloOff = A.haloOff.p;
+  a.haloIds = A.haloIds.p;
+  a.invDiag = A.invDiag.p;
+  a.rep = A.rep.p;
+  a.rowOf = A.rowOf.p;
   a.b = b;
+  a.xE = xE;
   a.x = x;
-  a.r = r;
-  a.p = p;
   a.z = z;
-  a.Ap = Ap;
   a.partials = partials;
   a.st = (CoarseState *)state;
   a.tol = tol;
   a.maxit = maxit;
   void *args[] = {&a};
-  NRSG_CUDA(cudaLaunchCooperativeKernel((const void *)coarse_pcg_kernel<T>, dim3(grid), dim3(kCT), args, 0, s));
+  NRSG_CUDA(cudaLaunchCooperativeKernel((const void *)coarse_pcg_kernel<T>, dim3(A.grid), dim3(kCT), args, A.smem, s));
   count_launch();
-  return grid;
+  return A.grid;
 }
 
 size_t coarse_state_bytes() { return sizeof(CoarseState); }
@@ -308,13 +444,13 @@ int coarse_state_read(const void *state_host, int *iters, double *res0, double *
   return st->err;
 }
 
-template int coarse_pcg_persistent<double>(long long, const double *, double, double, bool, long long, const int *,
-                                           const int *, long long, const int *, const double *, const double *,
-                                           const unsigned char *, const double *, double *, double *, double *,
-                                           double *, double *, double *, void *, int, double, int, cudaStream_t);
-template int coarse_pcg_persistent<float>(long long, const float *, float, float, bool, long long, const int *,
-                                          const int *, long long, const int *, const float *, const float *,
-                                          const unsigned char *, const float *, float *, float *, float *, float *,
-                                          float *, double *, void *, int, double, int, cudaStream_t);
+template void coarse_matrix_setup<double>(long long, const long long *, const long long *, const double *, long long,
+                                          const long long *, const int *, CoarseMatrix<double> &);
+template void coarse_matrix_setup<float>(long long, const long long *, const long long *, const double *, long long,
+                                         const long long *, const int *, CoarseMatrix<float> &);
+template int coarse_pcg_persistent<double>(const CoarseMatrix<double> &, const double *, double *, double *, double *,
+                                           double *, void *, int, double, int, cudaStream_t);
+template int coarse_pcg_persistent<float>(const CoarseMatrix<float> &, const float *, float *, float *, float *,
+                                          double *, void *, int, double, int, cudaStream_t);
 
 } // namespace nrsg

@@ -47,7 +47,7 @@ template <typename T> struct MGLevelDev {
 
 template <typename T> struct MGImpl : public MGState {
   Elliptic &el;
-  cudaStream_t s;
+  cudaStream_t &s; // the solver's stream (nrsg_elliptic_set_stream may replace it)
   MGPlan plan;
   std::vector<MGLevelDev<T>> lv;
   DevBuf<T> sRes, sRes2, sUpd, sTmp, rP, zP;
@@ -57,7 +57,10 @@ template <typename T> struct MGImpl : public MGState {
   bool persistentCoarse = false;
   static constexpr int kCoarseGridMax = 4096;
   DevBuf<double> cPartials;
-  DevBuf<unsigned char> cState, cGathered;
+  DevBuf<unsigned char> cState;
+  // assembled coarse operator and its row vectors
+  CoarseMatrix<T> cA;
+  DevBuf<T> cx, cz2;
   std::vector<int> coarseIters;
   T l0, l1;
   bool poisson;
@@ -128,9 +131,7 @@ template <typename T> struct MGImpl : public MGState {
       cPartials.alloc(3 * kCoarseGridMax);
       cState.alloc(coarse_state_bytes());
       NRSG_CUDA(cudaMemsetAsync(cState.p, 0, coarse_state_bytes(), s));
-      std::vector<unsigned char> flag(C.Nlocal, 0);
-      for (int id : C.gm.devIds) flag[id] = 1;
-      cGathered.upload(flag);
+      build_coarse_matrix(C);
     }
     if (!std::is_same<T, double>::value) {
       rP.alloc(el.fine.Nlocal);
@@ -164,6 +165,23 @@ template <typename T> struct MGImpl : public MGState {
   }
 
   // --------------------------------------------------------------- setup
+  // Assembled operator of the coarsest level in ELL form (rows padded to the
+  // widest row with zero entries on the row itself), its inverse diagonal, a
+  // representative E-vector node per row and the row of each E-vector node.
+  void build_coarse_matrix(const FieldLevel &C)
+  {
+    const std::vector<double> gg = C.d_ggeo64.download();
+    CsrMatrix A;
+    assemble_level(C.N, C.E, C.Dh, gg.data(), el.opt.lambda0, el.opt.lambda1, el.opt.poisson, C.gm, A);
+    std::vector<int> rep(A.nrow);
+    for (long long r = 0; r < A.nrow; ++r) rep[r] = C.gm.ids[C.gm.off[r]];
+    coarse_matrix_setup<T>(A.nrow, A.rowPtr.data(), A.col.data(), A.val.data(), C.Nlocal, A.rowOfNode.data(),
+                           rep.data(), cA);
+    const long long nv = std::max(A.nrow, 1LL);
+    cx.alloc(nv);
+    cz2.alloc(nv);
+  }
+
   void build_fdm(MGLevelDev<T> &v)
   {
     const FieldLevel &L = *v.L;
@@ -382,9 +400,7 @@ template <typename T> struct MGImpl : public MGState {
   {
     FieldLevel &L = *v.L;
     if (persistentCoarse) {
-      coarse_pcg_persistent<T>(L.E, v.ggeo.p, l0, l1, poisson, L.ngroups, L.d_gsOff.p, L.d_gsIds.p,
-                               (long long)L.maskIds.size(), L.d_mask.p, v.invDiag.p, v.invDegree.p, cGathered.p, b, x,
-                               cr.p, cp.p, cz.p, cAp.p, cPartials.p, cState.p, kCoarseGridMax, el.opt.coarseTol,
+      coarse_pcg_persistent<T>(cA, b, x, cx.p, cz2.p, cPartials.p, cState.p, kCoarseGridMax, el.opt.coarseTol,
                                el.opt.coarseMaxIter, s);
       return 0;
     }
@@ -490,7 +506,12 @@ template <typename T> struct MGImpl : public MGState {
       for (auto &v : lv) {
         if (v.smoothed) { out.push_back(v.down); out.push_back(v.up); }
       }
-    else
+    else if (what == "mg.coarseMatrix") {
+      // rows, ELL width, stored nonzeros, row blocks (CTAs), rows per block, matrix in shared memory
+      if (persistentCoarse)
+        out = {(double)cA.nrow, (double)cA.width, (double)cA.nnz, (double)cA.grid, (double)cA.chunk,
+               cA.matInSmem ? 1.0 : 0.0};
+    } else
       throw Error(NRSG_ERR_INVALID, "unknown array '" + what + "'");
     return out;
   }

@@ -27,4 +27,13 @@ void fdm_halo_maps(const FieldLevel &L, std::vector<int> &haloSrc, std::vector<i
                    std::vector<double> &wts);
 double hessenberg_spectral_radius(int n, const std::vector<double> &Hcol);
 
+// assembled level operator on the unmasked unique nodes (CSR, columns ascending)
+struct CsrMatrix {
+  long long nrow = 0;
+  std::vector<long long> rowPtr, col, rowOfNode; // rowOfNode: E-vector node -> row, -1 where masked
+  std::vector<double> val;
+};
+void assemble_level(int N, long long E, const std::vector<double> &Dh, const double *ggeo, double lam0, double lam1,
+                    bool poisson, const GatherMap &gm, CsrMatrix &A);
+
 } // namespace nrsg

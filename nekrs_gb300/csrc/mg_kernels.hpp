@@ -27,13 +27,31 @@ template <typename T>
 void launch_pcg_xr(long long n, const T *w, const T *p, const T *Ap, T *x, T *r, PcgScalars *sc, Reduce &red, int slot,
                    cudaStream_t s);
 
-// persistent cooperative Jacobi-PCG on an order-1 level (kernels_coarse.cu);
-// returns the grid size used.  `state` holds coarse_state_bytes() bytes.
+// assembled level operator on the device, partitioned into one row block per
+// CTA (kernels_coarse.cu)
+template <typename T> struct CoarseMatrix {
+  long long nrow = 0, nE = 0, nnz = 0;
+  int width = 0, grid = 0, chunk = 0, maxHalo = 0;
+  bool matInSmem = false;
+  size_t smem = 0;               // dynamic shared memory per CTA
+  DevBuf<unsigned short> lcol;   // [grid][width][chunk] local column: own row, or chunk + halo slot
+  DevBuf<T> val;                 // [grid][width][chunk], padding 0
+  DevBuf<int> haloOff, haloIds;  // per CTA: rows of other blocks it reads
+  DevBuf<T> invDiag;             // [nrow]
+  DevBuf<int> rep;               // [nrow] an E-vector node of each row
+  DevBuf<int> rowOf;             // [nE] row of each E-vector node, -1 where masked
+};
 template <typename T>
-int coarse_pcg_persistent(long long E, const T *ggeo, T lam0, T lam1, bool poisson, long long ngroups,
-                          const int *gsOff, const int *gsIds, long long nmask, const int *mask, const T *invDiag,
-                          const T *w, const unsigned char *gathered, const T *b, T *x, T *r, T *p, T *z, T *Ap,
-                          double *partials, void *state, int gridMax, double tol, int maxit, cudaStream_t s);
+void coarse_matrix_setup(long long n, const long long *rowPtr, const long long *col, const double *val, long long nE,
+                         const long long *rowOfNode, const int *rep, CoarseMatrix<T> &M);
+
+// persistent cooperative Jacobi-PCG on the assembled coarse operator: b and xE
+// are E-vectors, x and z row vectors (solution rows, exchanged z); returns the
+// grid size used.  `state` holds coarse_state_bytes() bytes, `partials`
+// 3 * gridMax doubles.
+template <typename T>
+int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *z, double *partials, void *state,
+                          int gridMax, double tol, int maxit, cudaStream_t s);
 size_t coarse_state_bytes();
 // decode a host copy of the state; returns the error flag (0 = ok)
 int coarse_state_read(const void *state_host, int *iters, double *res0, double *res);

@@ -1,6 +1,6 @@
 // Host-side p-multigrid setup: level schedule, FDM (Schwarz) operators,
-// neighbour-halo maps and the Hessenberg eigenvalue problem of the Arnoldi
-// lambda_max estimate.
+// neighbour-halo maps, the Hessenberg eigenvalue problem of the Arnoldi
+// lambda_max estimate and the assembled coarse operator.
 //
 // Reference behaviour (nekRS tree):
 //   schedule / default levels   src/solvers/elliptic/MG/parseMultigridSchedule.cpp:7-131,
@@ -12,6 +12,7 @@
 //                               edges masked), preFDM/postFDM kernels
 //   overlap weights             ellipticMultiGridSchwarz.cpp:792-834 (generate_weights)
 //   lambda_max eigenvalues      ellipticMultiGridLevelSetup.cpp:260-290 (LAPACK dgeev there)
+//   assembled coarse operator   ellipticBuildFEM.cpp:73-300 (ellipticBuildFEMHex3D)
 
 #include "mg_host.hpp"
 
@@ -477,6 +478,96 @@ double hessenberg_spectral_radius(int n, const std::vector<double> &Hcol)
     }
   }
   return rho;
+}
+
+// ---------------------------------------------------------------------------
+// Assembled level operator (the coarse-solver matrix).  The reference builds
+// it in ellipticBuildFEMHex3D (src/solvers/elliptic/MG/ellipticBuildFEM.cpp:
+// 73-230): per element the SEM stiffness matrix from ggeo and D, masked rows
+// and columns skipped, rows and columns numbered by the masked gather groups,
+// duplicates summed, exact zeros dropped.  Here each element matrix is the sum over quadrature
+// points q of the outer products of the gradient stencils at q
+// (A_nm = sum_q sum_ab Dg_a(q,n) G_ab(q) Dg_b(q,m), Dg_a(q,n) = D[q_a][n_a]
+// where n and q agree off direction a), times lambda0, plus lambda1 JW on the
+// diagonal of a Helmholtz operator.  Row r sums its members' contributions in
+// ascending E-vector order, which is ascending element order: an element adds
+// at most once to an entry, so the summation order is fixed.
+// ---------------------------------------------------------------------------
+void assemble_level(int N, long long E, const std::vector<double> &Dh, const double *ggeo, double lam0, double lam1,
+                    bool poisson, const GatherMap &gm, CsrMatrix &A)
+{
+  const int nq = N + 1, np = nq * nq * nq, ns = 3 * nq;
+  const long long nloc = E * np;
+  A.nrow = (long long)gm.off.size() - 1;
+  A.rowOfNode.assign(nloc, -1);
+  for (long long g = 0; g < A.nrow; ++g)
+    for (int q = gm.off[g]; q < gm.off[g + 1]; ++q) A.rowOfNode[gm.ids[q]] = g;
+  // element matrices [e][n][m]
+  std::vector<double> Ae((size_t)E * np * np, 0.0);
+#pragma omp parallel for schedule(static)
+  for (long long e = 0; e < E; ++e) {
+    double *M = &Ae[(size_t)e * np * np];
+    const double *g = ggeo + (size_t)e * 7 * np;
+    std::vector<int> sn(ns);
+    std::vector<double> sc(ns);
+    for (int k = 0; k < nq; ++k)
+      for (int j = 0; j < nq; ++j)
+        for (int i = 0; i < nq; ++i) {
+          const int q = i + nq * (j + nq * k);
+          for (int m = 0; m < nq; ++m) {
+            sn[m] = m + nq * (j + nq * k);
+            sc[m] = Dh[i * nq + m];
+            sn[nq + m] = i + nq * (m + nq * k);
+            sc[nq + m] = Dh[j * nq + m];
+            sn[2 * nq + m] = i + nq * (j + nq * m);
+            sc[2 * nq + m] = Dh[k * nq + m];
+          }
+          const double G[3][3] = {{g[0 * np + q], g[1 * np + q], g[4 * np + q]},
+                                  {g[1 * np + q], g[2 * np + q], g[3 * np + q]},
+                                  {g[4 * np + q], g[3 * np + q], g[5 * np + q]}};
+          for (int a = 0; a < ns; ++a) {
+            const double ca = sc[a];
+            if (ca == 0.0) continue;
+            const int na = sn[a], da = a / nq;
+            for (int b = 0; b < ns; ++b) {
+              const double cb = sc[b];
+              if (cb == 0.0) continue;
+              M[na * np + sn[b]] += lam0 * (ca * G[da][b / nq] * cb);
+            }
+          }
+        }
+    if (!poisson)
+      for (int n = 0; n < np; ++n) M[n * np + n] += lam1 * g[6 * np + n];
+  }
+  // rows: members in ascending E-vector order, then element columns
+  std::vector<std::vector<std::pair<long long, double>>> rows(A.nrow);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long r = 0; r < A.nrow; ++r) {
+    auto &row = rows[r];
+    for (int q = gm.off[r]; q < gm.off[r + 1]; ++q) {
+      const long long i = gm.ids[q], e = i / np;
+      const int n = (int)(i % np);
+      const double *M = &Ae[(size_t)e * np * np + (size_t)n * np];
+      for (int m = 0; m < np; ++m) {
+        const long long c = A.rowOfNode[e * np + m];
+        if (c < 0 || M[m] == 0.0) continue; // masked column, or an exact zero (dropped as the reference does)
+        size_t t = 0;
+        while (t < row.size() && row[t].first != c) ++t;
+        if (t == row.size()) row.push_back({c, 0.0});
+        row[t].second += M[m];
+      }
+    }
+    std::sort(row.begin(), row.end(), [](const auto &x, const auto &y) { return x.first < y.first; });
+  }
+  A.rowPtr.assign(A.nrow + 1, 0);
+  for (long long r = 0; r < A.nrow; ++r) A.rowPtr[r + 1] = A.rowPtr[r] + (long long)rows[r].size();
+  A.col.resize(A.rowPtr[A.nrow]);
+  A.val.resize(A.rowPtr[A.nrow]);
+  for (long long r = 0; r < A.nrow; ++r)
+    for (size_t t = 0; t < rows[r].size(); ++t) {
+      A.col[A.rowPtr[r] + t] = rows[r][t].first;
+      A.val[A.rowPtr[r] + t] = rows[r][t].second;
+    }
 }
 
 } // namespace nrsg

@@ -54,6 +54,8 @@ def lib():
         _lib.orc_mg_transfer.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, D, D]
         _lib.orc_hessenberg_rho.restype = ctypes.c_double
         _lib.orc_hessenberg_rho.argtypes = [ctypes.c_int, D]
+        _lib.orc_assemble_fem.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int] + \
+            [ctypes.c_void_p] * 5
         _lib.orc_global_ids.argtypes = [ctypes.c_int, ctypes.c_longlong, L, L]
         _lib.orc_gll.argtypes = [ctypes.c_int, D, D]
         _lib.orc_dmatrix.argtypes = [ctypes.c_int, D]
@@ -204,6 +206,19 @@ class Elliptic:
         out = np.zeros(nout)
         lib().orc_mg_transfer(self.h, level, 1 if restrict else 0, _p(v, D), _p(out, D))
         return out
+
+    def assemble(self, lambda0=1.0, lambda1=0.0, poisson=True):
+        """Assembled operator of this level (CSR: rowPtr, cols, vals), built as the reference's
+        FEM coarse-matrix builder does."""
+        nrow, nnz = ctypes.c_longlong(0), ctypes.c_longlong(0)
+        a = (self.h, float(lambda0), float(lambda1), int(poisson), ctypes.byref(nrow), ctypes.byref(nnz))
+        lib().orc_assemble_fem(*a, None, None, None)
+        rp = np.zeros(nrow.value + 1, np.int64)
+        cols = np.zeros(nnz.value, np.int64)
+        vals = np.zeros(nnz.value)
+        lib().orc_assemble_fem(*a, rp.ctypes.data_as(ctypes.c_void_p), cols.ctypes.data_as(ctypes.c_void_p),
+                               vals.ctypes.data_as(ctypes.c_void_p))
+        return rp, cols, vals
 
     def solve(self, rhs, x0=None):
         r = np.array(rhs, dtype=np.float64)

@@ -165,4 +165,19 @@ void orc_mg_transfer(void *h, int level, int restrict_, const double *in, double
 
 double orc_hessenberg_rho(int n, const double *H) { return hessenberg_rho_public(n, H); }
 
+// assembled fine-level operator (CSR); call with rowPtr == NULL for the sizes
+void orc_assemble_fem(void *h, double lambda0, double lambda1, int poisson, long long *nrow, long long *nnz,
+                      long long *rowPtr, long long *cols, double *vals)
+{
+  std::vector<long long> rp, c;
+  std::vector<double> v;
+  assemble_fem(((Elliptic *)h)->fine, lambda0, lambda1, poisson != 0, rp, c, v);
+  *nrow = (long long)rp.size() - 1;
+  *nnz = (long long)c.size();
+  if (!rowPtr) return;
+  std::memcpy(rowPtr, rp.data(), rp.size() * sizeof(long long));
+  std::memcpy(cols, c.data(), c.size() * sizeof(long long));
+  std::memcpy(vals, v.data(), v.size() * sizeof(double));
+}
+
 } // extern "C"

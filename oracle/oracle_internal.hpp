@@ -35,6 +35,9 @@ template <typename T> void gs_add(const Level &L, T *q);
 template <typename T> void apply_mask(const Level &L, T *q);
 template <typename T> T wdot(long long n, const T *w, const T *a, const T *b);
 
+void assemble_fem(const Level &L, double lambda0, double lambda1, bool poisson, std::vector<long long> &rowPtr,
+                  std::vector<long long> &cols, std::vector<double> &vals);
+
 struct MG; // multigrid state (oracle_mg.cpp)
 
 struct Elliptic {

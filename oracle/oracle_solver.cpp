@@ -14,6 +14,7 @@
 
 #include "oracle_internal.hpp"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -529,6 +530,88 @@ int Elliptic::pgmres(double *r, double *x, double tol, int maxit, double &rdotr)
     if (error <= tol) return iter;
   }
   return iter;
+}
+
+} // namespace orc
+
+namespace orc {
+
+// ---------------------------------------------------------------------------
+// Assembled level operator, following ellipticBuildFEMHex3D
+// (src/solvers/elliptic/MG/ellipticBuildFEM.cpp:73-300): per element and per
+// unmasked node pair (n, m) the stiffness entry is built term by term from
+// ggeo and D (rr, rs/sr, rt/tr, ss, st/ts, tt; lines 152-212), entries with
+// |val| > 0 are kept (line 227), rows/columns are the masked gather groups
+// (lines 98-117), entries are sorted by (row, column) and duplicates summed
+// (lines 258-297; summed here in element order).  The reference builds the
+// Poisson matrix (lambda1 = 0, line 90); a Helmholtz operator here adds
+// lambda1 JW on the diagonal, the same operator the level smoother applies.
+// ---------------------------------------------------------------------------
+void assemble_fem(const Level &L, double lambda0, double lambda1, bool poisson, std::vector<long long> &rowPtr,
+                  std::vector<long long> &cols, std::vector<double> &vals)
+{
+  const int nq = L.Nq, np = L.Np;
+  const double *D = L.D.data(); // D[i*nq + j] = l_j'(z_i)
+  std::vector<long long> num(L.Nlocal, -1);
+  const long long ng = (long long)L.gsOff.size() - 1;
+  for (long long g = 0; g < ng; ++g)
+    for (int q = L.gsOff[g]; q < L.gsOff[g + 1]; ++q) num[L.gsIds[q]] = g;
+  struct NZ { long long row, col, e; double val; };
+  std::vector<NZ> nz;
+  for (long long e = 0; e < L.E; ++e) {
+    const double *g = &L.ggeo[(size_t)e * 7 * np];
+    auto G = [&](int c, int i, int j, int k) { return g[c * np + i + nq * (j + nq * k)]; };
+    for (int nzc = 0; nzc < nq; ++nzc)
+      for (int ny = 0; ny < nq; ++ny)
+        for (int nx = 0; nx < nq; ++nx) {
+          const int idn = nx + nq * (ny + nq * nzc);
+          if (num[e * np + idn] < 0) continue;
+          for (int mz = 0; mz < nq; ++mz)
+            for (int my = 0; my < nq; ++my)
+              for (int mx = 0; mx < nq; ++mx) {
+                const int idm = mx + nq * (my + nq * mz);
+                if (num[e * np + idm] < 0) continue;
+                double val = 0;
+                if (ny == my && nzc == mz)
+                  for (int k = 0; k < nq; ++k) val += G(0, k, ny, nzc) * D[k * nq + nx] * D[k * nq + mx];
+                if (nzc == mz) {
+                  val += G(1, mx, ny, nzc) * D[mx * nq + nx] * D[ny * nq + my];
+                  val += G(1, nx, my, nzc) * D[nx * nq + mx] * D[my * nq + ny];
+                }
+                if (ny == my) {
+                  val += G(4, mx, ny, nzc) * D[mx * nq + nx] * D[nzc * nq + mz];
+                  val += G(4, nx, ny, mz) * D[nx * nq + mx] * D[mz * nq + nzc];
+                }
+                if (nx == mx && nzc == mz)
+                  for (int k = 0; k < nq; ++k) val += G(2, nx, k, nzc) * D[k * nq + ny] * D[k * nq + my];
+                if (nx == mx) {
+                  val += G(3, nx, my, nzc) * D[my * nq + ny] * D[nzc * nq + mz];
+                  val += G(3, nx, ny, mz) * D[ny * nq + my] * D[mz * nq + nzc];
+                }
+                if (nx == mx && ny == my)
+                  for (int k = 0; k < nq; ++k) val += G(5, nx, ny, k) * D[k * nq + nzc] * D[k * nq + mz];
+                double v = lambda0 * val;
+                if (!poisson && idn == idm) v += lambda1 * G(6, nx, ny, nzc);
+                if (std::fabs(v) > 0.0) nz.push_back({num[e * np + idn], num[e * np + idm], e, v});
+              }
+        }
+  }
+  std::stable_sort(nz.begin(), nz.end(), [](const NZ &a, const NZ &b) {
+    return a.row != b.row ? a.row < b.row : a.col < b.col;
+  });
+  rowPtr.assign(ng + 1, 0);
+  cols.clear();
+  vals.clear();
+  for (size_t i = 0; i < nz.size(); ++i) {
+    if (!cols.empty() && i > 0 && nz[i].row == nz[i - 1].row && nz[i].col == nz[i - 1].col) {
+      vals.back() += nz[i].val;
+      continue;
+    }
+    cols.push_back(nz[i].col);
+    vals.push_back(nz[i].val);
+    rowPtr[nz[i].row + 1]++;
+  }
+  for (long long r = 0; r < ng; ++r) rowPtr[r + 1] += rowPtr[r];
 }
 
 } // namespace orc

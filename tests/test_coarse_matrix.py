@@ -1,0 +1,69 @@
+"""Assembled level operator (the coarse-solver matrix), host code of the library
+against the oracle's restatement of the reference's FEM matrix builder and
+against the oracle's element-wise operator.  No GPU."""
+import numpy as np
+import pytest
+
+import nekrs_gb300 as G
+from nekrs_gb300 import workloads as W
+from oracle import oracle as O
+
+sp = pytest.importorskip("scipy.sparse")
+
+
+def _dense(rp, cols, vals):
+    n = len(rp) - 1
+    return sp.csr_matrix((vals, cols, rp), shape=(n, n))
+
+
+def _check(N, VX, EToV, EToB, lam0=1.0, lam1=0.0, poisson=True):
+    opts = "preconditioner=jacobi" + ("" if poisson else f";poisson=0;lambda0={lam0!r};lambda1={lam1!r}")
+    orc = O.Elliptic(N, VX, EToV, EToB, opts)
+    gg = orc.get("ggeo")
+    rp, cols, vals, rown = G.host_assemble_operator(N, EToV, EToB, gg, lam0, lam1, poisson)
+    rp2, cols2, vals2 = orc.assemble(lam0, lam1, poisson)
+    # same sparsity (exact zeros dropped in both), same values up to summation order
+    assert np.array_equal(rp, rp2) and np.array_equal(cols, cols2)
+    assert np.max(np.abs(vals - vals2)) <= 1e-14 * np.max(np.abs(vals2))
+    # rows are the masked gather groups, in order
+    off, ids = orc.get("gsOff"), orc.get("gsIds")
+    assert len(rp) - 1 == len(off) - 1
+    for g in (0, len(off) // 2, len(off) - 2):
+        assert np.all(rown[ids[off[g]:off[g + 1]]] == g)
+    assert np.all(rown[orc.get("maskIds")] == -1)
+    # the matrix is the level operator on continuous, masked vectors
+    A = _dense(rp, cols, vals)
+    u = np.random.default_rng(3).standard_normal(A.shape[0])
+    uE = np.where(rown >= 0, u[np.maximum(rown, 0)], 0.0)
+    AuE = orc.operator(uE)
+    ref = np.zeros(A.shape[0])
+    m = rown >= 0
+    ref[rown[m]] = AuE[m]
+    assert np.max(np.abs(A @ u - ref)) <= 1e-13 * np.max(np.abs(ref))
+    # symmetric
+    assert abs(A - A.T).max() <= 1e-15 * abs(A).max()
+    return A
+
+
+@pytest.mark.parametrize("N,n,eps", [(1, 4, 0.3), (1, 6, 0.3), (1, 3, 1.0), (2, 2, 0.3), (3, 2, 0.3)])
+def test_assembled_operator_matches_oracle(product_lib, oracle_mod, N, n, eps):
+    VX, EToV, EToB = W.kershaw_box(n, eps=eps)
+    A = _check(N, VX, EToV, EToB)
+    widths = np.diff(A.indptr)
+    if N == 1:
+        assert widths.max() <= 27
+    if N == 1 and eps == 1.0:
+        # rectilinear elements: the cross terms vanish exactly, a 7-point stencil remains
+        assert widths.max() == 7
+
+
+def test_assembled_helmholtz_operator(product_lib, oracle_mod):
+    VX, EToV, EToB = W.kershaw_box(4, eps=0.3)
+    _check(1, VX, EToV, EToB, lam0=1.3, lam1=0.7, poisson=False)
+
+
+def test_assembled_operator_neumann_faces(product_lib, oracle_mod):
+    VX, EToV, EToB = W.kershaw_box(3, 2, 2, eps=0.3, all_dirichlet=False)
+    EToB = EToB.copy()
+    EToB[0, 4] = 1
+    _check(1, VX, EToV, EToB)

@@ -112,8 +112,47 @@ def test_persistent_coarse_matches_host_driven(product_lib, torch_cuda):
         its.append(info["iterations"])
         sols.append(x.cpu().numpy())
         assert el.get("mg.coarseError")[0] == 0
+        if pers:
+            # the persistent solve runs on the assembled order-1 operator: one row per unmasked unique node
+            rows, width, nnz, grid, chunk, in_smem = el.get("mg.coarseMatrix")
+            assert rows == (n - 1) ** 3 and 7 <= width <= 27 and rows <= nnz <= rows * width
+            assert grid * chunk >= rows and in_smem == 1
+        else:
+            assert len(el.get("mg.coarseMatrix")) == 0
     assert its[0] == its[1]
     assert rel(sols[0], sols[1]) < 1e-10
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_persistent_coarse_many_row_blocks(product_lib, torch_cuda, prec):
+    """A coarse level spread over many CTAs (row blocks with halos, grid barriers between them) gives the
+    same preconditioner as the host-driven coarse loop on the E-vector level operator."""
+    torch = torch_cuda
+    N, n = 3, 16
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    base = (f"solver=pfcg;preconditioner=multigrid;smootherType=cheby+asm;mgPrecision={prec};"
+            f"residualTol=1e-9+relative;maxIterations=200;pMGSchedule={SCHED[3]}")
+    sols, its, cits = [], [], []
+    for pers in (1, 0):
+        el = G.Elliptic(N, VX, EToV, EToB, base + f";coarsePersistent={pers}")
+        if pers:
+            rows, width, nnz, grid, chunk, in_smem = el.get("mg.coarseMatrix")
+            assert rows == (n - 1) ** 3 and grid >= 8 and in_smem == 1
+        rhs = W.box_rhs(N, n, n, n, 11, el.get("ggeo"))
+        r = torch.from_numpy(rhs).cuda()
+        x = torch.zeros_like(r)
+        info = el.solve(r, x)
+        assert info["status"] == 0
+        its.append(info["iterations"])
+        cits.append(el.get("mg.coarseIters")[-1])
+        sols.append(x.cpu().numpy())
+        assert el.get("mg.coarseError")[0] == 0
+    if prec == "fp64":
+        assert its[0] == its[1] and abs(cits[0] - cits[1]) <= 1
+        assert rel(sols[0], sols[1]) < 1e-10
+    else:
+        assert abs(its[0] - its[1]) <= 1 and abs(cits[0] - cits[1]) <= 3
+        assert rel(sols[0], sols[1]) < 1e-7
 
 
 def test_mixed_precision_error_vs_fp64_oracle(product_lib, oracle_mod, torch_cuda):

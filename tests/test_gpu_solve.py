@@ -164,3 +164,31 @@ def test_jacobi_pcg_parity_tight_tolerance(product_lib, oracle_mod, torch_cuda):
     xo, io, xg, ig, el, orc = run_pair(torch_cuda, 5, 3, opts)
     assert abs(ig["iterations"] - io["iterations"]) <= 1
     assert rel(xg, xo) < 1e-10
+
+
+def test_solve_ordered_with_callers_torch_stream(product_lib, torch_cuda):
+    """Buffers written on the caller's torch stream are read only after those writes: the right-hand side
+    is copied in behind a GPU sleep on a side stream, right before the solve is called."""
+    torch = torch_cuda
+    N, n = 5, 4
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    opts = "preconditioner=jacobi;solver=pcg;residualTol=1e-10+relative;maxIterations=2000"
+    el = G.Elliptic(N, VX, EToV, EToB, opts)
+    rhs = W.box_rhs(N, n, n, n, 21, el.get("ggeo"))
+    rhs_d = torch.from_numpy(rhs).cuda()
+    r = rhs_d.clone()
+    x = torch.zeros_like(r)
+    ref = el.solve(r, x)
+    x_ref = x.cpu().numpy()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        r2 = torch.full_like(rhs_d, 1.0e3)
+        x2 = torch.full_like(rhs_d, -7.0)
+        torch.cuda._sleep(100_000_000)  # about 50 ms of GPU time before the writes below
+        r2.copy_(rhs_d)
+        x2.zero_()
+        info = el.solve(r2, x2)
+    side.synchronize()
+    assert info["iterations"] == ref["iterations"]
+    assert np.array_equal(x2.cpu().numpy(), x_ref)
