@@ -107,11 +107,20 @@ template <typename T> __device__ __forceinline__ void cta_partial2(T a, T b, dou
 }
 
 // Sum of the per-CTA partials of one slot, in warp 0 (valid in its lanes).
+// The first 160 partials are loaded at once (one L2 round trip for grids of
+// up to 160 CTAs), then added in a fixed order.
 __device__ __forceinline__ double grid_sum(const double *part)
 {
-  double v = 0;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) v += __ldcg(part + b);
-  return wsum(v);
+  const int G = (int)gridDim.x;
+  double v[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    const int b = threadIdx.x + 32 * j;
+    v[j] = b < G ? __ldcg(part + b) : 0.0;
+  }
+  double s = (v[0] + v[1]) + (v[2] + v[3]) + v[4];
+  for (int b = threadIdx.x + 160; b < G; b += 32) s += __ldcg(part + b);
+  return wsum(s);
 }
 
 // Grid barrier number `nb` (1, 2, ...).  Returns false in every thread of the
@@ -287,7 +296,8 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_pcg_kerne
     cta_partial2<T>(rr, rz, sh, a.partials + blockIdx.x, a.partials + gridDim.x + blockIdx.x);
     if (!grid_barrier(a.st, ++nb)) return;
     if (threadIdx.x < 32) {
-      const double srr = grid_sum(a.partials), srz = grid_sum(a.partials + gridDim.x);
+      const double srr = grid_sum(a.partials);
+      const double srz = grid_sum(a.partials + gridDim.x);
       if (threadIdx.x == 0) {
         ++it;
         rn = sqrt(srr);

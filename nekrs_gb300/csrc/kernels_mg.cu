@@ -20,6 +20,8 @@
 
 #include "mg_kernels.hpp"
 
+#include <type_traits>
+
 namespace nrsg {
 
 namespace {
@@ -378,12 +380,270 @@ __global__ void asm_combine_kernel(long long E, const int *__restrict__ haloPart
   for (int q = threadIdx.x; q < NP; q += blockDim.x) Su[e * NP + q] = s_u[q] * wts[e * NP + q];
 }
 
+// ---------------------------------------------------------------------------
+// FP32 FDM for order 7 (NQ = 8, extended NL = 10): one warp per element.
+// The generic kernel above gives every thread one line and reads each S entry
+// from shared memory once per multiply-add, so it is bound by shared-memory
+// wavefronts (about one per FMA).  Here each lane carries 4 lines (x
+// direction) or a bundle of 4 adjacent x-lines (y and z directions), so each
+// broadcast 128-bit load of an S row serves 4 lines, and the tile is laid out
+// (x stride 1 padded to 12, y stride 12, z stride 140 = 12 mod 32) so that
+// every 128-bit tile access of a warp is free of bank conflicts: in the y and
+// z phases lanes 3b..3b+2 cover one 12-float row; in the x phase the lines of
+// one 8-lane phase have distinct (y + z) mod 8 (kFdm8XLine).  Each output is
+// the same sequence of FMAs as in the generic kernel (l = 0..9 in order).
+// ---------------------------------------------------------------------------
+namespace fdm8 {
+constexpr int XS = 12, ZS = 140, WN = 10 * ZS; // tile strides; the z plane is padded to 140 floats
+constexpr int SR = 12, SN = 3 * 10 * SR;       // S rows padded to 12 floats, 3 directions
+constexpr int EPC = 4;                         // elements (warps) per CTA
+} // namespace fdm8
+
+// Tile offset of x-line r (0..3) of lane L (0..24), kFdm8XLine[r][L].  The
+// 100 lines (y, z) are grouped by (y + z) mod 8 (class sizes 13, 14, 13, 12,
+// 12, 12, 12, 12), each class ordered by y + z, then y; lanes 8p..8p+7 of
+// step r take line 3r + p of classes 0..7 and lane 24 takes the four lines
+// left over (class 0 #12, class 1 #12 and #13, class 2 #12).  Lines of one
+// 8-lane phase then start in distinct 4-bank groups.
+__device__ const short kFdm8XLine[4][32] = {
+    {0, 140, 280, 420, 560, 700, 840, 980, 1120, 12, 152, 292, 432, 572, 712, 852,
+     992, 1260, 24, 164, 304, 444, 584, 724, 1088, 0, 0, 0, 0, 0, 0, 0},
+    {864, 1132, 1272, 36, 176, 316, 456, 596, 736, 1004, 1144, 1284, 48, 188, 328, 468,
+     608, 876, 1016, 1156, 1296, 60, 200, 340, 1356, 0, 0, 0, 0, 0, 0, 0},
+    {480, 748, 888, 1028, 1168, 1308, 72, 212, 352, 620, 760, 900, 1040, 1180, 1320, 84,
+     224, 492, 632, 772, 912, 1052, 1192, 1332, 1228, 0, 0, 0, 0, 0, 0, 0},
+    {96, 364, 504, 644, 784, 924, 1064, 1204, 1344, 236, 376, 516, 656, 796, 936, 1076,
+     1216, 108, 248, 388, 528, 668, 808, 948, 1368, 0, 0, 0, 0, 0, 0, 0}};
+
+__device__ __forceinline__ void fdm8_row(const float *S, float sv[10])
+{
+  const float4 a = *(const float4 *)S, b = *(const float4 *)(S + 4), c = *(const float4 *)(S + 8);
+  sv[0] = a.x; sv[1] = a.y; sv[2] = a.z; sv[3] = a.w;
+  sv[4] = b.x; sv[5] = b.y; sv[6] = b.z; sv[7] = b.w;
+  sv[8] = c.x; sv[9] = c.y;
+}
+
+// out(i) = sum_l M[i][l] in(l) along x for the lane's 4 lines, in place
+__device__ __forceinline__ void fdm8_x(float *w, const float *M, const int base[4], int lane)
+{
+  if (lane >= 25) return;
+  float in[4][10], out[4][10];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const float4 a = *(const float4 *)(w + base[r]), b = *(const float4 *)(w + base[r] + 4);
+    const float2 c = *(const float2 *)(w + base[r] + 8);
+    in[r][0] = a.x; in[r][1] = a.y; in[r][2] = a.z; in[r][3] = a.w;
+    in[r][4] = b.x; in[r][5] = b.y; in[r][6] = b.z; in[r][7] = b.w;
+    in[r][8] = c.x; in[r][9] = c.y;
+  }
+#pragma unroll
+  for (int i = 0; i < 10; ++i) {
+    float sv[10];
+    fdm8_row(M + fdm8::SR * i, sv);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      float v = 0.f;
+#pragma unroll
+      for (int l = 0; l < 10; ++l) v = fmaf(sv[l], in[r][l], v);
+      out[r][i] = v;
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    *(float4 *)(w + base[r]) = make_float4(out[r][0], out[r][1], out[r][2], out[r][3]);
+    *(float4 *)(w + base[r] + 4) = make_float4(out[r][4], out[r][5], out[r][6], out[r][7]);
+    *(float2 *)(w + base[r] + 8) = make_float2(out[r][8], out[r][9]);
+  }
+}
+
+// the same along y (stride 12) or z (stride 140) for the lane's bundle of 4
+// adjacent x-lines; with `lam`, the forward z pass scales by 1/(lx + ly + lz)
+template <int STRIDE, bool SCALE>
+__device__ __forceinline__ void fdm8_yz(float *w, const float *M, int off, int lane, const float *lam, int y)
+{
+  if (lane >= 30) return;
+  float4 in[10];
+#pragma unroll
+  for (int l = 0; l < 10; ++l) in[l] = *(const float4 *)(w + off + STRIDE * l);
+  const int x0 = 4 * (lane % 3);
+#pragma unroll
+  for (int j = 0; j < 10; ++j) {
+    float sv[10];
+    fdm8_row(M + fdm8::SR * j, sv);
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int l = 0; l < 10; ++l) {
+      v.x = fmaf(sv[l], in[l].x, v.x);
+      v.y = fmaf(sv[l], in[l].y, v.y);
+      v.z = fmaf(sv[l], in[l].z, v.z);
+      v.w = fmaf(sv[l], in[l].w, v.w);
+    }
+    if (SCALE) {
+      float sc[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int x = x0 + c;
+        const float d = x < 10 ? (lam[x] + lam[10 + y]) + lam[20 + j] : 0.f;
+        sc[c] = d > 1e-5f ? 1.f / d : 0.f;
+      }
+      v.x *= sc[0];
+      v.y *= sc[1];
+      v.z *= sc[2];
+      v.w *= sc[3];
+    }
+    *(float4 *)(w + off + STRIDE * j) = v;
+  }
+}
+
+__device__ __forceinline__ int fdm8_ext(int f, int a, int b)
+{
+  using namespace fdm8;
+  switch (f) {
+  case 0: return 0 + XS * (a + 1) + ZS * (b + 1);
+  case 1: return 9 + XS * (a + 1) + ZS * (b + 1);
+  case 2: return (a + 1) + XS * 0 + ZS * (b + 1);
+  case 3: return (a + 1) + XS * 9 + ZS * (b + 1);
+  case 4: return (a + 1) + XS * (b + 1) + ZS * 0;
+  default: return (a + 1) + XS * (b + 1) + ZS * 9;
+  }
+}
+
+template <bool RAS>
+__global__ void __launch_bounds__(32 * fdm8::EPC, 5)
+    fdm8_kernel(long long E, const float *__restrict__ u, const int *__restrict__ haloSrc,
+                const float *__restrict__ Sx, const float *__restrict__ Sy, const float *__restrict__ Sz,
+                const float *__restrict__ lam, const float *__restrict__ wts, float *__restrict__ Su,
+                float *__restrict__ haloOut)
+{
+  using namespace fdm8;
+  constexpr int NP = 512, NF = 64;
+  __shared__ __align__(16) float s_w[EPC][WN];
+  __shared__ __align__(16) float s_F[EPC][SN]; // F[d][i][l] = S_d(l, i): forward rows
+  __shared__ __align__(16) float s_B[EPC][SN]; // B[d][i][l] = S_d(i, l): backward rows
+  __shared__ float s_lam[EPC][32];
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const long long e = (long long)blockIdx.x * EPC + wp;
+  if (e >= E) return; // whole warp; the kernel uses warp-level synchronisation only
+  float *w = s_w[wp], *F = s_F[wp], *B = s_B[wp], *lm = s_lam[wp];
+  // every global load of the element first, all independent (one round trip
+  // for S, lambda, u and the halo indices, one more for the halo values)
+  const float *Sd[3] = {Sx + e * 100, Sy + e * 100, Sz + e * 100};
+  float sreg[3][4];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int q = lane + 32 * m;
+      sreg[d][m] = q < 100 ? __ldg(Sd[d] + q) : 0.f;
+    }
+  const float lmv = lane < 30 ? __ldg(lam + e * 30 + lane) : 0.f;
+  const float4 *ue4 = (const float4 *)(u + e * NP);
+  float4 uv[4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m) uv[m] = __ldg(ue4 + lane + 32 * m);
+  const int *hs = haloSrc + e * 6 * NF;
+  int hsrc[12];
+#pragma unroll
+  for (int m = 0; m < 12; ++m) hsrc[m] = __ldg(hs + lane + 32 * m);
+  float hv[12];
+#pragma unroll
+  for (int m = 0; m < 12; ++m) hv[m] = hsrc[m] >= 0 ? __ldg(u + hsrc[m]) : 0.f;
+  // tile: zero, then own nodes and halo
+  for (int q = lane; q < WN / 4; q += 32) ((float4 *)w)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int q = lane + 32 * m;
+      if (q < 100) {
+        const int r = q % 10, c = q / 10; // S_d(r, c) = Sd[r + 10 c]
+        F[(d * 10 + c) * SR + r] = sreg[d][m];
+        B[(d * 10 + r) * SR + c] = sreg[d][m];
+      }
+    }
+  for (int q = lane; q < 60; q += 32) { // row pads (columns 10, 11)
+    const int row = q >> 1, col = 10 + (q & 1);
+    F[row * SR + col] = 0.f;
+    B[row * SR + col] = 0.f;
+  }
+  if (lane < 30) lm[lane] = lmv;
+  __syncwarp();
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const int q = lane + 32 * m;
+    const int i = (4 * q) & 7, j = (q >> 1) & 7, k = q >> 4;
+    float *dst = w + (i + 1) + XS * (j + 1) + ZS * (k + 1);
+    dst[0] = uv[m].x;
+    dst[1] = uv[m].y;
+    dst[2] = uv[m].z;
+    dst[3] = uv[m].w;
+  }
+#pragma unroll
+  for (int m = 0; m < 12; ++m) {
+    const int q = lane + 32 * m;
+    const int f = q / NF, pp = q % NF;
+    w[fdm8_ext(f, pp % 8, pp / 8)] = hv[m];
+  }
+  __syncwarp();
+  int base[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) base[r] = kFdm8XLine[r][lane];
+  const int offY = 4 * (lane % 3) + ZS * (lane / 3); // bundle (x quad, z) for the y pass
+  const int offZ = 4 * (lane % 3) + XS * (lane / 3); // bundle (x quad, y) for the z pass
+  fdm8_x(w, F, base, lane);
+  __syncwarp();
+  fdm8_yz<XS, false>(w, F + 10 * SR, offY, lane, lm, 0);
+  __syncwarp();
+  fdm8_yz<ZS, true>(w, F + 20 * SR, offZ, lane, lm, lane / 3);
+  __syncwarp();
+  fdm8_x(w, B, base, lane);
+  __syncwarp();
+  fdm8_yz<XS, false>(w, B + 10 * SR, offY, lane, lm, 0);
+  __syncwarp();
+  fdm8_yz<ZS, false>(w, B + 20 * SR, offZ, lane, lm, 0);
+  __syncwarp();
+  float *se = Su + e * NP;
+  for (int q = lane; q < NP / 4; q += 32) {
+    const int i = (4 * q) & 7, j = (q >> 1) & 7, k = q >> 4;
+    const float *src = w + (i + 1) + XS * (j + 1) + ZS * (k + 1);
+    float4 v = make_float4(src[0], src[1], src[2], src[3]);
+    if (RAS) {
+      const float4 wt = __ldg((const float4 *)(wts + e * NP) + q);
+      v.x *= wt.x;
+      v.y *= wt.y;
+      v.z *= wt.z;
+      v.w *= wt.w;
+    }
+    ((float4 *)se)[q] = v;
+  }
+  if (!RAS) {
+    float *ho = haloOut + e * 6 * NF;
+    for (int q = lane; q < 6 * NF; q += 32) {
+      const int f = q / NF, pp = q % NF;
+      ho[q] = w[fdm8_ext(f, pp % 8, pp / 8)];
+    }
+  }
+}
+
 template <typename T>
 void launch_fdm(int N, long long E, bool ras, const T *u, const int *haloSrc, const T *Sx, const T *Sy, const T *Sz,
                 const T *invL, const T *lam, const T *wts, T *Su, T *haloOut, cudaStream_t s)
 {
   if (E <= 0) return;
   const bool recip = (lam != nullptr);
+  if (std::is_same<T, float>::value && N == 7 && recip) {
+    const unsigned grid = (unsigned)((E + fdm8::EPC - 1) / fdm8::EPC);
+    const float *uf = (const float *)u, *Sxf = (const float *)Sx, *Syf = (const float *)Sy, *Szf = (const float *)Sz;
+    const float *lf = (const float *)lam, *wf = (const float *)wts;
+    if (ras)
+      fdm8_kernel<true><<<grid, 32 * fdm8::EPC, 0, s>>>(E, uf, haloSrc, Sxf, Syf, Szf, lf, wf, (float *)Su,
+                                                         (float *)haloOut);
+    else
+      fdm8_kernel<false><<<grid, 32 * fdm8::EPC, 0, s>>>(E, uf, haloSrc, Sxf, Syf, Szf, lf, wf, (float *)Su,
+                                                          (float *)haloOut);
+    NRSG_CHECK_LAUNCH();
+    return;
+  }
 #define NRSG_FDM(NQ)                                                                                       \
   {                                                                                                        \
     constexpr int EPB = FdmShape<NQ>::epb;                                                                 \

@@ -75,15 +75,19 @@ def test_default_levels_and_smoothed_coarse(product_lib, oracle_mod, torch_cuda)
     assert rel(xg, xo) < 1e-10
 
 
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("fp32", 2e-6)])
 @pytest.mark.parametrize("smoother", ["cheby+asm", "cheby+ras"])
 @pytest.mark.parametrize("N", [2, 5, 7])
-def test_schwarz_smoother_parity(product_lib, oracle_mod, torch_cuda, smoother, N):
+def test_schwarz_smoother_parity(product_lib, oracle_mod, torch_cuda, smoother, N, prec, tol):
+    """One application of the level-0 Schwarz smoother against the FP64 oracle (FP32 multigrid: within FP32
+    rounding of the six 1-D transforms; order 7 in FP32 runs the warp-per-element kernel)."""
     torch = torch_cuda
     n = 3
     VX, EToV, EToB = W.kershaw_box(n, eps=0.5)
     sched = f"p={N}+degree=2,p=1,p={N}+degree=2"
     opts = (f"solver=pfcg;preconditioner=multigrid;smootherType={smoother};mgPrecision=fp64;pMGSchedule={sched}")
     orc = O.Elliptic(N, VX, EToV, EToB, opts)
+    opts = opts.replace("mgPrecision=fp64", f"mgPrecision={prec}")
     el = G.Elliptic(N, VX, EToV, EToB, opts)
     u = np.random.default_rng(N).uniform(-1, 1, orc.Nlocal)
     u = orc.mask(orc.gs(u) * orc.get("invDegree"))  # a continuous, masked field
@@ -91,7 +95,7 @@ def test_schwarz_smoother_parity(product_lib, oracle_mod, torch_cuda, smoother, 
     ud = torch.from_numpy(u).cuda()
     out = torch.zeros_like(ud)
     el.mg_smoother(0, ud, out)
-    assert np.max(np.abs(out.cpu().numpy() - ref)) < 1e-12 * np.max(np.abs(ref))
+    assert np.max(np.abs(out.cpu().numpy() - ref)) < tol * np.max(np.abs(ref))
 
 
 def test_persistent_coarse_matches_host_driven(product_lib, torch_cuda):
