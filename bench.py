@@ -63,6 +63,9 @@ EXPECTED_ITERS = {"kershaw48-n7-mixed": 32, "kershaw32-n7-mixed": 25, "kershaw16
                   "kershaw32-n7-fp64": 53, "kershaw16-n7-jacobi": 1632,
                   "kershaw8-n7-jacobi": 800}
 METRIC = "Poisson DOFs/s (E*N^3 / time-to-tolerance)"
+# DRAM bytes (read + write) of one launch of the dominant kernel, from an ncu capture of the E=16^3 case of the
+# same solve scaled by the element count (the traffic grows with the elements; profiles/ has the capture)
+TRAFFIC = {}
 FP64_PLAIN = {"mgPrecision=mixed": "mgPrecision=fp64;axPrecision=fp64"}
 
 
@@ -250,6 +253,26 @@ def kernel_rooflines(G, el, N, E):
     return out, peak, src
 
 
+def fdm_roofline(G, el, N, E, peak):
+    """Achieved algorithmic GB/s of one fine-level fused FDM launch (the order-7 Schwarz local solve), CUDA
+    events on its stream.  Algorithmic bytes per element follow the reference's extended-element formulation:
+    read u_ext and write Su over (N+3)^3, S_x, S_y, S_z (3 (N+3)^2) and invL ((N+3)^3), 4 B each."""
+    import torch
+
+    if el.get("mg.bytes")[0] != 4:
+        return None
+    n = el.mg_level_size(0)
+    u = torch.rand(n, dtype=torch.float32, device="cuda")
+    su = torch.empty_like(u)
+    stream = torch.cuda.current_stream()
+    t = time_kernel(lambda: el.mg_fdm(0, u, su), stream)
+    nl = N + 3
+    per_el = 4.0 * (3 * nl ** 3 + 3 * nl ** 2)
+    flops = float(E) * (12 * nl * nl ** 3 + nl ** 3)
+    return {"launch_ms": t * 1e3, "achieved": per_el * E / t / 1e9, "unit": "GB/s", "algorithmic_bytes": per_el * E,
+            "fp32_tflops": flops / t / 1e12, "frac_of_hbm": per_el * E / t / 1e9 / peak}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -350,6 +373,8 @@ def main():
     e2e_s = float(np.mean(e2e_t))
     del rh, xh
 
+    peak, psrc = load_peaks()
+    fdm = fdm_roofline(G, el, N, E, peak) if "multigrid" in opts and "asm" in opts else None
     extra = {}
     if "mgPrecision=mixed" in opts and not args.no_fp64_plain:
         del el
@@ -377,13 +402,17 @@ def main():
     if el is None:
         el = G.Elliptic(N, VX, EToV, EToB, "preconditioner=jacobi")
     kr, peak, psrc = kernel_rooflines(G, el, N, E)
-    dominant = "ax_fp32x2" if "mixed" in opts else ("ax_stored_f64")
+    if fdm is not None:
+        kr["fdm_f32"] = fdm
+    # the dominant kernel of the solve by share of device time (profiles/: launch list of this workload)
+    dominant = "fdm_f32" if fdm is not None else ("ax_fp32x2" if "mixed" in opts else "ax_stored_f64")
     d = kr[dominant]
     roof = {"bound": "hbm", "kernel": dominant, "achieved": d["achieved"], "peak": peak, "unit": "GB/s",
-            "frac": d["achieved"] / peak, "traffic": None, "peak_source": psrc + " (MEASURED_PEAKS.json hbm_gbs)",
-            "launch_ms": d["launch_ms"], "kernels": kr,
-            "note": "FP64 axhelm is FP64-pipe bound on GB300 (1.25 TF/s nominal); ax_fp32x2 is its FP64-accurate "
-                    "FP32-pair form (FP32-pipe bound); ax_stored_f32 is the HBM-bound multigrid operator"}
+            "frac": d["achieved"] / peak, "traffic": TRAFFIC.get((args.workload, dominant)),
+            "peak_source": psrc + " (MEASURED_PEAKS.json hbm_gbs)", "launch_ms": d["launch_ms"], "kernels": kr,
+            "note": "fdm_f32: the order-7 FP32 Schwarz local solve, algorithmic bytes of the reference's extended-"
+                    "element form; FP64 axhelm is FP64-pipe bound on GB300 (1.25 TF/s nominal); ax_fp32x2 is its "
+                    "FP64-accurate FP32-pair form (FP32-pipe bound); ax_stored_f32 is the HBM-bound multigrid operator"}
 
     line = {"metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",

@@ -115,6 +115,14 @@ int nrsg_elliptic_get(nrsg_elliptic *el, const char *name, void *h_out, long lon
  * ellipticMultiGridSchwarz.cpp:1056-1156) applied once: Su = S u, FP64 in
  * and out (computed in the multigrid precision).  For parity checks. */
 int nrsg_elliptic_mg_smoother(nrsg_elliptic *el, int level, const double *d_u, double *d_Su);
+/* One launch of the fused FDM local solve of pMG level `level`
+ * (fusedFDM in pMGLevel::smoothSchwarz, ellipticMultiGridSchwarz.cpp:1064-1130)
+ * on device buffers of the multigrid precision (get "mg.bytes": 4 or 8) with
+ * mg_level_size(level) entries: d_Su = the element-local FDM result on the own
+ * nodes (RAS: times the overlap weights; ASM: the halo results stay inside
+ * the library for the combine step).  Asynchronous on the solver's stream; no
+ * gather-scatter or mask.  For kernel timing and parity checks. */
+int nrsg_elliptic_mg_fdm(nrsg_elliptic *el, int level, const void *d_u, void *d_Su);
 /* Number of E-vector nodes of pMG level `level` (-1 on error). */
 long long nrsg_elliptic_mg_level_size(nrsg_elliptic *el, int level);
 

@@ -72,6 +72,7 @@ def lib():
         L.nrsg_elliptic_mask.argtypes = [vp, vp]
         L.nrsg_elliptic_get.argtypes = [vp, ctypes.c_char_p, vp, ctypes.POINTER(LL)]
         L.nrsg_elliptic_mg_smoother.argtypes = [vp, ctypes.c_int, vp, vp]
+        L.nrsg_elliptic_mg_fdm.argtypes = [vp, ctypes.c_int, vp, vp]
         L.nrsg_elliptic_mg_level_size.restype = LL
         L.nrsg_elliptic_mg_level_size.argtypes = [vp, ctypes.c_int]
         d, f, i = ctypes.c_double, ctypes.c_float, ctypes.c_int
@@ -210,6 +211,11 @@ class Elliptic:
     def mg_smoother(self, level, u, Su):
         self._order_with(u, Su)
         check(lib().nrsg_elliptic_mg_smoother(self.h, level, _ptr(u), _ptr(Su)))
+
+    def mg_fdm(self, level, u, Su):
+        """One fused FDM launch of a level on buffers of the multigrid precision (asynchronous)."""
+        self._order_with(u, Su)
+        check(lib().nrsg_elliptic_mg_fdm(self.h, level, _ptr(u), _ptr(Su)))
 
     def mg_level_size(self, level):
         return lib().nrsg_elliptic_mg_level_size(self.h, level)

@@ -65,6 +65,29 @@ void FieldLevel::build(int N_, long long E_, const double *VX, const long long *
   d_mask.upload(maskIds);
   d_invDegree64.upload(gm.invDegree);
   ngroups = (long long)gm.devOff.size() - 1;
+  {
+    std::vector<int2> pairs;
+    std::vector<int> roff(1, 0), rids;
+    for (long long g = 0; g < ngroups; ++g) {
+      const int s0 = gm.devOff[g], s1 = gm.devOff[g + 1];
+      if (s1 - s0 == 2) {
+        pairs.push_back(make_int2(gm.devIds[s0], gm.devIds[s0 + 1]));
+      } else {
+        rids.insert(rids.end(), gm.devIds.begin() + s0, gm.devIds.begin() + s1);
+        roff.push_back((int)rids.size());
+      }
+    }
+    d_gsPairs.upload(pairs);
+    d_gsRestOff.upload(roff);
+    d_gsRestIds.upload(rids);
+    gsPlan.npairs = (long long)pairs.size();
+    gsPlan.nrest = (long long)roff.size() - 1;
+    gsPlan.nmask = (long long)maskIds.size();
+    gsPlan.pairs = d_gsPairs.p;
+    gsPlan.restOff = d_gsRestOff.p;
+    gsPlan.restIds = d_gsRestIds.p;
+    gsPlan.mask = d_mask.p;
+  }
   // volume = sum of JW over the E-vector (meshSetup.cpp:444)
   std::vector<double> gg = d_ggeo64.download();
   volume = 0;
@@ -172,8 +195,7 @@ void Elliptic::ax(const double *q, double *Aq)
 void Elliptic::op(const double *q, double *Aq)
 {
   ax(q, Aq);
-  launch_mask<double>((long long)fine.maskIds.size(), fine.d_mask.p, Aq, stream);
-  launch_gs<double>(fine.ngroups, fine.d_gsOff.p, fine.d_gsIds.p, Aq, stream);
+  launch_gs_mask<double>(fine.gsPlan, Aq, true, stream); // mask and gather-scatter
 }
 
 void Elliptic::precondition(const double *r, double *zz)
@@ -242,8 +264,7 @@ int Elliptic::solve(double *r, double *x, nrsg_solve_info *info)
   // r = b - A x0 (local Ax, ellipticSolve.cpp:91-103), mask, gather-scatter
   ax(x, Ap.p);
   launch_axpby<double>(n, -1.0, Ap.p, 1.0, r, stream);
-  launch_mask<double>((long long)fine.maskIds.size(), fine.d_mask.p, r, stream);
-  launch_gs<double>(fine.ngroups, fine.d_gsOff.p, fine.d_gsIds.p, r, stream);
+  launch_gs_mask<double>(fine.gsPlan, r, true, stream); // mask and gather-scatter
   NRSG_CUDA(cudaMemcpyAsync(x0.p, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
   launch_fill<double>(n, 0.0, x, stream);
   launch_wdot<double>(n, fine.d_invDegree64.p, r, nullptr, &d_scal.p->rdotr, red, 0, stream);
@@ -463,6 +484,11 @@ int nrsg_elliptic_mg_smoother(nrsg_elliptic *el, int level, const double *d_u, d
 {
   if (!el || !d_u || !d_Su) return NRSG_ERR_INVALID;
   NRSG_TRY(el->impl->mg_schwarz(level, d_u, d_Su))
+}
+int nrsg_elliptic_mg_fdm(nrsg_elliptic *el, int level, const void *d_u, void *d_Su)
+{
+  if (!el || !d_u || !d_Su) return NRSG_ERR_INVALID;
+  NRSG_TRY(el->impl->mg_fdm(level, d_u, d_Su))
 }
 long long nrsg_elliptic_mg_level_size(nrsg_elliptic *el, int level)
 {

@@ -26,6 +26,9 @@ struct FieldLevel {
   DevBuf<double> d_ggeo64, d_D64, d_z64, d_w64, d_VX64, d_invDegree64;
   DevBuf<float> d_ggeo32, d_D32, d_z32, d_w32, d_VX32, d_invDegree32;
   DevBuf<int> d_gsOff, d_gsIds, d_mask;
+  DevBuf<int2> d_gsPairs;                // gather-scatter plan (pairs + other groups + mask)
+  DevBuf<int> d_gsRestOff, d_gsRestIds;
+  GsPlan gsPlan;
 
   void build(int N, long long E, const double *VX, const long long *EToV, const int *EToB, const double *h_ggeo,
              cudaStream_t s);
@@ -83,6 +86,7 @@ struct Elliptic {
   std::vector<double> mg_get(const std::string &name);
   long long mg_level_size(int level);
   void mg_schwarz(int level, const double *u, double *Su);
+  void mg_fdm(int level, const void *u, void *Su);
 };
 
 // GMRES kernels (kernels_vec.cu)

@@ -411,8 +411,9 @@ namespace nrsg {
 // sum hi + lo of two floats (about 48 significant bits): products are formed
 // exactly with fmaf (TwoProduct), sums are accumulated with Knuth's TwoSum
 // and the rounding errors are carried in a second float.  D and the geometric
-// factors are split once at setup; q is split on load and A q is returned as
-// the double hi + lo.  Accuracy is about 2^-47 relative per term (FP64: 2^-53),
+// factors are split once at setup; q is split on load (integer bit
+// operations, no FP64 instructions) and A q is returned as the double hi + lo
+// (one FP64 add).  Accuracy is about 2^-47 relative per term (FP64: 2^-53),
 // i.e. ~1e-14 on the operator; see the parity tests for the measured error.
 // ===========================================================================
 namespace {
@@ -436,10 +437,35 @@ __device__ __forceinline__ void norm2(F2 a, float &hi, float &lo)
   hi = a.s + a.t;
   lo = a.t - (hi - a.s);
 }
+// x = hi + lo from the bits of x, without FP64 instructions (the FP64 pipe is
+// 1/64 of the FP32 rate): hi = x with its mantissa truncated to 23 bits, lo =
+// the 29 bits below, rounded to 24 bits (I2F) and scaled by 2^(e - 52).
+// Together about 2^-47 relative.  |x| < 2^-126 flushes to 0; for
+// |x| < 2^-74 lo (below the normal float range) flushes to 0.
 __device__ __forceinline__ void split_d(double x, float &hi, float &lo)
 {
-  hi = __double2float_rn(x);
-  lo = __double2float_rn(x - (double)hi);
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned w1 = (unsigned)(b >> 32), w0 = (unsigned)b;
+  const int ex = (int)((w1 >> 20) & 0x7FF);
+  const unsigned sign = w1 & 0x80000000u;
+  if (ex < 897 || ex > 1150) { // zero, subnormal, below/above the float range
+    hi = 0.f;
+    lo = 0.f;
+    return;
+  }
+  hi = __uint_as_float(sign | ((unsigned)(ex - 896) << 23) | ((w1 & 0xFFFFFu) << 3) | (w0 >> 29));
+  const float r = __uint2float_rn(w0 & 0x1FFFFFFFu);
+  lo = ex >= 949 ? __uint_as_float(sign | __float_as_uint(r * __uint_as_float((unsigned)(ex - 1075 + 127) << 23))) : 0.f;
+}
+// the double of a float from its bits (normal floats; zero and subnormals give 0)
+__device__ __forceinline__ double widen(float f)
+{
+  const unsigned u = __float_as_uint(f);
+  const unsigned ef = (u >> 23) & 0xFFu;
+  if (ef == 0u) return 0.0;
+  const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
+                               ((unsigned long long)(ef + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)b);
 }
 } // namespace
 
@@ -557,7 +583,7 @@ __global__ void __launch_bounds__(NQ *NQ *AxShape<NQ>::epb)
     for (int k = 0; k < NQ; ++k) {
       float h, l;
       norm2(aq[k], h, l);
-      Aq[base + k * NQ * NQ] = (double)h + (double)l;
+      Aq[base + k * NQ * NQ] = widen(h) + widen(l);
     }
   }
 }

@@ -25,7 +25,8 @@
 //   B  x += alpha p, r -= alpha Ap, z = invDiag r; partials (r, r), (r, z)
 // Per-thread products and warp sums run in the solve's precision (FP32 in
 // the mixed and FP32 multigrid; FP64 pipes are a small fraction of the FP32
-// ones on this part); sums across warps and CTAs are FP64.  Thread 0 forms
+// ones on this part); sums across warps and CTAs are FP64 (FP32 in the
+// pipelined FP32 variant).  Thread 0 forms
 // the scalars (alpha, beta, the convergence test) and shares them through
 // shared memory.
 // The grid barrier is one arrival counter per launch: each CTA adds 1 with a
@@ -106,6 +107,32 @@ template <typename T> __device__ __forceinline__ void cta_partial2(T a, T b, dou
   }
 }
 
+// Three CTA sums entirely in T (the pipelined variant; FP32 sums are enough
+// for a solve to 1e-4 and avoid the slow FP64 pipe), fixed order.  `sh`
+// holds 96 values of T.
+template <typename T>
+__device__ __forceinline__ void cta_partial3(T a, T b, T c, T *sh, T *dst0, T *dst1, T *dst2)
+{
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  a = wsum(a);
+  b = wsum(b);
+  c = wsum(c);
+  if (lane == 0) {
+    sh[wid] = a;
+    sh[32 + wid] = b;
+    sh[64 + wid] = c;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    const T x = wsum(sh[lane]), y = wsum(sh[32 + lane]), z = wsum(sh[64 + lane]);
+    if (lane == 0) {
+      *dst0 = x;
+      *dst1 = y;
+      *dst2 = z;
+    }
+  }
+}
+
 // Sum of the per-CTA partials of one slot, in warp 0 (valid in its lanes).
 // The first 160 partials are loaded at once (one L2 round trip for grids of
 // up to 160 CTAs), then added in a fixed order.
@@ -121,6 +148,30 @@ __device__ __forceinline__ double grid_sum(const double *part)
   double s = (v[0] + v[1]) + (v[2] + v[3]) + v[4];
   for (int b = threadIdx.x + 160; b < G; b += 32) s += __ldcg(part + b);
   return wsum(s);
+}
+
+// Sums of three consecutive slots of per-CTA partials, in warp 0: every load
+// is issued before the first add.
+template <typename T> __device__ __forceinline__ void grid_sum3(const T *part, T &s0, T &s1, T &s2)
+{
+  const int G = (int)gridDim.x;
+  T v[3][5];
+#pragma unroll
+  for (int q = 0; q < 3; ++q)
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      const int b = threadIdx.x + 32 * j;
+      v[q][j] = b < G ? __ldcg(part + q * G + b) : T(0);
+    }
+  T t[3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    t[q] = (v[q][0] + v[q][1]) + (v[q][2] + v[q][3]) + v[q][4];
+    for (int b = threadIdx.x + 160; b < G; b += 32) t[q] += __ldcg(part + q * G + b);
+  }
+  s0 = wsum(t[0]);
+  s1 = wsum(t[1]);
+  s2 = wsum(t[2]);
 }
 
 // Grid barrier number `nb` (1, 2, ...).  Returns false in every thread of the
@@ -165,6 +216,11 @@ template <typename T> __host__ __device__ __forceinline__ size_t vec_bytes(int c
 {
   return align16(sizeof(T) * (6 * (size_t)chunk + maxHalo) + sizeof(int) * (size_t)maxHalo);
 }
+// pipelined variant: m (own rows, then halo), x, r, u, w, z, q, s, p, 1/diag, the halo list
+template <typename T> __host__ __device__ __forceinline__ size_t vec_bytes_pipe(int chunk, int maxHalo)
+{
+  return align16(sizeof(T) * (10 * (size_t)chunk + maxHalo) + sizeof(int) * (size_t)maxHalo);
+}
 template <typename T> __host__ __device__ __forceinline__ size_t mat_bytes(int chunk, int width)
 {
   return align16((size_t)width * chunk * (sizeof(T) + sizeof(unsigned short)));
@@ -183,7 +239,8 @@ template <typename T> struct CoarseArgs {
   const T *b;                 // E-vector right-hand side (continuous, masked)
   T *xE;                      // E-vector solution
   T *x, *z;                   // [nrow]: the solution rows (for the scatter), z (for the halos)
-  double *partials;           // [3][gridDim]
+  T *z2;                      // [nrow]: second exchange buffer (pipelined variant)
+  double *partials;           // [3][gridDim] (pipelined: [2][3][gridDim])
   CoarseState *st;
   double tol;                 // relative
   int maxit;
@@ -324,6 +381,164 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_pcg_kerne
   }
 }
 
+// Pipelined Jacobi-PCG (Ghysels and Vanroose, "Hiding global synchronization
+// latency in the preconditioned conjugate gradient algorithm", Parallel
+// Computing 40 (2014), Alg. 4) in the same row-block layout: the dot products
+// (r,u), (w,u), (r,r) of an iteration and the exchange of m = M^-1 w complete
+// at one grid barrier, and the SpMV n = A m and all vector updates follow
+// without another; one barrier per iteration instead of two.  Mathematically
+// the same iterates as PCG; the convergence test reads ||r_i|| before the
+// update that would produce r_{i+1}, so the iteration count is PCG's.  The
+// published m and the partial sums alternate between two buffers by iteration
+// parity: a CTA rewrites a buffer only after passing a barrier that every
+// reader of its previous contents has reached.
+template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_ppcg_kernel(CoarseArgs<T> a)
+{
+  __shared__ T sh[96];
+  __shared__ T s_alpha, s_beta;
+  __shared__ int s_cont;
+  extern __shared__ __align__(16) unsigned char dsm[];
+  const int chunk = a.chunk, W = a.width, mh = a.maxHalo;
+  const long long start = (long long)blockIdx.x * chunk;
+  const int cnt = (int)min((long long)chunk, a.nrow - start);
+  const int h0 = __ldg(a.haloOff + blockIdx.x), nh = __ldg(a.haloOff + blockIdx.x + 1) - h0;
+  T *ms = (T *)dsm; // [chunk + maxHalo]: m (own rows, then halo)
+  T *xs = ms + chunk + mh, *rs = xs + chunk, *us = rs + chunk, *wv = us + chunk, *zv = wv + chunk;
+  T *qv = zv + chunk, *sv = qv + chunk, *pv = sv + chunk, *ids = pv + chunk;
+  int *hs = (int *)(ids + chunk);
+  const T *V;
+  const unsigned short *Lc;
+  {
+    const size_t off = (size_t)blockIdx.x * W * chunk;
+    if (a.matInSmem) {
+      T *svm = (T *)(dsm + vec_bytes_pipe<T>(chunk, mh));
+      unsigned short *sl = (unsigned short *)(svm + (size_t)W * chunk);
+      for (int i = threadIdx.x; i < W * chunk; i += kCT) {
+        svm[i] = __ldg(a.val + off + i);
+        sl[i] = __ldg(a.lcol + off + i);
+      }
+      V = svm;
+      Lc = sl;
+    } else {
+      V = a.val + off;
+      Lc = a.lcol + off;
+    }
+  }
+  for (int i = threadIdx.x; i < nh; i += kCT) hs[i] = __ldg(a.haloIds + h0 + i);
+  // exchange buffers: u0 goes through a.z, m_i through a.z2 (i even) / a.z (i odd)
+  // r0 = b, u0 = M^-1 r0 (published for the halos), x0 = 0
+  for (int t = threadIdx.x; t < cnt; t += kCT) {
+    const T ru = __ldg(a.b + __ldg(a.rep + start + t));
+    const T iv = __ldg(a.invDiag + start + t);
+    const T uu = iv * ru;
+    xs[t] = T(0);
+    rs[t] = ru;
+    us[t] = uu;
+    ids[t] = iv;
+    zv[t] = T(0);
+    qv[t] = T(0);
+    sv[t] = T(0);
+    pv[t] = T(0);
+    ms[t] = uu;
+    a.z[start + t] = uu;
+  }
+  if (!grid_barrier(a.st, 1)) return;
+  unsigned nb = 1;
+  // w0 = A u0
+#pragma unroll 4
+  for (int i = threadIdx.x; i < nh; i += kCT) ms[chunk + i] = __ldcg(a.z + hs[i]);
+  __syncthreads();
+  for (int t = threadIdx.x; t < cnt; t += kCT) {
+    T w = T(0);
+#pragma unroll 9
+    for (int k = 0; k < W; ++k) w = fma_t<T>(V[k * chunk + t], ms[Lc[k * chunk + t]], w);
+    wv[t] = w;
+  }
+  // scalars, kept by thread 0 of each CTA (identical in every CTA)
+  double r0 = 0, rn = 0, tol = 0, gamma_old = 1, alpha_old = 1;
+  int it = 0;
+  for (int i = 0;; ++i) {
+    T *mg = (i & 1) ? a.z : a.z2;
+    T *part = (T *)a.partials + (size_t)(i & 1) * 3 * gridDim.x; // partials in T
+    __syncthreads(); // the previous SpMV has read ms
+    // phase 1: partial (r,u), (w,u), (r,r); m = M^-1 w, published
+    T g = T(0), d = T(0), rr = T(0);
+    for (int t = threadIdx.x; t < cnt; t += kCT) {
+      const T ru = rs[t], uu = us[t], ww = wv[t];
+      g = fma_t<T>(ru, uu, g);
+      d = fma_t<T>(ww, uu, d);
+      rr = fma_t<T>(ru, ru, rr);
+      const T mm = ids[t] * ww;
+      ms[t] = mm;
+      mg[start + t] = mm;
+    }
+    cta_partial3<T>(g, d, rr, sh, part + blockIdx.x, part + gridDim.x + blockIdx.x, part + 2 * gridDim.x + blockIdx.x);
+    if (!grid_barrier(a.st, ++nb)) return;
+    if (threadIdx.x < 32) {
+      T sgT, sdT, srrT;
+      grid_sum3<T>(part, sgT, sdT, srrT);
+      const double sg = (double)sgT, sd = (double)sdT, srr = (double)srrT;
+      if (threadIdx.x == 0) {
+        // scalars in the solve's precision T (FP32 here: no FP64 divide or sqrt)
+        rn = (double)sqrt((T)srr);
+        if (i == 0) {
+          r0 = rn;
+          tol = a.tol * r0;
+        }
+        const int cont = (rn > tol && it < a.maxit && r0 > 0) ? 1 : 0;
+        if (cont) {
+          const T g = (T)sg, dd = (T)sd;
+          const T beta = (i == 0) ? T(0) : g / (T)gamma_old;
+          const T alpha = (i == 0) ? g / dd : g / (dd - beta * g / (T)alpha_old);
+          gamma_old = sg;
+          alpha_old = (double)alpha;
+          s_alpha = alpha;
+          s_beta = beta;
+          ++it;
+        }
+        s_cont = cont;
+      }
+    }
+    __syncthreads();
+    if (!s_cont) break;
+    const T alpha = s_alpha, beta = s_beta;
+    // phase 2: n = A m; recurrences
+#pragma unroll 4
+    for (int q = threadIdx.x; q < nh; q += kCT) ms[chunk + q] = __ldcg(mg + hs[q]);
+    __syncthreads();
+    for (int t = threadIdx.x; t < cnt; t += kCT) {
+      T nn = T(0);
+#pragma unroll 9
+      for (int k = 0; k < W; ++k) nn = fma_t<T>(V[k * chunk + t], ms[Lc[k * chunk + t]], nn);
+      const T z1 = fma_t<T>(beta, zv[t], nn);
+      const T q1 = fma_t<T>(beta, qv[t], ms[t]);
+      const T s1 = fma_t<T>(beta, sv[t], wv[t]);
+      const T p1 = fma_t<T>(beta, pv[t], us[t]);
+      zv[t] = z1;
+      qv[t] = q1;
+      sv[t] = s1;
+      pv[t] = p1;
+      xs[t] = fma_t<T>(alpha, p1, xs[t]);
+      rs[t] = fma_t<T>(-alpha, s1, rs[t]);
+      us[t] = fma_t<T>(-alpha, q1, us[t]);
+      wv[t] = fma_t<T>(-alpha, z1, wv[t]);
+    }
+  }
+  // E-vector solution: every copy of a row takes its value, masked nodes 0
+  for (int t = threadIdx.x; t < cnt; t += kCT) a.x[start + t] = xs[t];
+  if (!grid_barrier(a.st, ++nb)) return;
+  const long long tid = blockIdx.x * (long long)kCT + threadIdx.x, nth = (long long)gridDim.x * kCT;
+  for (long long i = tid; i < a.nE; i += nth) {
+    const int u = __ldg(a.rowOf + i);
+    a.xE[i] = u >= 0 ? __ldcg(a.x + u) : T(0);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.st->iters = it;
+    a.st->res0 = r0;
+    a.st->res = rn;
+  }
+}
+
 // Host: partition the rows over one CTA per SM, build each CTA's ELL block
 // (local columns: own rows 0..chunk-1, halo rows chunk..), its halo list and
 // the shared-memory plan.
@@ -382,14 +597,19 @@ void coarse_matrix_setup(long long n, const long long *rowPtr, const long long *
   std::vector<int> rowOf(nE);
   for (long long i = 0; i < nE; ++i) rowOf[i] = (int)rowOfNode[i];
   // shared memory: the row vectors and the halo list always; the matrix block when it fits
-  const size_t vBytes = vec_bytes<T>((int)chunk, maxHalo), mBytes = mat_bytes<T>((int)chunk, width);
+  // FP32 solves use the pipelined variant (one barrier per iteration); FP64
+  // keeps the two-barrier PCG, the same recurrences as the host-driven loop
+  M.pipelined = sizeof(T) == 4;
+  const void *kfn = M.pipelined ? (const void *)coarse_ppcg_kernel<T> : (const void *)coarse_pcg_kernel<T>;
+  const size_t vBytes = M.pipelined ? vec_bytes_pipe<T>((int)chunk, maxHalo) : vec_bytes<T>((int)chunk, maxHalo);
+  const size_t mBytes = mat_bytes<T>((int)chunk, width);
   const size_t limit = (size_t)optin > 2048 ? (size_t)optin - 2048 : 0; // static shared memory of the kernel
   if (vBytes > limit) throw Error(NRSG_ERR_BAD_CONFIG, "coarse level: row block too large for shared memory");
   M.matInSmem = vBytes + mBytes <= limit;
   M.smem = vBytes + (M.matInSmem ? mBytes : 0);
-  NRSG_CUDA(cudaFuncSetAttribute(coarse_pcg_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)M.smem));
+  NRSG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)M.smem));
   int perSM = 0;
-  NRSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, coarse_pcg_kernel<T>, kCT, M.smem));
+  NRSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kfn, kCT, M.smem));
   if (perSM < 1) throw Error(NRSG_ERR_CUDA, "coarse solver: kernel cannot be resident");
   M.nrow = n;
   M.nE = nE;
@@ -411,8 +631,8 @@ void coarse_matrix_setup(long long n, const long long *rowPtr, const long long *
 }
 
 template <typename T>
-int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *z, double *partials, void *state,
-                          int gridMax, double tol, int maxit, cudaStream_t s)
+int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *z, T *z2, double *partials,
+                          void *state, int gridMax, double tol, int maxit, cudaStream_t s)
 {
   if (A.grid > gridMax) throw Error(NRSG_ERR_CUDA, "coarse solver: partial-sum buffer too small");
   NRSG_CUDA(cudaMemsetAsync(state, 0, sizeof(CoarseState), s));
@@ -434,12 +654,14 @@ int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *
   a.xE = xE;
   a.x = x;
   a.z = z;
+  a.z2 = z2;
   a.partials = partials;
   a.st = (CoarseState *)state;
   a.tol = tol;
   a.maxit = maxit;
   void *args[] = {&a};
-  NRSG_CUDA(cudaLaunchCooperativeKernel((const void *)coarse_pcg_kernel<T>, dim3(A.grid), dim3(kCT), args, A.smem, s));
+  const void *kfn = A.pipelined ? (const void *)coarse_ppcg_kernel<T> : (const void *)coarse_pcg_kernel<T>;
+  NRSG_CUDA(cudaLaunchCooperativeKernel(kfn, dim3(A.grid), dim3(kCT), args, A.smem, s));
   count_launch();
   return A.grid;
 }
@@ -459,8 +681,8 @@ template void coarse_matrix_setup<double>(long long, const long long *, const lo
 template void coarse_matrix_setup<float>(long long, const long long *, const long long *, const double *, long long,
                                          const long long *, const int *, CoarseMatrix<float> &);
 template int coarse_pcg_persistent<double>(const CoarseMatrix<double> &, const double *, double *, double *, double *,
-                                           double *, void *, int, double, int, cudaStream_t);
+                                           double *, double *, void *, int, double, int, cudaStream_t);
 template int coarse_pcg_persistent<float>(const CoarseMatrix<float> &, const float *, float *, float *, float *,
-                                          double *, void *, int, double, int, cudaStream_t);
+                                          float *, double *, void *, int, double, int, cudaStream_t);
 
 } // namespace nrsg

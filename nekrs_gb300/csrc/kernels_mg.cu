@@ -171,14 +171,15 @@ __global__ void cheby1_kernel(long long n, T dc, T rc, const T *__restrict__ SAd
     d[i] = dc * dn + rc * r1;
   }
 }
+// rout = rin - Ad (rin may be rout), x = x + beta d (x = beta d when xzero)
 template <typename T>
-__global__ void cheby4_kernel(long long n, T beta, const T *__restrict__ Ad, const T *__restrict__ d, T *__restrict__ r,
-                              T *__restrict__ x)
+__global__ void cheby4_kernel(long long n, T beta, const T *__restrict__ Ad, const T *__restrict__ d, const T *rin,
+                              T *rout, T *__restrict__ x, bool xzero)
 {
   MG_LOOP(i, n)
   {
-    x[i] = x[i] + beta * d[i];
-    r[i] = r[i] - Ad[i];
+    x[i] = xzero ? beta * d[i] : x[i] + beta * d[i];
+    rout[i] = rin[i] - Ad[i];
   }
 }
 template <typename T>
@@ -187,9 +188,11 @@ void launch_cheby1_update(long long n, T dc, T rc, const T *SAd, T *d, T *r, T *
   cheby1_kernel<T><<<grid_for(n), kT, 0, s>>>(n, dc, rc, SAd, d, r, x);
   NRSG_CHECK_LAUNCH();
 }
-template <typename T> void launch_cheby4_update(long long n, T beta, const T *Ad, const T *d, T *r, T *x, cudaStream_t s)
+template <typename T>
+void launch_cheby4_update(long long n, T beta, const T *Ad, const T *d, const T *rin, T *rout, T *x, bool xzero,
+                          cudaStream_t s)
 {
-  cheby4_kernel<T><<<grid_for(n), kT, 0, s>>>(n, beta, Ad, d, r, x);
+  cheby4_kernel<T><<<grid_for(n), kT, 0, s>>>(n, beta, Ad, d, rin, rout, x, xzero);
   NRSG_CHECK_LAUNCH();
 }
 
@@ -349,35 +352,59 @@ __global__ void __launch_bounds__(FdmShape<NQ>::line *FdmShape<NQ>::epb)
 // ASM: add the neighbours' overlap results onto the nodes next to each face,
 // face by face in the order x-, x+, y-, y+, z-, z+, then weight.
 // haloPartner[h] is the halo index of the neighbour's halo point that maps
-// onto the node next to face point h (-1: none).
+// onto the node next to face point h (-1: none).  One warp per element, the
+// element's nodes in shared memory; every partner index and overlap value of
+// the element is loaded before the first add.
+constexpr int kAsmEpc = 8; // elements (warps) per CTA
 template <typename T, int NQ>
-__global__ void asm_combine_kernel(long long E, const int *__restrict__ haloPartner, const T *__restrict__ haloOut,
-                                   const T *__restrict__ wts, T *__restrict__ Su)
+__global__ void __launch_bounds__(32 * kAsmEpc)
+    asm_combine_kernel(long long E, const int *__restrict__ haloPartner, const T *__restrict__ haloOut,
+                       const T *__restrict__ wts, T *__restrict__ Su)
 {
-  constexpr int NP = NQ * NQ * NQ, NF = NQ * NQ, N = NQ - 1;
-  __shared__ T s_u[NP];
-  const long long e = blockIdx.x;
-  for (int q = threadIdx.x; q < NP; q += blockDim.x) s_u[q] = Su[e * NP + q];
-  __syncthreads();
-  for (int f = 0; f < 6; ++f) {
-    for (int p = threadIdx.x; p < NF; p += blockDim.x) {
-      const int hp = haloPartner[(e * 6 + f) * NF + p];
-      if (hp < 0) continue;
-      const int a = p % NQ, b = p / NQ;
-      int n;
-      switch (f) {
-      case 0: n = 1 + NQ * (a + NQ * b); break;
-      case 1: n = (N - 1) + NQ * (a + NQ * b); break;
-      case 2: n = a + NQ * (1 + NQ * b); break;
-      case 3: n = a + NQ * ((N - 1) + NQ * b); break;
-      case 4: n = a + NQ * (b + NQ * 1); break;
-      default: n = a + NQ * (b + NQ * (N - 1)); break;
-      }
-      s_u[n] += haloOut[hp];
+  constexpr int NP = NQ * NQ * NQ, NF = NQ * NQ, N = NQ - 1, PPF = (NF + 31) / 32;
+  __shared__ T s_u[kAsmEpc][NP];
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const long long e = (long long)blockIdx.x * kAsmEpc + wp;
+  if (e >= E) return; // whole warp; warp-level synchronisation only
+  T *su = s_u[wp];
+  const int *hp = haloPartner + e * 6 * NF;
+  int hidx[6][PPF];
+#pragma unroll
+  for (int f = 0; f < 6; ++f)
+#pragma unroll
+    for (int m = 0; m < PPF; ++m) {
+      const int p = lane + 32 * m;
+      hidx[f][m] = p < NF ? __ldg(hp + f * NF + p) : -1;
     }
-    __syncthreads();
+  T hval[6][PPF];
+#pragma unroll
+  for (int f = 0; f < 6; ++f)
+#pragma unroll
+    for (int m = 0; m < PPF; ++m) hval[f][m] = hidx[f][m] >= 0 ? __ldg(haloOut + hidx[f][m]) : T(0);
+  for (int q = lane; q < NP; q += 32) su[q] = Su[e * NP + q];
+  __syncwarp();
+#pragma unroll
+  for (int f = 0; f < 6; ++f) {
+#pragma unroll
+    for (int m = 0; m < PPF; ++m) {
+      const int p = lane + 32 * m;
+      if (p < NF && hidx[f][m] >= 0) {
+        const int a = p % NQ, b = p / NQ;
+        int n;
+        switch (f) {
+        case 0: n = 1 + NQ * (a + NQ * b); break;
+        case 1: n = (N - 1) + NQ * (a + NQ * b); break;
+        case 2: n = a + NQ * (1 + NQ * b); break;
+        case 3: n = a + NQ * ((N - 1) + NQ * b); break;
+        case 4: n = a + NQ * (b + NQ * 1); break;
+        default: n = a + NQ * (b + NQ * (N - 1)); break;
+        }
+        su[n] += hval[f][m];
+      }
+    }
+    __syncwarp();
   }
-  for (int q = threadIdx.x; q < NP; q += blockDim.x) Su[e * NP + q] = s_u[q] * wts[e * NP + q];
+  for (int q = lane; q < NP; q += 32) Su[e * NP + q] = su[q] * __ldg(wts + e * NP + q);
 }
 
 // ---------------------------------------------------------------------------
@@ -484,7 +511,7 @@ __device__ __forceinline__ void fdm8_yz(float *w, const float *M, int off, int l
       for (int c = 0; c < 4; ++c) {
         const int x = x0 + c;
         const float d = x < 10 ? (lam[x] + lam[10 + y]) + lam[20 + j] : 0.f;
-        sc[c] = d > 1e-5f ? 1.f / d : 0.f;
+        sc[c] = d > 1e-5f ? __frcp_rn(d) : 0.f; // the correctly rounded 1/d, as 1.f / d
       }
       v.x *= sc[0];
       v.y *= sc[1];
@@ -667,7 +694,9 @@ void launch_asm_combine(int N, long long E, const int *haloPartner, const T *hal
                         cudaStream_t s)
 {
   if (E <= 0) return;
-#define NRSG_ASMC(NQ) asm_combine_kernel<T, NQ><<<(unsigned)E, 128, 0, s>>>(E, haloPartner, haloOut, wts, Su)
+#define NRSG_ASMC(NQ)                                                                                      \
+  asm_combine_kernel<T, NQ><<<(unsigned)((E + kAsmEpc - 1) / kAsmEpc), 32 * kAsmEpc, 0, s>>>(E, haloPartner,     \
+                                                                                            haloOut, wts, Su)
   NRSG_DISPATCH_NQ_MG(N, NRSG_ASMC)
 #undef NRSG_ASMC
   NRSG_CHECK_LAUNCH();
@@ -699,7 +728,8 @@ void launch_random_fill(long long n, unsigned long long seed, double *v, cudaStr
   template void launch_coarsen<T>(int, int, long long, const T *, const T *, T *, cudaStream_t);           \
   template void launch_prolong<T>(int, int, long long, const T *, const T *, T *, cudaStream_t);           \
   template void launch_cheby1_update<T>(long long, T, T, const T *, T *, T *, T *, cudaStream_t);          \
-  template void launch_cheby4_update<T>(long long, T, const T *, const T *, T *, T *, cudaStream_t);       \
+  template void launch_cheby4_update<T>(long long, T, const T *, const T *, const T *, T *, T *, bool,       \
+                                        cudaStream_t);                                                      \
   template void launch_fdm<T>(int, long long, bool, const T *, const int *, const T *, const T *, const T *, \
                               const T *, const T *, const T *, T *, T *, cudaStream_t);                    \
   template void launch_asm_combine<T>(int, long long, const int *, const T *, const T *, T *, cudaStream_t);

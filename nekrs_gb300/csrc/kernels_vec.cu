@@ -106,6 +106,38 @@ template <typename T> void launch_gs(long long ng, const int *off, const int *id
 template void launch_gs<double>(long long, const int *, const int *, double *, cudaStream_t);
 template void launch_gs<float>(long long, const int *, const int *, float *, cudaStream_t);
 
+// gather-scatter by plan (pairs, then the other groups), then optionally the
+// mask, in one launch; each group sums its members in member order
+template <typename T> __global__ void gs_mask_kernel(GsPlan P, long long nmask, T *__restrict__ q)
+{
+  const long long n1 = P.npairs, n2 = n1 + P.nrest, n3 = n2 + nmask;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n3; t += (long long)gridDim.x * blockDim.x) {
+    if (t < n1) {
+      const int2 pr = __ldg(P.pairs + t);
+      const T v = q[pr.x] + q[pr.y];
+      q[pr.x] = v;
+      q[pr.y] = v;
+    } else if (t < n2) {
+      const long long g = t - n1;
+      const int s = __ldg(P.restOff + g), e = __ldg(P.restOff + g + 1);
+      T v = 0;
+      for (int m = s; m < e; ++m) v += q[__ldg(P.restIds + m)];
+      for (int m = s; m < e; ++m) q[__ldg(P.restIds + m)] = v;
+    } else {
+      q[__ldg(P.mask + (t - n2))] = T(0);
+    }
+  }
+}
+template <typename T> void launch_gs_mask(const GsPlan &P, T *q, bool mask, cudaStream_t s)
+{
+  const long long nm = mask ? P.nmask : 0, n = P.npairs + P.nrest + nm;
+  if (n <= 0) return;
+  gs_mask_kernel<T><<<vec_grid(n), kThreads, 0, s>>>(P, nm, q);
+  NRSG_CHECK_LAUNCH();
+}
+template void launch_gs_mask<double>(const GsPlan &, double *, bool, cudaStream_t);
+template void launch_gs_mask<float>(const GsPlan &, float *, bool, cudaStream_t);
+
 template <typename T> __global__ void mask_kernel(long long n, const int *__restrict__ ids, T *__restrict__ q)
 {
   for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < n; m += (long long)gridDim.x * blockDim.x)

@@ -24,6 +24,7 @@ struct MGState {
   virtual void apply(const double *r, double *z) = 0;
   virtual std::vector<double> info(const std::string &what) = 0;
   virtual void schwarz(int level, const double *u, double *Su) = 0;
+  virtual void fdm(int level, const void *u, void *Su) = 0;
   virtual long long level_size(int level) = 0;
   virtual int error() = 0;
 };
@@ -60,7 +61,7 @@ template <typename T> struct MGImpl : public MGState {
   DevBuf<unsigned char> cState;
   // assembled coarse operator and its row vectors
   CoarseMatrix<T> cA;
-  DevBuf<T> cx, cz2;
+  DevBuf<T> cx, cz2, cz3;
   std::vector<int> coarseIters;
   T l0, l1;
   bool poisson;
@@ -128,7 +129,7 @@ template <typename T> struct MGImpl : public MGState {
     NRSG_CUDA(cudaMemsetAsync(csc.p, 0, sizeof(PcgScalars), s));
     persistentCoarse = (C.N == 1) && o.coarse != "smooth" && o.coarsePersistent;
     if (persistentCoarse) {
-      cPartials.alloc(3 * kCoarseGridMax);
+      cPartials.alloc(6 * kCoarseGridMax);
       cState.alloc(coarse_state_bytes());
       NRSG_CUDA(cudaMemsetAsync(cState.p, 0, coarse_state_bytes(), s));
       build_coarse_matrix(C);
@@ -180,6 +181,7 @@ template <typename T> struct MGImpl : public MGState {
     const long long nv = std::max(A.nrow, 1LL);
     cx.alloc(nv);
     cz2.alloc(nv);
+    cz3.alloc(nv);
   }
 
   void build_fdm(MGLevelDev<T> &v)
@@ -297,8 +299,7 @@ template <typename T> struct MGImpl : public MGState {
   {
     FieldLevel &L = *v.L;
     launch_ax_stored<T>(L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, q, Aq, s);
-    launch_mask<T>((long long)L.maskIds.size(), L.d_mask.p, Aq, s);
-    launch_gs<T>(L.ngroups, L.d_gsOff.p, L.d_gsIds.p, Aq, s);
+    launch_gs_mask<T>(L.gsPlan, Aq, true, s);
   }
 
   // Schwarz: FDM (+ ASM combine) -> gs -> mask; u and Su must not alias
@@ -309,8 +310,7 @@ template <typename T> struct MGImpl : public MGState {
     launch_fdm<T>(L.N, L.E, ras, u, v.haloSrc.p, v.Sx.p, v.Sy.p, v.Sz.p, v.invL.p, v.lam.p, v.wts.p, Su, v.haloOut.p,
                   s);
     if (!ras) launch_asm_combine<T>(L.N, L.E, v.haloPartner.p, v.haloOut.p, v.wts.p, Su, s);
-    launch_gs<T>(L.ngroups, L.d_gsOff.p, L.d_gsIds.p, Su, s);
-    launch_mask<T>((long long)L.maskIds.size(), L.d_mask.p, Su, s);
+    launch_gs_mask<T>(L.gsPlan, Su, true, s);
   }
 
   void apply_S(MGLevelDev<T> &v, const T *r, T *Sr)
@@ -359,33 +359,45 @@ template <typename T> struct MGImpl : public MGState {
     launch_mask<T>((long long)v.L->maskIds.size(), v.L->d_mask.p, x, s);
   }
 
+  // 4th-kind / optimal 4th-kind Chebyshev over S (ellipticMultiGridLevel.cpp
+  // smoothChebyshevFourthKind).  With x = 0 on entry the first S is applied to
+  // r itself and the first update writes x = beta d (no zero fill, no copy of
+  // r).  No mask at the end: d is a combination of S outputs (masked) and x of
+  // masked vectors, so their masked entries are already 0.
   void smooth_cheby4(MGLevelDev<T> &v, const T *r, T *x, bool xIsZero)
   {
     const int degree = xIsZero ? v.down : v.up;
-    if (degree == 0) return;
+    if (degree == 0) {
+      if (xIsZero) launch_fill<T>(v.L->Nlocal, T(0), x, s);
+      return;
+    }
     const auto &betas = xIsZero ? v.downBetas : v.upBetas;
     const long long n = v.L->Nlocal;
     T *res = sRes.p, *Ad = sRes2.p, *d = sUpd.p;
     const double rho = v.lambda1;
-    if (xIsZero) {
-      launch_fill<T>(n, T(0), x, s);
-      NRSG_CUDA(cudaMemcpyAsync(res, r, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
-    } else {
+    const T *rcur = r;
+    bool xzero = xIsZero;
+    if (!xIsZero) {
       level_op(v, x, res);
       launch_axpby<T>(n, T(1), r, T(-1), res, s);
+      rcur = res;
     }
-    apply_S(v, res, Ad);
+    apply_S(v, rcur, Ad);
     launch_scale_copy<T>(n, (T)(4.0 / (3.0 * rho)), Ad, d, s);
     for (int k = 1; k < degree; ++k) {
       level_op(v, d, Ad);
-      launch_cheby4_update<T>(n, (T)betas[k - 1], Ad, d, res, x, s);
+      launch_cheby4_update<T>(n, (T)betas[k - 1], Ad, d, rcur, res, x, xzero, s);
+      rcur = res;
+      xzero = false;
       apply_S(v, res, Ad);
       const T dCoeff = (T)((2.0 * k - 1.0) / (2.0 * k + 3.0));
       const T rCoeff = (T)((8.0 * k + 4.0) / ((2.0 * k + 3.0) * rho));
       launch_axpby<T>(n, rCoeff, Ad, dCoeff, d, s);
     }
-    launch_axpby<T>(n, (T)betas.back(), d, T(1), x, s);
-    launch_mask<T>((long long)v.L->maskIds.size(), v.L->d_mask.p, x, s);
+    if (xzero)
+      launch_scale_copy<T>(n, (T)betas.back(), d, x, s);
+    else
+      launch_axpby<T>(n, (T)betas.back(), d, T(1), x, s);
   }
 
   void smooth(MGLevelDev<T> &v, const T *r, T *x, bool xIsZero)
@@ -400,8 +412,8 @@ template <typename T> struct MGImpl : public MGState {
   {
     FieldLevel &L = *v.L;
     if (persistentCoarse) {
-      coarse_pcg_persistent<T>(cA, b, x, cx.p, cz2.p, cPartials.p, cState.p, kCoarseGridMax, el.opt.coarseTol,
-                               el.opt.coarseMaxIter, s);
+      coarse_pcg_persistent<T>(cA, b, x, cx.p, cz2.p, cz3.p, cPartials.p, cState.p, kCoarseGridMax,
+                               el.opt.coarseTol, el.opt.coarseMaxIter, s);
       return 0;
     }
     const long long n = L.Nlocal;
@@ -449,8 +461,7 @@ template <typename T> struct MGImpl : public MGState {
     // coarsen: res *= invDegree(fine), restrict, gs, mask
     launch_axmy<T>(n, c.invDegreeFine.p, v.res.p, s);
     launch_coarsen<T>(v.L->N, c.L->N, c.L->E, c.R.p, v.res.p, c.rhs.p, s);
-    launch_gs<T>(c.L->ngroups, c.L->d_gsOff.p, c.L->d_gsIds.p, c.rhs.p, s);
-    launch_mask<T>((long long)c.L->maskIds.size(), c.L->d_mask.p, c.rhs.p, s);
+    launch_gs_mask<T>(c.L->gsPlan, c.rhs.p, true, s);
     vcycle(k + 1);
     launch_prolong<T>(v.L->N, c.L->N, c.L->E, c.R.p, c.x.p, v.x.p, s);
     smooth(v, v.rhs.p, v.x.p, false);
@@ -506,6 +517,8 @@ template <typename T> struct MGImpl : public MGState {
       for (auto &v : lv) {
         if (v.smoothed) { out.push_back(v.down); out.push_back(v.up); }
       }
+    else if (what == "mg.bytes")
+      out.push_back((double)sizeof(T)); // multigrid precision
     else if (what == "mg.coarseMatrix") {
       // rows, ELL width, stored nonzeros, row blocks (CTAs), rows per block, matrix in shared memory
       if (persistentCoarse)
@@ -525,6 +538,17 @@ template <typename T> struct MGImpl : public MGState {
     NRSG_CUDA(cudaMemcpyAsync(h.data(), cState.p, h.size(), cudaMemcpyDeviceToHost, s));
     NRSG_CUDA(cudaStreamSynchronize(s));
     return coarse_state_read(h.data(), nullptr, nullptr, nullptr);
+  }
+
+  // one fused FDM launch of level `level` on buffers of the multigrid
+  // precision (RAS: weighted own nodes; ASM: own nodes and the halo results)
+  void fdm(int level, const void *u, void *Su) override
+  {
+    auto &v = lv.at(level);
+    if (plan.base == 0 || !v.smoothed) throw Error(NRSG_ERR_INVALID, "level has no Schwarz smoother");
+    const FieldLevel &L = *v.L;
+    launch_fdm<T>(L.N, L.E, plan.base == 2, (const T *)u, v.haloSrc.p, v.Sx.p, v.Sy.p, v.Sz.p, v.invL.p, v.lam.p,
+                  v.wts.p, (T *)Su, v.haloOut.p, s);
   }
 
   void schwarz(int level, const double *u, double *Su) override
@@ -563,6 +587,11 @@ long long Elliptic::mg_level_size(int level)
 {
   if (!mg) throw Error(NRSG_ERR_INVALID, "no multigrid preconditioner");
   return mg->level_size(level);
+}
+void Elliptic::mg_fdm(int level, const void *u, void *Su)
+{
+  if (!mg) throw Error(NRSG_ERR_INVALID, "no multigrid preconditioner");
+  mg->fdm(level, u, Su);
 }
 void Elliptic::mg_schwarz(int level, const double *u, double *Su)
 {

@@ -9,7 +9,9 @@ template <typename T> void launch_coarsen(int Nf, int Nc, long long E, const T *
 template <typename T> void launch_prolong(int Nf, int Nc, long long E, const T *R, const T *qc, T *qf, cudaStream_t s);
 template <typename T>
 void launch_cheby1_update(long long n, T dc, T rc, const T *SAd, T *d, T *r, T *x, cudaStream_t s);
-template <typename T> void launch_cheby4_update(long long n, T beta, const T *Ad, const T *d, T *r, T *x, cudaStream_t s);
+template <typename T>
+void launch_cheby4_update(long long n, T beta, const T *Ad, const T *d, const T *rin, T *rout, T *x, bool xzero,
+                          cudaStream_t s);
 template <typename T>
 void launch_fdm(int N, long long E, bool ras, const T *u, const int *haloSrc, const T *Sx, const T *Sy, const T *Sz,
                 const T *invL, const T *lam, const T *wts, T *Su, T *haloOut, cudaStream_t s);
@@ -33,6 +35,7 @@ template <typename T> struct CoarseMatrix {
   long long nrow = 0, nE = 0, nnz = 0;
   int width = 0, grid = 0, chunk = 0, maxHalo = 0;
   bool matInSmem = false;
+  bool pipelined = false;        // one-barrier pipelined PCG (FP32)
   size_t smem = 0;               // dynamic shared memory per CTA
   DevBuf<unsigned short> lcol;   // [grid][width][chunk] local column: own row, or chunk + halo slot
   DevBuf<T> val;                 // [grid][width][chunk], padding 0
@@ -46,12 +49,12 @@ void coarse_matrix_setup(long long n, const long long *rowPtr, const long long *
                          const long long *rowOfNode, const int *rep, CoarseMatrix<T> &M);
 
 // persistent cooperative Jacobi-PCG on the assembled coarse operator: b and xE
-// are E-vectors, x and z row vectors (solution rows, exchanged z); returns the
-// grid size used.  `state` holds coarse_state_bytes() bytes, `partials`
-// 3 * gridMax doubles.
+// are E-vectors, x, z and z2 row vectors (solution rows, two exchange
+// buffers); returns the grid size used.  `state` holds coarse_state_bytes()
+// bytes, `partials` 6 * gridMax doubles.
 template <typename T>
-int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *z, double *partials, void *state,
-                          int gridMax, double tol, int maxit, cudaStream_t s);
+int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *z, T *z2, double *partials,
+                          void *state, int gridMax, double tol, int maxit, cudaStream_t s);
 size_t coarse_state_bytes();
 // decode a host copy of the state; returns the error flag (0 = ok)
 int coarse_state_read(const void *state_host, int *iters, double *res0, double *res);

@@ -141,6 +141,17 @@ template <typename T>
 void launch_ax_trilinear(int N, long long E, const T *VX, const T *gllz, const T *gllw, const T *D, T lambda0,
                          T lambda1, bool poisson, const T *q, T *Aq, cudaStream_t s);
 template <typename T> void launch_gs(long long ngroups, const int *off, const int *ids, T *q, cudaStream_t s);
+// Gather-scatter plan of one level: the groups of exactly two members as
+// index pairs (most of them: face-interior nodes), the other groups (>= 3
+// members) as CSR, and the Dirichlet mask ids.  Masked nodes belong to no
+// group, so one launch applies both.
+struct GsPlan {
+  long long npairs = 0, nrest = 0, nmask = 0;
+  const int2 *pairs = nullptr;
+  const int *restOff = nullptr, *restIds = nullptr;
+  const int *mask = nullptr;
+};
+template <typename T> void launch_gs_mask(const GsPlan &P, T *q, bool mask, cudaStream_t s);
 template <typename T> void launch_mask(long long n, const int *ids, T *q, cudaStream_t s);
 template <typename T>
 void launch_build_diag(int N, long long E, const T *ggeo, const T *D, T lambda0, T lambda1, bool poisson, T *diag,

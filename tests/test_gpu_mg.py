@@ -178,3 +178,36 @@ def test_mixed_precision_error_vs_fp64_oracle(product_lib, oracle_mod, torch_cud
     assert ig["res"] <= 1e-10 * ig["res0"]
     assert abs(ig["iterations"] - io["iterations"]) <= 2
     assert rel(x.cpu().numpy(), xo) < 1e-8
+
+
+@pytest.mark.parametrize("N", [3, 7])
+def test_fdm_entry_point_matches_smoother(product_lib, torch_cuda, N):
+    """RAS: one launch of the fused FDM entry point followed by gather-scatter and mask (done here on the
+    host in FP32, member order) equals the level-0 Schwarz smoother, bit for bit."""
+    torch = torch_cuda
+    n = 3
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.5)
+    opts = (f"solver=pfcg;preconditioner=multigrid;smootherType=cheby+ras;mgPrecision=fp32;"
+            f"pMGSchedule=p={N}+degree=2,p=1,p={N}+degree=2")
+    el = G.Elliptic(N, VX, EToV, EToB, opts)
+    assert el.get("mg.bytes")[0] == 4
+    m = el.mg_level_size(0)
+    u = np.random.default_rng(N).uniform(-1, 1, m).astype(np.float32)
+    ud = torch.from_numpy(u).cuda()
+    su = torch.zeros_like(ud)
+    el.mg_fdm(0, ud, su)
+    torch.cuda.synchronize()
+    s = su.cpu().numpy()
+    off, ids = el.get("gsOff"), el.get("gsIds")
+    out = s.copy()
+    for g in range(len(off) - 1):
+        mem = ids[off[g]:off[g + 1]]
+        if len(mem) > 1:
+            v = np.float32(0)
+            for k in mem:
+                v = np.float32(v + s[k])
+            out[mem] = v
+    out[el.get("maskIds")] = 0
+    ref = torch.zeros(m, dtype=torch.float64, device="cuda")
+    el.mg_smoother(0, torch.from_numpy(u.astype(np.float64)).cuda(), ref)
+    assert np.array_equal(out.astype(np.float64), ref.cpu().numpy())
