@@ -273,19 +273,191 @@ def fdm_roofline(G, el, N, E, peak):
             "fp32_tflops": flops / t / 1e12, "frac_of_hbm": per_el * E / t / 1e9 / peak}
 
 
+def mg_options(N, tol="1e-8"):
+    """Mixed-precision pMG-FPCG options for order N (levels N / 3 / 1, or N / 1 for N <= 3), optimal 4th-kind
+    Chebyshev(4) + ASM, coarse Jacobi-PCG on the assembled order-1 operator."""
+    mid = {9: 5, 8: 5, 7: 3, 6: 3, 5: 3, 4: 2}.get(N)
+    lv = [N] + ([mid] if mid else []) + [1]
+    down = [f"p={q}+degree=4" for q in lv[:-1]]
+    sched = ",".join(down + ["p=1"] + down[::-1])
+    return (f"solver=pfcg;residualTol={tol}+relative;maxIterations=400;preconditioner=multigrid;"
+            f"smootherType=fourthoptcheby+asm;pMGSchedule={sched};coarseSolver=jpcg;coarseTol=1e-4;mgPrecision=mixed")
+
+
+def run_batch(args):
+    """configs[3]: independent Poisson problems (cube side U{4..24}, N in {5,7,9}, eps U[0.3,1.0], seeded RHS),
+    mixed-precision pMG-FPCG to 1e-8, solved one after another and as one batch stepped one Krylov iteration
+    at a time (each problem on its own stream); DOF/s = sum of E*N^3 / wall time."""
+    import torch
+    import nekrs_gb300 as G
+    from nekrs_gb300 import workloads as W
+
+    rng = np.random.default_rng(3)
+    K = args.batch_problems
+    t0 = time.perf_counter()
+    els, rhs, dofs = [], [], 0
+    for k in range(K):
+        side, N, eps = int(rng.integers(4, 25)), int(rng.choice([5, 7, 9])), float(rng.uniform(0.3, 1.0))
+        VX, EToV, EToB = W.kershaw_box(side, eps=eps)
+        el = G.Elliptic(N, VX, EToV, EToB, mg_options(N))
+        els.append(el)
+        rhs.append(torch.from_numpy(W.box_rhs(N, side, side, side, 1000 + k, el.get("ggeo"))).cuda())
+        dofs += side ** 3 * N ** 3
+    setup_s = time.perf_counter() - t0
+    rs = [torch.empty_like(b) for b in rhs]
+    xs = [torch.zeros_like(b) for b in rhs]
+
+    def reset():
+        for r, x, b in zip(rs, xs, rhs):
+            r.copy_(b)
+            x.zero_()
+        torch.cuda.synchronize()
+
+    def sequential():
+        for el, r, x in zip(els, rs, xs):
+            el.solve(r, x)
+
+    out = {}
+    for name, fn in (("sequential", sequential), ("batched", lambda: G.solve_batch(els, rs, xs))):
+        for _ in range(max(1, args.warmup - 2)):
+            reset()
+            fn()
+        ts = []
+        for _ in range(args.steps):
+            reset()
+            t = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t)
+        out[name] = float(np.mean(ts))
+    its = [el.get("history").size for el in els]
+    print(json.dumps({"metric": "batched Poisson DOFs/s (sum of E*N^3 / wall time of the batch)",
+                      "value": dofs / out["batched"], "unit": "DOF/s", "n_gpus": 1, "steps": args.steps,
+                      "warmup": args.warmup, "ms_per_step": out["batched"] * 1e3, "higher_is_better": True,
+                      "dtype": "f64", "data": "synthetic (seeded Kershaw boxes, U[-1,1] mass-weighted RHS)",
+                      "config": {"workload": "batch", "problems": K, "dofs": dofs, "setup_s": setup_s,
+                                 "iterations_min_max": [int(min(its)), int(max(its))]},
+                      "sequential": {"value": dofs / out["sequential"], "ms_per_step": out["sequential"] * 1e3},
+                      "speedup_batched_vs_sequential": out["sequential"] / out["batched"]}))
+
+
+def run_serve(args):
+    """configs[4]: Poisson requests with exponential inter-arrival times (mean 2 ms) for `serve_seconds`;
+    operators (E log-uniform in [2^9, 2^15], N in {3..9}, eps U[0.3,1.0]) come from a resident pool built
+    before the clock starts; each request draws its tolerance from {1e-6, 1e-8, 1e-10} and a seeded RHS.
+    Requests are admitted FIFO onto free resident handles and stepped together one Krylov iteration at a
+    time; latency = completion - arrival.  The same trace is also served one solve at a time."""
+    import torch
+    import nekrs_gb300 as G
+    from nekrs_gb300 import workloads as W
+
+    rng = np.random.default_rng(11)
+    P = args.serve_pool
+    pool = []
+    t0 = time.perf_counter()
+    for k in range(P):
+        E = float(np.exp(rng.uniform(np.log(2 ** 9), np.log(2 ** 15))))
+        side = max(2, int(round(E ** (1.0 / 3.0))))
+        N, eps = int(rng.integers(3, 10)), float(rng.uniform(0.3, 1.0))
+        VX, EToV, EToB = W.kershaw_box(side, eps=eps)
+        el = G.Elliptic(N, VX, EToV, EToB, mg_options(N))
+        jw = torch.from_numpy(el.get("ggeo").reshape(side ** 3, 7, -1)[:, 6, :].ravel().copy()).cuda()
+        pool.append({"el": el, "jw": jw, "dofs": side ** 3 * N ** 3, "r": torch.empty_like(jw),
+                     "x": torch.empty_like(jw)})
+    setup_s = time.perf_counter() - t0
+    # request trace
+    gaps = rng.exponential(2e-3, size=int(args.serve_seconds / 2e-3 * 2) + 16)
+    arr = np.cumsum(gaps)
+    arr = arr[arr < args.serve_seconds]
+    reqs = [{"t": float(t), "op": int(rng.integers(P)), "tol": float(rng.choice([1e-6, 1e-8, 1e-10])),
+             "seed": int(rng.integers(1 << 31))} for t in arr]
+    gen = torch.Generator(device="cuda")
+
+    def prepare(q):
+        o = pool[q["op"]]
+        gen.manual_seed(q["seed"])
+        o["r"].copy_((torch.rand(o["jw"].numel(), generator=gen, device="cuda", dtype=torch.float64) * 2 - 1)
+                     * o["jw"])
+        o["x"].zero_()
+        o["el"].set_tolerance(q["tol"])
+
+    # warm every handle once
+    for o in pool:
+        prepare({"op": pool.index(o), "seed": 1, "tol": 1e-8})
+        o["el"].solve(o["r"], o["x"])
+    torch.cuda.synchronize()
+
+    def serve(concurrent):
+        lat = []
+        busy = {}  # op -> request
+        queue = []
+        nxt = 0
+        start = time.perf_counter()
+        while nxt < len(reqs) or queue or busy:
+            now = time.perf_counter() - start
+            while nxt < len(reqs) and reqs[nxt]["t"] <= now:
+                queue.append(reqs[nxt])
+                nxt += 1
+            if concurrent:
+                rest = []
+                for q in queue:
+                    if q["op"] in busy:
+                        rest.append(q)
+                        continue
+                    prepare(q)
+                    pool[q["op"]]["el"].solve_begin(pool[q["op"]]["r"], pool[q["op"]]["x"])
+                    busy[q["op"]] = q
+                queue = rest
+                for op in list(busy):
+                    info = pool[op]["el"].solve_advance()
+                    if info is not None:
+                        lat.append(time.perf_counter() - start - busy.pop(op)["t"])
+            elif queue:
+                q = queue.pop(0)
+                prepare(q)
+                pool[q["op"]]["el"].solve(pool[q["op"]]["r"], pool[q["op"]]["x"])
+                lat.append(time.perf_counter() - start - q["t"])
+            elif nxt < len(reqs):
+                time.sleep(max(0.0, min(1e-3, reqs[nxt]["t"] - now)))
+        total = time.perf_counter() - start
+        lat = np.array(lat)
+        return {"solves": int(lat.size), "solves_per_s": lat.size / total, "wall_s": total,
+                "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                "mean_ms": float(lat.mean() * 1e3)}
+
+    conc = serve(True)
+    seq = serve(False)
+    print(json.dumps({"metric": "serving p99 latency (arrival to solution)", "value": conc["p99_ms"], "unit": "ms",
+                      "n_gpus": 1, "higher_is_better": False, "dtype": "f64",
+                      "data": "synthetic (seeded Kershaw boxes and RHS, exponential arrivals)",
+                      "config": {"workload": "serve", "arrivals_s": args.serve_seconds, "requests": len(reqs),
+                                 "pool": P, "setup_s": setup_s, "mean_interarrival_ms": 2.0},
+                      "concurrent": conc, "sequential": seq,
+                      "solves_per_s_vs_sequential": conc["solves_per_s"] / seq["solves_per_s"]}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + ["batch", "serve"])
+    ap.add_argument("--batch-problems", type=int, default=64, help="problems in the batch workload (config: 256)")
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window of the serve workload (config: 60)")
+    ap.add_argument("--serve-pool", type=int, default=24, help="resident operators of the serve workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-plain", action="store_true")
     ap.add_argument("--solve-only", action="store_true",
                     help="time the device-resident solves only (no e2e, FP64 comparison or kernel rooflines)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.workload in ("batch", "serve"):
+        import torch
+
+        torch.cuda.set_device(dist_info()[2])
+        (run_batch if args.workload == "batch" else run_serve)(args)
+        return
     nel, N, eps, opts, desc = WORKLOADS[args.workload]
 
     if args.impl == "reference":

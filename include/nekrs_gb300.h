@@ -91,6 +91,27 @@ int nrsg_elliptic_set_stream(nrsg_elliptic *el, void *cuda_stream);
  * entry and is overwritten with the final residual; d_x holds x0 on entry
  * and the solution on exit.  Both are device E-vectors of E*Np doubles. */
 int nrsg_elliptic_solve(nrsg_elliptic *el, double *d_r, double *d_x, nrsg_solve_info *info);
+/* Change the residual tolerance (residualTol, "+relative" when relative != 0)
+ * and maxIterations of a handle between solves (the .par SOLVER TOLERANCE /
+ * MAXIMUM ITERATIONS of the next ellipticSolve). */
+int nrsg_elliptic_set_tolerance(nrsg_elliptic *el, double tol, int relative, int maxIterations);
+/* Resumable form of the same solve (PCG / flexible PCG; GMRES runs to
+ * completion inside the first advance).  begin() queues the initial residual
+ * on the solver's stream and returns; each advance() call returns without
+ * waiting on the device: it consumes the residual norm of the last queued
+ * iteration once that has landed, queues the next iteration, and sets *done
+ * = 1 (with *info filled and the solve's status returned) when the solve has
+ * finished.  One solve per handle at a time.  Handles on different streams
+ * advance concurrently (nrsg_elliptic_solve_batch, serving loops).  No
+ * reference counterpart (ellipticSolve is blocking). */
+int nrsg_elliptic_solve_begin(nrsg_elliptic *el, double *d_r, double *d_x);
+int nrsg_elliptic_solve_advance(nrsg_elliptic *el, int *done, nrsg_solve_info *info);
+/* n independent solves, each on its own handle (and stream), stepped together
+ * one Krylov iteration at a time until all have finished.  info[k] receives
+ * each solve's result; returns the first hard error, else the first
+ * NRSG_ERR_MAXIT, else NRSG_OK. */
+int nrsg_elliptic_solve_batch(int n, nrsg_elliptic *const *els, double *const *d_r, double *const *d_x,
+                              nrsg_solve_info *info);
 /* Same solve on host buffers: copies in, solves, copies back. */
 int nrsg_elliptic_solve_host(nrsg_elliptic *el, double *h_r, double *h_x, nrsg_solve_info *info);
 

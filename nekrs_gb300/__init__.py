@@ -66,6 +66,11 @@ def lib():
         L.nrsg_elliptic_set_stream.argtypes = [vp, vp]
         L.nrsg_elliptic_solve.argtypes = [vp, vp, vp, ctypes.POINTER(SolveInfo)]
         L.nrsg_elliptic_solve_host.argtypes = [vp, vp, vp, ctypes.POINTER(SolveInfo)]
+        L.nrsg_elliptic_solve_begin.argtypes = [vp, vp, vp]
+        L.nrsg_elliptic_set_tolerance.argtypes = [vp, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        L.nrsg_elliptic_solve_advance.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(SolveInfo)]
+        L.nrsg_elliptic_solve_batch.argtypes = [ctypes.c_int, ctypes.POINTER(vp), ctypes.POINTER(vp),
+                                                ctypes.POINTER(vp), ctypes.POINTER(SolveInfo)]
         for f in ("nrsg_elliptic_operator", "nrsg_elliptic_ax", "nrsg_elliptic_precondition"):
             getattr(L, f).argtypes = [vp, vp, vp]
         L.nrsg_elliptic_gs.argtypes = [vp, vp]
@@ -167,6 +172,37 @@ class Elliptic:
         self._order_with(r, x)
         info = SolveInfo()
         code = lib().nrsg_elliptic_solve(self.h, _ptr(r), _ptr(x), ctypes.byref(info))
+        if code not in (NRSG_OK, 1):
+            check(code)
+        return info.as_dict()
+
+    def _own_stream(self):
+        """A stream of this handle alone (batched and resumable solves run handles concurrently); waits for
+        the caller's current torch stream so that buffers it wrote are in place."""
+        import torch
+
+        torch.cuda.current_stream().synchronize()
+        if getattr(self, "_batch_stream", None) is None:
+            self._batch_stream = torch.cuda.Stream()
+        s = self._batch_stream.cuda_stream
+        if s != self._stream:
+            self.set_stream(s)
+
+    def set_tolerance(self, tol, relative=True, max_iterations=400):
+        check(lib().nrsg_elliptic_set_tolerance(self.h, float(tol), int(relative), int(max_iterations)))
+
+    def solve_begin(self, r, x):
+        """Queue a resumable solve (see solve_advance); r and x are device E-vectors."""
+        self._own_stream()
+        check(lib().nrsg_elliptic_solve_begin(self.h, _ptr(r), _ptr(x)))
+
+    def solve_advance(self):
+        """Advance the resumable solve without waiting on the device: None while running, else the info dict."""
+        done = ctypes.c_int(0)
+        info = SolveInfo()
+        code = lib().nrsg_elliptic_solve_advance(self.h, ctypes.byref(done), ctypes.byref(info))
+        if not done.value:
+            return None
         if code not in (NRSG_OK, 1):
             check(code)
         return info.as_dict()
@@ -278,6 +314,22 @@ def host_assemble_operator(N, EToV, EToB, ggeo, lambda0=1.0, lambda1=0.0, poisso
     check(lib().nrsg_host_assemble_operator(*args, ctypes.byref(nrow), ctypes.byref(nnz), rp.ctypes.data,
                                             cols.ctypes.data, vals.ctypes.data, rown.ctypes.data))
     return rp, cols, vals, rown
+
+
+def solve_batch(solvers, rs, xs):
+    """Independent solves on distinct handles, stepped together one Krylov iteration at a time
+    (nrsg_elliptic_solve_batch); returns the list of info dicts."""
+    n = len(solvers)
+    for el in solvers:
+        el._own_stream()
+    H = (vp * n)(*[el.h for el in solvers])
+    R = (vp * n)(*[_ptr(r) for r in rs])
+    X = (vp * n)(*[_ptr(x) for x in xs])
+    infos = (SolveInfo * n)()
+    code = lib().nrsg_elliptic_solve_batch(n, H, R, X, infos)
+    if code not in (NRSG_OK, 1):
+        check(code)
+    return [infos[k].as_dict() for k in range(n)]
 
 
 # ---- kernel-level entry points ---------------------------------------------

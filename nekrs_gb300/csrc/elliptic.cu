@@ -144,6 +144,7 @@ Elliptic::Elliptic(const nrsg_mesh_desc *m, const char *options)
   red.slots = kRedSlots;
   NRSG_CUDA(cudaEventCreate(&ev0));
   NRSG_CUDA(cudaEventCreate(&ev1));
+  NRSG_CUDA(cudaEventCreateWithFlags(&evRead, cudaEventDisableTiming));
 
   if (opt.axPrecision == "fp32x2") {
     if (opt.trilinear) throw Error(NRSG_ERR_BAD_CONFIG, "axPrecision = fp32x2 needs stored geometric factors");
@@ -176,6 +177,7 @@ Elliptic::~Elliptic()
   if (h_y) cudaFreeHost(h_y);
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
+  if (evRead) cudaEventDestroy(evRead);
   mg_release();
   if (ownStream && stream) cudaStreamDestroy(stream);
 }
@@ -217,49 +219,56 @@ double Elliptic::read_scalar(const double *d_src)
   return h_scal->pad;
 }
 
-// PCG / flexible PCG (PCG.cpp:86-203); scalars live in d_scal.
-int Elliptic::pcg(double *r, double *x, double tol, int maxit, double &rnorm)
+// PCG / flexible PCG (PCG.cpp:86-203); scalars live in d_scal.  One
+// iteration: z = M r, (r, z), (z, Ap_old) for the flexible form, p update,
+// A p, (p, A p), x and r update with (r, r); then the 8-byte residual copy to
+// pinned host memory and its event.
+void Elliptic::pcg_issue_iteration()
 {
   const long long n = fine.Nlocal;
   const double *wt = fine.d_invDegree64.p;
   const bool flexible = (opt.solver == "pfcg");
   PcgScalars *sc = d_scal.p;
-  launch_fill<double>(n, 0.0, p.p, stream);
-  int it = 0;
-  const double sqrtFac = std::sqrt(1.0 / fine.volume);
-  do {
-    ++it;
-    if (opt.precon == "jacobi") {
-      launch_jacobi_rdotz(n, wt, invDiag.p, r, z.p, sc, red, 0, stream);
+  double *r = st.r, *x = st.x;
+  const int it = ++st.it;
+  if (opt.precon == "jacobi") {
+    launch_jacobi_rdotz(n, wt, invDiag.p, r, z.p, sc, red, 0, stream);
+  } else {
+    const double *zz = r;
+    if (opt.precon != "none") {
+      precondition(r, z.p);
+      zz = z.p;
     } else {
-      const double *zz = r;
-      if (opt.precon != "none") {
-        precondition(r, z.p);
-        zz = z.p;
-      } else {
-        NRSG_CUDA(cudaMemcpyAsync(z.p, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
-      }
-      launch_scalar_move(&sc->rdotz_old, &sc->rdotz, nullptr, stream);
-      launch_wdot<double>(n, wt, r, zz, &sc->rdotz, red, 0, stream);
+      NRSG_CUDA(cudaMemcpyAsync(z.p, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
     }
-    if (flexible && it > 1) launch_wdot<double>(n, wt, z.p, Ap.p, &sc->zAp, red, 1, stream);
-    launch_update_p(n, z.p, p.p, sc, it == 1, flexible, stream);
-    op(p.p, Ap.p);
-    launch_wdot<double>(n, wt, p.p, Ap.p, &sc->pAp, red, 2, stream);
-    launch_update_xr(n, wt, p.p, Ap.p, x, r, sc, red, 3, stream);
-    const double rdotr = read_scalar(&sc->rdotr);
-    rnorm = std::sqrt(rdotr) * sqrtFac;
-    history.push_back(rnorm);
-    if (!std::isfinite(rnorm)) { status = NRSG_ERR_NAN; break; }
-  } while (rnorm > tol && it < maxit);
-  return it;
+    launch_scalar_move(&sc->rdotz_old, &sc->rdotz, nullptr, stream);
+    launch_wdot<double>(n, wt, r, zz, &sc->rdotz, red, 0, stream);
+  }
+  if (flexible && it > 1) launch_wdot<double>(n, wt, z.p, Ap.p, &sc->zAp, red, 1, stream);
+  launch_update_p(n, z.p, p.p, sc, it == 1, flexible, stream);
+  op(p.p, Ap.p);
+  launch_wdot<double>(n, wt, p.p, Ap.p, &sc->pAp, red, 2, stream);
+  launch_update_xr(n, wt, p.p, Ap.p, x, r, sc, red, 3, stream);
+  NRSG_CUDA(cudaMemcpyAsync(&h_scal->rdotr, &sc->rdotr, sizeof(double), cudaMemcpyDeviceToHost, stream));
+  NRSG_CUDA(cudaEventRecord(evRead, stream));
 }
 
-int Elliptic::solve(double *r, double *x, nrsg_solve_info *info)
+void Elliptic::finish_issue()
 {
+  launch_axpby<double>(fine.Nlocal, 1.0, x0.p, 1.0, st.x, stream);
+  NRSG_CUDA(cudaEventRecord(ev1, stream));
+  st.phase = 3;
+}
+
+void Elliptic::begin(double *r, double *x)
+{
+  if (st.phase != 0 && st.phase != 4) throw Error(NRSG_ERR_INVALID, "a solve is already in progress on this handle");
   const long long n = fine.Nlocal;
   history.clear();
   status = NRSG_OK;
+  st = StepState();
+  st.r = r;
+  st.x = x;
   NRSG_CUDA(cudaEventRecord(ev0, stream));
   // r = b - A x0 (local Ax, ellipticSolve.cpp:91-103), mask, gather-scatter
   ax(x, Ap.p);
@@ -268,36 +277,94 @@ int Elliptic::solve(double *r, double *x, nrsg_solve_info *info)
   NRSG_CUDA(cudaMemcpyAsync(x0.p, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
   launch_fill<double>(n, 0.0, x, stream);
   launch_wdot<double>(n, fine.d_invDegree64.p, r, nullptr, &d_scal.p->rdotr, red, 0, stream);
-  const double res0 = std::sqrt(read_scalar(&d_scal.p->rdotr) / fine.volume);
-  if (!std::isfinite(res0)) throw Error(NRSG_ERR_NAN, "unreasonable res0Norm (NaN/Inf right-hand side)");
-  double tol = opt.tol;
-  if (opt.relative) tol *= res0;
-  double res = res0;
-  int iters = 0;
-  if (res0 > 0) {
-    if (opt.solver == "pcg" || opt.solver == "pfcg")
-      iters = pcg(r, x, tol, opt.maxIter, res);
-    else
-      iters = pgmres(r, x, tol, opt.maxIter, res);
+  NRSG_CUDA(cudaMemcpyAsync(&h_scal->rdotr, &d_scal.p->rdotr, sizeof(double), cudaMemcpyDeviceToHost, stream));
+  NRSG_CUDA(cudaEventRecord(evRead, stream));
+  st.phase = 1;
+}
+
+static bool event_done(cudaEvent_t ev, bool block)
+{
+  if (block) {
+    NRSG_CUDA(cudaEventSynchronize(ev));
+    return true;
   }
-  launch_axpby<double>(n, 1.0, x0.p, 1.0, x, stream);
-  NRSG_CUDA(cudaEventRecord(ev1, stream));
-  NRSG_CUDA(cudaEventSynchronize(ev1));
-  float ms = 0;
-  NRSG_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-  if (status == NRSG_OK && iters >= opt.maxIter && res > tol) status = NRSG_ERR_MAXIT;
-  if (mg_error()) {
-    status = NRSG_ERR_CUDA;
-    set_last_error("coarse-level solver: grid barrier wait exceeded its limit");
+  const cudaError_t e = cudaEventQuery(ev);
+  if (e == cudaErrorNotReady) return false;
+  NRSG_CUDA(e);
+  return true;
+}
+
+bool Elliptic::advance(bool block, nrsg_solve_info *info)
+{
+  for (;;) {
+    if (st.phase == 1) {
+      if (!event_done(evRead, block)) return false;
+      st.res0 = std::sqrt(h_scal->rdotr / fine.volume);
+      if (!std::isfinite(st.res0)) {
+        st.phase = 4;
+        throw Error(NRSG_ERR_NAN, "unreasonable res0Norm (NaN/Inf right-hand side)");
+      }
+      st.tol = opt.relative ? opt.tol * st.res0 : opt.tol;
+      st.res = st.res0;
+      if (st.res0 > 0 && opt.maxIter > 0) {
+        if (opt.solver == "pcg" || opt.solver == "pfcg") {
+          launch_fill<double>(fine.Nlocal, 0.0, p.p, stream);
+          pcg_issue_iteration();
+          st.phase = 2;
+        } else {
+          double res = st.res0;
+          st.it = pgmres(st.r, st.x, st.tol, opt.maxIter, res);
+          st.res = res;
+          finish_issue();
+        }
+      } else {
+        finish_issue();
+      }
+    } else if (st.phase == 2) {
+      if (!event_done(evRead, block)) return false;
+      const double rnorm = std::sqrt(h_scal->rdotr) * std::sqrt(1.0 / fine.volume);
+      history.push_back(rnorm);
+      st.res = rnorm;
+      if (!std::isfinite(rnorm)) {
+        status = NRSG_ERR_NAN;
+        finish_issue();
+      } else if (rnorm > st.tol && st.it < opt.maxIter) {
+        pcg_issue_iteration();
+        if (!block) return false;
+      } else {
+        finish_issue();
+      }
+    } else if (st.phase == 3) {
+      if (!event_done(ev1, block)) return false;
+      float ms = 0;
+      NRSG_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+      if (status == NRSG_OK && st.it >= opt.maxIter && st.res > st.tol) status = NRSG_ERR_MAXIT;
+      if (mg_error()) {
+        status = NRSG_ERR_CUDA;
+        set_last_error("coarse-level solver: grid barrier wait exceeded its limit");
+      }
+      lastIters = st.it;
+      st.info.iterations = st.it;
+      st.info.status = status;
+      st.info.res0 = st.res0;
+      st.info.res = st.res;
+      st.info.solve_ms = ms;
+      st.phase = 4;
+      if (info) *info = st.info;
+      return true;
+    } else if (st.phase == 4) {
+      if (info) *info = st.info;
+      return true;
+    } else {
+      throw Error(NRSG_ERR_INVALID, "no solve in progress on this handle");
+    }
   }
-  lastIters = iters;
-  if (info) {
-    info->iterations = iters;
-    info->status = status;
-    info->res0 = res0;
-    info->res = res;
-    info->solve_ms = ms;
-  }
+}
+
+int Elliptic::solve(double *r, double *x, nrsg_solve_info *info)
+{
+  begin(r, x);
+  advance(true, info);
   return status;
 }
 
@@ -380,6 +447,76 @@ int nrsg_elliptic_solve(nrsg_elliptic *el, double *d_r, double *d_x, nrsg_solve_
     nrsg::set_last_error(e.what());
     return NRSG_ERR_INVALID;
   }
+}
+
+int nrsg_elliptic_set_tolerance(nrsg_elliptic *el, double tol, int relative, int maxIterations)
+{
+  if (!el || !(tol > 0) || maxIterations < 1) return NRSG_ERR_INVALID;
+  NRSG_TRY({
+    auto &E = *el->impl;
+    if (E.st.phase != 0 && E.st.phase != 4) throw Error(NRSG_ERR_INVALID, "a solve is in progress on this handle");
+    E.opt.tol = tol;
+    E.opt.relative = relative != 0;
+    E.opt.maxIter = maxIterations;
+  })
+}
+
+int nrsg_elliptic_solve_begin(nrsg_elliptic *el, double *d_r, double *d_x)
+{
+  if (!el || !d_r || !d_x) return NRSG_ERR_INVALID;
+  NRSG_TRY(el->impl->begin(d_r, d_x))
+}
+
+int nrsg_elliptic_solve_advance(nrsg_elliptic *el, int *done, nrsg_solve_info *info)
+{
+  if (!el || !done) return NRSG_ERR_INVALID;
+  *done = 0;
+  try {
+    if (el->impl->advance(false, info)) {
+      *done = 1;
+      return el->impl->st.info.status;
+    }
+    return NRSG_OK;
+  } catch (const Error &e) {
+    nrsg::set_last_error(e.what());
+    *done = 1;
+    return e.code;
+  } catch (const std::exception &e) {
+    nrsg::set_last_error(e.what());
+    *done = 1;
+    return NRSG_ERR_INVALID;
+  }
+}
+
+int nrsg_elliptic_solve_batch(int n, nrsg_elliptic *const *els, double *const *d_r, double *const *d_x,
+                              nrsg_solve_info *info)
+{
+  if (n < 0 || (n > 0 && (!els || !d_r || !d_x))) return NRSG_ERR_INVALID;
+  std::vector<int> state(n, 0); // 0 running, 1 done
+  std::vector<int> code(n, NRSG_OK);
+  for (int k = 0; k < n; ++k) {
+    code[k] = nrsg_elliptic_solve_begin(els[k], d_r[k], d_x[k]);
+    if (code[k] != NRSG_OK) state[k] = 1;
+  }
+  int left = 0;
+  for (int k = 0; k < n; ++k) left += state[k] == 0;
+  while (left > 0) {
+    for (int k = 0; k < n; ++k) {
+      if (state[k]) continue;
+      int done = 0;
+      const int c = nrsg_elliptic_solve_advance(els[k], &done, info ? &info[k] : nullptr);
+      if (done) {
+        state[k] = 1;
+        code[k] = c;
+        --left;
+      }
+    }
+  }
+  for (int k = 0; k < n; ++k)
+    if (code[k] != NRSG_OK && code[k] != NRSG_ERR_MAXIT) return code[k];
+  for (int k = 0; k < n; ++k)
+    if (code[k] != NRSG_OK) return code[k];
+  return NRSG_OK;
 }
 
 int nrsg_elliptic_solve_host(nrsg_elliptic *el, double *h_r, double *h_x, nrsg_solve_info *info)

@@ -74,10 +74,26 @@ struct Elliptic {
   void op(const double *q, double *Aq);
   void precondition(const double *r, double *z);
   double read_scalar(const double *d_src);
-  int pcg(double *r, double *x, double tol, int maxit, double &rnorm);
   void gmres_setup();
   int pgmres(double *r, double *x, double tol, int maxit, double &rnorm);
   int solve(double *r, double *x, nrsg_solve_info *info);
+
+  // Resumable solve (PCG / flexible PCG): begin() queues the initial residual,
+  // advance() consumes each residual norm once its copy has landed and queues
+  // the next iteration; with block = false it never waits on the device.
+  // solve() is begin() + advance(block = true).  GMRES runs inside begin().
+  struct StepState {
+    int phase = 0; // 0 idle, 1 res0 in flight, 2 iteration in flight, 3 final update in flight, 4 done
+    double *r = nullptr, *x = nullptr;
+    double res0 = 0, tol = 0, res = 0;
+    int it = 0;
+    nrsg_solve_info info{};
+  } st;
+  cudaEvent_t evRead = nullptr;
+  void begin(double *r, double *x);
+  bool advance(bool block, nrsg_solve_info *info);
+  void pcg_issue_iteration();
+  void finish_issue();
 
   void mg_setup();
   void mg_apply(const double *r, double *z);

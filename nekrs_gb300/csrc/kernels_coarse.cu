@@ -41,6 +41,7 @@
 #include "mg_kernels.hpp"
 
 #include <algorithm>
+#include <mutex>
 
 namespace nrsg {
 
@@ -539,6 +540,28 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_ppcg_kern
   }
 }
 
+// The dynamic shared-memory limit is an attribute of the kernel function, not
+// of a launch, and every solver in the process shares the function: raise it
+// to the largest size any solver on the device has needed, never lower it.
+static void raise_dynamic_smem(const void *kfn, size_t bytes)
+{
+  static std::mutex m;
+  static std::vector<std::pair<std::pair<int, const void *>, size_t>> set;
+  int dev = 0;
+  NRSG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(m);
+  for (auto &e : set)
+    if (e.first.first == dev && e.first.second == kfn) {
+      if (bytes > e.second) {
+        NRSG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+        e.second = bytes;
+      }
+      return;
+    }
+  NRSG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  set.push_back({{dev, kfn}, bytes});
+}
+
 // Host: partition the rows over one CTA per SM, build each CTA's ELL block
 // (local columns: own rows 0..chunk-1, halo rows chunk..), its halo list and
 // the shared-memory plan.
@@ -607,7 +630,7 @@ void coarse_matrix_setup(long long n, const long long *rowPtr, const long long *
   if (vBytes > limit) throw Error(NRSG_ERR_BAD_CONFIG, "coarse level: row block too large for shared memory");
   M.matInSmem = vBytes + mBytes <= limit;
   M.smem = vBytes + (M.matInSmem ? mBytes : 0);
-  NRSG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)M.smem));
+  raise_dynamic_smem(kfn, M.smem);
   int perSM = 0;
   NRSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kfn, kCT, M.smem));
   if (perSM < 1) throw Error(NRSG_ERR_CUDA, "coarse solver: kernel cannot be resident");
@@ -630,11 +653,34 @@ void coarse_matrix_setup(long long n, const long long *rowPtr, const long long *
   M.rowOf.upload(rowOf);
 }
 
+// Persistent coarse kernels of all solvers in the process are ordered on the
+// device (each waits for the previous one, whatever its stream): every one
+// occupies a CTA on every SM, and solvers on different streams (batched and
+// served solves) must not have two such grids in flight at once.
+namespace {
+struct CoarseGate {
+  std::mutex m;
+  cudaEvent_t ev[64] = {};
+};
+CoarseGate &coarse_gate()
+{
+  static CoarseGate g;
+  return g;
+}
+} // namespace
+
 template <typename T>
 int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *z, T *z2, double *partials,
                           void *state, int gridMax, double tol, int maxit, cudaStream_t s)
 {
   if (A.grid > gridMax) throw Error(NRSG_ERR_CUDA, "coarse solver: partial-sum buffer too small");
+  int dev = 0;
+  NRSG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) throw Error(NRSG_ERR_CUDA, "coarse solver: device index out of range");
+  CoarseGate &gate = coarse_gate();
+  std::lock_guard<std::mutex> lock(gate.m);
+  if (!gate.ev[dev]) NRSG_CUDA(cudaEventCreateWithFlags(&gate.ev[dev], cudaEventDisableTiming));
+  NRSG_CUDA(cudaStreamWaitEvent(s, gate.ev[dev], 0));
   NRSG_CUDA(cudaMemsetAsync(state, 0, sizeof(CoarseState), s));
   CoarseArgs<T> a;
   a.nrow = A.nrow;
@@ -663,6 +709,7 @@ int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *
   const void *kfn = A.pipelined ? (const void *)coarse_ppcg_kernel<T> : (const void *)coarse_pcg_kernel<T>;
   NRSG_CUDA(cudaLaunchCooperativeKernel(kfn, dim3(A.grid), dim3(kCT), args, A.smem, s));
   count_launch();
+  NRSG_CUDA(cudaEventRecord(gate.ev[dev], s));
   return A.grid;
 }
 
