@@ -63,9 +63,9 @@ EXPECTED_ITERS = {"kershaw48-n7-mixed": 32, "kershaw32-n7-mixed": 25, "kershaw16
                   "kershaw32-n7-fp64": 53, "kershaw16-n7-jacobi": 1632,
                   "kershaw8-n7-jacobi": 800}
 METRIC = "Poisson DOFs/s (E*N^3 / time-to-tolerance)"
-# DRAM bytes (read + write) of one launch of the dominant kernel, from an ncu capture of the E=16^3 case of the
-# same solve scaled by the element count (the traffic grows with the elements; profiles/ has the capture)
-TRAFFIC = {}
+# DRAM bytes (read + write) of one launch of the dominant kernel, from an ncu capture of the E=32^3 case of the
+# same solve scaled by the element count (every launch streams each element's data once): 237.3 MB at E=32^3
+TRAFFIC = {("kershaw48-n7-mixed", "fdm_f32"): 237.3e6 * 3.375}
 FP64_PLAIN = {"mgPrecision=mixed": "mgPrecision=fp64;axPrecision=fp64"}
 
 
@@ -331,12 +331,14 @@ def run_batch(args):
             ts.append(time.perf_counter() - t)
         out[name] = float(np.mean(ts))
     its = [el.get("history").size for el in els]
+    graphs = [el.get("graph.segments").tolist() for el in els[:2]]
     print(json.dumps({"metric": "batched Poisson DOFs/s (sum of E*N^3 / wall time of the batch)",
                       "value": dofs / out["batched"], "unit": "DOF/s", "n_gpus": 1, "steps": args.steps,
                       "warmup": args.warmup, "ms_per_step": out["batched"] * 1e3, "higher_is_better": True,
                       "dtype": "f64", "data": "synthetic (seeded Kershaw boxes, U[-1,1] mass-weighted RHS)",
                       "config": {"workload": "batch", "problems": K, "dofs": dofs, "setup_s": setup_s,
-                                 "iterations_min_max": [int(min(its)), int(max(its))]},
+                                 "iterations_min_max": [int(min(its)), int(max(its))],
+                                 "graph_segments_first_two": graphs},
                       "sequential": {"value": dofs / out["sequential"], "ms_per_step": out["sequential"] * 1e3},
                       "speedup_batched_vs_sequential": out["sequential"] / out["batched"]}))
 
@@ -576,7 +578,7 @@ def main():
     kr, peak, psrc = kernel_rooflines(G, el, N, E)
     if fdm is not None:
         kr["fdm_f32"] = fdm
-    # the dominant kernel of the solve by share of device time (profiles/: launch list of this workload)
+    # the dominant kernel of the solve by share of device time (ncu launch list of this workload)
     dominant = "fdm_f32" if fdm is not None else ("ax_fp32x2" if "mixed" in opts else "ax_stored_f64")
     d = kr[dominant]
     roof = {"bound": "hbm", "kernel": dominant, "achieved": d["achieved"], "peak": peak, "unit": "GB/s",

@@ -27,7 +27,16 @@ namespace nrsg {
 static thread_local std::string g_last_error;
 void set_last_error(const std::string &msg) { g_last_error = msg; }
 static std::atomic<long long> g_launches{0};
-void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+static thread_local long long *t_tally = nullptr;
+void count_launch()
+{
+  if (t_tally)
+    ++*t_tally;
+  else
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void set_launch_tally(long long *tally) { t_tally = tally; }
+void add_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 // ---------------------------------------------------------------------------
 // Level setup
@@ -178,6 +187,7 @@ Elliptic::~Elliptic()
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
   if (evRead) cudaEventDestroy(evRead);
+  graph_release();
   mg_release();
   if (ownStream && stream) cudaStreamDestroy(stream);
 }
@@ -225,12 +235,118 @@ double Elliptic::read_scalar(const double *d_src)
 // pinned host memory and its event.
 void Elliptic::pcg_issue_iteration()
 {
+  const int it = ++st.it;
+  if (it >= 2 && graphs_usable()) {
+    if (iterGraph.empty() || graphR != st.r || graphX != st.x) {
+      try {
+        build_iteration_graph();
+      } catch (const Error &) {
+        graph_release();
+        graphsFailed = true; // capture not possible here: stay on ordinary launches
+      }
+    }
+    if (!graphsFailed) {
+      for (auto &g : iterGraph) {
+        if (g.coarse) {
+          mg_coarse_launch();
+        } else {
+          NRSG_CUDA(cudaGraphLaunch(g.exec, stream));
+          add_launches(g.kernels);
+        }
+      }
+      NRSG_CUDA(cudaEventRecord(evRead, stream));
+      return;
+    }
+  }
+  issue_iteration_kernels(it == 1);
+  NRSG_CUDA(cudaEventRecord(evRead, stream));
+}
+
+bool Elliptic::graphs_usable()
+{
+  if (!opt.graphs || graphsFailed || stream == nullptr) return false;
+  if (opt.solver != "pcg" && opt.solver != "pfcg") return false;
+  return opt.precon != "multigrid" || mg_graph_capturable();
+}
+
+void Elliptic::end_segment()
+{
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(stream, &g);
+  if (e != cudaSuccess || !g) {
+    if (g) cudaGraphDestroy(g);
+    capturing = false;
+    set_launch_tally(nullptr);
+    throw Error(NRSG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  }
+  GraphSeg seg;
+  const cudaError_t ei = cudaGraphInstantiate(&seg.exec, g, 0);
+  cudaGraphDestroy(g);
+  if (ei != cudaSuccess) {
+    capturing = false;
+    set_launch_tally(nullptr);
+    throw Error(NRSG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
+  }
+  seg.kernels = capTally;
+  iterGraph.push_back(seg);
+}
+
+// called by the multigrid at the coarse solve while an iteration is captured
+void Elliptic::capture_split()
+{
+  end_segment();
+  GraphSeg c;
+  c.coarse = true;
+  iterGraph.push_back(c);
+  capTally = 0;
+  NRSG_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+}
+
+void Elliptic::build_iteration_graph()
+{
+  graph_release();
+  capTally = 0;
+  set_launch_tally(&capTally);
+  capturing = true;
+  const cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    capturing = false;
+    set_launch_tally(nullptr);
+    throw Error(NRSG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  }
+  try {
+    issue_iteration_kernels(false);
+  } catch (...) {
+    cudaGraph_t g = nullptr;
+    cudaStreamEndCapture(stream, &g);
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    capturing = false;
+    set_launch_tally(nullptr);
+    throw;
+  }
+  end_segment();
+  capturing = false;
+  set_launch_tally(nullptr);
+  graphR = st.r;
+  graphX = st.x;
+}
+
+void Elliptic::graph_release()
+{
+  for (auto &g : iterGraph)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  iterGraph.clear();
+  graphR = graphX = nullptr;
+}
+
+void Elliptic::issue_iteration_kernels(bool first)
+{
   const long long n = fine.Nlocal;
   const double *wt = fine.d_invDegree64.p;
   const bool flexible = (opt.solver == "pfcg");
   PcgScalars *sc = d_scal.p;
   double *r = st.r, *x = st.x;
-  const int it = ++st.it;
   if (opt.precon == "jacobi") {
     launch_jacobi_rdotz(n, wt, invDiag.p, r, z.p, sc, red, 0, stream);
   } else {
@@ -244,13 +360,12 @@ void Elliptic::pcg_issue_iteration()
     launch_scalar_move(&sc->rdotz_old, &sc->rdotz, nullptr, stream);
     launch_wdot<double>(n, wt, r, zz, &sc->rdotz, red, 0, stream);
   }
-  if (flexible && it > 1) launch_wdot<double>(n, wt, z.p, Ap.p, &sc->zAp, red, 1, stream);
-  launch_update_p(n, z.p, p.p, sc, it == 1, flexible, stream);
+  if (flexible && !first) launch_wdot<double>(n, wt, z.p, Ap.p, &sc->zAp, red, 1, stream);
+  launch_update_p(n, z.p, p.p, sc, first, flexible, stream);
   op(p.p, Ap.p);
   launch_wdot<double>(n, wt, p.p, Ap.p, &sc->pAp, red, 2, stream);
   launch_update_xr(n, wt, p.p, Ap.p, x, r, sc, red, 3, stream);
   NRSG_CUDA(cudaMemcpyAsync(&h_scal->rdotr, &sc->rdotr, sizeof(double), cudaMemcpyDeviceToHost, stream));
-  NRSG_CUDA(cudaEventRecord(evRead, stream));
 }
 
 void Elliptic::finish_issue()
@@ -604,7 +719,12 @@ int nrsg_elliptic_get(nrsg_elliptic *el, const char *name, void *h_out, long lon
     else if (s == "invDegree") put(L.gm.invDegree);
     else if (s == "D") put(L.Dh);
     else if (s == "history") put(E.history);
-    else if (s == "ggeo") put(L.d_ggeo64.download());
+    else if (s == "graph.segments") {
+      // segments of the captured steady-state iteration (0: ordinary launches), and how many are coarse solves
+      long long nc = 0;
+      for (auto &g : E.iterGraph) nc += g.coarse ? 1 : 0;
+      put(std::vector<double>{(double)E.iterGraph.size(), (double)nc, E.graphsFailed ? 1.0 : 0.0});
+    } else if (s == "ggeo") put(L.d_ggeo64.download());
     else if (s == "invDiag") put(E.invDiag.download());
     else if (s == "x" || s == "y" || s == "z") {
       std::vector<double> X, Y, Z;

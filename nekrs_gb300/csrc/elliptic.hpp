@@ -93,7 +93,29 @@ struct Elliptic {
   void begin(double *r, double *x);
   bool advance(bool block, nrsg_solve_info *info);
   void pcg_issue_iteration();
+  void issue_iteration_kernels(bool first);
   void finish_issue();
+
+  // CUDA graphs of the steady-state PCG iteration (iterations 2, 3, ...),
+  // split at the persistent coarse solve, which stays an ordinary launch
+  // (ordered against every other solver's, see kernels_coarse.cu).  Used on
+  // non-legacy streams; rebuilt when the solve's r / x change.
+  struct GraphSeg {
+    cudaGraphExec_t exec = nullptr;
+    bool coarse = false;
+    long long kernels = 0;
+  };
+  std::vector<GraphSeg> iterGraph;
+  double *graphR = nullptr, *graphX = nullptr;
+  bool capturing = false, graphsFailed = false;
+  long long capTally = 0;
+  bool graphs_usable();
+  void build_iteration_graph();
+  void end_segment();
+  void capture_split();
+  void graph_release();
+  void mg_coarse_launch();
+  bool mg_graph_capturable();
 
   void mg_setup();
   void mg_apply(const double *r, double *z);

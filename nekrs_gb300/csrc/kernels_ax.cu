@@ -21,8 +21,10 @@ template <int NQ> struct AxShape {
   static constexpr int epb = plane >= 128 ? 1 : (128 + plane - 1) / plane;
 };
 
+// FP32 order 7: at most 80 registers so that 6 CTAs (24 warps) fit per SM
+// (measured 2.7% faster at E=48^3 than the unbounded 100-register build)
 template <typename T, int NQ, bool POISSON>
-__global__ void __launch_bounds__(NQ *NQ *AxShape<NQ>::epb)
+__global__ void __launch_bounds__(NQ *NQ *AxShape<NQ>::epb, (sizeof(T) == 4 && NQ == 8) ? 6 : 1)
     ax_stored_kernel(long long E, const T *__restrict__ ggeo, const T *__restrict__ D, T lambda0, T lambda1,
                      const T *__restrict__ q, T *__restrict__ Aq)
 {

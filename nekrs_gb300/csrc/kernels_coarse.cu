@@ -46,7 +46,7 @@
 namespace nrsg {
 
 namespace {
-constexpr int kCT = 1024;              // threads per CTA (one CTA per SM)
+constexpr int kCT = 1024;              // most threads per CTA (one CTA per SM; a row block of fewer rows uses fewer)
 constexpr long long kSpinLimit = 1LL << 22;
 constexpr int kMinRowsPerCta = 128;
 
@@ -85,7 +85,7 @@ template <typename T> __device__ __forceinline__ void cta_partial(T a, double *s
   if (lane == 0) sh[wid] = (double)a;
   __syncthreads();
   if (wid == 0) {
-    const double x = wsum(sh[lane]); // kCT / 32 == 32 warps
+    const double x = wsum(lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0);
     if (lane == 0) *dst0 = x;
   }
 }
@@ -100,7 +100,8 @@ template <typename T> __device__ __forceinline__ void cta_partial2(T a, T b, dou
   }
   __syncthreads();
   if (wid == 0) {
-    const double x = wsum(sh[lane]), y = wsum(sh[32 + lane]);
+    const bool in = lane < (int)(blockDim.x >> 5);
+    const double x = wsum(in ? sh[lane] : 0.0), y = wsum(in ? sh[32 + lane] : 0.0);
     if (lane == 0) {
       *dst0 = x;
       *dst1 = y;
@@ -125,7 +126,8 @@ __device__ __forceinline__ void cta_partial3(T a, T b, T c, T *sh, T *dst0, T *d
   }
   __syncthreads();
   if (wid == 0) {
-    const T x = wsum(sh[lane]), y = wsum(sh[32 + lane]), z = wsum(sh[64 + lane]);
+    const bool in = lane < (int)(blockDim.x >> 5);
+    const T x = wsum(in ? sh[lane] : T(0)), y = wsum(in ? sh[32 + lane] : T(0)), z = wsum(in ? sh[64 + lane] : T(0));
     if (lane == 0) {
       *dst0 = x;
       *dst1 = y;
@@ -267,7 +269,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_pcg_kerne
     if (a.matInSmem) {
       T *sv = (T *)(dsm + vec_bytes<T>(chunk, mh));
       unsigned short *sl = (unsigned short *)(sv + (size_t)W * chunk);
-      for (int i = threadIdx.x; i < W * chunk; i += kCT) {
+      for (int i = threadIdx.x; i < W * chunk; i += blockDim.x) {
         sv[i] = __ldg(a.val + off + i);
         sl[i] = __ldg(a.lcol + off + i);
       }
@@ -278,10 +280,10 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_pcg_kerne
       Lc = a.lcol + off;
     }
   }
-  for (int i = threadIdx.x; i < nh; i += kCT) hs[i] = __ldg(a.haloIds + h0 + i);
+  for (int i = threadIdx.x; i < nh; i += blockDim.x) hs[i] = __ldg(a.haloIds + h0 + i);
   T *zg = a.z + start;
   T rr = T(0), rz = T(0);
-  for (int t = threadIdx.x; t < cnt; t += kCT) {
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
     const T ru = __ldg(a.b + __ldg(a.rep + start + t));
     const T iv = __ldg(a.invDiag + start + t);
     const T zu = iv * ru;
@@ -317,10 +319,10 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_pcg_kerne
     const T beta = s_beta;
     // A: halo of z, then w = A z, p, Ap, (p, Ap)
 #pragma unroll 4
-    for (int i = threadIdx.x; i < nh; i += kCT) zs[chunk + i] = __ldcg(a.z + hs[i]);
+    for (int i = threadIdx.x; i < nh; i += blockDim.x) zs[chunk + i] = __ldcg(a.z + hs[i]);
     __syncthreads();
     T pap = T(0);
-    for (int t = threadIdx.x; t < cnt; t += kCT) {
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
       T w = T(0);
 #pragma unroll 9
       for (int k = 0; k < W; ++k) w = fma_t<T>(V[k * chunk + t], zs[Lc[k * chunk + t]], w);
@@ -341,7 +343,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_pcg_kerne
     // B: x += alpha p, r -= alpha Ap, z = invDiag r, (r, r), (r, z)
     rr = T(0);
     rz = T(0);
-    for (int t = threadIdx.x; t < cnt; t += kCT) {
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
       xs[t] = fma_t<T>(alpha, ps[t], xs[t]);
       const T ru = fma_t<T>(-alpha, aps[t], rs[t]);
       rs[t] = ru;
@@ -368,9 +370,9 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_pcg_kerne
     __syncthreads();
   }
   // E-vector solution: every copy of a row takes its value, masked nodes 0
-  for (int t = threadIdx.x; t < cnt; t += kCT) a.x[start + t] = xs[t];
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) a.x[start + t] = xs[t];
   if (!grid_barrier(a.st, ++nb)) return;
-  const long long tid = blockIdx.x * (long long)kCT + threadIdx.x, nth = (long long)gridDim.x * kCT;
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x, nth = (long long)gridDim.x * blockDim.x;
   for (long long i = tid; i < a.nE; i += nth) {
     const int u = __ldg(a.rowOf + i);
     a.xE[i] = u >= 0 ? __ldcg(a.x + u) : T(0);
@@ -414,7 +416,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_ppcg_kern
     if (a.matInSmem) {
       T *svm = (T *)(dsm + vec_bytes_pipe<T>(chunk, mh));
       unsigned short *sl = (unsigned short *)(svm + (size_t)W * chunk);
-      for (int i = threadIdx.x; i < W * chunk; i += kCT) {
+      for (int i = threadIdx.x; i < W * chunk; i += blockDim.x) {
         svm[i] = __ldg(a.val + off + i);
         sl[i] = __ldg(a.lcol + off + i);
       }
@@ -425,10 +427,10 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_ppcg_kern
       Lc = a.lcol + off;
     }
   }
-  for (int i = threadIdx.x; i < nh; i += kCT) hs[i] = __ldg(a.haloIds + h0 + i);
+  for (int i = threadIdx.x; i < nh; i += blockDim.x) hs[i] = __ldg(a.haloIds + h0 + i);
   // exchange buffers: u0 goes through a.z, m_i through a.z2 (i even) / a.z (i odd)
   // r0 = b, u0 = M^-1 r0 (published for the halos), x0 = 0
-  for (int t = threadIdx.x; t < cnt; t += kCT) {
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
     const T ru = __ldg(a.b + __ldg(a.rep + start + t));
     const T iv = __ldg(a.invDiag + start + t);
     const T uu = iv * ru;
@@ -447,9 +449,9 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_ppcg_kern
   unsigned nb = 1;
   // w0 = A u0
 #pragma unroll 4
-  for (int i = threadIdx.x; i < nh; i += kCT) ms[chunk + i] = __ldcg(a.z + hs[i]);
+  for (int i = threadIdx.x; i < nh; i += blockDim.x) ms[chunk + i] = __ldcg(a.z + hs[i]);
   __syncthreads();
-  for (int t = threadIdx.x; t < cnt; t += kCT) {
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
     T w = T(0);
 #pragma unroll 9
     for (int k = 0; k < W; ++k) w = fma_t<T>(V[k * chunk + t], ms[Lc[k * chunk + t]], w);
@@ -464,7 +466,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_ppcg_kern
     __syncthreads(); // the previous SpMV has read ms
     // phase 1: partial (r,u), (w,u), (r,r); m = M^-1 w, published
     T g = T(0), d = T(0), rr = T(0);
-    for (int t = threadIdx.x; t < cnt; t += kCT) {
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
       const T ru = rs[t], uu = us[t], ww = wv[t];
       g = fma_t<T>(ru, uu, g);
       d = fma_t<T>(ww, uu, d);
@@ -505,9 +507,9 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_ppcg_kern
     const T alpha = s_alpha, beta = s_beta;
     // phase 2: n = A m; recurrences
 #pragma unroll 4
-    for (int q = threadIdx.x; q < nh; q += kCT) ms[chunk + q] = __ldcg(mg + hs[q]);
+    for (int q = threadIdx.x; q < nh; q += blockDim.x) ms[chunk + q] = __ldcg(mg + hs[q]);
     __syncthreads();
-    for (int t = threadIdx.x; t < cnt; t += kCT) {
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
       T nn = T(0);
 #pragma unroll 9
       for (int k = 0; k < W; ++k) nn = fma_t<T>(V[k * chunk + t], ms[Lc[k * chunk + t]], nn);
@@ -526,9 +528,9 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_ppcg_kern
     }
   }
   // E-vector solution: every copy of a row takes its value, masked nodes 0
-  for (int t = threadIdx.x; t < cnt; t += kCT) a.x[start + t] = xs[t];
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) a.x[start + t] = xs[t];
   if (!grid_barrier(a.st, ++nb)) return;
-  const long long tid = blockIdx.x * (long long)kCT + threadIdx.x, nth = (long long)gridDim.x * kCT;
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x, nth = (long long)gridDim.x * blockDim.x;
   for (long long i = tid; i < a.nE; i += nth) {
     const int u = __ldg(a.rowOf + i);
     a.xE[i] = u >= 0 ? __ldcg(a.x + u) : T(0);
@@ -632,8 +634,9 @@ void coarse_matrix_setup(long long n, const long long *rowPtr, const long long *
   M.smem = vBytes + (M.matInSmem ? mBytes : 0);
   raise_dynamic_smem(kfn, M.smem);
   int perSM = 0;
-  NRSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kfn, kCT, M.smem));
+  NRSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kfn, std::min<long long>(kCT, std::max<long long>(32, (chunk + 31) / 32 * 32)), M.smem));
   if (perSM < 1) throw Error(NRSG_ERR_CUDA, "coarse solver: kernel cannot be resident");
+  M.threads = (int)std::min<long long>(kCT, std::max<long long>(32, (chunk + 31) / 32 * 32));
   M.nrow = n;
   M.nE = nE;
   M.width = width;
@@ -707,7 +710,7 @@ int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *
   a.maxit = maxit;
   void *args[] = {&a};
   const void *kfn = A.pipelined ? (const void *)coarse_ppcg_kernel<T> : (const void *)coarse_pcg_kernel<T>;
-  NRSG_CUDA(cudaLaunchCooperativeKernel(kfn, dim3(A.grid), dim3(kCT), args, A.smem, s));
+  NRSG_CUDA(cudaLaunchCooperativeKernel(kfn, dim3(A.grid), dim3(A.threads), args, A.smem, s));
   count_launch();
   NRSG_CUDA(cudaEventRecord(gate.ev[dev], s));
   return A.grid;

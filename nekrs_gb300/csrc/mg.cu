@@ -25,6 +25,8 @@ struct MGState {
   virtual std::vector<double> info(const std::string &what) = 0;
   virtual void schwarz(int level, const double *u, double *Su) = 0;
   virtual void fdm(int level, const void *u, void *Su) = 0;
+  virtual void coarse_launch() = 0;
+  virtual bool graph_capturable() = 0;
   virtual long long level_size(int level) = 0;
   virtual int error() = 0;
 };
@@ -412,6 +414,10 @@ template <typename T> struct MGImpl : public MGState {
   {
     FieldLevel &L = *v.L;
     if (persistentCoarse) {
+      if (el.capturing) {
+        el.capture_split(); // the coarse solve is launched between the iteration's graph segments
+        return 0;
+      }
       coarse_pcg_persistent<T>(cA, b, x, cx.p, cz2.p, cz3.p, cPartials.p, cState.p, kCoarseGridMax,
                                el.opt.coarseTol, el.opt.coarseMaxIter, s);
       return 0;
@@ -551,6 +557,14 @@ template <typename T> struct MGImpl : public MGState {
                   v.wts.p, (T *)Su, v.haloOut.p, s);
   }
 
+  void coarse_launch() override
+  {
+    auto &c = lv.back();
+    coarse_pcg(c, c.rhs.p, c.x.p);
+  }
+  // host-driven coarse iterations read the device between launches: not capturable
+  bool graph_capturable() override { return persistentCoarse || el.opt.coarse == "smooth"; }
+
   void schwarz(int level, const double *u, double *Su) override
   {
     auto &v = lv.at(level);
@@ -588,6 +602,12 @@ long long Elliptic::mg_level_size(int level)
   if (!mg) throw Error(NRSG_ERR_INVALID, "no multigrid preconditioner");
   return mg->level_size(level);
 }
+void Elliptic::mg_coarse_launch()
+{
+  if (mg) mg->coarse_launch();
+}
+bool Elliptic::mg_graph_capturable() { return mg && mg->graph_capturable(); }
+
 void Elliptic::mg_fdm(int level, const void *u, void *Su)
 {
   if (!mg) throw Error(NRSG_ERR_INVALID, "no multigrid preconditioner");

@@ -34,6 +34,7 @@ void launch_pcg_xr(long long n, const T *w, const T *p, const T *Ap, T *x, T *r,
 template <typename T> struct CoarseMatrix {
   long long nrow = 0, nE = 0, nnz = 0;
   int width = 0, grid = 0, chunk = 0, maxHalo = 0;
+  int threads = 1024;            // threads per CTA: the row block rounded up to a warp, at most 1024
   bool matInSmem = false;
   bool pipelined = false;        // one-barrier pipelined PCG (FP32)
   size_t smem = 0;               // dynamic shared memory per CTA

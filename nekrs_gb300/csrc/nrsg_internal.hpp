@@ -30,6 +30,10 @@ void set_last_error(const std::string &msg);
 
 // Every launcher ends with NRSG_CHECK_LAUNCH(), which also counts the launch.
 void count_launch();
+// while a tally is set on this thread, count_launch() adds to it instead of
+// the process counter (kernels recorded into a CUDA graph are not launched)
+void set_launch_tally(long long *tally);
+void add_launches(long long n);
 #define NRSG_CHECK_LAUNCH()                                                                                \
   do {                                                                                                     \
     ::nrsg::count_launch();                                                                                \
@@ -97,6 +101,7 @@ struct Options {
   double coarseTol = 1e-4;
   int coarseMaxIter = 200;
   bool coarsePersistent = true;     // order-1 coarse Jacobi-PCG as one cooperative kernel
+  bool graphs = true;               // CUDA graphs of the steady-state PCG iteration (non-legacy streams)
   std::string mgPrecision = "fp64"; // fp64 | fp32 | mixed
   std::string axPrecision = "fp64"; // fine-level operator: fp64 | fp32x2 (FP64-accurate FP32-pair arithmetic)
   bool poisson = true;

@@ -398,6 +398,7 @@ Options parse_options(const char *text)
       else if (key == "coarsetol") o.coarseTol = std::stod(v);
       else if (key == "coarsemaxiterations") o.coarseMaxIter = std::stoi(v);
       else if (key == "coarsepersistent") o.coarsePersistent = std::stoi(v) != 0;
+      else if (key == "cudagraphs") o.graphs = std::stoi(v) != 0;
       else if (key == "mgprecision") o.mgPrecision = v;
       else if (key == "axprecision") {
         if (v != "fp64" && v != "fp32x2") throw Error(NRSG_ERR_BAD_CONFIG, "axPrecision must be fp64 or fp32x2");
