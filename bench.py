@@ -30,10 +30,11 @@ sys.path.insert(0, ROOT)
 
 SCHED7 = "p=7+degree=2,p=3+degree=2,p=1,p=3+degree=2,p=7+degree=2"
 PMG = "preconditioner=multigrid;smootherType=cheby+asm;pMGSchedule=" + SCHED7 + ";coarseSolver=jpcg;coarseTol=1e-4"
-# mixed-precision headline: optimal 4th-kind Chebyshev (degree 4) over ASM; at E=48^3 it reaches 1e-8 in 32
-# iterations against 76 for Chebyshev(2)+ASM, and takes 0.71x the time (measured on the GB300)
-SCHED7_4 = "p=7+degree=4,p=3+degree=4,p=1,p=3+degree=4,p=7+degree=4"
-PMG4 = ("preconditioner=multigrid;smootherType=fourthoptcheby+asm;pMGSchedule=" + SCHED7_4 +
+# mixed-precision headline: optimal 4th-kind Chebyshev (degree 5) over RAS; at E=48^3 it reaches 1e-8 in 26
+# iterations in 0.73 s, against 32 / 0.81 s for optimal 4th-kind (4) + ASM and 76 / 1.54 s for Chebyshev(2) + ASM
+# (measured on the GB300)
+SCHED7_5 = "p=7+degree=5,p=3+degree=5,p=1,p=3+degree=5,p=7+degree=5"
+PMG4 = ("preconditioner=multigrid;smootherType=fourthoptcheby+ras;pMGSchedule=" + SCHED7_5 +
         ";coarseSolver=jpcg;coarseTol=1e-4")
 
 # name: (elements per side, N, eps, options, description)
@@ -41,12 +42,18 @@ WORKLOADS = {
     "kershaw48-n7-mixed": (48, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
                            ";mgPrecision=mixed",
                            "Kershaw box E=48^3 N=7 eps=0.3: FP64 flexible PCG, FP32 pMG 7/3/1 (optimal 4th-kind "
-                           "Chebyshev(4)+ASM FDM, coarse Jacobi-PCG 1e-4 on the assembled order-1 operator), "
+                           "Chebyshev(5)+RAS FDM, coarse Jacobi-PCG 1e-4 on the assembled order-1 operator), "
                            "FP64-accurate FP32-pair fine operator, to 1e-8 relative"),
     "kershaw32-n7-mixed": (32, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
                            ";mgPrecision=mixed", "the kershaw48-n7-mixed solve on E=32^3 (profiling size)"),
     "kershaw16-n7-mixed": (16, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
                            ";mgPrecision=mixed", "the kershaw48-n7-mixed solve on E=16^3 (profiling size)"),
+    "kershaw20-n7-bps5": (20, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;preconditioner=multigrid;"
+                          "smootherType=fourthoptcheby+ras;pMGSchedule=p=7+degree=3,p=3+degree=3,p=1,p=3+degree=3,"
+                          "p=7+degree=3;coarseSolver=jpcg;coarseTol=1e-4;mgPrecision=mixed",
+                          "the reference's BPS5 case (examples/kershaw: E=20^3, N=7, eps=0.3, RAS + optimal 4th-kind "
+                          "Chebyshev(3), levels 7/3/1, RHS 3 pi^2 sin(pi x) sin(pi y) sin(pi z) on [-0.5,0.5]^3, 1e-8), "
+                          "coarse Jacobi-PCG 1e-4 in place of BoomerAMG; the reference reports 28 iterations"),
     "kershaw32-n7-fp64": (32, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG +
                           ";mgPrecision=fp64;axPrecision=fp64",
                           "Kershaw box E=32^3 N=7 eps=0.3: plain FP64 pMG-PCG (flexible), Chebyshev(2)+ASM, "
@@ -59,13 +66,13 @@ WORKLOADS = {
 DEFAULT_WORKLOAD = "kershaw48-n7-mixed"
 # iterations to tolerance of each workload (measured on the GPU; the solvers are parity-tested against the
 # oracle), used by the reference arm to project its per-iteration CPU time to a full solve
-EXPECTED_ITERS = {"kershaw48-n7-mixed": 32, "kershaw32-n7-mixed": 25, "kershaw16-n7-mixed": 22,
+EXPECTED_ITERS = {"kershaw48-n7-mixed": 26, "kershaw32-n7-mixed": 21, "kershaw16-n7-mixed": 18, "kershaw20-n7-bps5": 31,
                   "kershaw32-n7-fp64": 53, "kershaw16-n7-jacobi": 1632,
                   "kershaw8-n7-jacobi": 800}
 METRIC = "Poisson DOFs/s (E*N^3 / time-to-tolerance)"
 # DRAM bytes (read + write) of one launch of the dominant kernel, from an ncu capture of the E=32^3 case of the
 # same solve scaled by the element count (every launch streams each element's data once): 237.3 MB at E=32^3
-TRAFFIC = {("kershaw48-n7-mixed", "fdm_f32"): 237.3e6 * 3.375}
+TRAFFIC = {}
 FP64_PLAIN = {"mgPrecision=mixed": "mgPrecision=fp64;axPrecision=fp64"}
 
 
@@ -253,10 +260,11 @@ def kernel_rooflines(G, el, N, E):
     return out, peak, src
 
 
-def fdm_roofline(G, el, N, E, peak):
+def fdm_roofline(G, el, N, E, peak, ras):
     """Achieved algorithmic GB/s of one fine-level fused FDM launch (the order-7 Schwarz local solve), CUDA
-    events on its stream.  Algorithmic bytes per element follow the reference's extended-element formulation:
-    read u_ext and write Su over (N+3)^3, S_x, S_y, S_z (3 (N+3)^2) and invL ((N+3)^3), 4 B each."""
+    events on its stream.  Algorithmic bytes per element follow the reference's extended-element formulation
+    (fusedFDM), 4 B each: read u_ext ((N+3)^3), S_x, S_y, S_z (3 (N+3)^2) and invL ((N+3)^3), then ASM: write
+    Su_ext ((N+3)^3); RAS: read the weights and write Su on the own nodes (2 (N+1)^3)."""
     import torch
 
     if el.get("mg.bytes")[0] != 4:
@@ -267,21 +275,21 @@ def fdm_roofline(G, el, N, E, peak):
     stream = torch.cuda.current_stream()
     t = time_kernel(lambda: el.mg_fdm(0, u, su), stream)
     nl = N + 3
-    per_el = 4.0 * (3 * nl ** 3 + 3 * nl ** 2)
+    per_el = 4.0 * (2 * nl ** 3 + 3 * nl ** 2 + (2 * (N + 1) ** 3 if ras else nl ** 3))
     flops = float(E) * (12 * nl * nl ** 3 + nl ** 3)
     return {"launch_ms": t * 1e3, "achieved": per_el * E / t / 1e9, "unit": "GB/s", "algorithmic_bytes": per_el * E,
             "fp32_tflops": flops / t / 1e12, "frac_of_hbm": per_el * E / t / 1e9 / peak}
 
 
 def mg_options(N, tol="1e-8"):
-    """Mixed-precision pMG-FPCG options for order N (levels N / 3 / 1, or N / 1 for N <= 3), optimal 4th-kind
-    Chebyshev(4) + ASM, coarse Jacobi-PCG on the assembled order-1 operator."""
+    """Mixed-precision pMG-FPCG options for order N (levels N / 3 / 1, or N / 1 for N <= 3), the headline's
+    optimal 4th-kind Chebyshev(5) + RAS, coarse Jacobi-PCG on the assembled order-1 operator."""
     mid = {9: 5, 8: 5, 7: 3, 6: 3, 5: 3, 4: 2}.get(N)
     lv = [N] + ([mid] if mid else []) + [1]
-    down = [f"p={q}+degree=4" for q in lv[:-1]]
+    down = [f"p={q}+degree=5" for q in lv[:-1]]
     sched = ",".join(down + ["p=1"] + down[::-1])
     return (f"solver=pfcg;residualTol={tol}+relative;maxIterations=400;preconditioner=multigrid;"
-            f"smootherType=fourthoptcheby+asm;pMGSchedule={sched};coarseSolver=jpcg;coarseTol=1e-4;mgPrecision=mixed")
+            f"smootherType=fourthoptcheby+ras;pMGSchedule={sched};coarseSolver=jpcg;coarseTol=1e-4;mgPrecision=mixed")
 
 
 def run_batch(args):
@@ -484,7 +492,12 @@ def main():
     t0 = time.perf_counter()
     el = G.Elliptic(N, VX, EToV, EToB, opts)
     setup_s = time.perf_counter() - t0
-    rhs = W.box_rhs(N, nel, nel, nel, 1234 + rank, el.get("ggeo"))
+    if args.workload.endswith("bps5"):
+        # kershaw.udf: P0 = 3 pi^2 sin(pi x) sin(pi y) sin(pi z) at every node of the mesh on [-0.5, 0.5]^3
+        xs, ys, zs = (el.get(c) - 0.5 for c in ("x", "y", "z"))
+        rhs = 3 * np.pi ** 2 * np.sin(np.pi * xs) * np.sin(np.pi * ys) * np.sin(np.pi * zs)
+    else:
+        rhs = W.box_rhs(N, nel, nel, nel, 1234 + rank, el.get("ggeo"))
     rhs_d = torch.from_numpy(rhs).cuda()
     r = torch.empty_like(rhs_d)
     x = torch.zeros_like(rhs_d)
@@ -548,8 +561,20 @@ def main():
     del rh, xh
 
     peak, psrc = load_peaks()
-    fdm = fdm_roofline(G, el, N, E, peak) if "multigrid" in opts and "asm" in opts else None
+    fdm = (fdm_roofline(G, el, N, E, peak, "ras" in opts)
+           if "multigrid" in opts and ("asm" in opts or "ras" in opts) else None)
     extra = {}
+    # time-to-tolerance at the other tolerances of the mixed-precision config
+    tols = {}
+    if "mgPrecision=mixed" in opts and not args.no_fp64_plain:
+        for tol in (1e-6, 1e-10):
+            el.set_tolerance(tol)
+            r.copy_(rhs_d)
+            x.zero_()
+            it = el.solve(r, x)
+            tols[tol] = {"mixed_s": it["solve_ms"] / 1e3, "mixed_iterations": it["iterations"],
+                         "x": x.cpu().numpy().copy()}
+        el.set_tolerance(1e-8)
     if "mgPrecision=mixed" in opts and not args.no_fp64_plain:
         del el
         torch.cuda.empty_cache()
@@ -569,6 +594,19 @@ def main():
                                "options": plain_fp64_options(opts)}
         extra["speedup_mixed_vs_fp64_plain"] = value / world / extra["fp64_plain"]["value"]
         extra["error_vs_fp64"] = float(np.linalg.norm(x_mixed - xp) / np.linalg.norm(xp))
+        ttt = {"1e-08": {"mixed_s": t_step, "mixed_iterations": infos[-1]["iterations"],
+                         "fp64_s": ip["solve_ms"] / 1e3, "fp64_iterations": ip["iterations"],
+                         "error_vs_fp64": extra["error_vs_fp64"]}}
+        for tol, v in tols.items():
+            elp.set_tolerance(tol)
+            r.copy_(rhs_d)
+            x.zero_()
+            it = elp.solve(r, x)
+            xq = x.cpu().numpy()
+            ttt[f"{tol:.0e}"] = {"mixed_s": v["mixed_s"], "mixed_iterations": v["mixed_iterations"],
+                                 "fp64_s": it["solve_ms"] / 1e3, "fp64_iterations": it["iterations"],
+                                 "error_vs_fp64": float(np.linalg.norm(v["x"] - xq) / np.linalg.norm(xq))}
+        extra["time_to_tolerance"] = ttt
         del elp
         torch.cuda.empty_cache()
         el = None

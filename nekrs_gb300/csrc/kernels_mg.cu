@@ -368,6 +368,15 @@ __global__ void __launch_bounds__(32 * kAsmEpc)
   if (e >= E) return; // whole warp; warp-level synchronisation only
   T *su = s_u[wp];
   const int *hp = haloPartner + e * 6 * NF;
+  constexpr int NPL = (NP + 31) / 32; // nodes per lane
+  // every independent load first (own nodes, weights, partner indices), then the gathers
+  T own[NPL], wt[NPL];
+#pragma unroll
+  for (int m = 0; m < NPL; ++m) {
+    const int q = lane + 32 * m;
+    own[m] = q < NP ? Su[e * NP + q] : T(0);
+    wt[m] = q < NP ? __ldg(wts + e * NP + q) : T(0);
+  }
   int hidx[6][PPF];
 #pragma unroll
   for (int f = 0; f < 6; ++f)
@@ -381,7 +390,11 @@ __global__ void __launch_bounds__(32 * kAsmEpc)
   for (int f = 0; f < 6; ++f)
 #pragma unroll
     for (int m = 0; m < PPF; ++m) hval[f][m] = hidx[f][m] >= 0 ? __ldg(haloOut + hidx[f][m]) : T(0);
-  for (int q = lane; q < NP; q += 32) su[q] = Su[e * NP + q];
+#pragma unroll
+  for (int m = 0; m < NPL; ++m) {
+    const int q = lane + 32 * m;
+    if (q < NP) su[q] = own[m];
+  }
   __syncwarp();
 #pragma unroll
   for (int f = 0; f < 6; ++f) {
@@ -404,7 +417,11 @@ __global__ void __launch_bounds__(32 * kAsmEpc)
     }
     __syncwarp();
   }
-  for (int q = lane; q < NP; q += 32) Su[e * NP + q] = su[q] * __ldg(wts + e * NP + q);
+#pragma unroll
+  for (int m = 0; m < NPL; ++m) {
+    const int q = lane + 32 * m;
+    if (q < NP) Su[e * NP + q] = su[q] * wt[m];
+  }
 }
 
 // ---------------------------------------------------------------------------

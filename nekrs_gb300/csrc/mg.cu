@@ -230,7 +230,15 @@ template <typename T> struct MGImpl : public MGState {
     fdm_halo_maps(L, src, partner, w);
     v.haloSrc.upload(src);
     v.haloPartner.upload(partner);
-    std::vector<T> wt(w.begin(), w.end());
+    // ASM weights its combined overlap result by the overlap weights
+    // (generate_weights); RAS restricts each element's own nodes with the
+    // level's inverse degree (fusedFDM with p_restrict gets elliptic->o_invDegree,
+    // ellipticMultiGridSchwarz.cpp:1069-1077, fusedFDM.c:209-215)
+    std::vector<T> wt;
+    if (plan.base == 2)
+      wt.assign(L.gm.invDegree.begin(), L.gm.invDegree.end());
+    else
+      wt.assign(w.begin(), w.end());
     v.wts.upload(wt);
     if (plan.base == 1) v.haloOut.alloc(src.size());
   }

@@ -670,11 +670,14 @@ template <typename T> static void smooth_schwarz(MGT<T> &M, MGLevel<T> &lv, cons
           t2[X(i, j, k)] = v;
         }
     if (ras) {
+      // restrict with the level's inverse degree (the weights argument of
+      // fusedFDM, elliptic->o_invDegree: ellipticMultiGridSchwarz.cpp:1069-1077,
+      // fusedFDM.c:209-215)
       for (int k = 0; k < nq; ++k)
         for (int j = 0; j < nq; ++j)
           for (int i = 0; i < nq; ++i) {
             const long long id = e * np + i + nq * (j + nq * k);
-            out[id] = t2[X(i + 1, j + 1, k + 1)] * F.wts[id];
+            out[id] = t2[X(i + 1, j + 1, k + 1)] * lv.invDegree[id];
           }
     } else {
       std::memcpy(&Sext[e * npe], t2.data(), sizeof(T) * npe);

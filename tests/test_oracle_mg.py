@@ -80,8 +80,11 @@ def test_schwarz_matches_reference_kernels(oracle_mod, smoother, N):
     _ext_gs(off, ids, w1)
     el = np.arange(E, dtype=np.int32)
     if smoother == "cheby+ras":
+        # RAS: the reference passes the level's inverse degree as the restriction weights
+        # (fusedFDMKernel(..., o_invL, elliptic->o_invDegree, o_work1), ellipticMultiGridSchwarz.cpp:1069-1077)
         Su = np.zeros(o.Nlocal)
-        getattr(REF, f"ref_fdmr_d_N{N}")(ctypes.byref(cE), P(el), P(Su), P(Sx), P(Sy), P(Sz), P(invL), P(wts), P(w1))
+        invDeg = np.ascontiguousarray(o.get("invDegree"))
+        getattr(REF, f"ref_fdmr_d_N{N}")(ctypes.byref(cE), P(el), P(Su), P(Sx), P(Sy), P(Sz), P(invL), P(invDeg), P(w1))
     else:
         w2 = np.zeros(E * npe)
         getattr(REF, f"ref_fdma_d_N{N}")(ctypes.byref(cE), P(el), P(w2), P(Sx), P(Sy), P(Sz), P(invL), P(w1))
