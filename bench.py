@@ -71,8 +71,8 @@ EXPECTED_ITERS = {"kershaw48-n7-mixed": 26, "kershaw32-n7-mixed": 21, "kershaw16
                   "kershaw8-n7-jacobi": 800}
 METRIC = "Poisson DOFs/s (E*N^3 / time-to-tolerance)"
 # DRAM bytes (read + write) of one launch of the dominant kernel, from an ncu capture of the E=32^3 case of the
-# same solve scaled by the element count (every launch streams each element's data once): 237.3 MB at E=32^3
-TRAFFIC = {}
+# same solve scaled by the element count (every launch streams each element's data once): 273.1 MB at E=32^3
+TRAFFIC = {("kershaw48-n7-mixed", "fdm_f32"): 273.1e6 * 3.375}
 FP64_PLAIN = {"mgPrecision=mixed": "mgPrecision=fp64;axPrecision=fp64"}
 
 
