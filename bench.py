@@ -147,6 +147,25 @@ def dist_info():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def replica_step_time(t_step):
+    """The step time of the whole job: the max of the ranks' step times (each rank solves its own replica;
+    the only collective is this scalar reduction, after the timed region)."""
+    import torch
+    import torch.distributed as dist
+
+    if not dist.is_initialized() or dist.get_world_size() == 1:
+        return t_step
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    tt = torch.tensor([t_step], dtype=torch.float64, device=dev)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def job_value(dofs_per_replica, world, t_step):
+    """Whole-job DOF/s: the DOFs of all replicas over the job's step time."""
+    return dofs_per_replica * world / t_step
+
+
 def cpu_sample(nel, N, eps, opts, gpu_iters, budget_s=20.0, probe_iters=2):
     """CPU oracle (all host threads) on the same workload: it is timed on a box
     small enough to set up in seconds (same N, options, element deformation),
@@ -529,12 +548,8 @@ def main():
     failed = [i["status"] for i in infos if i["status"] != 0]
     if failed:
         raise SystemExit(f"solve failed with status {failed[0]}: {G.last_error() if hasattr(G, 'last_error') else ''}")
-    t_step = float(np.mean([i["solve_ms"] for i in infos])) / 1e3
-    if world > 1:
-        tt = torch.tensor([t_step], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_step = tt.item()
-    value = dofs * world / t_step
+    t_step = replica_step_time(float(np.mean([i["solve_ms"] for i in infos])) / 1e3)
+    value = job_value(dofs, world, t_step)
     x_mixed = x.cpu().numpy().copy()
     if args.solve_only:
         if rank == 0:
