@@ -323,6 +323,8 @@ def run_batch(args):
     K = args.batch_problems
     t0 = time.perf_counter()
     els, rhs, dofs = [], [], 0
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
     for k in range(K):
         side, N, eps = int(rng.integers(4, 25)), int(rng.choice([5, 7, 9])), float(rng.uniform(0.3, 1.0))
         VX, EToV, EToB = W.kershaw_box(side, eps=eps)
@@ -331,6 +333,8 @@ def run_batch(args):
         rhs.append(torch.from_numpy(W.box_rhs(N, side, side, side, 1000 + k, el.get("ggeo"))).cuda())
         dofs += side ** 3 * N ** 3
     setup_s = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    footprint = max(0, free0 - torch.cuda.mem_get_info()[0])
     rs = [torch.empty_like(b) for b in rhs]
     xs = [torch.zeros_like(b) for b in rhs]
 
@@ -364,6 +368,7 @@ def run_batch(args):
                       "warmup": args.warmup, "ms_per_step": out["batched"] * 1e3, "higher_is_better": True,
                       "dtype": "f64", "data": "synthetic (seeded Kershaw boxes, U[-1,1] mass-weighted RHS)",
                       "config": {"workload": "batch", "problems": K, "dofs": dofs, "setup_s": setup_s,
+                                 "hbm_bytes": int(footprint),
                                  "iterations_min_max": [int(min(its)), int(max(its))],
                                  "graph_segments_first_two": graphs},
                       "sequential": {"value": dofs / out["sequential"], "ms_per_step": out["sequential"] * 1e3},
@@ -374,8 +379,9 @@ def run_serve(args):
     """configs[4]: Poisson requests with exponential inter-arrival times (mean 2 ms) for `serve_seconds`;
     operators (E log-uniform in [2^9, 2^15], N in {3..9}, eps U[0.3,1.0]) come from a resident pool built
     before the clock starts; each request draws its tolerance from {1e-6, 1e-8, 1e-10} and a seeded RHS.
-    Requests are admitted FIFO onto free resident handles and stepped together one Krylov iteration at a
-    time; latency = completion - arrival.  The same trace is also served one solve at a time."""
+    Requests are admitted FIFO onto free resident handles while the device footprint of the operators in
+    flight stays within an HBM budget, and are stepped together one Krylov iteration at a time; latency =
+    completion - arrival.  The same trace is also served one solve at a time."""
     import torch
     import nekrs_gb300 as G
     from nekrs_gb300 import workloads as W
@@ -389,11 +395,18 @@ def run_serve(args):
         side = max(2, int(round(E ** (1.0 / 3.0))))
         N, eps = int(rng.integers(3, 10)), float(rng.uniform(0.3, 1.0))
         VX, EToV, EToB = W.kershaw_box(side, eps=eps)
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
         el = G.Elliptic(N, VX, EToV, EToB, mg_options(N))
         jw = torch.from_numpy(el.get("ggeo").reshape(side ** 3, 7, -1)[:, 6, :].ravel().copy()).cuda()
-        pool.append({"el": el, "jw": jw, "dofs": side ** 3 * N ** 3, "r": torch.empty_like(jw),
-                     "x": torch.empty_like(jw)})
+        o = {"el": el, "jw": jw, "dofs": side ** 3 * N ** 3, "r": torch.empty_like(jw), "x": torch.empty_like(jw)}
+        torch.cuda.synchronize()
+        o["bytes"] = max(0, free0 - torch.cuda.mem_get_info()[0])  # device footprint of the operator and its buffers
+        pool.append(o)
     setup_s = time.perf_counter() - t0
+    # admission by HBM footprint: the operators whose requests are in flight (being stepped, so their working
+    # set is hot) may hold at most this many bytes together
+    budget = args.serve_hbm_fraction * torch.cuda.mem_get_info()[1]
     # request trace
     gaps = rng.exponential(2e-3, size=int(args.serve_seconds / 2e-3 * 2) + 16)
     arr = np.cumsum(gaps)
@@ -429,10 +442,13 @@ def run_serve(args):
                 nxt += 1
             if concurrent:
                 rest = []
+                inflight = sum(pool[op]["bytes"] for op in busy)
                 for q in queue:
-                    if q["op"] in busy:
+                    need = pool[q["op"]]["bytes"]
+                    if q["op"] in busy or (busy and inflight + need > budget):
                         rest.append(q)
                         continue
+                    inflight += need
                     prepare(q)
                     pool[q["op"]]["el"].solve_begin(pool[q["op"]]["r"], pool[q["op"]]["x"])
                     busy[q["op"]] = q
@@ -460,7 +476,8 @@ def run_serve(args):
                       "n_gpus": 1, "higher_is_better": False, "dtype": "f64",
                       "data": "synthetic (seeded Kershaw boxes and RHS, exponential arrivals)",
                       "config": {"workload": "serve", "arrivals_s": args.serve_seconds, "requests": len(reqs),
-                                 "pool": P, "setup_s": setup_s, "mean_interarrival_ms": 2.0},
+                                 "pool": P, "setup_s": setup_s, "mean_interarrival_ms": 2.0,
+                                 "pool_bytes": int(sum(o["bytes"] for o in pool)), "inflight_budget_bytes": int(budget)},
                       "concurrent": conc, "sequential": seq,
                       "solves_per_s_vs_sequential": conc["solves_per_s"] / seq["solves_per_s"]}))
 
@@ -475,6 +492,8 @@ def main():
     ap.add_argument("--batch-problems", type=int, default=64, help="problems in the batch workload (config: 256)")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window of the serve workload (config: 60)")
     ap.add_argument("--serve-pool", type=int, default=24, help="resident operators of the serve workload")
+    ap.add_argument("--serve-hbm-fraction", type=float, default=0.5,
+                    help="HBM share the operators of in-flight requests may hold together (admission)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-plain", action="store_true")
     ap.add_argument("--solve-only", action="store_true",
