@@ -49,6 +49,7 @@ namespace {
 constexpr int kCT = 1024;              // most threads per CTA (one CTA per SM; a row block of fewer rows uses fewer)
 constexpr long long kSpinLimit = 1LL << 22;
 constexpr int kMinRowsPerCta = 128;
+constexpr long long kOneCtaRows = 4096; // 10 FP32 row vectors = 160 KB of shared memory
 
 struct CoarseState {
   unsigned arrive;
@@ -579,6 +580,9 @@ void coarse_matrix_setup(long long n, const long long *rowPtr, const long long *
   int width = 1;
   for (long long r = 0; r < n; ++r) width = std::max(width, (int)(rowPtr[r + 1] - rowPtr[r]));
   long long grid = std::min<long long>(sms, std::max<long long>(1, (n + kMinRowsPerCta - 1) / kMinRowsPerCta));
+  // a level whose row vectors fit one CTA's shared memory is solved by one CTA: no grid barrier ever
+  // waits, so it is an ordinary launch (no cooperative launch, no ordering against other solvers)
+  if (n <= kOneCtaRows) grid = 1;
   const long long chunk = std::max<long long>(1, (n + grid - 1) / grid);
   grid = std::max<long long>(1, (n + chunk - 1) / chunk);
   std::vector<int> haloOff(grid + 1, 0), haloIds;
@@ -680,10 +684,14 @@ int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *
   int dev = 0;
   NRSG_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) throw Error(NRSG_ERR_CUDA, "coarse solver: device index out of range");
+  const bool cooperative = A.grid > 1;
   CoarseGate &gate = coarse_gate();
-  std::lock_guard<std::mutex> lock(gate.m);
-  if (!gate.ev[dev]) NRSG_CUDA(cudaEventCreateWithFlags(&gate.ev[dev], cudaEventDisableTiming));
-  NRSG_CUDA(cudaStreamWaitEvent(s, gate.ev[dev], 0));
+  std::unique_lock<std::mutex> lock(gate.m, std::defer_lock);
+  if (cooperative) {
+    lock.lock();
+    if (!gate.ev[dev]) NRSG_CUDA(cudaEventCreateWithFlags(&gate.ev[dev], cudaEventDisableTiming));
+    NRSG_CUDA(cudaStreamWaitEvent(s, gate.ev[dev], 0));
+  }
   NRSG_CUDA(cudaMemsetAsync(state, 0, sizeof(CoarseState), s));
   CoarseArgs<T> a;
   a.nrow = A.nrow;
@@ -710,9 +718,14 @@ int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *
   a.maxit = maxit;
   void *args[] = {&a};
   const void *kfn = A.pipelined ? (const void *)coarse_ppcg_kernel<T> : (const void *)coarse_pcg_kernel<T>;
-  NRSG_CUDA(cudaLaunchCooperativeKernel(kfn, dim3(A.grid), dim3(A.threads), args, A.smem, s));
-  count_launch();
-  NRSG_CUDA(cudaEventRecord(gate.ev[dev], s));
+  if (cooperative) {
+    NRSG_CUDA(cudaLaunchCooperativeKernel(kfn, dim3(A.grid), dim3(A.threads), args, A.smem, s));
+    count_launch();
+    NRSG_CUDA(cudaEventRecord(gate.ev[dev], s));
+  } else {
+    NRSG_CUDA(cudaLaunchKernel(kfn, dim3(1), dim3(A.threads), args, A.smem, s));
+    count_launch();
+  }
   return A.grid;
 }
 

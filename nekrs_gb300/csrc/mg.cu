@@ -422,8 +422,8 @@ template <typename T> struct MGImpl : public MGState {
   {
     FieldLevel &L = *v.L;
     if (persistentCoarse) {
-      if (el.capturing) {
-        el.capture_split(); // the coarse solve is launched between the iteration's graph segments
+      if (el.capturing && cA.grid > 1) {
+        el.capture_split(); // a cooperative coarse solve is launched between the iteration's graph segments
         return 0;
       }
       coarse_pcg_persistent<T>(cA, b, x, cx.p, cz2.p, cz3.p, cPartials.p, cState.p, kCoarseGridMax,

@@ -132,7 +132,7 @@ def test_persistent_coarse_many_row_blocks(product_lib, torch_cuda, prec):
     """A coarse level spread over many CTAs (row blocks with halos, grid barriers between them) gives the
     same preconditioner as the host-driven coarse loop on the E-vector level operator."""
     torch = torch_cuda
-    N, n = 3, 16
+    N, n = 3, 20  # 19^3 = 6859 coarse rows: more than one CTA holds
     VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
     base = (f"solver=pfcg;preconditioner=multigrid;smootherType=cheby+asm;mgPrecision={prec};"
             f"residualTol=1e-9+relative;maxIterations=200;pMGSchedule={SCHED[3]}")
