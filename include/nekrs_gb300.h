@@ -78,7 +78,10 @@ long long nrsg_kernel_launches(void);
  * maxIterations, preconditioner (none | jacobi | multigrid), smootherType,
  * pMGSchedule, coarseSolver, mgPrecision (fp64 | fp32 | mixed), axPrecision
  * (fp64 | fp32x2), lambda0,
- * lambda1, poisson, elementMap (trilinear). */
+ * lambda1, poisson, elementMap (trilinear), initialGuess (previous |
+ * projectionAconj | projection: solution projection of
+ * ellipticSolutionProjection.cpp, with residualProjectionVectors (8) and
+ * residualProjectionStart (5)), cudaGraphs. */
 int nrsg_elliptic_create(const nrsg_mesh_desc *mesh, const char *options, nrsg_elliptic **out);
 int nrsg_elliptic_destroy(nrsg_elliptic *el);
 /* Run all later work of `el` on `cuda_stream` (a cudaStream_t; NULL = the

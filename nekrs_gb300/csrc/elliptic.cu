@@ -176,6 +176,13 @@ Elliptic::Elliptic(const nrsg_mesh_desc *m, const char *options)
     mg_setup();
   }
   if (opt.solver == "pgmres" || opt.solver == "pfgmres") gmres_setup();
+  if (opt.projection) {
+    if (opt.projVecs < 1 || opt.projVecs > 64) throw Error(NRSG_ERR_BAD_CONFIG, "residualProjectionVectors must be 1..64");
+    projXX.alloc((size_t)opt.projVecs * n);
+    projBB.alloc((size_t)(opt.projection == 1 ? opt.projVecs : 1) * n);
+    projXbar.alloc(n);
+    projAlpha.alloc(opt.projVecs);
+  }
   NRSG_CUDA(cudaStreamSynchronize(stream));
 }
 
@@ -370,9 +377,87 @@ void Elliptic::issue_iteration_kernels(bool first)
 
 void Elliptic::finish_issue()
 {
+  if (opt.projection) proj_post(st.x);
   launch_axpby<double>(fine.Nlocal, 1.0, x0.p, 1.0, st.x, stream);
   NRSG_CUDA(cudaEventRecord(ev1, stream));
   st.phase = 3;
+}
+
+// ---- solution projection (ellipticSolutionProjection.cpp) ----------------
+// pre (:143-182, :262-272): alpha_k = (x_k, r)_invDegree, xbar = sum alpha_k x_k,
+// r -= A xbar (A-conjugate) or r -= sum alpha_k b_k (classic, b_k = A x_k).
+void Elliptic::proj_pre(double *r)
+{
+  const long long n = fine.Nlocal;
+  ++projStep;
+  if (projStep < opt.projStart || projM <= 0) return;
+  const double *w = fine.d_invDegree64.p;
+  launch_multi_wdot(n, w, projXX.p, projM, r, projAlpha.p, red, 0, stream);
+  launch_accumulate(n, projM, projAlpha.p, projXX.p, projXbar.p, stream);
+  if (opt.projection == 1)
+    launch_accumulate(n, projM, projAlpha.p, projBB.p, z.p, stream);
+  else
+    op(projXbar.p, z.p);
+  launch_axpby<double>(n, -1.0, z.p, 1.0, r, stream);
+}
+
+// updateProjectionSpace (:40-140): A-orthonormalise the newest basis vector
+// by one classical Gram-Schmidt pass; drop it when it is dependent (1e-7).
+void Elliptic::proj_update_space()
+{
+  const long long n = fine.Nlocal;
+  const int m = projM;
+  if (m <= 0) return;
+  const bool classic = opt.projection == 1;
+  const double *w = fine.d_invDegree64.p;
+  const double *b = projBB.p + (size_t)(classic ? m - 1 : 0) * n;
+  launch_multi_wdot(n, w, projXX.p, m, b, projAlpha.p, red, 0, stream);
+  std::vector<double> alpha(m);
+  NRSG_CUDA(cudaMemcpyAsync(alpha.data(), projAlpha.p, sizeof(double) * m, cudaMemcpyDeviceToHost, stream));
+  launch_multi_scaled_sub(n, m, projAlpha.p, projXX.p, stream);
+  if (classic) launch_multi_scaled_sub(n, m, projAlpha.p, projBB.p, stream);
+  NRSG_CUDA(cudaStreamSynchronize(stream));
+  const double normOrig = alpha[m - 1];
+  double sumAlpha = 0;
+  for (int k = 0; k < m - 1; ++k) sumAlpha += alpha[k] * alpha[k];
+  const double normNew = std::sqrt(normOrig - sumAlpha);
+  if (normNew / normOrig > 1e-7) {
+    const double sc = 1.0 / normNew;
+    launch_scale_inplace(n, sc, projXX.p + (size_t)(m - 1) * n, stream);
+    if (classic) launch_scale_inplace(n, sc, projBB.p + (size_t)(m - 1) * n, stream);
+  } else {
+    --projM;
+  }
+}
+
+// post (:183-221, :273-279): the correction x joins the basis; x += xbar
+void Elliptic::proj_post(double *x)
+{
+  const long long n = fine.Nlocal;
+  if (projStep < opt.projStart) return;
+  const size_t bytes = sizeof(double) * n;
+  if (projM == 0) {
+    projM = 1;
+    NRSG_CUDA(cudaMemcpyAsync(projXX.p, x, bytes, cudaMemcpyDeviceToDevice, stream));
+  } else if (projM == opt.projVecs) {
+    projM = 1;
+    launch_axpby<double>(n, 1.0, projXbar.p, 1.0, x, stream);
+    NRSG_CUDA(cudaMemcpyAsync(projXX.p, x, bytes, cudaMemcpyDeviceToDevice, stream));
+  } else {
+    ++projM;
+    NRSG_CUDA(cudaMemcpyAsync(projXX.p + (size_t)(projM - 1) * n, x, bytes, cudaMemcpyDeviceToDevice, stream));
+    launch_axpby<double>(n, 1.0, projXbar.p, 1.0, x, stream);
+  }
+  const int prev = projM;
+  const int bOff = opt.projection == 1 ? projM - 1 : 0;
+  op(projXX.p + (size_t)(projM - 1) * n, projBB.p + (size_t)bOff * n);
+  proj_update_space();
+  if (projM < prev) { // the new vector was dependent: restart the space from x
+    projM = 1;
+    NRSG_CUDA(cudaMemcpyAsync(projXX.p, x, bytes, cudaMemcpyDeviceToDevice, stream));
+    op(projXX.p, projBB.p);
+    proj_update_space();
+  }
 }
 
 void Elliptic::begin(double *r, double *x)
@@ -391,6 +476,7 @@ void Elliptic::begin(double *r, double *x)
   launch_gs_mask<double>(fine.gsPlan, r, true, stream); // mask and gather-scatter
   NRSG_CUDA(cudaMemcpyAsync(x0.p, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
   launch_fill<double>(n, 0.0, x, stream);
+  if (opt.projection) proj_pre(r);
   launch_wdot<double>(n, fine.d_invDegree64.p, r, nullptr, &d_scal.p->rdotr, red, 0, stream);
   NRSG_CUDA(cudaMemcpyAsync(&h_scal->rdotr, &d_scal.p->rdotr, sizeof(double), cudaMemcpyDeviceToHost, stream));
   NRSG_CUDA(cudaEventRecord(evRead, stream));
@@ -719,6 +805,7 @@ int nrsg_elliptic_get(nrsg_elliptic *el, const char *name, void *h_out, long lon
     else if (s == "invDegree") put(L.gm.invDegree);
     else if (s == "D") put(L.Dh);
     else if (s == "history") put(E.history);
+    else if (s == "proj.vectors") put(std::vector<double>{(double)E.projM, (double)E.projStep});
     else if (s == "graph.segments") {
       // segments of the captured steady-state iteration (0: ordinary launches), and how many are coarse solves
       long long nc = 0;

@@ -117,6 +117,17 @@ struct Elliptic {
   void mg_coarse_launch();
   bool mg_graph_capturable();
 
+  // Solution projection for the initial guess (SolutionProjection,
+  // ellipticSolutionProjection.cpp): a basis of up to projVecs previous
+  // solutions, A-orthonormal (A-conjugate form) or with their A-images
+  // (classic form); pre() runs on the device without host reads, post()
+  // reads the Gram-Schmidt coefficients for its dependence test.
+  DevBuf<double> projXX, projBB, projXbar, projAlpha;
+  int projM = 0, projStep = 0;
+  void proj_pre(double *r);
+  void proj_post(double *x);
+  void proj_update_space();
+
   void mg_setup();
   void mg_apply(const double *r, double *z);
   void mg_release();

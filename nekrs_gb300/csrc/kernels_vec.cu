@@ -136,6 +136,48 @@ template <typename T> void launch_gs_mask(const GsPlan &P, T *q, bool mask, cuda
   NRSG_CHECK_LAUNCH();
 }
 template void launch_gs_mask<double>(const GsPlan &, double *, bool, cudaStream_t);
+
+__global__ void accumulate_kernel(long long n, int m, const double *__restrict__ alpha, const double *__restrict__ X,
+                                  double *__restrict__ y)
+{
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double v = alpha[0] * X[i];
+    for (int k = 1; k < m; ++k) v += alpha[k] * X[(size_t)k * n + i];
+    y[i] = v;
+  }
+}
+void launch_accumulate(long long n, int m, const double *alpha, const double *X, double *y, cudaStream_t s)
+{
+  if (n <= 0 || m <= 0) return;
+  accumulate_kernel<<<vec_grid(n), kThreads, 0, s>>>(n, m, alpha, X, y);
+  NRSG_CHECK_LAUNCH();
+}
+__global__ void multi_scaled_sub_kernel(long long n, int m, const double *__restrict__ alpha, double *__restrict__ X)
+{
+  double *xm = X + (size_t)(m - 1) * n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double v = xm[i];
+    for (int k = 0; k < m - 1; ++k) v = -alpha[k] * X[(size_t)k * n + i] + v;
+    xm[i] = v;
+  }
+}
+void launch_multi_scaled_sub(long long n, int m, const double *alpha, double *X, cudaStream_t s)
+{
+  if (n <= 0 || m <= 1) return;
+  multi_scaled_sub_kernel<<<vec_grid(n), kThreads, 0, s>>>(n, m, alpha, X);
+  NRSG_CHECK_LAUNCH();
+}
+__global__ void scale_inplace_kernel(long long n, double a, double *x)
+{
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    x[i] *= a;
+}
+void launch_scale_inplace(long long n, double a, double *x, cudaStream_t s)
+{
+  if (n <= 0) return;
+  scale_inplace_kernel<<<vec_grid(n), kThreads, 0, s>>>(n, a, x);
+  NRSG_CHECK_LAUNCH();
+}
 template void launch_gs_mask<float>(const GsPlan &, float *, bool, cudaStream_t);
 
 template <typename T> __global__ void mask_kernel(long long n, const int *__restrict__ ids, T *__restrict__ q)

@@ -102,6 +102,9 @@ struct Options {
   int coarseMaxIter = 200;
   bool coarsePersistent = true;     // order-1 coarse Jacobi-PCG as one cooperative kernel
   bool graphs = true;               // CUDA graphs of the steady-state PCG iteration (non-legacy streams)
+  int projection = 0;               // initialGuess: 0 none, 1 projection (classic), 2 projectionAconj
+  int projVecs = 8;                 // residualProjectionVectors
+  int projStart = 5;                // residualProjectionStart
   std::string mgPrecision = "fp64"; // fp64 | fp32 | mixed
   std::string axPrecision = "fp64"; // fine-level operator: fp64 | fp32x2 (FP64-accurate FP32-pair arithmetic)
   bool poisson = true;
@@ -157,6 +160,11 @@ struct GsPlan {
   const int *mask = nullptr;
 };
 template <typename T> void launch_gs_mask(const GsPlan &P, T *q, bool mask, cudaStream_t s);
+// solution projection (accumulate.okl, multiScaledAddwOffset.okl): y = sum_k alpha_k X_k (k < m), and
+// X_{m-1} -= sum_{k < m-1} alpha_k X_k; X holds m vectors of n; alpha on the device
+void launch_accumulate(long long n, int m, const double *alpha, const double *X, double *y, cudaStream_t s);
+void launch_multi_scaled_sub(long long n, int m, const double *alpha, double *X, cudaStream_t s);
+void launch_scale_inplace(long long n, double a, double *x, cudaStream_t s);
 template <typename T> void launch_mask(long long n, const int *ids, T *q, cudaStream_t s);
 template <typename T>
 void launch_build_diag(int N, long long E, const T *ggeo, const T *D, T lambda0, T lambda1, bool poisson, T *diag,

@@ -399,6 +399,13 @@ Options parse_options(const char *text)
       else if (key == "coarsemaxiterations") o.coarseMaxIter = std::stoi(v);
       else if (key == "coarsepersistent") o.coarsePersistent = std::stoi(v) != 0;
       else if (key == "cudagraphs") o.graphs = std::stoi(v) != 0;
+      else if (key == "initialguess") {
+        if (v == "projectionaconj" || v == "projection-aconj") o.projection = 2;
+        else if (v == "projection") o.projection = 1;
+        else if (v == "none" || v == "previous") o.projection = 0;
+        else throw Error(NRSG_ERR_BAD_CONFIG, "unknown initialGuess '" + v + "'");
+      } else if (key == "residualprojectionvectors") o.projVecs = std::stoi(v);
+      else if (key == "residualprojectionstart") o.projStart = std::stoi(v);
       else if (key == "mgprecision") o.mgPrecision = v;
       else if (key == "axprecision") {
         if (v != "fp64" && v != "fp32x2") throw Error(NRSG_ERR_BAD_CONFIG, "axPrecision must be fp64 or fp32x2");

@@ -40,6 +40,9 @@ struct Options {
   double lambda0 = 1.0, lambda1 = 0.0;
   bool trilinear = false;                // ELEMENT MAP = TRILINEAR
   unsigned long long seed = 0x5eed;      // Arnoldi start vector seed
+  int projection = 0;                    // INITIAL GUESS: 0 none, 1 PROJECTION (classic), 2 PROJECTION-ACONJ
+  int projVecs = 8;                      // RESIDUAL PROJECTION VECTORS
+  int projStart = 5;                     // RESIDUAL PROJECTION START
 };
 Options parse_options(const std::string &text);
 

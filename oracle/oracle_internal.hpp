@@ -56,6 +56,12 @@ struct Elliptic {
   int pcg(double *r, double *x, double tol, int maxit, double &rnorm);
   int pgmres(double *r, double *x, double tol, int maxit, double &rnorm);
   int solve(double *r, double *x, double &res0, double &res);
+  // solution projection state (ellipticSolutionProjection.cpp)
+  std::vector<double> projXX, projBB, projXbar;
+  int projM = 0, projStep = 0;
+  void proj_pre(double *r);
+  void proj_post(double *x);
+  void proj_update_space();
 };
 
 void mg_setup(Elliptic &el);

@@ -78,6 +78,10 @@ Options parse_options(const std::string &text)
     else if (key == "lambda1") o.lambda1 = std::stod(lv);
     else if (key == "elementmap") o.trilinear = (lv == "trilinear");
     else if (key == "seed") o.seed = std::stoull(lv);
+    else if (key == "initialguess")
+      o.projection = (lv == "projectionaconj" || lv == "projection-aconj") ? 2 : (lv == "projection" ? 1 : 0);
+    else if (key == "residualprojectionvectors") o.projVecs = std::stoi(lv);
+    else if (key == "residualprojectionstart") o.projStart = std::stoi(lv);
   }
   return o;
 }
@@ -407,6 +411,110 @@ int Elliptic::pcg(double *r, double *x, double tol, int maxit, double &rnorm)
 }
 
 // ellipticSolve (ellipticSolve.cpp:32-190), x0 taken from x on input.
+// ---------------------------------------------------------------------------
+// Solution projection (initial guess from previous solutions), restated from
+// SolutionProjection (src/solvers/elliptic/ellipticSolutionProjection.cpp):
+// pre() (:143-182, :262-272) projects the residual onto the stored basis,
+// post() (:183-221, :273-279) adds the new solution to the basis and
+// A-orthonormalises it by one classical Gram-Schmidt pass with the
+// dependence test of updateProjectionSpace (:40-140); accumulate.okl and
+// multiScaledAddwOffset.okl give the summation orders.  Weighted inner
+// products use invDegree.
+// ---------------------------------------------------------------------------
+void Elliptic::proj_update_space()
+{
+  const long long n = fine.Nlocal;
+  const int m = projM;
+  if (m <= 0) return;
+  const bool classic = o.projection == 1;
+  const double *w = fine.invDegree.data();
+  const double *b = &projBB[(size_t)(classic ? m - 1 : 0) * n];
+  std::vector<double> alpha(m);
+  for (int k = 0; k < m; ++k) alpha[k] = wdot<double>(n, w, &projXX[(size_t)k * n], b);
+  const double normOrig = alpha[m - 1];
+  double *xm = &projXX[(size_t)(m - 1) * n];
+  for (long long i = 0; i < n; ++i) {
+    double v = xm[i];
+    for (int k = 0; k < m - 1; ++k) v = -alpha[k] * projXX[(size_t)k * n + i] + v;
+    xm[i] = v;
+  }
+  if (classic) {
+    double *bm = &projBB[(size_t)(m - 1) * n];
+    for (long long i = 0; i < n; ++i) {
+      double v = bm[i];
+      for (int k = 0; k < m - 1; ++k) v = -alpha[k] * projBB[(size_t)k * n + i] + v;
+      bm[i] = v;
+    }
+  }
+  double sumAlpha = 0;
+  for (int k = 0; k < m - 1; ++k) sumAlpha += alpha[k] * alpha[k];
+  const double normNew = std::sqrt(normOrig - sumAlpha);
+  if (normNew / normOrig > 1e-7) {
+    const double sc = 1.0 / normNew;
+    for (long long i = 0; i < n; ++i) xm[i] *= sc;
+    if (classic)
+      for (long long i = 0; i < n; ++i) projBB[(size_t)(m - 1) * n + i] *= sc;
+  } else {
+    --projM; // linearly dependent: discard
+  }
+}
+
+void Elliptic::proj_pre(double *r)
+{
+  const long long n = fine.Nlocal;
+  ++projStep;
+  if (projStep < o.projStart || projM <= 0) return;
+  const double *w = fine.invDegree.data();
+  const int m = projM;
+  std::vector<double> alpha(m);
+  for (int k = 0; k < m; ++k) alpha[k] = wdot<double>(n, w, &projXX[(size_t)k * n], r);
+  for (long long i = 0; i < n; ++i) {
+    double v = alpha[0] * projXX[i];
+    for (int k = 1; k < m; ++k) v += alpha[k] * projXX[(size_t)k * n + i];
+    projXbar[i] = v;
+  }
+  std::vector<double> t(n);
+  if (o.projection == 1) {
+    for (long long i = 0; i < n; ++i) {
+      double v = alpha[0] * projBB[i];
+      for (int k = 1; k < m; ++k) v += alpha[k] * projBB[(size_t)k * n + i];
+      t[i] = v;
+    }
+  } else {
+    op(projXbar.data(), t.data());
+  }
+  for (long long i = 0; i < n; ++i) r[i] = -1.0 * t[i] + 1.0 * r[i];
+}
+
+void Elliptic::proj_post(double *x)
+{
+  const long long n = fine.Nlocal;
+  if (projStep < o.projStart) return;
+  const int maxv = o.projVecs;
+  if (projM == 0) {
+    projM = 1;
+    std::copy(x, x + n, projXX.begin());
+  } else if (projM == maxv) {
+    projM = 1;
+    for (long long i = 0; i < n; ++i) x[i] = 1.0 * projXbar[i] + 1.0 * x[i];
+    std::copy(x, x + n, projXX.begin());
+  } else {
+    ++projM;
+    std::copy(x, x + n, projXX.begin() + (size_t)(projM - 1) * n);
+    for (long long i = 0; i < n; ++i) x[i] = 1.0 * projXbar[i] + 1.0 * x[i];
+  }
+  const int prev = projM;
+  const int bOff = o.projection == 1 ? projM - 1 : 0;
+  op(&projXX[(size_t)(projM - 1) * n], &projBB[(size_t)bOff * n]);
+  proj_update_space();
+  if (projM < prev) { // the new vector was dependent: restart the space from x
+    projM = 1;
+    std::copy(x, x + n, projXX.begin());
+    op(projXX.data(), projBB.data());
+    proj_update_space();
+  }
+}
+
 int Elliptic::solve(double *r, double *x, double &res0, double &res)
 {
   const long long n = fine.Nlocal;
@@ -416,6 +524,14 @@ int Elliptic::solve(double *r, double *x, double &res0, double &res)
   apply_mask(fine, r);
   gs_add(fine, r);
   for (long long i = 0; i < n; ++i) x[i] = 0;
+  if (o.projection) {
+    if (projXX.empty()) {
+      projXX.assign((size_t)o.projVecs * n, 0.0);
+      projBB.assign((size_t)(o.projection == 1 ? o.projVecs : 1) * n, 0.0);
+      projXbar.assign(n, 0.0);
+    }
+    proj_pre(r);
+  }
   res0 = norm(r);
   double tol = o.tol;
   if (o.relative) tol *= res0;
@@ -427,6 +543,7 @@ int Elliptic::solve(double *r, double *x, double &res0, double &res)
     iters = pcg(r, x, tol, o.maxIter, res);
   else
     iters = pgmres(r, x, tol, o.maxIter, res);
+  if (o.projection) proj_post(x);
   for (long long i = 0; i < n; ++i) x[i] += x0[i];
   if (std::isnan(res)) status = 3;
   else if (iters >= o.maxIter && res > tol) status = 1;

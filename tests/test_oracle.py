@@ -108,3 +108,33 @@ def test_oracle_krylov_converges(oracle_mod, solver):
     r = b - el.operator(x)
     w = el.get("invDegree")
     assert np.sqrt((w * r * r).sum() / el.volume) <= 2e-8 * info["res0"]
+
+
+@pytest.mark.parametrize("form", ["projectionAconj", "projection"])
+def test_oracle_solution_projection(oracle_mod, form):
+    """Solution projection (ellipticSolutionProjection.cpp): right-hand sides drawn from a
+    two-dimensional space are solved from the projected initial guess in a few iterations once
+    the basis holds two solutions; every solve still meets the absolute tolerance."""
+    VX, EToV, EToB = O.box_mesh(3, 3, 3, 0.3)
+    N = 4
+    base = "preconditioner=jacobi;solver=pcg;residualTol=1e-9;maxIterations=2000"
+    plain = O.Elliptic(N, VX, EToV, EToB, base)
+    proj = O.Elliptic(N, VX, EToV, EToB, base + f";initialGuess={form};residualProjectionVectors=4;"
+                      "residualProjectionStart=2")
+    b1 = O.box_rhs(N, 3, 3, 3, 7, plain.get("ggeo"))
+    b2 = O.box_rhs(N, 3, 3, 3, 8, plain.get("ggeo"))
+    w = plain.get("invDegree")
+    its_plain, its_proj = [], []
+    for k in range(6):
+        rhs = np.cos(0.4 * k) * b1 + np.sin(0.4 * k) * b2
+        x0, i0 = plain.solve(rhs)
+        x1, i1 = proj.solve(rhs)
+        assert i0["status"] == 0 and i1["status"] == 0
+        its_plain.append(i0["iterations"])
+        its_proj.append(i1["iterations"])
+        b = plain.gs(plain.mask(rhs))
+        r = b - plain.operator(x1)
+        assert np.sqrt((w * r * r).sum() / plain.volume) <= 2e-9
+        assert np.linalg.norm(x1 - x0) <= 1e-6 * np.linalg.norm(x0)
+    assert its_proj[0] == its_plain[0]  # projection starts at the second solve
+    assert max(its_proj[3:]) < min(its_plain) // 3, (its_plain, its_proj)
