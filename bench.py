@@ -494,12 +494,16 @@ def main():
     ap.add_argument("--serve-pool", type=int, default=24, help="resident operators of the serve workload")
     ap.add_argument("--serve-hbm-fraction", type=float, default=0.5,
                     help="HBM share the operators of in-flight requests may hold together (admission)")
+    ap.add_argument("--mesh", default=None,
+                    help="read the mesh from a Nek5000 .re2 box file (e.g. the reference's kershaw.re2); the "
+                         "workload's order, eps and options apply, the right-hand side is the BPS5 one")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-plain", action="store_true")
     ap.add_argument("--solve-only", action="store_true",
                     help="time the device-resident solves only (no e2e, FP64 comparison or kernel rooflines)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    args.workload_name = args.workload
     if args.workload in ("batch", "serve"):
         import torch
 
@@ -524,13 +528,19 @@ def main():
     import nekrs_gb300 as G
     from nekrs_gb300 import workloads as W
 
-    E = nel ** 3
+    if args.mesh:
+        from nekrs_gb300 import re2 as R
+
+        VX, EToV, EToB = R.kershaw_mesh_from_re2(args.mesh, eps)
+        args.workload_name = f"{args.workload}@{os.path.basename(args.mesh)}"
+    else:
+        VX, EToV, EToB = W.kershaw_box(nel, eps=eps)
+    E = VX.shape[0]
     dofs = E * N ** 3
-    VX, EToV, EToB = W.kershaw_box(nel, eps=eps)
     t0 = time.perf_counter()
     el = G.Elliptic(N, VX, EToV, EToB, opts)
     setup_s = time.perf_counter() - t0
-    if args.workload.endswith("bps5"):
+    if args.workload.endswith("bps5") or args.mesh:
         # kershaw.udf: P0 = 3 pi^2 sin(pi x) sin(pi y) sin(pi z) at every node of the mesh on [-0.5, 0.5]^3
         xs, ys, zs = (el.get(c) - 0.5 for c in ("x", "y", "z"))
         rhs = 3 * np.pi ** 2 * np.sin(np.pi * xs) * np.sin(np.pi * ys) * np.sin(np.pi * zs)
@@ -574,7 +584,7 @@ def main():
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
                               "warmup": args.warmup, "ms_per_step": t_step * 1e3, "solve_only": True,
-                              "config": {"workload": args.workload, "iterations": infos[-1]["iterations"],
+                              "config": {"workload": args.workload_name, "iterations": infos[-1]["iterations"],
                                          "coarse_iterations_last_vcycle": el.get("mg.coarseIters").tolist()
                                          if "multigrid" in opts else None},
                               "gpu_launches": int(launches), "clocks": clk}))
@@ -663,7 +673,7 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Kershaw box, U[-1,1] mass-weighted RHS)",
-            "config": {"workload": args.workload, "description": desc, "elements": E, "N": N,
+            "config": {"workload": args.workload_name, "description": desc, "elements": E, "N": N,
                        "dofs_per_solve": dofs, "iterations": infos[-1]["iterations"],
                        "time_to_tolerance_s": t_step, "setup_s": setup_s,
                        "l2": "inputs larger than L2 (E-vectors 8*E*Np B, geometric factors 56*E*Np B)",

@@ -178,6 +178,55 @@ int nrsg_host_assemble_operator(int N, long long E, const long long *h_EToV, con
                                 double lambda0, double lambda1, int poisson, long long *nrow, long long *nnz,
                                 long long *h_rowPtr, long long *h_cols, double *h_vals, long long *h_rowOfNode);
 
+/* ---- mesh ingestion: Nek5000 binary .re2 files (host only) --------------
+ * Replaces the mesh read nekRS delegates to Nek5000 (src/io/re2Reader.cpp:4-41
+ * for the header; Nek5000 core/reader_re2.f: read_re2_hdr :543-620,
+ * readp_re2_mesh :68-157, readp_re2_curve :159-286, readp_re2_bc :288-428)
+ * and the vertex numbering parCon computes from the coordinates
+ * (core/map2.f:471-540 calling parrsb_conn_mesh).  Versions v002, v003 and
+ * v004 (8-byte words), either byte order, 3-D meshes. */
+typedef struct {
+  int version;       /* 2, 3 or 4 */
+  int ndim;          /* 3 */
+  long long nelgt;   /* elements */
+  long long nelgv;   /* fluid elements (the first nelgv) */
+  long long ncurve;  /* curved-side records */
+  int nbcFields;     /* boundary sections in the file */
+  int byteSwapped;   /* written with the other byte order */
+} nrsg_re2_header;
+
+int nrsg_re2_read_header(const char *path, nrsg_re2_header *hdr);
+/* Element corners [nelgt][8][3] in hypercube order v = i + 2j + 4k (the
+ * file's pre-processor corners 3<->4 and 7<->8 swapped, as meshNekReader.cpp:30
+ * maps them) and group ids [nelgt]; either output may be NULL. */
+int nrsg_re2_read_elements(const char *path, double *h_VX, int *h_group);
+/* Curved sides, ncurve records: element (0-based), pre-processor face
+ * (0-based), 5 parameters, type character; any output may be NULL. */
+int nrsg_re2_read_curves(const char *path, long long *h_elem, int *h_face, double *h_params, char *h_type);
+/* Boundary section `field` (0-based): per element and pre-processor face the
+ * 3-character code, NUL-terminated in 4 bytes (h_cbc [nelgt][6][4]; faces
+ * without a record read "E  "), and its 5 parameters (h_bc [nelgt][6][5]). */
+int nrsg_re2_read_bc(const char *path, int field, char *h_cbc, double *h_bc);
+/* Boundary ids in nekRS face order (t-, s-, r+, s+, r-, t+), the mapping of
+ * meshNekReader.cpp:66-80: a face whose code equals codes[k] (trailing blanks
+ * optional) gets ids[k], every other face 0.  Pass the result as h_EToB with
+ * ids that are boundary types (NRSG_BC_*), as a .usr / boundaryTypeMap pair
+ * would assign them. */
+int nrsg_re2_boundary_ids(long long E, const char *h_cbc, int ncodes, const char *const *codes, const int *ids,
+                          int *h_EToB);
+/* Global vertex ids from corner coordinates (parrsb_conn_mesh, parRSB
+ * con.c:221-321: findMinNeighborDistance :85-117, find_unique_vertices
+ * con-unique-vertices.c:385-446, matchPeriodicFaces con-periodic.c:266-281),
+ * for one process: corners closer than tol x their nearest-edge length in
+ * every coordinate share an id; ids are numbered in the order of the sorted
+ * segments (x, then y, then z); faces coded "P  " are matched with the
+ * element and face their parameters name (h_cbc / h_bc as read by
+ * nrsg_re2_read_bc, or NULL for none).  h_VX hypercube order; h_EToV [E][8]
+ * receives 1-based ids, *nvertices their count.  tol = 0.2 is Nek5000's
+ * default (core/reader_rea.f:50). */
+int nrsg_mesh_connect(long long E, const double *h_VX, double tol, const char *h_cbc, const double *h_bc,
+                      long long *h_EToV, long long *nvertices);
+
 /* ---- kernel-level entry points (one launch each, on `stream`) ---------- */
 
 /* ellipticPartialAxCoeffHex3D (kernels/elliptic/ellipticPartialAxCoeffHex3D.okl),

@@ -295,11 +295,20 @@ template <typename T> void apply_mask(const Level &L, T *q)
   for (int m : L.maskIds) q[m] = 0;
 }
 
+// Deterministic: fixed blocks summed in parallel, block sums added in order,
+// so the result does not depend on the thread count or schedule.
 template <typename T> T wdot(long long n, const T *w, const T *a, const T *b)
 {
+  const long long B = 4096, nb = (n + B - 1) / B;
+  std::vector<double> part(nb);
+#pragma omp parallel for schedule(static)
+  for (long long k = 0; k < nb; ++k) {
+    double s = 0;
+    for (long long i = k * B; i < std::min(n, (k + 1) * B); ++i) s += (double)w[i] * (double)a[i] * (double)b[i];
+    part[k] = s;
+  }
   double s = 0;
-#pragma omp parallel for reduction(+ : s)
-  for (long long i = 0; i < n; ++i) s += (double)w[i] * (double)a[i] * (double)b[i];
+  for (long long k = 0; k < nb; ++k) s += part[k];
   return (T)s;
 }
 
