@@ -274,6 +274,10 @@ def kernel_rooflines(G, el, N, E):
     t = time_kernel(lambda: G.ax_stored_f32(N, E, g32, D32, 1.0, 0.0, True, q32, a32, cs), stream)
     out["ax_stored_f32"] = {"launch_ms": t * 1e3, "achieved": 32.0 * n / t / 1e9, "unit": "GB/s",
                             "algorithmic_bytes": 32.0 * n}
+    if N == 7:
+        t = time_kernel(lambda: G.ax_pipe_f32(N, E, g32, D32, 1.0, 0.0, True, q32, a32, cs), stream)
+        out["ax_pipe_f32"] = {"launch_ms": t * 1e3, "achieved": 32.0 * n / t / 1e9, "unit": "GB/s",
+                              "algorithmic_bytes": 32.0 * n}
     for v in out.values():
         v["frac_of_hbm"] = v["achieved"] / peak
     return out, peak, src

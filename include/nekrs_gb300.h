@@ -235,6 +235,14 @@ int nrsg_ax_stored_f64(int N, long long E, const double *d_ggeo, const double *d
                        double lambda1, int poisson, const double *d_q, double *d_Aq, void *stream);
 int nrsg_ax_stored_f32(int N, long long E, const float *d_ggeo, const float *d_D, float lambda0,
                        float lambda1, int poisson, const float *d_q, float *d_Aq, void *stream);
+/* The same FP32 operator for N = 7 through a bulk-copy pipeline: persistent
+ * CTAs stream each chunk of 3 elements' geometric factors and q into shared
+ * memory (cp.async.bulk, completion on an mbarrier) one stage ahead of the
+ * compute; results are bit-identical to nrsg_ax_stored_f32.  d_ggeo and d_q
+ * must be 16-byte aligned; other N or unaligned pointers return
+ * NRSG_ERR_INVALID. */
+int nrsg_ax_pipe_f32(int N, long long E, const float *d_ggeo, const float *d_D, float lambda0, float lambda1,
+                     int poisson, const float *d_q, float *d_Aq, void *stream);
 /* ellipticPartialAxTrilinearHex3D: geometry recomputed from d_VX [E][8][3]. */
 int nrsg_ax_trilinear_f64(int N, long long E, const double *d_VX, const double *d_gllz, const double *d_gllw,
                           const double *d_D, double lambda0, double lambda1, int poisson, const double *d_q,

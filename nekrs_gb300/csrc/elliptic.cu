@@ -540,9 +540,10 @@ bool Elliptic::advance(bool block, nrsg_solve_info *info)
       float ms = 0;
       NRSG_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
       if (status == NRSG_OK && st.it >= opt.maxIter && st.res > st.tol) status = NRSG_ERR_MAXIT;
-      if (mg_error()) {
+      if (const int me = mg_error()) {
         status = NRSG_ERR_CUDA;
-        set_last_error("coarse-level solver: grid barrier wait exceeded its limit");
+        set_last_error(me == 2 ? "pipelined axhelm: a bulk copy did not complete within its wait limit"
+                               : "coarse-level solver: grid barrier wait exceeded its limit");
       }
       lastIters = st.it;
       st.info.iterations = st.it;
@@ -921,6 +922,13 @@ int nrsg_ax_stored_f32(int N, long long E, const float *ggeo, const float *D, fl
                        const float *q, float *Aq, void *s)
 {
   NRSG_TRY(nrsg::launch_ax_stored<float>(N, E, ggeo, D, l0, l1, poisson != 0, q, Aq, (cudaStream_t)s))
+}
+
+int nrsg_ax_pipe_f32(int N, long long E, const float *ggeo, const float *D, float l0, float l1, int poisson,
+                     const float *q, float *Aq, void *s)
+{
+  if (N != 7 || E < 1 || !ggeo || !D || !q || !Aq || (((uintptr_t)ggeo | (uintptr_t)q) & 15)) return NRSG_ERR_INVALID;
+  NRSG_TRY(nrsg::launch_ax_pipe(N, E, ggeo, D, l0, l1, poisson != 0, q, Aq, (cudaStream_t)s))
 }
 int nrsg_ax_trilinear_f64(int N, long long E, const double *VX, const double *z, const double *w, const double *D,
                           double l0, double l1, int poisson, const double *q, double *Aq, void *s)

@@ -116,6 +116,217 @@ __global__ void __launch_bounds__(NQ *NQ *AxShape<NQ>::epb, (sizeof(T) == 4 && N
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 order-7 axhelm through a bulk-copy pipeline (sm_90+ cp.async.bulk into
+// shared memory, completion counted on an mbarrier).  Persistent CTAs walk
+// chunks of kPipeEps consecutive elements; while the chunk in one stage is
+// computed, the next chunk's geometric factors (one contiguous slab of 6 or 7
+// x 2 KB per element) and q (one slab for the chunk) stream into the other
+// stage, so every SM keeps HBM requests in flight through the compute phases
+// that leave the plain kernel's loads bursty.  The arithmetic is that of
+// ax_stored_kernel<float, 8, POISSON> operation for operation (bit-identical
+// results); only where the operands come from differs.
+// ---------------------------------------------------------------------------
+constexpr int kPipeEps = 3;    // elements per stage (3 x 64 threads)
+constexpr int kPipeStages = 2;
+constexpr unsigned kPipeSpinLimit = 1u << 22;
+__device__ unsigned g_ax_pipe_err = 0;
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity)
+{
+  unsigned ok;
+  asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+               "selp.u32 %0, 1, 0, p;\n\t}"
+               : "=r"(ok)
+               : "r"(smem_addr(bar)), "r"(parity)
+               : "memory");
+  return ok != 0;
+}
+// global -> shared bulk copy (16-byte aligned addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar)
+{
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+template <bool POISSON> constexpr int pipe_factors() { return POISSON ? 6 : 7; }
+template <bool POISSON> constexpr size_t pipe_smem_bytes()
+{
+  return (size_t)kPipeStages * kPipeEps * (pipe_factors<POISSON>() + 1) * 512 * sizeof(float);
+}
+
+template <bool POISSON>
+__global__ void __launch_bounds__(64 * kPipeEps, 2)
+    ax_pipe_kernel(long long E, const float *__restrict__ ggeo, const float *__restrict__ D, float lambda0,
+                   float lambda1, const float *__restrict__ q, float *__restrict__ Aq)
+{
+  constexpr int NQ = 8, NP = 512, NG = pipe_factors<POISSON>();
+  extern __shared__ __align__(128) unsigned char pipe_smem[];
+  float *sg = reinterpret_cast<float *>(pipe_smem);           // [stage][element][factor][NP]
+  float *sq = sg + (size_t)kPipeStages * kPipeEps * NG * NP;  // [stage][element][NP]
+  __shared__ float s_D[NQ][NQ + 1];
+  __shared__ float s_q[kPipeEps][NQ][NQ];
+  __shared__ float s_Gr[kPipeEps][NQ][NQ];
+  __shared__ float s_Gs[kPipeEps][NQ][NQ];
+  __shared__ __align__(8) unsigned long long bar[kPipeStages];
+
+  const int tid = threadIdx.x;
+  const int el = tid / 64, t = tid % 64, i = t % NQ, j = t / NQ;
+  const long long nchunk = (E + kPipeEps - 1) / kPipeEps;
+  if (tid < 64) s_D[j][i] = D[j * NQ + i];
+  if (tid == 0) {
+    for (int st = 0; st < kPipeStages; ++st) mbar_init(&bar[st], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  auto issue = [&](long long c, int st) {
+    const long long e0 = c * kPipeEps;
+    const int ne = (int)(E - e0 < kPipeEps ? E - e0 : kPipeEps);
+    mbar_arrive_expect_tx(&bar[st], (unsigned)(ne * (NG + 1) * NP * sizeof(float)));
+    for (int x = 0; x < ne; ++x)
+      bulk_copy_g2s(sg + ((size_t)st * kPipeEps + x) * NG * NP, ggeo + (e0 + x) * 7 * NP, NG * NP * sizeof(float),
+                    &bar[st]);
+    bulk_copy_g2s(sq + (size_t)st * kPipeEps * NP, q + e0 * NP, ne * NP * sizeof(float), &bar[st]);
+  };
+  if (tid == 0)
+    for (int st = 0; st < kPipeStages; ++st) {
+      const long long c = blockIdx.x + (long long)st * gridDim.x;
+      if (c < nchunk) issue(c, st);
+    }
+
+  int it = 0;
+  for (long long c = blockIdx.x; c < nchunk; c += gridDim.x, ++it) {
+    const int st = it % kPipeStages;
+    const unsigned parity = (it / kPipeStages) & 1;
+    unsigned spins = 0;
+    bool late = false;
+    while (!mbar_try_wait(&bar[st], parity))
+      if (++spins > kPipeSpinLimit) {
+        late = true;
+        break;
+      }
+    if (__syncthreads_or(late)) {
+      // a copy did not land within the limit: flag it, give the other stage's
+      // copies a bounded wait, and leave (the host reads the flag after the solve)
+      if (tid == 0) {
+        atomicExch(&g_ax_pipe_err, 1u);
+        for (int k = 1; k < kPipeStages; ++k) {
+          const long long c2 = c + (long long)k * gridDim.x;
+          if (c2 >= nchunk) break;
+          const int s2 = (it + k) % kPipeStages;
+          unsigned n2 = 0;
+          while (!mbar_try_wait(&bar[s2], ((it + k) / kPipeStages) & 1) && ++n2 < kPipeSpinLimit) {
+          }
+        }
+      }
+      return;
+    }
+    const long long e = c * kPipeEps + el;
+    const bool active = e < E;
+    const float *gs = sg + ((size_t)st * kPipeEps + el) * NG * NP + t;
+    const float *qs = sq + ((size_t)st * kPipeEps + el) * NP;
+    float r_q[NQ], r_Aq[NQ];
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      r_q[k] = active ? qs[k * NQ * NQ + t] : 0.f;
+      r_Aq[k] = 0;
+    }
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      const int o = k * NQ * NQ;
+      float G00 = 0, G01 = 0, G11 = 0, G12 = 0, G02 = 0, G22 = 0, GWJ = 0;
+      if (active) {
+        G00 = gs[0 * NP + o];
+        G01 = gs[1 * NP + o];
+        G11 = gs[2 * NP + o];
+        G12 = gs[3 * NP + o];
+        G02 = gs[4 * NP + o];
+        G22 = gs[5 * NP + o];
+        if (!POISSON) GWJ = gs[6 * NP + o];
+      }
+      s_q[el][j][i] = r_q[k];
+      float qt = 0;
+#pragma unroll
+      for (int m = 0; m < NQ; ++m) qt += s_D[k][m] * r_q[m];
+      __syncthreads();
+      float qr = 0, qsd = 0;
+#pragma unroll
+      for (int m = 0; m < NQ; ++m) {
+        qr += s_D[i][m] * s_q[el][j][m];
+        qsd += s_D[j][m] * s_q[el][m][i];
+      }
+      s_Gr[el][j][i] = lambda0 * (G00 * qr + G01 * qsd + G02 * qt);
+      s_Gs[el][j][i] = lambda0 * (G01 * qr + G11 * qsd + G12 * qt);
+      const float Gt = lambda0 * (G02 * qr + G12 * qsd + G22 * qt);
+      float auk = POISSON ? 0.f : GWJ * lambda1 * r_q[k];
+      __syncthreads();
+#pragma unroll
+      for (int m = 0; m < NQ; ++m) {
+        auk += s_D[m][j] * s_Gs[el][m][i];
+        r_Aq[m] += s_D[k][m] * Gt;
+        auk += s_D[m][i] * s_Gr[el][j][m];
+      }
+      r_Aq[k] += auk;
+      __syncthreads();
+    }
+    if (active) {
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) Aq[e * NP + k * NQ * NQ + t] = r_Aq[k];
+    }
+    // every thread has read this stage (the last __syncthreads of the plane
+    // loop): refill it with the chunk kPipeStages grid-strides ahead
+    if (tid == 0) {
+      const long long cn = c + (long long)kPipeStages * gridDim.x;
+      if (cn < nchunk) issue(cn, st);
+    }
+  }
+}
+
+bool launch_ax_pipe(int N, long long E, const float *ggeo, const float *D, float lambda0, float lambda1, bool poisson,
+                    const float *q, float *Aq, cudaStream_t s)
+{
+  if (N != 7 || E <= 0) return false;
+  if (((uintptr_t)ggeo | (uintptr_t)q) & 15) return false; // bulk copies need 16-byte aligned sources
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    NRSG_CUDA(cudaGetDevice(&dev));
+    NRSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  }
+  const long long nchunk = (E + kPipeEps - 1) / kPipeEps;
+  const unsigned grid = (unsigned)std::min<long long>(nchunk, 2LL * sms);
+  if (poisson) {
+    raise_dynamic_smem((const void *)ax_pipe_kernel<true>, pipe_smem_bytes<true>());
+    ax_pipe_kernel<true><<<grid, 64 * kPipeEps, pipe_smem_bytes<true>(), s>>>(E, ggeo, D, lambda0, lambda1, q, Aq);
+  } else {
+    raise_dynamic_smem((const void *)ax_pipe_kernel<false>, pipe_smem_bytes<false>());
+    ax_pipe_kernel<false><<<grid, 64 * kPipeEps, pipe_smem_bytes<false>(), s>>>(E, ggeo, D, lambda0, lambda1, q, Aq);
+  }
+  NRSG_CHECK_LAUNCH();
+  return true;
+}
+
+unsigned ax_pipe_error(cudaStream_t s)
+{
+  unsigned h = 0, zero = 0;
+  NRSG_CUDA(cudaMemcpyFromSymbolAsync(&h, g_ax_pipe_err, sizeof(h), 0, cudaMemcpyDeviceToHost, s));
+  NRSG_CUDA(cudaStreamSynchronize(s));
+  if (h) NRSG_CUDA(cudaMemcpyToSymbolAsync(g_ax_pipe_err, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, s));
+  return h;
+}
+
 // Geometric factors of a trilinear hexahedron at GLL node (r,s,t) from its
 // 8 vertices (CCW order 0:(-,-,-) 1:(+,-,-) 2:(+,+,-) 3:(-,+,-), 4-7 at t=+1).
 template <typename T>

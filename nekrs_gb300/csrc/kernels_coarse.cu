@@ -546,7 +546,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_ppcg_kern
 // The dynamic shared-memory limit is an attribute of the kernel function, not
 // of a launch, and every solver in the process shares the function: raise it
 // to the largest size any solver on the device has needed, never lower it.
-static void raise_dynamic_smem(const void *kfn, size_t bytes)
+void raise_dynamic_smem(const void *kfn, size_t bytes)
 {
   static std::mutex m;
   static std::vector<std::pair<std::pair<int, const void *>, size_t>> set;

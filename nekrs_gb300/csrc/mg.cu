@@ -308,7 +308,10 @@ template <typename T> struct MGImpl : public MGState {
   void level_op(MGLevelDev<T> &v, const T *q, T *Aq)
   {
     FieldLevel &L = *v.L;
-    launch_ax_stored<T>(L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, q, Aq, s);
+    bool done = false;
+    if constexpr (std::is_same<T, float>::value)
+      done = el.opt.axPipeline && launch_ax_pipe(L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, q, Aq, s);
+    if (!done) launch_ax_stored<T>(L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, q, Aq, s);
     launch_gs_mask<T>(L.gsPlan, Aq, true, s);
   }
 
@@ -547,6 +550,7 @@ template <typename T> struct MGImpl : public MGState {
 
   int error() override
   {
+    if (std::is_same<T, float>::value && el.opt.axPipeline && ax_pipe_error(s)) return 2;
     if (!persistentCoarse) return 0;
     std::vector<unsigned char> h(coarse_state_bytes());
     NRSG_CUDA(cudaMemcpyAsync(h.data(), cState.p, h.size(), cudaMemcpyDeviceToHost, s));

@@ -102,6 +102,7 @@ struct Options {
   int coarseMaxIter = 200;
   bool coarsePersistent = true;     // order-1 coarse Jacobi-PCG as one cooperative kernel
   bool graphs = true;               // CUDA graphs of the steady-state PCG iteration (non-legacy streams)
+  bool axPipeline = true;           // FP32 order-7 levels: bulk-copy pipelined axhelm
   int projection = 0;               // initialGuess: 0 none, 1 projection (classic), 2 projectionAconj
   int projVecs = 8;                 // residualProjectionVectors
   int projStart = 5;                // residualProjectionStart
@@ -165,6 +166,13 @@ template <typename T> void launch_gs_mask(const GsPlan &P, T *q, bool mask, cuda
 void launch_accumulate(long long n, int m, const double *alpha, const double *X, double *y, cudaStream_t s);
 void launch_multi_scaled_sub(long long n, int m, const double *alpha, double *X, cudaStream_t s);
 void launch_scale_inplace(long long n, double a, double *x, cudaStream_t s);
+// Raise (never lower) a kernel function's dynamic shared-memory limit on the current device.
+void raise_dynamic_smem(const void *kfn, size_t bytes);
+// FP32 order-7 Poisson axhelm through the bulk-copy pipeline (false: not applicable, caller
+// launches the plain kernel); its wait-limit flag is read and cleared by ax_pipe_error.
+bool launch_ax_pipe(int N, long long E, const float *ggeo, const float *D, float lambda0, float lambda1, bool poisson,
+                    const float *q, float *Aq, cudaStream_t s);
+unsigned ax_pipe_error(cudaStream_t s);
 template <typename T> void launch_mask(long long n, const int *ids, T *q, cudaStream_t s);
 template <typename T>
 void launch_build_diag(int N, long long E, const T *ggeo, const T *D, T lambda0, T lambda1, bool poisson, T *diag,

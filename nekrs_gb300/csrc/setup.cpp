@@ -399,6 +399,7 @@ Options parse_options(const char *text)
       else if (key == "coarsemaxiterations") o.coarseMaxIter = std::stoi(v);
       else if (key == "coarsepersistent") o.coarsePersistent = std::stoi(v) != 0;
       else if (key == "cudagraphs") o.graphs = std::stoi(v) != 0;
+      else if (key == "axpipeline") o.axPipeline = std::stoi(v) != 0;
       else if (key == "initialguess") {
         if (v == "projectionaconj" || v == "projection-aconj") o.projection = 2;
         else if (v == "projection") o.projection = 1;

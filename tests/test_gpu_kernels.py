@@ -162,3 +162,53 @@ def test_ax_fp32x2_is_fp64_accurate(product_lib, oracle_mod, torch_cuda, N, pois
     G.ax_fp32x2(N, el.E, gp, Dp, l0, l1, poisson, dev(torch, q), out)
     torch.cuda.synchronize()
     assert relerr(out.cpu().numpy(), ref) < 2e-13
+
+
+@pytest.mark.parametrize("E", [1, 2, 3, 4, 7, 913, 5000])
+@pytest.mark.parametrize("poisson", [True, False])
+def test_ax_pipe_f32_bit_identical(product_lib, torch_cuda, E, poisson):
+    """The bulk-copy pipelined FP32 order-7 axhelm equals the plain kernel bit for bit: partial last chunks
+    (E not a multiple of 3), one chunk per CTA, and several chunks per CTA (both stage parities)."""
+    torch = torch_cuda
+    N, Np = 7, 512
+    gen = torch.Generator(device="cuda").manual_seed(E + 17 * poisson)
+    g = torch.rand(E * 7 * Np, device="cuda", generator=gen, dtype=torch.float32) + 0.5
+    D = torch.from_numpy(O.dmatrix(N).astype(np.float32).ravel()).cuda()
+    q = torch.rand(E * Np, device="cuda", generator=gen, dtype=torch.float32) - 0.5
+    a_ref = torch.full_like(q, float("nan"))
+    a_pipe = torch.full_like(q, float("nan"))
+    cs = torch.cuda.current_stream().cuda_stream
+    G.ax_stored_f32(N, E, g, D, 1.3, 0.7, poisson, q, a_ref, cs)
+    G.ax_pipe_f32(N, E, g, D, 1.3, 0.7, poisson, q, a_pipe, cs)
+    torch.cuda.synchronize()
+    assert torch.equal(a_ref, a_pipe)
+
+
+def test_ax_pipe_f32_rejects_unaligned_and_other_orders(product_lib, torch_cuda):
+    torch = torch_cuda
+    E, Np = 4, 512
+    g = torch.rand(E * 7 * Np + 1, device="cuda")
+    q = torch.rand(E * Np + 1, device="cuda")
+    a = torch.empty(E * Np, device="cuda")
+    D = torch.rand(64, device="cuda")
+    cs = torch.cuda.current_stream().cuda_stream
+    with pytest.raises(G.NrsgError):
+        G.ax_pipe_f32(7, E, g[1:], D, 1.0, 0.0, True, q[:-1], a, cs)
+    with pytest.raises(G.NrsgError):
+        G.ax_pipe_f32(5, E, g[:-1], D, 1.0, 0.0, True, q[:-1], a, cs)
+
+
+def test_mg_solve_same_with_and_without_ax_pipeline(product_lib, torch_cuda):
+    torch = torch_cuda
+    N, n = 7, 5
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    opts = ("solver=pfcg;residualTol=1e-8+relative;maxIterations=200;preconditioner=multigrid;"
+            "smootherType=fourthoptcheby+ras;pMGSchedule=p=7+degree=5,p=3+degree=5,p=1,p=3+degree=5,p=7+degree=5;"
+            "mgPrecision=mixed")
+    a = G.Elliptic(N, VX, EToV, EToB, opts + ";axPipeline=1")
+    b = G.Elliptic(N, VX, EToV, EToB, opts + ";axPipeline=0")
+    rhs = torch.from_numpy(W.box_rhs(N, n, n, n, 3, a.get("ggeo"))).cuda()
+    xa, xb = torch.zeros_like(rhs), torch.zeros_like(rhs)
+    ia, ib = a.solve(rhs.clone(), xa), b.solve(rhs.clone(), xb)
+    assert ia["status"] == 0 and ia["iterations"] == ib["iterations"]
+    assert torch.equal(xa, xb)
