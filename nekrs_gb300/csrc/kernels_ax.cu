@@ -117,6 +117,111 @@ __global__ void __launch_bounds__(NQ *NQ *AxShape<NQ>::epb, (sizeof(T) == 4 && N
 }
 
 // ---------------------------------------------------------------------------
+// FP32 order-7 axhelm with vector shared-memory traffic.  Same thread layout,
+// register pencils and arithmetic as ax_stored_kernel<float, 8, POISSON>
+// (bit-identical results), but every operand row a thread contracts against
+// is read as two 16-byte loads: D and its transpose are both kept, and each
+// plane of q and of G_s is stored twice (row-major and transposed) so that the
+// column sums read rows too.  Row strides: 8 floats for the planes written
+// row-major (conflict-free 32-thread stores, 4 distinct rows per read), 12
+// floats for the transposed planes and D (8 distinct rows per read land on
+// disjoint bank quads).  This cuts the shared-memory wavefronts per node and
+// plane from about 75 to about 25, which is what bounds the plain kernel.
+// ---------------------------------------------------------------------------
+template <bool POISSON>
+__global__ void __launch_bounds__(128, 5)
+    ax8v_kernel(long long E, const float *__restrict__ ggeo, const float *__restrict__ D, float lambda0,
+                float lambda1, const float *__restrict__ q, float *__restrict__ Aq)
+{
+  constexpr int NQ = 8, NP = 512, EPB = 2, RT = 12;
+  __shared__ __align__(16) float s_D[NQ][RT];   // D[a][b] at [a][b]
+  __shared__ __align__(16) float s_DT[NQ][RT];  // D[a][b] at [b][a]
+  __shared__ __align__(16) float s_q[EPB][NQ][NQ];
+  __shared__ __align__(16) float s_qT[EPB][NQ][RT];
+  __shared__ __align__(16) float s_Gr[EPB][NQ][NQ];
+  __shared__ __align__(16) float s_GsT[EPB][NQ][RT];
+
+  const int t = threadIdx.x;
+  const int i = t % NQ, j = t / NQ;
+  const int el = threadIdx.y;
+  const long long e = (long long)blockIdx.x * EPB + el;
+  const bool active = e < E;
+  if (el == 0) {
+    const float d = D[j * NQ + i];
+    s_D[j][i] = d;
+    s_DT[i][j] = d;
+  }
+  float r_q[NQ], r_Aq[NQ];
+  const long long base = e * NP + t;
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    r_q[k] = active ? q[base + k * NQ * NQ] : 0.f;
+    r_Aq[k] = 0;
+  }
+  constexpr int NG = POISSON ? 6 : 7;
+  const float *g = ggeo + e * 7 * NP + t;
+  float gpre[NG * NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k)
+#pragma unroll
+    for (int c = 0; c < NG; ++c) gpre[c * NQ + k] = active ? __ldg(g + c * NP + k * NQ * NQ) : 0.f;
+  __syncthreads();
+
+  auto row8 = [](const float *p, float (&v)[NQ]) {
+    const float4 a = *reinterpret_cast<const float4 *>(p);
+    const float4 b = *reinterpret_cast<const float4 *>(p + 4);
+    v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+  };
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    const float G00 = gpre[0 * NQ + k], G01 = gpre[1 * NQ + k], G11 = gpre[2 * NQ + k];
+    const float G12 = gpre[3 * NQ + k], G02 = gpre[4 * NQ + k], G22 = gpre[5 * NQ + k];
+    const float GWJ = POISSON ? 0.f : gpre[(NG - 1) * NQ + k];
+    s_q[el][j][i] = r_q[k];
+    s_qT[el][i][j] = r_q[k];
+    float Dk[NQ];
+    row8(&s_D[k][0], Dk);
+    float qt = 0;
+#pragma unroll
+    for (int m = 0; m < NQ; ++m) qt += Dk[m] * r_q[m];
+    __syncthreads();
+    float Di[NQ], Dj[NQ], qrow[NQ], qcol[NQ];
+    row8(&s_D[i][0], Di);
+    row8(&s_D[j][0], Dj);
+    row8(&s_q[el][j][0], qrow);
+    row8(&s_qT[el][i][0], qcol);
+    float qr = 0, qs = 0;
+#pragma unroll
+    for (int m = 0; m < NQ; ++m) {
+      qr += Di[m] * qrow[m];
+      qs += Dj[m] * qcol[m];
+    }
+    s_Gr[el][j][i] = lambda0 * (G00 * qr + G01 * qs + G02 * qt);
+    s_GsT[el][i][j] = lambda0 * (G01 * qr + G11 * qs + G12 * qt);
+    const float Gt = lambda0 * (G02 * qr + G12 * qs + G22 * qt);
+    float auk = POISSON ? 0.f : GWJ * lambda1 * r_q[k];
+    __syncthreads();
+    float DTi[NQ], DTj[NQ], gsc[NQ], grr[NQ];
+    row8(&s_DT[j][0], DTj);
+    row8(&s_DT[i][0], DTi);
+    row8(&s_GsT[el][i][0], gsc);
+    row8(&s_Gr[el][j][0], grr);
+#pragma unroll
+    for (int m = 0; m < NQ; ++m) {
+      auk += DTj[m] * gsc[m];
+      r_Aq[m] += Dk[m] * Gt;
+      auk += DTi[m] * grr[m];
+    }
+    r_Aq[k] += auk;
+    __syncthreads();
+  }
+  if (active) {
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) Aq[base + k * NQ * NQ] = r_Aq[k];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // FP32 order-7 axhelm through a bulk-copy pipeline (sm_90+ cp.async.bulk into
 // shared memory, completion counted on an mbarrier).  Persistent CTAs walk
 // chunks of kPipeEps consecutive elements; while the chunk in one stage is
@@ -454,6 +559,17 @@ void launch_ax_stored(int N, long long E, const T *ggeo, const T *D, T lambda0, 
                       T *Aq, cudaStream_t s)
 {
   if (E <= 0) return;
+  if constexpr (std::is_same<T, float>::value) {
+    if (N == 7) {
+      const unsigned grid = (unsigned)((E + 1) / 2);
+      if (poisson)
+        ax8v_kernel<true><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, D, lambda0, lambda1, q, Aq);
+      else
+        ax8v_kernel<false><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, D, lambda0, lambda1, q, Aq);
+      NRSG_CHECK_LAUNCH();
+      return;
+    }
+  }
 #define NRSG_AX(NQ)                                                                                        \
   {                                                                                                        \
     constexpr int EPB = AxShape<NQ>::epb;                                                                  \

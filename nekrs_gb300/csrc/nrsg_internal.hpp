@@ -102,7 +102,7 @@ struct Options {
   int coarseMaxIter = 200;
   bool coarsePersistent = true;     // order-1 coarse Jacobi-PCG as one cooperative kernel
   bool graphs = true;               // CUDA graphs of the steady-state PCG iteration (non-legacy streams)
-  bool axPipeline = true;           // FP32 order-7 levels: bulk-copy pipelined axhelm
+  bool axPipeline = false;          // FP32 order-7 levels: bulk-copy pipelined axhelm
   int projection = 0;               // initialGuess: 0 none, 1 projection (classic), 2 projectionAconj
   int projVecs = 8;                 // residualProjectionVectors
   int projStart = 5;                // residualProjectionStart
