@@ -81,8 +81,23 @@ long long nrsg_kernel_launches(void);
  * lambda1, poisson, elementMap (trilinear), initialGuess (previous |
  * projectionAconj | projection: solution projection of
  * ellipticSolutionProjection.cpp, with residualProjectionVectors (8) and
- * residualProjectionStart (5)), cudaGraphs. */
+ * residualProjectionStart (5)), cudaGraphs, nFields, stressFormulation,
+ * axPipeline. */
 int nrsg_elliptic_create(const nrsg_mesh_desc *mesh, const char *options, nrsg_elliptic **out);
+/* Block (vector) Helmholtz, the velocity solve (tombo.cpp:224-228): options
+ * "solver = pcg+block" (or nFields = 2 | 3) and stressFormulation = true.
+ * Every vector of the handle (solve, operator, preconditioner) then holds
+ * nFields fields one after another, fieldOffset = E*Np; norms sum over the
+ * fields (weightedNorm2Many).  Preconditioner jacobi (block diagonal,
+ * ellipticBlockBuildDiagonalHex3D) or none.  The per-field entry points
+ * nrsg_elliptic_gs / _mask act on one field. */
+/* Per-node coefficient fields (elliptic->o_lambda0 / o_lambda1, the
+ * p_lambda = 1 kernels; ELLIPTIC COEFF FIELD): device arrays of E*Np doubles
+ * shared by the fields (loffset = 0) or nFields*E*Np with loffset = E*Np.
+ * d_lambda1 NULL means 0.  Copied into the handle; rebuilds the Jacobi
+ * diagonal (ellipticUpdateJacobi).  Needs preconditioner jacobi or none. */
+int nrsg_elliptic_set_coefficients(nrsg_elliptic *el, const double *d_lambda0, const double *d_lambda1,
+                                   long long loffset);
 int nrsg_elliptic_destroy(nrsg_elliptic *el);
 /* Run all later work of `el` on `cuda_stream` (a cudaStream_t; NULL = the
  * legacy default stream) instead of the library's own non-blocking stream,

@@ -68,6 +68,7 @@ def lib():
         L.nrsg_elliptic_solve_host.argtypes = [vp, vp, vp, ctypes.POINTER(SolveInfo)]
         L.nrsg_elliptic_solve_begin.argtypes = [vp, vp, vp]
         L.nrsg_elliptic_set_tolerance.argtypes = [vp, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        L.nrsg_elliptic_set_coefficients.argtypes = [vp, vp, vp, LL]
         L.nrsg_elliptic_solve_advance.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(SolveInfo)]
         L.nrsg_elliptic_solve_batch.argtypes = [ctypes.c_int, ctypes.POINTER(vp), ctypes.POINTER(vp),
                                                 ctypes.POINTER(vp), ctypes.POINTER(SolveInfo)]
@@ -188,6 +189,11 @@ class Elliptic:
         s = self._batch_stream.cuda_stream
         if s != self._stream:
             self.set_stream(s)
+
+    def set_coefficients(self, lambda0, lambda1=None, loffset=0):
+        """Per-node coefficient fields (device buffers of E*Np, or nFields*E*Np with loffset = E*Np)."""
+        self._order_with(lambda0, lambda1)
+        check(lib().nrsg_elliptic_set_coefficients(self.h, _ptr(lambda0), _ptr(lambda1), loffset))
 
     def set_tolerance(self, tol, relative=True, max_iterations=400):
         check(lib().nrsg_elliptic_set_tolerance(self.h, float(tol), int(relative), int(max_iterations)))

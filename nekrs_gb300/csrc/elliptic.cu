@@ -137,7 +137,21 @@ Elliptic::Elliptic(const nrsg_mesh_desc *m, const char *options)
   NRSG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   ownStream = true;
   fine.build(m->N, m->Nelements, m->h_VX, m->h_EToV, m->h_EToB, m->h_ggeo, stream);
-  const long long n = fine.Nlocal;
+  if (opt.nfields < 1 || opt.nfields > 3) throw Error(NRSG_ERR_BAD_CONFIG, "nFields must be 1..3");
+  if (opt.stress && opt.nfields != 3) throw Error(NRSG_ERR_BAD_CONFIG, "stressFormulation needs the 3-field block solver");
+  if (block_mode() && (opt.precon == "multigrid" || opt.axPrecision == "fp32x2" || opt.trilinear))
+    throw Error(NRSG_ERR_BAD_CONFIG, "the block solver takes preconditioner = jacobi or none and stored FP64 geometry");
+  const long long n = nT();
+  if (opt.nfields > 1) {
+    wBlock.alloc(n);
+    for (int f = 0; f < opt.nfields; ++f)
+      NRSG_CUDA(cudaMemcpyAsync(wBlock.p + (size_t)f * fine.Nlocal, fine.d_invDegree64.p, sizeof(double) * fine.Nlocal,
+                                cudaMemcpyDeviceToDevice, stream));
+  }
+  if (opt.stress) {
+    vgeo.alloc((size_t)12 * fine.Nlocal);
+    launch_vgeo(fine.N, fine.E, fine.d_VX64.p, fine.d_z64.p, fine.d_w64.p, fine.d_D64.p, vgeo.p, stream);
+  }
   p.alloc(n);
   z.alloc(n);
   Ap.alloc(n);
@@ -168,10 +182,7 @@ Elliptic::Elliptic(const nrsg_mesh_desc *m, const char *options)
   }
   if (opt.precon == "jacobi") {
     invDiag.alloc(n);
-    launch_build_diag<double>(fine.N, fine.E, fine.d_ggeo64.p, fine.d_D64.p, opt.lambda0, opt.lambda1, opt.poisson,
-                              invDiag.p, stream);
-    launch_gs<double>(fine.ngroups, fine.d_gsOff.p, fine.d_gsIds.p, invDiag.p, stream);
-    launch_recip<double>(n, invDiag.p, stream);
+    build_jacobi();
   } else if (opt.precon == "multigrid") {
     mg_setup();
   }
@@ -201,6 +212,16 @@ Elliptic::~Elliptic()
 
 void Elliptic::ax(const double *q, double *Aq)
 {
+  if (block_mode()) {
+    const double *l0p = coef ? lam0.p : nullptr, *l1p = coef ? lam1.p : nullptr;
+    if (opt.stress)
+      launch_stress_ax(fine.N, fine.E, fine.Nlocal, loffset, vgeo.p, fine.d_D64.p, l0p, l1p, opt.lambda0,
+                       opt.poisson ? 0.0 : opt.lambda1, q, Aq, stream);
+    else
+      launch_block_ax(fine.N, fine.E, opt.nfields, fine.Nlocal, loffset, fine.d_ggeo64.p, fine.d_D64.p, l0p, l1p,
+                      opt.lambda0, opt.lambda1, opt.poisson, q, Aq, stream);
+    return;
+  }
   if (ggeoPairs.p)
     launch_ax_fp32x2(fine.N, fine.E, ggeoPairs.p, DPairs.p, opt.lambda0, opt.lambda1, opt.poisson, q, Aq, stream);
   else if (opt.trilinear)
@@ -214,12 +235,57 @@ void Elliptic::ax(const double *q, double *Aq)
 void Elliptic::op(const double *q, double *Aq)
 {
   ax(q, Aq);
-  launch_gs_mask<double>(fine.gsPlan, Aq, true, stream); // mask and gather-scatter
+  gs_mask_fields(Aq); // mask and gather-scatter
+}
+
+void Elliptic::gs_mask_fields(double *v)
+{
+  for (int f = 0; f < opt.nfields; ++f) launch_gs_mask<double>(fine.gsPlan, v + (size_t)f * fine.Nlocal, true, stream);
+}
+
+// Jacobi: diag(A) per field, gather-scatter, reciprocal
+// (ellipticUpdateJacobi.cpp:32-90; block form ellipticBlockBuildDiagonalHex3D)
+void Elliptic::build_jacobi()
+{
+  if (block_mode())
+    launch_block_diag(fine.N, fine.E, opt.nfields, fine.Nlocal, loffset, fine.d_ggeo64.p, fine.d_D64.p,
+                      coef ? lam0.p : nullptr, coef ? lam1.p : nullptr, opt.lambda0, opt.lambda1, opt.poisson,
+                      invDiag.p, stream);
+  else
+    launch_build_diag<double>(fine.N, fine.E, fine.d_ggeo64.p, fine.d_D64.p, opt.lambda0, opt.lambda1, opt.poisson,
+                              invDiag.p, stream);
+  for (int f = 0; f < opt.nfields; ++f)
+    launch_gs<double>(fine.ngroups, fine.d_gsOff.p, fine.d_gsIds.p, invDiag.p + (size_t)f * fine.Nlocal, stream);
+  launch_recip<double>(nT(), invDiag.p, stream);
+}
+
+// per-node coefficient fields (elliptic->o_lambda0 / o_lambda1, p_lambda = 1):
+// loff = 0 shares one array between the fields, loff = Nlocal gives each its own
+void Elliptic::set_coefficients(const double *d_lambda0, const double *d_lambda1, long long loff)
+{
+  if (!d_lambda0) throw Error(NRSG_ERR_INVALID, "lambda0 field required");
+  if (loff != 0 && loff != fine.Nlocal) throw Error(NRSG_ERR_INVALID, "loffset must be 0 or E*Np");
+  if (opt.precon == "multigrid") throw Error(NRSG_ERR_BAD_CONFIG, "coefficient fields need preconditioner = jacobi or none");
+  const size_t n = (size_t)(loff ? opt.nfields : 1) * fine.Nlocal;
+  if (lam0.n != n) {
+    lam0.alloc(n);
+    lam1.alloc(n);
+  }
+  NRSG_CUDA(cudaMemcpyAsync(lam0.p, d_lambda0, n * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+  if (d_lambda1)
+    NRSG_CUDA(cudaMemcpyAsync(lam1.p, d_lambda1, n * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+  else
+    launch_fill<double>((long long)n, 0.0, lam1.p, stream);
+  loffset = loff;
+  coef = true;
+  graph_release();
+  if (opt.precon == "jacobi") build_jacobi();
+  NRSG_CUDA(cudaStreamSynchronize(stream));
 }
 
 void Elliptic::precondition(const double *r, double *zz)
 {
-  const long long n = fine.Nlocal;
+  const long long n = nT();
   if (opt.precon == "jacobi") {
     launch_axmyz<double>(n, r, invDiag.p, zz, stream);
   } else if (opt.precon == "multigrid") {
@@ -349,8 +415,8 @@ void Elliptic::graph_release()
 
 void Elliptic::issue_iteration_kernels(bool first)
 {
-  const long long n = fine.Nlocal;
-  const double *wt = fine.d_invDegree64.p;
+  const long long n = nT();
+  const double *wt = wT();
   const bool flexible = (opt.solver == "pfcg");
   PcgScalars *sc = d_scal.p;
   double *r = st.r, *x = st.x;
@@ -378,7 +444,7 @@ void Elliptic::issue_iteration_kernels(bool first)
 void Elliptic::finish_issue()
 {
   if (opt.projection) proj_post(st.x);
-  launch_axpby<double>(fine.Nlocal, 1.0, x0.p, 1.0, st.x, stream);
+  launch_axpby<double>(nT(), 1.0, x0.p, 1.0, st.x, stream);
   NRSG_CUDA(cudaEventRecord(ev1, stream));
   st.phase = 3;
 }
@@ -388,10 +454,10 @@ void Elliptic::finish_issue()
 // r -= A xbar (A-conjugate) or r -= sum alpha_k b_k (classic, b_k = A x_k).
 void Elliptic::proj_pre(double *r)
 {
-  const long long n = fine.Nlocal;
+  const long long n = nT();
   ++projStep;
   if (projStep < opt.projStart || projM <= 0) return;
-  const double *w = fine.d_invDegree64.p;
+  const double *w = wT();
   launch_multi_wdot(n, w, projXX.p, projM, r, projAlpha.p, red, 0, stream);
   launch_accumulate(n, projM, projAlpha.p, projXX.p, projXbar.p, stream);
   if (opt.projection == 1)
@@ -405,11 +471,11 @@ void Elliptic::proj_pre(double *r)
 // by one classical Gram-Schmidt pass; drop it when it is dependent (1e-7).
 void Elliptic::proj_update_space()
 {
-  const long long n = fine.Nlocal;
+  const long long n = nT();
   const int m = projM;
   if (m <= 0) return;
   const bool classic = opt.projection == 1;
-  const double *w = fine.d_invDegree64.p;
+  const double *w = wT();
   const double *b = projBB.p + (size_t)(classic ? m - 1 : 0) * n;
   launch_multi_wdot(n, w, projXX.p, m, b, projAlpha.p, red, 0, stream);
   std::vector<double> alpha(m);
@@ -433,7 +499,7 @@ void Elliptic::proj_update_space()
 // post (:183-221, :273-279): the correction x joins the basis; x += xbar
 void Elliptic::proj_post(double *x)
 {
-  const long long n = fine.Nlocal;
+  const long long n = nT();
   if (projStep < opt.projStart) return;
   const size_t bytes = sizeof(double) * n;
   if (projM == 0) {
@@ -463,7 +529,7 @@ void Elliptic::proj_post(double *x)
 void Elliptic::begin(double *r, double *x)
 {
   if (st.phase != 0 && st.phase != 4) throw Error(NRSG_ERR_INVALID, "a solve is already in progress on this handle");
-  const long long n = fine.Nlocal;
+  const long long n = nT();
   history.clear();
   status = NRSG_OK;
   st = StepState();
@@ -473,11 +539,11 @@ void Elliptic::begin(double *r, double *x)
   // r = b - A x0 (local Ax, ellipticSolve.cpp:91-103), mask, gather-scatter
   ax(x, Ap.p);
   launch_axpby<double>(n, -1.0, Ap.p, 1.0, r, stream);
-  launch_gs_mask<double>(fine.gsPlan, r, true, stream); // mask and gather-scatter
+  gs_mask_fields(r); // mask and gather-scatter
   NRSG_CUDA(cudaMemcpyAsync(x0.p, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
   launch_fill<double>(n, 0.0, x, stream);
   if (opt.projection) proj_pre(r);
-  launch_wdot<double>(n, fine.d_invDegree64.p, r, nullptr, &d_scal.p->rdotr, red, 0, stream);
+  launch_wdot<double>(n, wT(), r, nullptr, &d_scal.p->rdotr, red, 0, stream);
   NRSG_CUDA(cudaMemcpyAsync(&h_scal->rdotr, &d_scal.p->rdotr, sizeof(double), cudaMemcpyDeviceToHost, stream));
   NRSG_CUDA(cudaEventRecord(evRead, stream));
   st.phase = 1;
@@ -509,7 +575,7 @@ bool Elliptic::advance(bool block, nrsg_solve_info *info)
       st.res = st.res0;
       if (st.res0 > 0 && opt.maxIter > 0) {
         if (opt.solver == "pcg" || opt.solver == "pfcg") {
-          launch_fill<double>(fine.Nlocal, 0.0, p.p, stream);
+          launch_fill<double>(nT(), 0.0, p.p, stream);
           pcg_issue_iteration();
           st.phase = 2;
         } else {
@@ -726,8 +792,8 @@ int nrsg_elliptic_solve_host(nrsg_elliptic *el, double *h_r, double *h_x, nrsg_s
   if (!el || !h_r || !h_x) return NRSG_ERR_INVALID;
   try {
     auto &E = *el->impl;
-    const size_t bytes = sizeof(double) * E.fine.Nlocal;
-    if (!E.io_r.p) { E.io_r.alloc(E.fine.Nlocal); E.io_x.alloc(E.fine.Nlocal); }
+    const size_t bytes = sizeof(double) * E.nT();
+    if (!E.io_r.p) { E.io_r.alloc(E.nT()); E.io_x.alloc(E.nT()); }
     NRSG_CUDA(cudaMemcpyAsync(E.io_r.p, h_r, bytes, cudaMemcpyHostToDevice, E.stream));
     NRSG_CUDA(cudaMemcpyAsync(E.io_x.p, h_x, bytes, cudaMemcpyHostToDevice, E.stream));
     const int st = E.solve(E.io_r.p, E.io_x.p, info);
@@ -922,6 +988,13 @@ int nrsg_ax_stored_f32(int N, long long E, const float *ggeo, const float *D, fl
                        const float *q, float *Aq, void *s)
 {
   NRSG_TRY(nrsg::launch_ax_stored<float>(N, E, ggeo, D, l0, l1, poisson != 0, q, Aq, (cudaStream_t)s))
+}
+
+int nrsg_elliptic_set_coefficients(nrsg_elliptic *el, const double *d_lambda0, const double *d_lambda1,
+                                   long long loffset)
+{
+  if (!el) return NRSG_ERR_INVALID;
+  NRSG_TRY(el->impl->set_coefficients(d_lambda0, d_lambda1, loffset))
 }
 
 int nrsg_ax_pipe_f32(int N, long long E, const float *ggeo, const float *D, float l0, float l1, int poisson,

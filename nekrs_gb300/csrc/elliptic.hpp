@@ -62,6 +62,19 @@ struct Elliptic {
   DevBuf<double> gV, gZ, gW, gB, gY;
   double *h_y = nullptr;                  // pinned: y[0..nr] + nw
 
+  // Block (vector) solve: nfields fields at fieldOffset = Nlocal, weights
+  // invDegree repeated per field; optional per-node coefficients
+  // (elliptic->o_lambda0 / o_lambda1 with loffset); stress form on vgeo.
+  DevBuf<double> wBlock, lam0, lam1, vgeo;
+  bool coef = false;
+  long long loffset = 0;
+  long long nT() const { return fine.Nlocal * opt.nfields; }
+  const double *wT() const { return opt.nfields > 1 ? wBlock.p : fine.d_invDegree64.p; }
+  bool block_mode() const { return opt.nfields > 1 || coef || opt.stress; }
+  void gs_mask_fields(double *v);
+  void build_jacobi();
+  void set_coefficients(const double *d_lambda0, const double *d_lambda1, long long loff);
+
   std::unique_ptr<MGState, MGDeleter> mg;
   std::vector<double> history;
   int status = NRSG_OK;

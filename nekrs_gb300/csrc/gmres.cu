@@ -14,7 +14,7 @@ void Elliptic::gmres_setup()
 {
   const int nr = opt.nVector;
   if (nr < 1 || nr > 64) throw Error(NRSG_ERR_BAD_CONFIG, "nVector must be 1..64");
-  const long long n = fine.Nlocal;
+  const long long n = nT();
   const bool flexible = (opt.solver == "pfgmres");
   gV.alloc((size_t)nr * n);
   gZ.alloc((size_t)(flexible ? nr : 1) * n);
@@ -26,8 +26,8 @@ void Elliptic::gmres_setup()
 
 int Elliptic::pgmres(double *r, double *x, double tol, int maxit, double &rdotr)
 {
-  const long long n = fine.Nlocal;
-  const double *wt = fine.d_invDegree64.p;
+  const long long n = nT();
+  const double *wt = wT();
   const int nr = opt.nVector;
   const int ld = nr + 1;
   const bool flexible = (opt.solver == "pfgmres");

@@ -103,6 +103,8 @@ struct Options {
   bool coarsePersistent = true;     // order-1 coarse Jacobi-PCG as one cooperative kernel
   bool graphs = true;               // CUDA graphs of the steady-state PCG iteration (non-legacy streams)
   bool axPipeline = false;          // FP32 order-7 levels: bulk-copy pipelined axhelm
+  int nfields = 1;                  // block solver: fields at fieldOffset = Nlocal ("solver = pcg+block" -> 3)
+  bool stress = false;              // stressFormulation: symmetric-gradient operator (nfields = 3)
   int projection = 0;               // initialGuess: 0 none, 1 projection (classic), 2 projectionAconj
   int projVecs = 8;                 // residualProjectionVectors
   int projStart = 5;                // residualProjectionStart
@@ -166,6 +168,18 @@ template <typename T> void launch_gs_mask(const GsPlan &P, T *q, bool mask, cuda
 void launch_accumulate(long long n, int m, const double *alpha, const double *X, double *y, cudaStream_t s);
 void launch_multi_scaled_sub(long long n, int m, const double *alpha, double *X, cudaStream_t s);
 void launch_scale_inplace(long long n, double a, double *x, cudaStream_t s);
+// block (vector) Helmholtz, kernels_block.cu
+void launch_vgeo(int N, long long E, const double *VX, const double *gllz, const double *gllw, const double *D,
+                 double *vgeo, cudaStream_t s);
+void launch_block_ax(int N, long long E, int nf, long long offset, long long loffset, const double *ggeo,
+                     const double *D, const double *lam0, const double *lam1, double l0, double l1, bool poisson,
+                     const double *q, double *Aq, cudaStream_t s);
+void launch_stress_ax(int N, long long E, long long offset, long long loffset, const double *vgeo, const double *D,
+                      const double *lam0, const double *lam1, double l0, double l1, const double *q, double *Aq,
+                      cudaStream_t s);
+void launch_block_diag(int N, long long E, int nf, long long offset, long long loffset, const double *ggeo,
+                       const double *D, const double *lam0, const double *lam1, double l0, double l1, bool poisson,
+                       double *diag, cudaStream_t s);
 // Raise (never lower) a kernel function's dynamic shared-memory limit on the current device.
 void raise_dynamic_smem(const void *kfn, size_t bytes);
 // FP32 order-7 Poisson axhelm through the bulk-copy pipeline (false: not applicable, caller

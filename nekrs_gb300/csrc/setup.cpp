@@ -381,6 +381,7 @@ Options parse_options(const char *text)
         else throw Error(NRSG_ERR_BAD_CONFIG, "unknown solver '" + v + "'");
         const auto p = v.find("nvector=");
         if (p != std::string::npos) o.nVector = std::stoi(v.substr(p + 8));
+        if (v.find("block") != std::string::npos) o.nfields = 3;
       } else if (key == "residualtol") {
         o.tol = std::stod(v.substr(0, v.find('+')));
         o.relative = v.find("relative") != std::string::npos;
@@ -400,6 +401,8 @@ Options parse_options(const char *text)
       else if (key == "coarsepersistent") o.coarsePersistent = std::stoi(v) != 0;
       else if (key == "cudagraphs") o.graphs = std::stoi(v) != 0;
       else if (key == "axpipeline") o.axPipeline = std::stoi(v) != 0;
+      else if (key == "nfields") o.nfields = std::stoi(v);
+      else if (key == "stressformulation") o.stress = (v == "true" || v == "1" || v == "yes");
       else if (key == "initialguess") {
         if (v == "projectionaconj" || v == "projection-aconj") o.projection = 2;
         else if (v == "projection") o.projection = 1;

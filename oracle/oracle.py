@@ -60,6 +60,11 @@ def lib():
         _lib.orc_gll.argtypes = [ctypes.c_int, D, D]
         _lib.orc_dmatrix.argtypes = [ctypes.c_int, D]
         _lib.orc_interp.argtypes = [ctypes.c_int, ctypes.c_int, D]
+        vp, ci, cd, cl = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_longlong
+        _lib.orc_block_vgeo.argtypes = [vp, vp]
+        _lib.orc_block_ax.argtypes = [vp, ci, ci, ci, cl, vp, vp, cd, cd, vp, vp]
+        _lib.orc_block_diag.argtypes = [vp, ci, ci, cl, vp, vp, cd, cd, vp]
+        _lib.orc_block_solve.argtypes = [vp, ci, ci, ci, cl, vp, vp, cd, cd, ci, cd, ci, ci, vp, vp, vp]
     return _lib
 
 
@@ -140,6 +145,45 @@ class Elliptic:
         out = np.zeros(n, dtype=dt)
         lib().orc_get(self.h, name.encode(), out.ctypes.data_as(ctypes.c_void_p))
         return out
+
+    # ---- block (vector) Helmholtz: nf fields at fieldOffset = Nlocal; lam0 / lam1 per node
+    # (length Nlocal, or nf*Nlocal with loffset = Nlocal) or None for the scalars l0 / l1
+    @staticmethod
+    def _lam(a):
+        return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+    def block_vgeo(self):
+        n = self.get("ggeo").size // 7
+        out = np.zeros(12 * n)
+        lib().orc_block_vgeo(self.h, out.ctypes.data)
+        return out
+
+    def block_ax(self, q, nf=3, stress=False, poisson=False, lam0=None, lam1=None, l0=1.0, l1=0.0, loffset=0):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        out = np.zeros_like(q)
+        a0, a1 = self._lam(lam0), self._lam(lam1)
+        lib().orc_block_ax(self.h, nf, int(stress), int(poisson), loffset, None if a0 is None else a0.ctypes.data,
+                           None if a1 is None else a1.ctypes.data, l0, l1, q.ctypes.data, out.ctypes.data)
+        return out
+
+    def block_inv_diag(self, nf=3, poisson=False, lam0=None, lam1=None, l0=1.0, l1=0.0, loffset=0):
+        n = self.get("invDegree").size
+        out = np.zeros(nf * n)
+        a0, a1 = self._lam(lam0), self._lam(lam1)
+        lib().orc_block_diag(self.h, nf, int(poisson), loffset, None if a0 is None else a0.ctypes.data,
+                             None if a1 is None else a1.ctypes.data, l0, l1, out.ctypes.data)
+        return out
+
+    def block_solve(self, rhs, nf=3, stress=False, poisson=False, lam0=None, lam1=None, l0=1.0, l1=0.0, loffset=0,
+                    jacobi=True, tol=1e-8, relative=True, maxit=1000, x0=None):
+        r = np.array(rhs, dtype=np.float64)
+        x = np.zeros_like(r) if x0 is None else np.array(x0, dtype=np.float64)
+        info = np.zeros(4)
+        a0, a1 = self._lam(lam0), self._lam(lam1)
+        lib().orc_block_solve(self.h, nf, int(stress), int(poisson), loffset, None if a0 is None else a0.ctypes.data,
+                              None if a1 is None else a1.ctypes.data, l0, l1, int(jacobi), tol, int(relative), maxit,
+                              r.ctypes.data, x.ctypes.data, info.ctypes.data)
+        return x, {"iterations": int(info[0]), "res0": info[1], "res": info[2], "status": int(info[3]), "r": r}
 
     @property
     def volume(self):

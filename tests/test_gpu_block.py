@@ -1,0 +1,122 @@
+"""Block (vector) Helmholtz on the GPU against the oracle's restatement: the
+block axhelm with scalar and per-node coefficients, the stress (symmetric
+gradient) operator, the block Jacobi diagonal, and whole PCG solves over 3
+fields (the velocity solve next to the pressure solve)."""
+import numpy as np
+import pytest
+
+import nekrs_gb300 as G
+from nekrs_gb300 import workloads as W
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+BASE = "preconditioner=jacobi;solver=pcg+block;residualTol=1e-8+relative;maxIterations=3000;poisson=0;lambda0=1.0;lambda1=0.0"
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+def coefficient_fields(el_o, nf):
+    x, y, z = el_o.get("x"), el_o.get("y"), el_o.get("z")
+    mu = 1.0 + 0.5 * np.sin(3 * x) * np.cos(2 * y) + 0.2 * z  # viscosity-like, positive
+    h = 20.0 + 5.0 * np.cos(x + y + z)                         # rho * bd0 / dt-like
+    return mu, h
+
+
+@pytest.mark.parametrize("N,nf,stress,kind", [(3, 3, False, "scalar"), (5, 3, False, "shared"),
+                                              (7, 2, False, "perfield"), (5, 3, True, "scalar"),
+                                              (7, 3, True, "shared"), (4, 3, True, "perfield")])
+def test_block_operator_and_jacobi(product_lib, oracle_mod, torch_cuda, N, nf, stress, kind):
+    torch = torch_cuda
+    n = 3
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    opts = BASE.replace("pcg+block", "pcg") + f";nFields={nf};lambda1=0.8" + (";stressFormulation=true" if stress else "")
+    orc = O.Elliptic(N, VX, EToV, EToB, "preconditioner=jacobi")
+    el = G.Elliptic(N, VX, EToV, EToB, opts)
+    Nl = orc.get("invDegree").size
+    lam0 = lam1 = None
+    loff = 0
+    if kind != "scalar":
+        mu, h = coefficient_fields(orc, nf)
+        if kind == "perfield":
+            lam0 = np.concatenate([mu * (1 + 0.1 * f) for f in range(nf)])
+            lam1 = np.concatenate([h * (1 - 0.1 * f) for f in range(nf)])
+            loff = Nl
+        else:
+            lam0, lam1 = mu, h
+        el.set_coefficients(torch.from_numpy(lam0).cuda(), torch.from_numpy(lam1).cuda(), loff)
+    q = np.random.default_rng(N).standard_normal(nf * Nl)
+    ref = orc.block_ax(q, nf=nf, stress=stress, poisson=False, lam0=lam0, lam1=lam1, l0=1.0, l1=0.8, loffset=loff)
+    out = torch.zeros(nf * Nl, dtype=torch.float64, device="cuda")
+    el.ax(torch.from_numpy(q).cuda(), out)
+    torch.cuda.synchronize()
+    assert rel(out.cpu().numpy(), ref) < 1e-13
+    dref = orc.block_inv_diag(nf=nf, poisson=False, lam0=lam0, lam1=lam1, l0=1.0, l1=0.8, loffset=loff)
+    assert rel(el.get("invDiag"), dref) < 1e-13
+
+
+@pytest.mark.parametrize("N,stress,kind", [(5, False, "shared"), (7, True, "shared"), (5, True, "scalar"),
+                                           (3, False, "perfield")])
+def test_block_pcg_solve_parity(product_lib, oracle_mod, torch_cuda, N, stress, kind):
+    torch = torch_cuda
+    n = 3
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    opts = BASE + ";lambda1=10.0;residualTol=1e-10+relative" + (";stressFormulation=true" if stress else "")
+    orc = O.Elliptic(N, VX, EToV, EToB, "preconditioner=jacobi")
+    el = G.Elliptic(N, VX, EToV, EToB, opts)
+    Nl = orc.get("invDegree").size
+    lam0 = lam1 = None
+    loff = 0
+    if kind != "scalar":
+        mu, h = coefficient_fields(orc, 3)
+        if kind == "perfield":
+            lam0, lam1, loff = np.concatenate([mu, 1.2 * mu, 0.8 * mu]), np.concatenate([h, h, 2 * h]), Nl
+        else:
+            lam0, lam1 = mu, h
+        el.set_coefficients(torch.from_numpy(lam0).cuda(), torch.from_numpy(lam1).cuda(), loff)
+    rhs = np.concatenate([W.box_rhs(N, n, n, n, s, orc.get("ggeo")) for s in (5, 6, 7)])
+    xo, io = orc.block_solve(rhs, nf=3, stress=stress, poisson=False, lam0=lam0, lam1=lam1, l0=1.0, l1=10.0,
+                             loffset=loff, tol=1e-10, relative=True, maxit=3000)
+    r = torch.from_numpy(rhs.copy()).cuda()
+    x = torch.zeros_like(r)
+    ig = el.solve(r, x)
+    torch.cuda.synchronize()
+    assert io["status"] == 0 and ig["status"] == 0
+    assert abs(ig["res0"] - io["res0"]) <= 1e-12 * io["res0"]
+    # Jacobi-PCG runs 100-450 iterations here; rounding differences (FMA contraction, reduction order)
+    # may move the stopping iteration by one per hundred
+    assert abs(ig["iterations"] - io["iterations"]) <= max(1, io["iterations"] // 100)
+    assert rel(x.cpu().numpy(), xo) < 1e-7
+
+
+def test_block_of_identical_fields_equals_scalar_solves(product_lib, torch_cuda):
+    """Three copies of one right-hand side through the 3-field solver give three copies of the scalar
+    Helmholtz solution (same operator per field; the block norm is the sum over the fields)."""
+    torch = torch_cuda
+    N, n = 5, 3
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    s1 = G.Elliptic(N, VX, EToV, EToB, BASE.replace("pcg+block", "pcg") + ";lambda1=10.0;residualTol=1e-12")
+    s3 = G.Elliptic(N, VX, EToV, EToB, BASE + ";lambda1=10.0;residualTol=1e-12")
+    b = W.box_rhs(N, n, n, n, 8, s1.get("ggeo"))
+    r1, x1 = torch.from_numpy(b.copy()).cuda(), torch.zeros(b.size, dtype=torch.float64, device="cuda")
+    r3 = torch.from_numpy(np.concatenate([b, b, b])).cuda()
+    x3 = torch.zeros_like(r3)
+    i1, i3 = s1.solve(r1, x1), s3.solve(r3, x3)
+    torch.cuda.synchronize()
+    assert i1["status"] == 0 and i3["status"] == 0
+    assert abs(i3["res0"] - np.sqrt(3) * i1["res0"]) <= 1e-12 * i3["res0"]
+    xs = x3.cpu().numpy().reshape(3, -1)
+    for f in range(3):
+        assert rel(xs[f], x1.cpu().numpy()) < 1e-8
+
+
+def test_block_rejects_multigrid_and_bad_field_counts(product_lib, torch_cuda):
+    VX, EToV, EToB = W.kershaw_box(2, eps=0.3)
+    with pytest.raises(G.NrsgError):
+        G.Elliptic(3, VX, EToV, EToB, "solver=pcg+block;preconditioner=multigrid")
+    with pytest.raises(G.NrsgError):
+        G.Elliptic(3, VX, EToV, EToB, "solver=pcg;nFields=2;stressFormulation=true;preconditioner=jacobi")
+    with pytest.raises(G.NrsgError):
+        G.Elliptic(3, VX, EToV, EToB, "solver=pcg;nFields=4;preconditioner=jacobi")

@@ -138,3 +138,29 @@ def test_oracle_solution_projection(oracle_mod, form):
         assert np.linalg.norm(x1 - x0) <= 1e-6 * np.linalg.norm(x0)
     assert its_proj[0] == its_plain[0]  # projection starts at the second solve
     assert max(its_proj[3:]) < min(its_plain) // 3, (its_plain, its_proj)
+
+
+def test_oracle_block_helmholtz_sanity(oracle_mod):
+    """Block / stress restatement: one field with scalar coefficients is the scalar Helmholtz operator
+    bit for bit; constant coefficient arrays equal the scalars; the stress operator annihilates a rigid
+    rotation and is symmetric; its PCG converges."""
+    N, n = 4, 3
+    VX, EToV, EToB = O.box_mesh(n, n, n, 0.3)
+    el = O.Elliptic(N, VX, EToV, EToB, "preconditioner=jacobi")
+    hel = O.Elliptic(N, VX, EToV, EToB, "preconditioner=jacobi;lambda0=1.3;lambda1=0.7;poisson=0")
+    Nl = el.get("invDegree").size
+    rng = np.random.default_rng(0)
+    q = rng.standard_normal(Nl)
+    b = el.block_ax(q, nf=1, l0=1.3, l1=0.7)
+    assert np.array_equal(b, hel.ax(q))
+    assert np.array_equal(el.block_ax(q, nf=1, lam0=np.full(Nl, 1.3), lam1=np.full(Nl, 0.7)), b)
+    assert np.array_equal(el.block_inv_diag(nf=1, l0=1.3, l1=0.7), hel.get("invDiag"))
+    x, y = el.get("x"), el.get("y")
+    rot = np.concatenate([y, -x, np.zeros_like(x)])
+    assert np.abs(el.block_ax(rot, nf=3, stress=True, l0=1.0, l1=0.0)).max() < 1e-12
+    u, v = rng.standard_normal(3 * Nl), rng.standard_normal(3 * Nl)
+    Au, Av = el.block_ax(u, nf=3, stress=True, l1=0.5), el.block_ax(v, nf=3, stress=True, l1=0.5)
+    assert abs(v @ Au - u @ Av) < 1e-12 * abs(v @ Au)
+    rhs = np.concatenate([O.box_rhs(N, n, n, n, s, el.get("ggeo")) for s in (1, 2, 3)])
+    _, info = el.block_solve(rhs, nf=3, stress=True, l0=1.0, l1=10.0, tol=1e-8)
+    assert info["status"] == 0 and info["res"] <= 1e-8 * info["res0"]
