@@ -82,7 +82,7 @@ long long nrsg_kernel_launches(void);
  * projectionAconj | projection: solution projection of
  * ellipticSolutionProjection.cpp, with residualProjectionVectors (8) and
  * residualProjectionStart (5)), cudaGraphs, nFields, stressFormulation,
- * axPipeline. */
+ * axPipeline, coarseGridDiscretization (fem | fem+galerkin). */
 int nrsg_elliptic_create(const nrsg_mesh_desc *mesh, const char *options, nrsg_elliptic **out);
 /* Block (vector) Helmholtz, the velocity solve (tombo.cpp:224-228): options
  * "solver = pcg+block" (or nFields = 2 | 3) and stressFormulation = true.
@@ -192,6 +192,17 @@ double nrsg_host_hessenberg_rho(int n, const double *h_H);
 int nrsg_host_assemble_operator(int N, long long E, const long long *h_EToV, const int *h_EToB, const double *h_ggeo,
                                 double lambda0, double lambda1, int poisson, long long *nrow, long long *nnz,
                                 long long *h_rowPtr, long long *h_cols, double *h_vals, long long *h_rowOfNode);
+
+/* Galerkin coarse operator (coarseGridDiscretization = FEM+Galerkin;
+ * ellipticBuildFEMGalerkinHex3D, src/solvers/elliptic/MG/ellipticBuildFEM.cpp:
+ * 384-520): the order-1 system B^T A_f B, A_f the order-Nf operator in FP32
+ * on h_ggeo_fine ([E][7][(Nf+1)^3]), B the trilinear basis at the order-Nf
+ * GLL nodes; rows are the order-1 level's masked gather groups.  Same calling
+ * convention as nrsg_host_assemble_operator (h_rowOfNode: E*8 entries). */
+int nrsg_host_assemble_galerkin(int Nf, long long E, const long long *h_EToV, const int *h_EToB,
+                                const double *h_ggeo_fine, double lambda0, double lambda1, int poisson,
+                                long long *nrow, long long *nnz, long long *h_rowPtr, long long *h_cols,
+                                double *h_vals, long long *h_rowOfNode);
 
 /* ---- mesh ingestion: Nek5000 binary .re2 files (host only) --------------
  * Replaces the mesh read nekRS delegates to Nek5000 (src/io/re2Reader.cpp:4-41

@@ -61,6 +61,8 @@ def lib():
         L.nrsg_host_setup_maps.argtypes = [ctypes.c_int, LL] + [vp] * 10
         L.nrsg_host_assemble_operator.argtypes = ([ctypes.c_int, LL, vp, vp, vp, ctypes.c_double, ctypes.c_double,
                                                    ctypes.c_int] + [vp] * 6)
+        L.nrsg_host_assemble_galerkin.argtypes = ([ctypes.c_int, LL, vp, vp, vp, ctypes.c_double, ctypes.c_double,
+                                                   ctypes.c_int] + [vp] * 6)
         L.nrsg_elliptic_create.argtypes = [ctypes.POINTER(MeshDesc), ctypes.c_char_p, ctypes.POINTER(vp)]
         L.nrsg_elliptic_destroy.argtypes = [vp]
         L.nrsg_elliptic_set_stream.argtypes = [vp, vp]
@@ -321,6 +323,24 @@ def host_assemble_operator(N, EToV, EToB, ggeo, lambda0=1.0, lambda1=0.0, poisso
     check(lib().nrsg_host_assemble_operator(*args, ctypes.byref(nrow), ctypes.byref(nnz), rp.ctypes.data,
                                             cols.ctypes.data, vals.ctypes.data, rown.ctypes.data))
     return rp, cols, vals, rown
+
+
+def host_assemble_galerkin(Nf, EToV, EToB, ggeo_fine, lambda0=1.0, lambda1=0.0, poisson=True):
+    """Galerkin order-1 coarse operator B^T A_f B (host code of the library): (rowPtr, cols, vals, rowOfNode)."""
+    EToV = np.ascontiguousarray(EToV, dtype=np.int64)
+    EToB = np.ascontiguousarray(EToB, dtype=np.int32)
+    g = np.ascontiguousarray(ggeo_fine, dtype=np.float64)
+    E = EToV.shape[0]
+    nrow, nnz = LL(0), LL(0)
+    a = (Nf, E, EToV.ctypes.data, EToB.ctypes.data, g.ctypes.data, float(lambda0), float(lambda1), int(poisson),
+         ctypes.byref(nrow), ctypes.byref(nnz))
+    check(lib().nrsg_host_assemble_galerkin(*a, None, None, None, None))
+    rp = np.zeros(nrow.value + 1, np.int64)
+    cols = np.zeros(nnz.value, np.int64)
+    vals = np.zeros(nnz.value)
+    ron = np.zeros(E * 8, np.int64)
+    check(lib().nrsg_host_assemble_galerkin(*a, rp.ctypes.data, cols.ctypes.data, vals.ctypes.data, ron.ctypes.data))
+    return rp, cols, vals, ron
 
 
 def solve_batch(solvers, rs, xs):

@@ -978,6 +978,37 @@ int nrsg_host_assemble_operator(int N, long long E, const long long *h_EToV, con
   })
 }
 
+int nrsg_host_assemble_galerkin(int Nf, long long E, const long long *h_EToV, const int *h_EToB,
+                                const double *h_ggeo_fine, double lambda0, double lambda1, int poisson,
+                                long long *nrow, long long *nnz, long long *h_rowPtr, long long *h_cols,
+                                double *h_vals, long long *h_rowOfNode)
+{
+  if (Nf < 1 || E < 1 || !h_EToV || !h_EToB || !h_ggeo_fine || !nrow || !nnz) return NRSG_ERR_INVALID;
+  NRSG_TRY({
+    std::vector<long long> ids;
+    nrsg::nek_global_ids(1, E, h_EToV, ids);
+    nrsg::GatherMap um, gm;
+    nrsg::build_gather(ids, um);
+    std::vector<int> mask;
+    nrsg::dirichlet_nodes(1, E, h_EToB, um, mask);
+    for (int m : mask) ids[m] = 0;
+    nrsg::build_gather(ids, gm);
+    std::vector<double> z, w, D;
+    nrsg::gll_nodes(Nf, z, w);
+    nrsg::diff_matrix(z, D);
+    std::vector<double> Ae;
+    nrsg::galerkin_element_matrices(Nf, E, D, z, h_ggeo_fine, lambda0, lambda1, poisson != 0, Ae);
+    nrsg::CsrMatrix A;
+    nrsg::assemble_rows(8, E, Ae, gm, A);
+    *nrow = A.nrow;
+    *nnz = A.rowPtr[A.nrow];
+    if (h_rowPtr) std::memcpy(h_rowPtr, A.rowPtr.data(), A.rowPtr.size() * sizeof(long long));
+    if (h_cols) std::memcpy(h_cols, A.col.data(), A.col.size() * sizeof(long long));
+    if (h_vals) std::memcpy(h_vals, A.val.data(), A.val.size() * sizeof(double));
+    if (h_rowOfNode) std::memcpy(h_rowOfNode, A.rowOfNode.data(), A.rowOfNode.size() * sizeof(long long));
+  })
+}
+
 // ---- kernel-level entry points --------------------------------------------
 int nrsg_ax_stored_f64(int N, long long E, const double *ggeo, const double *D, double l0, double l1, int poisson,
                        const double *q, double *Aq, void *s)

@@ -173,9 +173,19 @@ template <typename T> struct MGImpl : public MGState {
   // representative E-vector node per row and the row of each E-vector node.
   void build_coarse_matrix(const FieldLevel &C)
   {
-    const std::vector<double> gg = C.d_ggeo64.download();
     CsrMatrix A;
-    assemble_level(C.N, C.E, C.Dh, gg.data(), el.opt.lambda0, el.opt.lambda1, el.opt.poisson, C.gm, A);
+    if (el.opt.galerkin) {
+      // B^T A_fine B from the finest level's FP32 operator (ellipticMultiGridSetup.cpp:260-261)
+      if (C.N != 1) throw Error(NRSG_ERR_BAD_CONFIG, "the Galerkin coarse operator needs an order-1 coarsest level");
+      const std::vector<double> gf = el.fine.d_ggeo64.download();
+      std::vector<double> Ae;
+      galerkin_element_matrices(el.fine.N, el.fine.E, el.fine.Dh, el.fine.z, gf.data(), el.opt.lambda0,
+                                el.opt.lambda1, el.opt.poisson, Ae);
+      assemble_rows(8, C.E, Ae, C.gm, A);
+    } else {
+      const std::vector<double> gg = C.d_ggeo64.download();
+      assemble_level(C.N, C.E, C.Dh, gg.data(), el.opt.lambda0, el.opt.lambda1, el.opt.poisson, C.gm, A);
+    }
     std::vector<int> rep(A.nrow);
     for (long long r = 0; r < A.nrow; ++r) rep[r] = C.gm.ids[C.gm.off[r]];
     coarse_matrix_setup<T>(A.nrow, A.rowPtr.data(), A.col.data(), A.val.data(), C.Nlocal, A.rowOfNode.data(),

@@ -35,5 +35,8 @@ struct CsrMatrix {
 };
 void assemble_level(int N, long long E, const std::vector<double> &Dh, const double *ggeo, double lam0, double lam1,
                     bool poisson, const GatherMap &gm, CsrMatrix &A);
+void assemble_rows(int np, long long E, const std::vector<double> &Ae, const GatherMap &gm, CsrMatrix &A);
+void galerkin_element_matrices(int Nf, long long E, const std::vector<double> &Dh, const std::vector<double> &z,
+                               const double *ggeo, double lam0, double lam1, bool poisson, std::vector<double> &Ae);
 
 } // namespace nrsg

@@ -497,11 +497,6 @@ void assemble_level(int N, long long E, const std::vector<double> &Dh, const dou
                     bool poisson, const GatherMap &gm, CsrMatrix &A)
 {
   const int nq = N + 1, np = nq * nq * nq, ns = 3 * nq;
-  const long long nloc = E * np;
-  A.nrow = (long long)gm.off.size() - 1;
-  A.rowOfNode.assign(nloc, -1);
-  for (long long g = 0; g < A.nrow; ++g)
-    for (int q = gm.off[g]; q < gm.off[g + 1]; ++q) A.rowOfNode[gm.ids[q]] = g;
   // element matrices [e][n][m]
   std::vector<double> Ae((size_t)E * np * np, 0.0);
 #pragma omp parallel for schedule(static)
@@ -539,6 +534,19 @@ void assemble_level(int N, long long E, const std::vector<double> &Dh, const dou
     if (!poisson)
       for (int n = 0; n < np; ++n) M[n * np + n] += lam1 * g[6 * np + n];
   }
+  assemble_rows(np, E, Ae, gm, A);
+}
+
+// Element matrices M[e][m][n] (row m, column n) into the CSR operator whose
+// rows are the masked gather groups; masked rows / columns and exact zeros
+// are dropped, duplicates summed in element order.
+void assemble_rows(int np, long long E, const std::vector<double> &Ae, const GatherMap &gm, CsrMatrix &A)
+{
+  const long long nloc = E * np;
+  A.nrow = (long long)gm.off.size() - 1;
+  A.rowOfNode.assign(nloc, -1);
+  for (long long g = 0; g < A.nrow; ++g)
+    for (int q = gm.off[g]; q < gm.off[g + 1]; ++q) A.rowOfNode[gm.ids[q]] = g;
   // rows: members in ascending E-vector order, then element columns
   std::vector<std::vector<std::pair<long long, double>>> rows(A.nrow);
 #pragma omp parallel for schedule(dynamic, 256)
@@ -568,6 +576,83 @@ void assemble_level(int N, long long E, const std::vector<double> &Dh, const dou
       A.col[A.rowPtr[r] + t] = rows[r][t].first;
       A.val[A.rowPtr[r] + t] = rows[r][t].second;
     }
+}
+
+// Galerkin coarse operator (ellipticBuildFEMGalerkinHex3D,
+// src/solvers/elliptic/MG/ellipticBuildFEM.cpp:384-520): per element, the
+// fine-level FP32 operator applied to each trilinear basis function sampled
+// at the fine GLL nodes (ellipticGenerateCoarseBasisHex3D :344-382; the
+// reference runs its pfloat ellipticAx on all elements at once), projected
+// on every basis function in FP64: M[e][m][n] = sum_k (double)(A_f b_n)_k b_m(k).
+// The FP32 operator follows the serial ellipticPartialAxCoeffHex3D order.
+void galerkin_element_matrices(int Nf, long long E, const std::vector<double> &Dh, const std::vector<double> &z,
+                               const double *ggeo, double lam0, double lam1, bool poisson, std::vector<double> &Ae)
+{
+  const int nq = Nf + 1, np = nq * nq * nq;
+  std::vector<double> b((size_t)8 * np);
+  for (int c = 0; c < 8; ++c)
+    for (int k = 0; k < nq; ++k)
+      for (int j = 0; j < nq; ++j)
+        for (int i = 0; i < nq; ++i) {
+          const double zr = (c & 1) ? 0.5 * (1 + z[i]) : 0.5 * (1 - z[i]);
+          const double zs = (c & 2) ? 0.5 * (1 + z[j]) : 0.5 * (1 - z[j]);
+          const double zt = (c & 4) ? 0.5 * (1 + z[k]) : 0.5 * (1 - z[k]);
+          b[(size_t)c * np + i + nq * (j + nq * k)] = zr * zs * zt;
+        }
+  std::vector<float> D32(Dh.begin(), Dh.end());
+  Ae.assign((size_t)E * 64, 0.0);
+  const float l0 = (float)lam0, l1 = (float)lam1;
+#pragma omp parallel for schedule(static)
+  for (long long e = 0; e < E; ++e) {
+    std::vector<float> g32((size_t)7 * np), q(np), Aq(np), Gr(np), Gs(np), Gt(np);
+    for (size_t t = 0; t < g32.size(); ++t) g32[t] = (float)ggeo[(size_t)e * 7 * np + t];
+    for (int c = 0; c < 8; ++c) {
+      for (int t = 0; t < np; ++t) q[t] = (float)b[(size_t)c * np + t];
+      for (int k = 0; k < nq; ++k)
+        for (int j = 0; j < nq; ++j)
+          for (int i = 0; i < nq; ++i) {
+            const int n = i + nq * (j + nq * k);
+            float qr = 0, qs = 0, qt = 0;
+            for (int m = 0; m < nq; ++m) {
+              qr += D32[i * nq + m] * q[m + nq * (j + nq * k)];
+              qs += D32[j * nq + m] * q[i + nq * (m + nq * k)];
+              qt += D32[k * nq + m] * q[i + nq * (j + nq * m)];
+            }
+            const float G00 = g32[0 * np + n], G01 = g32[1 * np + n], G11 = g32[2 * np + n];
+            const float G12 = g32[3 * np + n], G02 = g32[4 * np + n], G22 = g32[5 * np + n];
+            float a = G00 * qr;
+            a += G01 * qs;
+            a += G02 * qt;
+            float bb = G01 * qr;
+            bb += G11 * qs;
+            bb += G12 * qt;
+            float cc = G02 * qr;
+            cc += G12 * qs;
+            cc += G22 * qt;
+            Gr[n] = l0 * a;
+            Gs[n] = l0 * bb;
+            Gt[n] = l0 * cc;
+          }
+      for (int k = 0; k < nq; ++k)
+        for (int j = 0; j < nq; ++j)
+          for (int i = 0; i < nq; ++i) {
+            const int n = i + nq * (j + nq * k);
+            const float r0 = poisson ? 0.f : g32[6 * np + n] * l1 * q[n];
+            float ar = 0, as = 0, at = 0;
+            for (int m = 0; m < nq; ++m) {
+              ar += D32[m * nq + i] * Gr[m + nq * (j + nq * k)];
+              as += D32[m * nq + j] * Gs[i + nq * (m + nq * k)];
+              at += D32[m * nq + k] * Gt[i + nq * (j + nq * m)];
+            }
+            Aq[n] = ar + as + at + r0;
+          }
+      for (int m = 0; m < 8; ++m) {
+        double val = 0;
+        for (int t = 0; t < np; ++t) val += (double)Aq[t] * b[(size_t)m * np + t];
+        Ae[(size_t)e * 64 + m * 8 + c] = val;
+      }
+    }
+  }
 }
 
 } // namespace nrsg

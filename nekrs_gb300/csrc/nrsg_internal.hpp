@@ -98,6 +98,7 @@ struct Options {
   double minEigFactor = 0.1, maxEigFactor = 1.1;
   std::string schedule;
   std::string coarse = "jpcg";
+  bool galerkin = false;            // coarseGridDiscretization = FEM+Galerkin: B^T A_fine B on the order-1 level
   double coarseTol = 1e-4;
   int coarseMaxIter = 200;
   bool coarsePersistent = true;     // order-1 coarse Jacobi-PCG as one cooperative kernel

@@ -35,6 +35,7 @@ struct Options {
   std::string coarse = "jpcg";           // jpcg (on-device Jacobi-PCG) | smooth
   double coarseTol = 1e-4;
   int coarseMaxIter = 200;
+  bool galerkin = false;                 // coarseGridDiscretization = FEM+Galerkin
   std::string mgPrecision = "fp64";      // fp64 | fp32
   bool poisson = true;
   double lambda0 = 1.0, lambda1 = 0.0;

@@ -262,6 +262,10 @@ template <typename T> struct MGT {
   // coarse PCG scratch
   std::vector<T> cp, cz, cAp, cr;
   std::vector<int> coarseIters;
+  // Galerkin coarse operator (CSR over the coarsest level's masked gather groups)
+  std::vector<long long> gRowPtr, gCol, gRowOfNode;
+  std::vector<T> gVal, gInvDiag;
+  std::vector<long long> gRep;
 };
 
 struct MG {
@@ -941,6 +945,49 @@ template <typename T> static int coarse_pcg(MGT<T> &M, MGLevel<T> &lv, const T *
   return it;
 }
 
+// coarse solve on the Galerkin matrix: the same Jacobi-PCG on its rows
+// (rhs of a row = the assembled E-vector value of one of its nodes; the
+// solution is scattered back to every node of the row, 0 on masked nodes)
+template <typename T> static int coarse_pcg_csr(MGT<T> &M, MGLevel<T> &lv, const T *b, T *x)
+{
+  const long long nr = (long long)M.gRowPtr.size() - 1, n = lv.L->Nlocal;
+  std::vector<T> xr(nr, 0), r(nr), p(nr, 0), z(nr), Ap(nr);
+  for (long long i = 0; i < nr; ++i) r[i] = b[M.gRep[i]];
+  auto dot = [&](const std::vector<T> &a, const std::vector<T> &c) {
+    double s = 0;
+    for (long long i = 0; i < nr; ++i) s += (double)a[i] * (double)c[i];
+    return s;
+  };
+  const double r0 = std::sqrt(dot(r, r));
+  int it = 0;
+  if (r0 > 0) {
+    const double tol = M.o.coarseTol * r0;
+    double rdotz1 = 0, rdotz2 = 0, rn = r0;
+    while (rn > tol && it < M.o.coarseMaxIter) {
+      ++it;
+      for (long long i = 0; i < nr; ++i) z[i] = M.gInvDiag[i] * r[i];
+      rdotz2 = rdotz1;
+      rdotz1 = dot(r, z);
+      const double beta = (it == 1) ? 0.0 : rdotz1 / rdotz2;
+      for (long long i = 0; i < nr; ++i) p[i] = z[i] + (T)beta * p[i];
+      for (long long i = 0; i < nr; ++i) {
+        T s = 0;
+        for (long long t = M.gRowPtr[i]; t < M.gRowPtr[i + 1]; ++t) s += M.gVal[t] * p[M.gCol[t]];
+        Ap[i] = s;
+      }
+      const T alpha = (T)(rdotz1 / (dot(p, Ap) + 1e-300));
+      for (long long i = 0; i < nr; ++i) {
+        xr[i] += alpha * p[i];
+        r[i] -= alpha * Ap[i];
+      }
+      rn = std::sqrt(dot(r, r));
+    }
+  }
+  for (long long i = 0; i < n; ++i) x[i] = M.gRowOfNode[i] < 0 ? T(0) : xr[M.gRowOfNode[i]];
+  M.coarseIters.push_back(it);
+  return it;
+}
+
 // ---------------------------------------------------------------------------
 // V-cycle
 // ---------------------------------------------------------------------------
@@ -951,6 +998,8 @@ template <typename T> static void vcycle(MGT<T> &M, int k)
   if (k == base) {
     if (M.o.coarse == "smooth")
       smooth(M, lv, lv.rhs.data(), lv.x.data(), true);
+    else if (M.o.galerkin)
+      coarse_pcg_csr(M, lv, lv.rhs.data(), lv.x.data());
     else
       coarse_pcg(M, lv, lv.rhs.data(), lv.x.data());
     return;
@@ -1093,6 +1142,24 @@ template <typename T> static void build_mg(Elliptic &el, MGT<T> &M, MG &mg)
       build_diag<T>(L, lv.ggeo.data(), lv.D.data(), M.lambda0, M.lambda1, M.poisson, lv.invDiag.data());
       gs_add(L, lv.invDiag.data());
       for (auto &v : lv.invDiag) v = (T)1 / v;
+    }
+  }
+  if (o.galerkin) {
+    const Level &C = *M.levels.back().L;
+    if (C.N != 1) throw std::runtime_error("the Galerkin coarse operator needs an order-1 coarsest level");
+    std::vector<double> vals;
+    assemble_galerkin(el.fine, C, (double)M.lambda0, (double)M.lambda1, M.poisson, M.gRowPtr, M.gCol, vals);
+    const long long nr = (long long)M.gRowPtr.size() - 1;
+    M.gVal.assign(vals.begin(), vals.end());
+    M.gInvDiag.assign(nr, T(0));
+    for (long long i = 0; i < nr; ++i)
+      for (long long t = M.gRowPtr[i]; t < M.gRowPtr[i + 1]; ++t)
+        if (M.gCol[t] == i) M.gInvDiag[i] = (T)(1.0 / vals[t]);
+    M.gRowOfNode.assign(C.Nlocal, -1);
+    M.gRep.assign(nr, 0);
+    for (long long g = 0; g < nr; ++g) {
+      M.gRep[g] = C.gsIds[C.gsOff[g]];
+      for (int t = C.gsOff[g]; t < C.gsOff[g + 1]; ++t) M.gRowOfNode[C.gsIds[t]] = g;
     }
   }
   size_t nmax = 0;

@@ -70,6 +70,8 @@ Options parse_options(const std::string &text)
     else if (key == "maxeigenvalueboundfactor") o.maxEigFactor = std::stod(lv);
     else if (key == "pmgschedule") o.schedule = lv;
     else if (key == "coarsesolver") o.coarse = lv;
+    else if (key == "coarsegriddiscretization") o.galerkin = (lv == "fem+galerkin" || lv == "galerkin");
+    else if (key == "galerkincoarseoperator") o.galerkin = (lv == "true" || lv == "1" || lv == "yes");
     else if (key == "coarsetol") o.coarseTol = std::stod(lv);
     else if (key == "coarsemaxiterations") o.coarseMaxIter = std::stoi(lv);
     else if (key == "mgprecision") o.mgPrecision = lv;
@@ -730,6 +732,73 @@ void assemble_fem(const Level &L, double lambda0, double lambda1, bool poisson, 
   vals.clear();
   for (size_t i = 0; i < nz.size(); ++i) {
     if (!cols.empty() && i > 0 && nz[i].row == nz[i - 1].row && nz[i].col == nz[i - 1].col) {
+      vals.back() += nz[i].val;
+      continue;
+    }
+    cols.push_back(nz[i].col);
+    vals.push_back(nz[i].val);
+    rowPtr[nz[i].row + 1]++;
+  }
+  for (long long r = 0; r < ng; ++r) rowPtr[r + 1] += rowPtr[r];
+}
+
+// ---------------------------------------------------------------------------
+// Galerkin coarse operator, following ellipticBuildFEMGalerkinHex3D
+// (src/solvers/elliptic/MG/ellipticBuildFEM.cpp:384-520): the eight trilinear
+// basis functions sampled at the fine GLL nodes (ellipticGenerateCoarseBasisHex3D
+// :344-382), each copied into every element and run through the fine level's
+// pfloat operator (ellipticAx, all elements at once), then projected on each
+// basis function in dfloat (lines 465-495); masked rows / columns skipped,
+// |val| > dropTol (0) kept, row = the projected function m, column = the
+// applied function n; sorted and duplicates summed as assemble_fem.
+// ---------------------------------------------------------------------------
+void assemble_galerkin(const Level &F, const Level &C, double lambda0, double lambda1, bool poisson,
+                       std::vector<long long> &rowPtr, std::vector<long long> &cols, std::vector<double> &vals)
+{
+  const int nqf = F.Nq, npf = F.Np;
+  std::vector<double> b((size_t)8 * npf);
+  for (int jj = 1; jj <= 8; ++jj)
+    for (int k = 0; k < nqf; ++k)
+      for (int j = 0; j < nqf; ++j)
+        for (int i = 0; i < nqf; ++i) {
+          const double zr = (jj % 2 == 0) ? 0.5 * (1 + F.z[i]) : 0.5 * (1 - F.z[i]);
+          const double zs = (jj == 3 || jj == 4 || jj == 7 || jj == 8) ? 0.5 * (1 + F.z[j]) : 0.5 * (1 - F.z[j]);
+          const double zt = (jj > 4) ? 0.5 * (1 + F.z[k]) : 0.5 * (1 - F.z[k]);
+          b[(size_t)(jj - 1) * npf + i + nqf * (j + nqf * k)] = zr * zs * zt;
+        }
+  std::vector<float> g32(F.ggeo.begin(), F.ggeo.end()), D32(F.D.begin(), F.D.end());
+  std::vector<float> q(F.Nlocal), Aq(F.Nlocal);
+  std::vector<std::vector<float>> AqAll(8);
+  for (int n = 0; n < 8; ++n) {
+    for (long long e = 0; e < F.E; ++e)
+      for (int t = 0; t < npf; ++t) q[e * npf + t] = (float)b[(size_t)n * npf + t];
+    ax_stored<float>(F, g32.data(), D32.data(), (float)lambda0, (float)lambda1, poisson, q.data(), Aq.data());
+    AqAll[n] = Aq;
+  }
+  std::vector<long long> num(C.Nlocal, -1);
+  const long long ng = (long long)C.gsOff.size() - 1;
+  for (long long g = 0; g < ng; ++g)
+    for (int t = C.gsOff[g]; t < C.gsOff[g + 1]; ++t) num[C.gsIds[t]] = g;
+  struct NZ { long long row, col; double val; };
+  std::vector<NZ> nz;
+  for (long long e = 0; e < C.E; ++e)
+    for (int n = 0; n < 8; ++n) {
+      if (num[e * 8 + n] < 0) continue;
+      for (int m = 0; m < 8; ++m) {
+        if (num[e * 8 + m] < 0) continue;
+        double val = 0;
+        for (int t = 0; t < npf; ++t) val += (double)AqAll[n][e * npf + t] * b[(size_t)m * npf + t];
+        if (std::fabs(val) > 0.0) nz.push_back({num[e * 8 + m], num[e * 8 + n], val});
+      }
+    }
+  std::stable_sort(nz.begin(), nz.end(), [](const NZ &a, const NZ &c) {
+    return a.row != c.row ? a.row < c.row : a.col < c.col;
+  });
+  rowPtr.assign(ng + 1, 0);
+  cols.clear();
+  vals.clear();
+  for (size_t i = 0; i < nz.size(); ++i) {
+    if (i > 0 && nz[i].row == nz[i - 1].row && nz[i].col == nz[i - 1].col) {
       vals.back() += nz[i].val;
       continue;
     }

@@ -67,3 +67,47 @@ def test_assembled_operator_neumann_faces(product_lib, oracle_mod):
     EToB = EToB.copy()
     EToB[0, 4] = 1
     _check(1, VX, EToV, EToB)
+
+
+@pytest.mark.parametrize("N,n,eps,poisson", [(3, 3, 0.3, True), (7, 2, 1.0, True), (5, 3, 0.5, False)])
+def test_galerkin_operator_matches_oracle(product_lib, oracle_mod, N, n, eps, poisson):
+    """coarseGridDiscretization = FEM+Galerkin: the library's B^T A_f B (host code) equals the oracle's
+    restatement of ellipticBuildFEMGalerkinHex3D bit for bit; rows are the order-1 level's masked groups."""
+    VX, EToV, EToB = W.kershaw_box(n, eps=eps)
+    fine = O.Elliptic(N, VX, EToV, EToB, "preconditioner=none")
+    coarse = O.Elliptic(1, VX, EToV, EToB, "preconditioner=none")
+    l1 = 0.0 if poisson else 2.0
+    ref = fine.assemble_galerkin(coarse, 1.0, l1, poisson)
+    rp, cols, vals, ron = G.host_assemble_galerkin(N, EToV, EToB, fine.get("ggeo"), 1.0, l1, poisson)
+    assert np.array_equal(rp, ref[0]) and np.array_equal(cols, ref[1]) and np.array_equal(vals, ref[2])
+    fem = G.host_assemble_operator(1, EToV, EToB, coarse.get("ggeo"))
+    assert np.array_equal(ron, fem[3])
+    A = sp.csr_matrix((vals, cols, rp))
+    # symmetric up to the FP32 rounding of the fine operator; positive diagonal
+    assert abs(A - A.T).max() <= 1e-6 * abs(A).max()
+    assert (A.diagonal() > 0).all()
+
+
+def test_galerkin_of_an_order_one_level_is_its_fem_operator(product_lib, oracle_mod):
+    """With an order-1 fine level the coarse basis is the identity: B^T A B is the FEM operator evaluated in
+    FP32 (the pfloat ellipticAx the reference projects)."""
+    VX, EToV, EToB = W.kershaw_box(4, eps=0.3)
+    c = O.Elliptic(1, VX, EToV, EToB, "preconditioner=none")
+    rp, cols, vals, _ = G.host_assemble_galerkin(1, EToV, EToB, c.get("ggeo"))
+    frp, fcols, fvals, _ = G.host_assemble_operator(1, EToV, EToB, c.get("ggeo"))
+    Ag, Af = sp.csr_matrix((vals, cols, rp)), sp.csr_matrix((fvals, fcols, frp))
+    assert abs(Ag - Af).max() <= 1e-6 * abs(Af).max()
+
+
+def test_oracle_mg_with_galerkin_coarse_converges(oracle_mod):
+    VX, EToV, EToB = W.kershaw_box(4, eps=0.3)
+    opts = ("solver=pfcg;residualTol=1e-8+relative;maxIterations=200;preconditioner=multigrid;"
+            "smootherType=fourthoptcheby+asm;pMGSchedule=p=5+degree=2,p=3+degree=2,p=1,p=3+degree=2,p=5+degree=2;"
+            "mgPrecision=fp64")
+    its = {}
+    for g in ("fem", "fem+galerkin"):
+        el = O.Elliptic(5, VX, EToV, EToB, opts + f";coarseGridDiscretization={g}")
+        x, info = el.solve(W.box_rhs(5, 4, 4, 4, 3, el.get("ggeo")))
+        assert info["status"] == 0 and info["res"] <= 1e-8 * info["res0"]
+        its[g] = info["iterations"]
+    assert abs(its["fem"] - its["fem+galerkin"]) <= 3, its
