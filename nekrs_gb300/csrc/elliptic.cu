@@ -142,6 +142,17 @@ Elliptic::Elliptic(const nrsg_mesh_desc *m, const char *options)
   if (block_mode() && (opt.precon == "multigrid" || opt.axPrecision == "fp32x2" || opt.trilinear))
     throw Error(NRSG_ERR_BAD_CONFIG, "the block solver takes preconditioner = jacobi or none and stored FP64 geometry");
   const long long n = nT();
+  // all-Neumann Poisson problem: no face is Dirichlet (ellipticSetup.cpp:187-205)
+  if (opt.poisson && opt.nfields == 1) {
+    allNeumann = true;
+    for (int bc : fine.EToBh)
+      if (bc > 0 && bc != NRSG_BC_NEUMANN) { allNeumann = false; break; }
+    if (allNeumann) {
+      ones.alloc(fine.Nlocal);
+      launch_fill<double>(fine.Nlocal, 1.0, ones.p, stream);
+      d_sum.alloc(1);
+    }
+  }
   if (opt.nfields > 1) {
     wBlock.alloc(n);
     for (int f = 0; f < opt.nfields; ++f)
@@ -293,6 +304,14 @@ void Elliptic::precondition(const double *r, double *zz)
   } else {
     NRSG_CUDA(cudaMemcpyAsync(zz, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
   }
+  if (allNeumann) zero_mean(zz); // ellipticPreconditioner.cpp:82-83
+}
+
+// ellipticZeroMean (ellipticZeroMean.cpp:31-44): q -= sum(q) / (E Np) over the E-vector
+void Elliptic::zero_mean(double *q)
+{
+  launch_wdot<double>(fine.Nlocal, nullptr, q, ones.p, d_sum.p, red, 4, stream);
+  launch_sub_mean<double>(fine.Nlocal, d_sum.p, (double)fine.Nlocal, q, stream);
 }
 
 double Elliptic::read_scalar(const double *d_src)
@@ -420,7 +439,7 @@ void Elliptic::issue_iteration_kernels(bool first)
   const bool flexible = (opt.solver == "pfcg");
   PcgScalars *sc = d_scal.p;
   double *r = st.r, *x = st.x;
-  if (opt.precon == "jacobi") {
+  if (opt.precon == "jacobi" && !allNeumann) {
     launch_jacobi_rdotz(n, wt, invDiag.p, r, z.p, sc, red, 0, stream);
   } else {
     const double *zz = r;
@@ -445,6 +464,7 @@ void Elliptic::finish_issue()
 {
   if (opt.projection) proj_post(st.x);
   launch_axpby<double>(nT(), 1.0, x0.p, 1.0, st.x, stream);
+  if (allNeumann) zero_mean(st.x); // ellipticSolve.cpp:188-189
   NRSG_CUDA(cudaEventRecord(ev1, stream));
   st.phase = 3;
 }
@@ -539,6 +559,7 @@ void Elliptic::begin(double *r, double *x)
   // r = b - A x0 (local Ax, ellipticSolve.cpp:91-103), mask, gather-scatter
   ax(x, Ap.p);
   launch_axpby<double>(n, -1.0, Ap.p, 1.0, r, stream);
+  if (allNeumann) zero_mean(r); // ellipticSolve.cpp:101
   gs_mask_fields(r); // mask and gather-scatter
   NRSG_CUDA(cudaMemcpyAsync(x0.p, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
   launch_fill<double>(n, 0.0, x, stream);
@@ -872,6 +893,7 @@ int nrsg_elliptic_get(nrsg_elliptic *el, const char *name, void *h_out, long lon
     else if (s == "invDegree") put(L.gm.invDegree);
     else if (s == "D") put(L.Dh);
     else if (s == "history") put(E.history);
+    else if (s == "allNeumann") put(std::vector<double>{E.allNeumann ? 1.0 : 0.0});
     else if (s == "proj.vectors") put(std::vector<double>{(double)E.projM, (double)E.projStep});
     else if (s == "graph.segments") {
       // segments of the captured steady-state iteration (0: ordinary launches), and how many are coarse solves

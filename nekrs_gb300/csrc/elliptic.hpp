@@ -72,6 +72,11 @@ struct Elliptic {
   const double *wT() const { return opt.nfields > 1 ? wBlock.p : fine.d_invDegree64.p; }
   bool block_mode() const { return opt.nfields > 1 || coef || opt.stress; }
   void gs_mask_fields(double *v);
+  // null space of the all-Neumann Poisson operator (ellipticSetup.cpp:187-205):
+  // remove the E-vector mean from r, z and x (ellipticZeroMean)
+  bool allNeumann = false;
+  DevBuf<double> ones, d_sum;
+  void zero_mean(double *q);
   void build_jacobi();
   void set_coefficients(const double *d_lambda0, const double *d_lambda1, long long loff);
 

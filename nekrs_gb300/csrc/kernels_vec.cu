@@ -167,6 +167,23 @@ void launch_multi_scaled_sub(long long n, int m, const double *alpha, double *X,
   multi_scaled_sub_kernel<<<vec_grid(n), kThreads, 0, s>>>(n, m, alpha, X);
   NRSG_CHECK_LAUNCH();
 }
+// q -= (T)(sum / denom) with the sum already reduced on the device (ellipticZeroMean; the
+// projection of a singular coarse right-hand side)
+template <typename T>
+__global__ void sub_mean_kernel(long long n, const double *__restrict__ sum, double denom, T *__restrict__ q)
+{
+  const T mean = (T)(sum[0] / denom);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    q[i] -= mean;
+}
+template <typename T> void launch_sub_mean(long long n, const double *sum, double denom, T *q, cudaStream_t s)
+{
+  if (n <= 0) return;
+  sub_mean_kernel<T><<<vec_grid(n), kThreads, 0, s>>>(n, sum, denom, q);
+  NRSG_CHECK_LAUNCH();
+}
+template void launch_sub_mean<double>(long long, const double *, double, double *, cudaStream_t);
+template void launch_sub_mean<float>(long long, const double *, double, float *, cudaStream_t);
 __global__ void scale_inplace_kernel(long long n, double a, double *x)
 {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)

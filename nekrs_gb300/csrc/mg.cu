@@ -64,6 +64,9 @@ template <typename T> struct MGImpl : public MGState {
   // assembled coarse operator and its row vectors
   CoarseMatrix<T> cA;
   DevBuf<T> cx, cz2, cz3;
+  DevBuf<T> cOnes;          // all-Neumann: ones on the coarsest level, for its rhs mean
+  DevBuf<double> cSum;
+  double cUnknowns = 0;     // sum of the coarsest level's invDegree = its assembled unknowns
   std::vector<int> coarseIters;
   T l0, l1;
   bool poisson;
@@ -129,6 +132,13 @@ template <typename T> struct MGImpl : public MGState {
     cr.alloc(C.Nlocal);
     csc.alloc(1);
     NRSG_CUDA(cudaMemsetAsync(csc.p, 0, sizeof(PcgScalars), s));
+    if (el.allNeumann) {
+      cOnes.alloc(C.Nlocal);
+      launch_fill<T>(C.Nlocal, T(1), cOnes.p, s);
+      cSum.alloc(1);
+      cUnknowns = 0;
+      for (double w : C.gm.invDegree) cUnknowns += w;
+    }
     persistentCoarse = (C.N == 1) && o.coarse != "smooth" && o.coarsePersistent;
     if (persistentCoarse) {
       cPartials.alloc(6 * kCoarseGridMax);
@@ -431,6 +441,18 @@ template <typename T> struct MGImpl : public MGState {
       smooth_cheby4(v, r, x, xIsZero);
   }
 
+  // all-Neumann problems: the assembled coarse operator annihilates constants and
+  // the Krylov coarse solve needs a consistent right-hand side, so the rhs's
+  // mean over the assembled unknowns (invDegree-weighted E-vector mean) is
+  // removed first (the reference's BoomerAMG instead smooths on its coarsest
+  // level when told of the null space, hypreWrapper.cpp:143-147)
+  void project_coarse_rhs(MGLevelDev<T> &v, T *b)
+  {
+    const long long n = v.L->Nlocal;
+    launch_wdot<T>(n, v.invDegree.p, b, cOnes.p, cSum.p, el.red, 5, s);
+    launch_sub_mean<T>(n, cSum.p, cUnknowns, b, s);
+  }
+
   int coarse_pcg(MGLevelDev<T> &v, const T *b, T *x)
   {
     FieldLevel &L = *v.L;
@@ -439,6 +461,7 @@ template <typename T> struct MGImpl : public MGState {
         el.capture_split(); // a cooperative coarse solve is launched between the iteration's graph segments
         return 0;
       }
+      if (el.allNeumann) project_coarse_rhs(v, const_cast<T *>(b));
       coarse_pcg_persistent<T>(cA, b, x, cx.p, cz2.p, cz3.p, cPartials.p, cState.p, kCoarseGridMax,
                                el.opt.coarseTol, el.opt.coarseMaxIter, s);
       return 0;
@@ -447,6 +470,7 @@ template <typename T> struct MGImpl : public MGState {
     const Options &o = el.opt;
     const T *w = v.invDegree.p;
     PcgScalars *sc = csc.p;
+    if (el.allNeumann) project_coarse_rhs(v, const_cast<T *>(b));
     launch_fill<T>(n, T(0), x, s);
     NRSG_CUDA(cudaMemcpyAsync(cr.p, b, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
     launch_fill<T>(n, T(0), cp.p, s);

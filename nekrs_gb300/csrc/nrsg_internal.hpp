@@ -169,6 +169,7 @@ template <typename T> void launch_gs_mask(const GsPlan &P, T *q, bool mask, cuda
 void launch_accumulate(long long n, int m, const double *alpha, const double *X, double *y, cudaStream_t s);
 void launch_multi_scaled_sub(long long n, int m, const double *alpha, double *X, cudaStream_t s);
 void launch_scale_inplace(long long n, double a, double *x, cudaStream_t s);
+template <typename T> void launch_sub_mean(long long n, const double *sum, double denom, T *q, cudaStream_t s);
 // block (vector) Helmholtz, kernels_block.cu
 void launch_vgeo(int N, long long E, const double *VX, const double *gllz, const double *gllw, const double *D,
                  double *vgeo, cudaStream_t s);

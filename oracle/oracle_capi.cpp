@@ -92,6 +92,7 @@ long long orc_size(void *h, const char *name)
   if (s == "invDiag") return (long long)el->invDiag.size();
   if (s == "D") return (long long)L.D.size();
   if (s == "history") return (long long)el->history.size();
+  if (s == "allNeumann") return 1;
   return -1;
 }
 int orc_get(void *h, const char *name, void *out)
@@ -113,6 +114,7 @@ int orc_get(void *h, const char *name, void *out)
   if (s == "invDiag") return cp(el->invDiag);
   if (s == "D") return cp(L.D);
   if (s == "history") return cp(el->history);
+  if (s == "allNeumann") return cp(std::vector<double>{el->allNeumann ? 1.0 : 0.0});
   return -1;
 }
 double orc_volume(void *h) { return ((Elliptic *)h)->fine.volume; }

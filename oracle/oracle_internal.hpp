@@ -48,6 +48,8 @@ struct Elliptic {
   std::vector<double> invDiag;            // Jacobi preconditioner
   std::shared_ptr<MG> mg;
   std::vector<double> history;            // residual norm per iteration
+  bool allNeumann = false;                // Poisson with no Dirichlet face: constant null space
+  void zero_mean(double *q) const;
   int status = 0;                         // 0 ok, 1 max-iterations, 3 NaN
 
   void setup(int N, long long E, const double *VX, const long long *EToV, const int *EToB, const std::string &opt);

@@ -259,6 +259,7 @@ template <typename T> struct MGT {
   Options o;
   bool poisson = true;
   T lambda0 = 1, lambda1 = 0;
+  bool allNeumann = false;               // singular coarse system: project its right-hand side
   // coarse PCG scratch
   std::vector<T> cp, cz, cAp, cr;
   std::vector<int> coarseIters;
@@ -919,6 +920,17 @@ template <typename T> static int coarse_pcg(MGT<T> &M, MGLevel<T> &lv, const T *
   std::fill(x, x + n, T(0));
   std::memcpy(r, b, sizeof(T) * n);
   std::fill(p, p + n, T(0));
+  if (M.allNeumann) {
+    // all-Neumann: the assembled coarse operator annihilates constants; remove the rhs's component along
+    // them (its mean over the assembled unknowns) so that the Krylov solve sees a consistent system
+    double sw = 0, swb = 0;
+    for (long long i = 0; i < n; ++i) {
+      sw += (double)w[i];
+      swb += (double)w[i] * (double)r[i];
+    }
+    const T mean = (T)(swb / sw);
+    for (long long i = 0; i < n; ++i) r[i] -= mean;
+  }
   const double r0 = std::sqrt((double)wdot<T>(n, w, r, r));
   if (r0 == 0) return 0;
   const double tol = M.o.coarseTol * r0;
@@ -953,6 +965,12 @@ template <typename T> static int coarse_pcg_csr(MGT<T> &M, MGLevel<T> &lv, const
   const long long nr = (long long)M.gRowPtr.size() - 1, n = lv.L->Nlocal;
   std::vector<T> xr(nr, 0), r(nr), p(nr, 0), z(nr), Ap(nr);
   for (long long i = 0; i < nr; ++i) r[i] = b[M.gRep[i]];
+  if (M.allNeumann) {
+    double sr = 0;
+    for (long long i = 0; i < nr; ++i) sr += (double)r[i];
+    const T mean = (T)(sr / (double)nr);
+    for (long long i = 0; i < nr; ++i) r[i] -= mean;
+  }
   auto dot = [&](const std::vector<T> &a, const std::vector<T> &c) {
     double s = 0;
     for (long long i = 0; i < nr; ++i) s += (double)a[i] * (double)c[i];
@@ -1086,6 +1104,7 @@ template <typename T> static void build_mg(Elliptic &el, MGT<T> &M, MG &mg)
   const Options &o = el.o;
   M.o = o;
   M.poisson = o.poisson;
+  M.allNeumann = el.allNeumann;
   M.lambda0 = (T)o.lambda0;
   M.lambda1 = (T)o.lambda1;
   // smoother family

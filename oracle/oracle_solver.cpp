@@ -333,6 +333,13 @@ void Elliptic::setup(int N, long long E, const double *VX, const long long *EToV
 {
   o = parse_options(opt);
   build_level(fine, N, E, VX, EToV, EToB);
+  // ellipticSetup.cpp:187-205: a Poisson problem with no face other than Neumann (4) has a constant null space
+  allNeumann = false;
+  if (o.poisson) {
+    allNeumann = true;
+    for (long long i = 0; i < E * 6; ++i)
+      if (EToB[i] > 0 && EToB[i] != 4) allNeumann = false;
+  }
   if (o.precon == "jacobi") {
     invDiag.resize(fine.Nlocal);
     build_diag<double>(fine, fine.ggeo.data(), fine.D.data(), o.lambda0, o.lambda1, o.poisson, invDiag.data());
@@ -368,6 +375,17 @@ void Elliptic::precond(const double *r, double *z)
   } else {
     std::memcpy(z, r, sizeof(double) * n);
   }
+  if (allNeumann) zero_mean(z); // ellipticPreconditioner.cpp:82-83
+}
+
+// ellipticZeroMean (ellipticZeroMean.cpp:31-44): q -= sum(q) / (E Np)
+void Elliptic::zero_mean(double *q) const
+{
+  const long long n = fine.Nlocal;
+  double s = 0;
+  for (long long i = 0; i < n; ++i) s += q[i];
+  const double mean = s / (double)n;
+  for (long long i = 0; i < n; ++i) q[i] += -mean;
 }
 
 double Elliptic::norm(const double *r) const
@@ -532,6 +550,7 @@ int Elliptic::solve(double *r, double *x, double &res0, double &res)
   std::vector<double> Ax0(n), x0(x, x + n);
   ax(x, Ax0.data());
   for (long long i = 0; i < n; ++i) r[i] = -Ax0[i] + r[i];
+  if (allNeumann) zero_mean(r); // ellipticSolve.cpp:101
   apply_mask(fine, r);
   gs_add(fine, r);
   for (long long i = 0; i < n; ++i) x[i] = 0;
@@ -556,6 +575,7 @@ int Elliptic::solve(double *r, double *x, double &res0, double &res)
     iters = pgmres(r, x, tol, o.maxIter, res);
   if (o.projection) proj_post(x);
   for (long long i = 0; i < n; ++i) x[i] += x0[i];
+  if (allNeumann) zero_mean(x); // ellipticSolve.cpp:188-189
   if (std::isnan(res)) status = 3;
   else if (iters >= o.maxIter && res > tol) status = 1;
   return iters;

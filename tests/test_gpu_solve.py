@@ -192,3 +192,33 @@ def test_solve_ordered_with_callers_torch_stream(product_lib, torch_cuda):
     side.synchronize()
     assert info["iterations"] == ref["iterations"]
     assert np.array_equal(x2.cpu().numpy(), x_ref)
+
+
+@pytest.mark.parametrize("precon", ["jacobi", "multigrid"])
+def test_all_neumann_poisson_parity(product_lib, oracle_mod, torch_cuda, precon):
+    """Poisson with Neumann faces only (ellipticSetup.cpp:187-205): the constant null space is handled as the
+    reference does (ellipticZeroMean on r, on every preconditioned z and on x); parity with the oracle."""
+    torch = torch_cuda
+    N, n = 5, 4
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3, all_dirichlet=False)
+    if precon == "jacobi":
+        opts = "preconditioner=jacobi;solver=pcg;residualTol=1e-8+relative;maxIterations=3000"
+    else:
+        opts = ("solver=pfcg;residualTol=1e-8+relative;maxIterations=200;preconditioner=multigrid;"
+                "smootherType=fourthoptcheby+asm;pMGSchedule=p=5+degree=2,p=3+degree=2,p=1,p=3+degree=2,"
+                "p=5+degree=2;mgPrecision=fp64")
+    orc = O.Elliptic(N, VX, EToV, EToB, opts)
+    rhs = W.box_rhs(N, n, n, n, 3, orc.get("ggeo")) + 1e-3  # a right-hand side with a nonzero mean
+    xo, io = orc.solve(rhs)
+    el = G.Elliptic(N, VX, EToV, EToB, opts)
+    assert el.get("allNeumann")[0] == 1 and orc.get("allNeumann")[0] == 1
+    r = torch.from_numpy(rhs.copy()).cuda()
+    x = torch.zeros_like(r)
+    ig = el.solve(r, x)
+    torch.cuda.synchronize()
+    xg = x.cpu().numpy()
+    assert ig["status"] == 0 and io["status"] == 0
+    assert abs(ig["res0"] - io["res0"]) <= 1e-12 * io["res0"]
+    assert abs(ig["iterations"] - io["iterations"]) <= max(1, io["iterations"] // 100)
+    assert abs(xg.sum()) <= 1e-12 * np.abs(xg).sum()
+    assert rel(xg, xo) < 1e-7

@@ -164,3 +164,25 @@ def test_oracle_block_helmholtz_sanity(oracle_mod):
     rhs = np.concatenate([O.box_rhs(N, n, n, n, s, el.get("ggeo")) for s in (1, 2, 3)])
     _, info = el.block_solve(rhs, nf=3, stress=True, l0=1.0, l1=10.0, tol=1e-8)
     assert info["status"] == 0 and info["res"] <= 1e-8 * info["res0"]
+
+
+@pytest.mark.parametrize("precon", ["jacobi", "multigrid"])
+def test_oracle_all_neumann_null_space(oracle_mod, precon):
+    """All-Neumann Poisson (no Dirichlet face): the oracle detects the null space, removes the mean as
+    ellipticZeroMean does, converges, and returns a zero-mean solution of the projected system."""
+    N, n = 4, 3
+    VX, EToV, EToB = O.box_mesh(n, n, n, 0.3, all_dirichlet=False)
+    opts = (f"preconditioner={precon};solver=pfcg;residualTol=1e-10+relative;maxIterations=3000;"
+            "pMGSchedule=p=4+degree=2,p=1,p=4+degree=2;smootherType=cheby+asm;mgPrecision=fp64")
+    el = O.Elliptic(N, VX, EToV, EToB, opts)
+    assert el.get("allNeumann")[0] == 1
+    rhs = O.box_rhs(N, n, n, n, 5, el.get("ggeo")) + 1e-3
+    x, info = el.solve(rhs)
+    assert info["status"] == 0
+    assert abs(x.sum()) <= 1e-12 * np.abs(x).sum()
+    b = rhs - rhs.mean()
+    r = el.gs(b) - el.operator(x)
+    w = el.get("invDegree")
+    assert np.sqrt((w * r * r).sum() / el.volume) <= 1e-9 * info["res0"] * 10
+    dirichlet = O.Elliptic(N, VX, EToV, np.where(EToB > 0, 1, 0).astype(np.int32), opts)
+    assert dirichlet.get("allNeumann")[0] == 0
