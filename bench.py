@@ -316,7 +316,7 @@ def mg_options(N, tol="1e-8"):
 
 
 def run_batch(args):
-    """configs[3]: independent Poisson problems (cube side U{4..24}, N in {5,7,9}, eps U[0.3,1.0], seeded RHS),
+    """Batched solves: independent Poisson problems (cube side U{4..24}, N in {5,7,9}, eps U[0.3,1.0], seeded RHS),
     mixed-precision pMG-FPCG to 1e-8, solved one after another and as one batch stepped one Krylov iteration
     at a time (each problem on its own stream); DOF/s = sum of E*N^3 / wall time."""
     import torch
@@ -380,7 +380,7 @@ def run_batch(args):
 
 
 def run_serve(args):
-    """configs[4]: Poisson requests with exponential inter-arrival times (mean 2 ms) for `serve_seconds`;
+    """Serving loop: Poisson requests with exponential inter-arrival times (mean 2 ms) for `serve_seconds`;
     operators (E log-uniform in [2^9, 2^15], N in {3..9}, eps U[0.3,1.0]) come from a resident pool built
     before the clock starts; each request draws its tolerance from {1e-6, 1e-8, 1e-10} and a seeded RHS.
     Requests are admitted FIFO onto free resident handles while the device footprint of the operators in
