@@ -379,6 +379,93 @@ def run_batch(args):
                       "speedup_batched_vs_sequential": out["sequential"] / out["batched"]}))
 
 
+def run_velocity(args):
+    """Velocity Helmholtz step (the block solve next to the pressure solve): 3 fields on a Kershaw box E=32^3,
+    N=7, stress formulation with a variable viscosity field mu(x) and the mass coefficient h = rho bd0 / dt
+    (per-node fields, shared by the components), block Jacobi-PCG to 1e-6 relative (nekRS's velocity
+    defaults); DOF/s = 3 E N^3 / time-to-tolerance, CUDA events on the solver's stream."""
+    import torch
+    import nekrs_gb300 as G
+    from nekrs_gb300 import workloads as W
+
+    n, N = 32, 7
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    opts = ("solver=pcg+block;preconditioner=jacobi;residualTol=1e-6+relative;maxIterations=1000;poisson=0;"
+            "stressFormulation=true")
+    t0 = time.perf_counter()
+    el = G.Elliptic(N, VX, EToV, EToB, opts)
+    x, y, z = (torch.from_numpy(el.get(c)).cuda() for c in ("x", "y", "z"))
+    mu = 1.0 + 0.5 * torch.sin(3 * x) * torch.cos(2 * y) + 0.2 * z
+    h = torch.full_like(mu, 1.0 * 1.5 / 1e-3)  # rho bd0 / dt with BDF2 bd0 = 3/2, dt = 1e-3
+    el.set_coefficients(mu, h, 0)
+    setup_s = time.perf_counter() - t0
+    g = el.get("ggeo")
+    rhs = torch.from_numpy(np.concatenate([W.box_rhs(N, n, n, n, 500 + c, g) for c in range(3)])).cuda()
+    r, xs = torch.empty_like(rhs), torch.zeros_like(rhs)
+
+    def step():
+        r.copy_(rhs)
+        xs.zero_()
+        return el.solve(r, xs)
+
+    for _ in range(args.warmup):
+        step()
+    infos = [step() for _ in range(args.steps)]
+    t = float(np.mean([i["solve_ms"] for i in infos])) / 1e3
+    dofs = 3 * n ** 3 * N ** 3
+    print(json.dumps({"metric": "velocity Helmholtz DOFs/s (3 E N^3 / time-to-tolerance)", "value": dofs / t,
+                      "unit": "DOF/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": t * 1e3, "higher_is_better": True, "dtype": "f64",
+                      "data": "synthetic (seeded Kershaw box, U[-1,1] mass-weighted RHS per component)",
+                      "config": {"workload": "velocity", "elements": n ** 3, "N": N, "fields": 3,
+                                 "options": opts, "iterations": infos[-1]["iterations"], "setup_s": setup_s,
+                                 "status": infos[-1]["status"]}}))
+
+
+def run_projection(args):
+    """Pressure solves of a time-stepping caller: a sequence of right-hand sides that rotate slowly in a
+    two-dimensional space (E=32^3, N=7, the mixed-precision pMG-FPCG of the headline, 1e-8 absolute on the
+    first solve's residual scale), solved with and without the A-conjugate solution projection
+    (residualProjectionVectors 8, start 5): iterations and time per solve over the sequence."""
+    import torch
+    import nekrs_gb300 as G
+    from nekrs_gb300 import workloads as W
+
+    n, N, nsolve = 32, 7, 20
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    base = "solver=pfcg;maxIterations=400;" + PMG4 + ";mgPrecision=mixed"
+    probe = G.Elliptic(N, VX, EToV, EToB, base + ";residualTol=1e-8+relative")
+    g = probe.get("ggeo")
+    b1 = torch.from_numpy(W.box_rhs(N, n, n, n, 71, g)).cuda()
+    b2 = torch.from_numpy(W.box_rhs(N, n, n, n, 72, g)).cuda()
+    r, x = torch.empty_like(b1), torch.zeros_like(b1)
+    r.copy_(b1)
+    tol = 1e-8 * probe.solve(r, x)["res0"]
+    del probe
+    out = {}
+    for name, extra in (("none", ""), ("projectionAconj", ";initialGuess=projectionAconj;residualProjectionVectors=8;"
+                                                         "residualProjectionStart=5")):
+        el = G.Elliptic(N, VX, EToV, EToB, base + f";residualTol={tol}" + extra)
+        its, ms = [], []
+        for k in range(nsolve):
+            r.copy_(float(np.cos(0.1 * k)) * b1 + float(np.sin(0.1 * k)) * b2)
+            x.zero_()
+            info = el.solve(r, x)
+            its.append(info["iterations"])
+            ms.append(info["solve_ms"])
+        out[name] = {"iterations": its, "ms_per_solve": float(np.mean(ms[5:])), "iterations_after_start":
+                     float(np.mean(its[5:]))}
+        del el
+    dofs = n ** 3 * N ** 3
+    t = out["projectionAconj"]["ms_per_solve"] / 1e3
+    print(json.dumps({"metric": "Poisson DOFs/s over a solve sequence with solution projection", "value": dofs / t,
+                      "unit": "DOF/s", "n_gpus": 1, "steps": nsolve, "warmup": 0, "ms_per_step": t * 1e3,
+                      "higher_is_better": True, "dtype": "f64", "data": "synthetic (rotating seeded RHS pair)",
+                      "config": {"workload": "projection", "elements": n ** 3, "N": N, "absolute_tol": tol},
+                      "sequence": out,
+                      "speedup_vs_no_projection": out["none"]["ms_per_solve"] / out["projectionAconj"]["ms_per_solve"]}))
+
+
 def run_serve(args):
     """Serving loop: Poisson requests with exponential inter-arrival times (mean 2 ms) for `serve_seconds`;
     operators (E log-uniform in [2^9, 2^15], N in {3..9}, eps U[0.3,1.0]) come from a resident pool built
@@ -492,7 +579,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + ["batch", "serve"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
+                    choices=sorted(WORKLOADS) + ["batch", "serve", "velocity", "projection"])
     ap.add_argument("--batch-problems", type=int, default=64, help="problems in the batch workload (config: 256)")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window of the serve workload (config: 60)")
     ap.add_argument("--serve-pool", type=int, default=24, help="resident operators of the serve workload")
@@ -508,11 +596,12 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     args.workload_name = args.workload
-    if args.workload in ("batch", "serve"):
+    if args.workload in ("batch", "serve", "velocity", "projection"):
         import torch
 
         torch.cuda.set_device(dist_info()[2])
-        (run_batch if args.workload == "batch" else run_serve)(args)
+        {"batch": run_batch, "serve": run_serve, "velocity": run_velocity,
+         "projection": run_projection}[args.workload](args)
         return
     nel, N, eps, opts, desc = WORKLOADS[args.workload]
 
