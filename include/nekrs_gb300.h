@@ -82,7 +82,7 @@ long long nrsg_kernel_launches(void);
  * projectionAconj | projection: solution projection of
  * ellipticSolutionProjection.cpp, with residualProjectionVectors (8) and
  * residualProjectionStart (5)), cudaGraphs, nFields, stressFormulation,
- * axPipeline, coarseGridDiscretization (fem | fem+galerkin). */
+ * axPipeline, coarseGridDiscretization (fem | fem+galerkin | semfem). */
 int nrsg_elliptic_create(const nrsg_mesh_desc *mesh, const char *options, nrsg_elliptic **out);
 /* Block (vector) Helmholtz, the velocity solve (tombo.cpp:224-228): options
  * "solver = pcg+block" (or nFields = 2 | 3) and stressFormulation = true.
@@ -203,6 +203,17 @@ int nrsg_host_assemble_galerkin(int Nf, long long E, const long long *h_EToV, co
                                 const double *h_ggeo_fine, double lambda0, double lambda1, int poisson,
                                 long long *nrow, long long *nnz, long long *h_rowPtr, long long *h_cols,
                                 double *h_vals, long long *h_rowOfNode);
+
+/* SEMFEM operator (coarseGridDiscretization = SEMFEM; SEMFEMSolver_t::build,
+ * src/solvers/elliptic/SEMFEMSolverBuild.cpp:218-335, 551-700): linear
+ * tetrahedra (the eight corner tetrahedra of every sub-hexahedron of the
+ * order-N GLL grid) on the trilinear nodes of h_VX, lambda0 times the
+ * stiffness, accumulated in FP32 as the reference does; rows are the order-N
+ * level's masked gather groups.  Same calling convention as
+ * nrsg_host_assemble_operator. */
+int nrsg_host_assemble_semfem(int N, long long E, const double *h_VX, const long long *h_EToV, const int *h_EToB,
+                              double lambda0, long long *nrow, long long *nnz, long long *h_rowPtr, long long *h_cols,
+                              double *h_vals, long long *h_rowOfNode);
 
 /* ---- mesh ingestion: Nek5000 binary .re2 files (host only) --------------
  * Replaces the mesh read nekRS delegates to Nek5000 (src/io/re2Reader.cpp:4-41

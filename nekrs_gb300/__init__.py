@@ -63,6 +63,7 @@ def lib():
                                                    ctypes.c_int] + [vp] * 6)
         L.nrsg_host_assemble_galerkin.argtypes = ([ctypes.c_int, LL, vp, vp, vp, ctypes.c_double, ctypes.c_double,
                                                    ctypes.c_int] + [vp] * 6)
+        L.nrsg_host_assemble_semfem.argtypes = [ctypes.c_int, LL, vp, vp, vp, ctypes.c_double] + [vp] * 6
         L.nrsg_elliptic_create.argtypes = [ctypes.POINTER(MeshDesc), ctypes.c_char_p, ctypes.POINTER(vp)]
         L.nrsg_elliptic_destroy.argtypes = [vp]
         L.nrsg_elliptic_set_stream.argtypes = [vp, vp]
@@ -340,6 +341,24 @@ def host_assemble_galerkin(Nf, EToV, EToB, ggeo_fine, lambda0=1.0, lambda1=0.0, 
     vals = np.zeros(nnz.value)
     ron = np.zeros(E * 8, np.int64)
     check(lib().nrsg_host_assemble_galerkin(*a, rp.ctypes.data, cols.ctypes.data, vals.ctypes.data, ron.ctypes.data))
+    return rp, cols, vals, ron
+
+
+def host_assemble_semfem(N, VX, EToV, EToB, lambda0=1.0):
+    """SEMFEM operator (linear tetrahedra on the order-N GLL grid; host code of the library):
+    (rowPtr, cols, vals, rowOfNode)."""
+    VX = np.ascontiguousarray(VX, dtype=np.float64)
+    EToV = np.ascontiguousarray(EToV, dtype=np.int64)
+    EToB = np.ascontiguousarray(EToB, dtype=np.int32)
+    E = EToV.shape[0]
+    nrow, nnz = LL(0), LL(0)
+    a = (N, E, VX.ctypes.data, EToV.ctypes.data, EToB.ctypes.data, float(lambda0), ctypes.byref(nrow), ctypes.byref(nnz))
+    check(lib().nrsg_host_assemble_semfem(*a, None, None, None, None))
+    rp = np.zeros(nrow.value + 1, np.int64)
+    cols = np.zeros(nnz.value, np.int64)
+    vals = np.zeros(nnz.value)
+    ron = np.zeros(E * (N + 1) ** 3, np.int64)
+    check(lib().nrsg_host_assemble_semfem(*a, rp.ctypes.data, cols.ctypes.data, vals.ctypes.data, ron.ctypes.data))
     return rp, cols, vals, ron
 
 

@@ -1031,6 +1031,34 @@ int nrsg_host_assemble_galerkin(int Nf, long long E, const long long *h_EToV, co
   })
 }
 
+int nrsg_host_assemble_semfem(int N, long long E, const double *h_VX, const long long *h_EToV, const int *h_EToB,
+                              double lambda0, long long *nrow, long long *nnz, long long *h_rowPtr, long long *h_cols,
+                              double *h_vals, long long *h_rowOfNode)
+{
+  if (N < 1 || E < 1 || !h_VX || !h_EToV || !h_EToB || !nrow || !nnz) return NRSG_ERR_INVALID;
+  NRSG_TRY({
+    std::vector<long long> ids;
+    nrsg::nek_global_ids(N, E, h_EToV, ids);
+    nrsg::GatherMap um, gm;
+    nrsg::build_gather(ids, um);
+    std::vector<int> mask;
+    nrsg::dirichlet_nodes(N, E, h_EToB, um, mask);
+    for (int m : mask) ids[m] = 0;
+    nrsg::build_gather(ids, gm);
+    std::vector<double> z, w, X, Y, Z;
+    nrsg::gll_nodes(N, z, w);
+    nrsg::trilinear_nodes(N, E, h_VX, z, X, Y, Z);
+    nrsg::CsrMatrix A;
+    nrsg::semfem_assemble(N, E, X.data(), Y.data(), Z.data(), gm, mask, lambda0, A);
+    *nrow = A.nrow;
+    *nnz = A.rowPtr[A.nrow];
+    if (h_rowPtr) std::memcpy(h_rowPtr, A.rowPtr.data(), A.rowPtr.size() * sizeof(long long));
+    if (h_cols) std::memcpy(h_cols, A.col.data(), A.col.size() * sizeof(long long));
+    if (h_vals) std::memcpy(h_vals, A.val.data(), A.val.size() * sizeof(double));
+    if (h_rowOfNode) std::memcpy(h_rowOfNode, A.rowOfNode.data(), A.rowOfNode.size() * sizeof(long long));
+  })
+}
+
 // ---- kernel-level entry points --------------------------------------------
 int nrsg_ax_stored_f64(int N, long long E, const double *ggeo, const double *D, double l0, double l1, int poisson,
                        const double *q, double *Aq, void *s)

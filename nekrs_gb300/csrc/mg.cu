@@ -140,6 +140,9 @@ template <typename T> struct MGImpl : public MGState {
       for (double w : C.gm.invDegree) cUnknowns += w;
     }
     persistentCoarse = (C.N == 1) && o.coarse != "smooth" && o.coarsePersistent;
+    if ((o.galerkin || o.semfem) && !persistentCoarse)
+      throw Error(NRSG_ERR_BAD_CONFIG, "coarseGridDiscretization FEM+Galerkin / SEMFEM needs an order-1 coarsest level "
+                                       "solved on its assembled operator (coarseSolver = jpcg)");
     if (persistentCoarse) {
       cPartials.alloc(6 * kCoarseGridMax);
       cState.alloc(coarse_state_bytes());
@@ -186,12 +189,16 @@ template <typename T> struct MGImpl : public MGState {
     CsrMatrix A;
     if (el.opt.galerkin) {
       // B^T A_fine B from the finest level's FP32 operator (ellipticMultiGridSetup.cpp:260-261)
-      if (C.N != 1) throw Error(NRSG_ERR_BAD_CONFIG, "the Galerkin coarse operator needs an order-1 coarsest level");
       const std::vector<double> gf = el.fine.d_ggeo64.download();
       std::vector<double> Ae;
       galerkin_element_matrices(el.fine.N, el.fine.E, el.fine.Dh, el.fine.z, gf.data(), el.opt.lambda0,
                                 el.opt.lambda1, el.opt.poisson, Ae);
       assemble_rows(8, C.E, Ae, C.gm, A);
+    } else if (el.opt.semfem) {
+      // SEMFEMSolver_t on the coarsest level (ellipticMultiGridSetup.cpp:219-250)
+      std::vector<double> X, Y, Z;
+      trilinear_nodes(C.N, C.E, C.VXh.data(), C.z, X, Y, Z);
+      semfem_assemble(C.N, C.E, X.data(), Y.data(), Z.data(), C.gm, C.maskIds, el.opt.lambda0, A);
     } else {
       const std::vector<double> gg = C.d_ggeo64.download();
       assemble_level(C.N, C.E, C.Dh, gg.data(), el.opt.lambda0, el.opt.lambda1, el.opt.poisson, C.gm, A);

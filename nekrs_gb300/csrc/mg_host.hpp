@@ -36,6 +36,8 @@ struct CsrMatrix {
 void assemble_level(int N, long long E, const std::vector<double> &Dh, const double *ggeo, double lam0, double lam1,
                     bool poisson, const GatherMap &gm, CsrMatrix &A);
 void assemble_rows(int np, long long E, const std::vector<double> &Ae, const GatherMap &gm, CsrMatrix &A);
+void semfem_assemble(int N, long long E, const double *x, const double *y, const double *z, const GatherMap &gm,
+                     const std::vector<int> &maskIds, double lam0, CsrMatrix &A);
 void galerkin_element_matrices(int Nf, long long E, const std::vector<double> &Dh, const std::vector<double> &z,
                                const double *ggeo, double lam0, double lam1, bool poisson, std::vector<double> &Ae);
 

@@ -655,4 +655,117 @@ void galerkin_element_matrices(int Nf, long long E, const std::vector<double> &D
   }
 }
 
+// SEMFEM operator (SEMFEMSolver_t::build, src/solvers/elliptic/
+// SEMFEMSolverBuild.cpp:218-335 with fem_assembly_host :551-700): the
+// linear-tetrahedron Poisson stiffness on the level's GLL sub-grid. Every
+// sub-hexahedron of every element is covered by its eight corner tetrahedra
+// (mesh_connectivity :859-940: each corner and its three edge neighbours), each
+// integrated with the 4-point rule of weight 1/24 (:12-34) using the signed
+// Jacobian determinant of the corner map; lambda0 scales everything (the
+// reference takes the first entry of its coefficient, no mass term). Entries
+// between unmasked nodes accumulate in FP32 in the reference's loop order
+// (element, sub-hex z / y / x, tetrahedron, i, j); rows are the level's masked
+// gather groups.
+void semfem_assemble(int N, long long E, const double *x, const double *y, const double *z, const GatherMap &gm,
+                     const std::vector<int> &maskIds, double lam0, CsrMatrix &A)
+{
+  const int nq = N + 1, np = nq * nq * nq;
+  static const int vc[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {1, 1, 0}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+  static const int tm[8][4] = {{0, 2, 1, 4}, {1, 0, 3, 5}, {2, 6, 3, 0}, {3, 2, 7, 1},
+                               {4, 5, 6, 0}, {5, 7, 4, 1}, {6, 7, 2, 4}, {7, 3, 6, 5}};
+  static const double dphi[4][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {-1, -1, -1}};
+  A.nrow = (long long)gm.off.size() - 1;
+  A.rowOfNode.assign((size_t)E * np, -1);
+  for (long long g = 0; g < A.nrow; ++g)
+    for (int q = gm.off[g]; q < gm.off[g + 1]; ++q) A.rowOfNode[gm.ids[q]] = g;
+  // element-interior nodes carry no global id (they are gathered with nothing) but are unknowns of the
+  // SEMFEM system (the reference numbers every unmasked node): one row each, after the shared rows
+  std::vector<char> masked((size_t)E * np, 0);
+  for (int m : maskIds) masked[m] = 1;
+  for (long long i = 0; i < E * np; ++i)
+    if (A.rowOfNode[i] < 0 && !masked[i]) A.rowOfNode[i] = A.nrow++;
+  std::vector<std::vector<std::pair<long long, float>>> rows(A.nrow);
+  for (long long e = 0; e < E; ++e)
+    for (int sz = 0; sz < nq - 1; ++sz)
+      for (int sy = 0; sy < nq - 1; ++sy)
+        for (int sx = 0; sx < nq - 1; ++sx) {
+          int idx[8];
+          for (int v = 0; v < 8; ++v) idx[v] = (sx + vc[v][0]) + (sy + vc[v][1]) * nq + (sz + vc[v][2]) * nq * nq;
+          for (int t = 0; t < 8; ++t) {
+            double xt[3][4];
+            for (int k = 0; k < 4; ++k) {
+              const long long node = e * np + idx[tm[t][k]];
+              xt[0][k] = x[node];
+              xt[1][k] = y[node];
+              xt[2][k] = z[node];
+            }
+            double J[3][3];
+            for (int a = 0; a < 3; ++a)
+              for (int b = 0; b < 3; ++b) {
+                J[a][b] = 0.0;
+                for (int k = 0; k < 4; ++k) J[a][b] += xt[a][k] * dphi[k][b];
+              }
+            const double det = J[0][0] * (J[1][1] * J[2][2] - J[2][1] * J[1][2]) -
+                               J[0][1] * (J[1][0] * J[2][2] - J[2][0] * J[1][2]) +
+                               J[0][2] * (J[1][0] * J[2][1] - J[2][0] * J[1][1]);
+            const double id = 1.0 / det;
+            double Ji[3][3];
+            Ji[0][0] = id * (J[1][1] * J[2][2] - J[2][1] * J[1][2]);
+            Ji[0][1] = id * (J[0][2] * J[2][1] - J[2][2] * J[0][1]);
+            Ji[0][2] = id * (J[0][1] * J[1][2] - J[1][1] * J[0][2]);
+            Ji[1][0] = id * (J[1][2] * J[2][0] - J[2][2] * J[1][0]);
+            Ji[1][1] = id * (J[0][0] * J[2][2] - J[2][0] * J[0][2]);
+            Ji[1][2] = id * (J[0][2] * J[1][0] - J[1][2] * J[0][0]);
+            Ji[2][0] = id * (J[1][0] * J[2][1] - J[2][0] * J[1][1]);
+            Ji[2][1] = id * (J[0][1] * J[2][0] - J[2][1] * J[0][0]);
+            Ji[2][2] = id * (J[0][0] * J[1][1] - J[1][0] * J[0][1]);
+            // the integrand is constant on a tetrahedron: each of the 4 points adds the same term
+            double Al[4][4] = {};
+            for (int q = 0; q < 4; ++q)
+              for (int i = 0; i < 4; ++i)
+                for (int j = 0; j < 4; ++j) {
+                  double f = 0.0;
+                  for (int al = 0; al < 3; ++al) {
+                    double a = 0.0, b = 0.0;
+                    for (int be = 0; be < 3; ++be) {
+                      a += dphi[i][be] * Ji[be][al];
+                      b += dphi[j][be] * Ji[be][al];
+                    }
+                    f += a * b;
+                  }
+                  Al[i][j] += f * det * (1.0 / 24.0);
+                }
+            for (int i = 0; i < 4; ++i)
+              for (int j = 0; j < 4; ++j) {
+                const long long r = A.rowOfNode[e * np + idx[tm[t][i]]], c = A.rowOfNode[e * np + idx[tm[t][j]]];
+                if (r < 0 || c < 0) continue;
+                auto &row = rows[r];
+                size_t k = 0;
+                while (k < row.size() && row[k].first != c) ++k;
+                if (k == row.size()) row.push_back({c, 0.0f});
+                row[k].second += lam0 * Al[i][j];
+              }
+          }
+        }
+  A.rowPtr.assign(A.nrow + 1, 0);
+  for (long long r = 0; r < A.nrow; ++r) {
+    auto &row = rows[r];
+    std::sort(row.begin(), row.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
+    long long kept = 0;
+    for (auto &p : row) kept += std::fabs((double)p.second) > 0.0;
+    A.rowPtr[r + 1] = A.rowPtr[r] + kept;
+  }
+  A.col.resize(A.rowPtr[A.nrow]);
+  A.val.resize(A.rowPtr[A.nrow]);
+  for (long long r = 0; r < A.nrow; ++r) {
+    long long t = A.rowPtr[r];
+    for (auto &p : rows[r])
+      if (std::fabs((double)p.second) > 0.0) {
+        A.col[t] = p.first;
+        A.val[t] = p.second;
+        ++t;
+      }
+  }
+}
+
 } // namespace nrsg

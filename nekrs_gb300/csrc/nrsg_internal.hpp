@@ -99,6 +99,7 @@ struct Options {
   std::string schedule;
   std::string coarse = "jpcg";
   bool galerkin = false;            // coarseGridDiscretization = FEM+Galerkin: B^T A_fine B on the order-1 level
+  bool semfem = false;              // coarseGridDiscretization = SEMFEM: linear tetrahedra on the coarse GLL grid
   double coarseTol = 1e-4;
   int coarseMaxIter = 200;
   bool coarsePersistent = true;     // order-1 coarse Jacobi-PCG as one cooperative kernel

@@ -397,9 +397,10 @@ Options parse_options(const char *text)
       else if (key == "pmgschedule") o.schedule = v;
       else if (key == "coarsesolver") o.coarse = v;
       else if (key == "coarsegriddiscretization") {
-        if (v == "fem+galerkin" || v == "galerkin") o.galerkin = true;
-        else if (v == "fem") o.galerkin = false;
-        else throw Error(NRSG_ERR_BAD_CONFIG, "coarseGridDiscretization '" + v + "' (fem | fem+galerkin)");
+        o.galerkin = (v == "fem+galerkin" || v == "galerkin");
+        o.semfem = (v == "semfem");
+        if (!o.galerkin && !o.semfem && v != "fem")
+          throw Error(NRSG_ERR_BAD_CONFIG, "coarseGridDiscretization '" + v + "' (fem | fem+galerkin | semfem)");
       } else if (key == "galerkincoarseoperator") o.galerkin = (v == "true" || v == "1" || v == "yes");
       else if (key == "coarsetol") o.coarseTol = std::stod(v);
       else if (key == "coarsemaxiterations") o.coarseMaxIter = std::stoi(v);

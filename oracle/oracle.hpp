@@ -36,6 +36,7 @@ struct Options {
   double coarseTol = 1e-4;
   int coarseMaxIter = 200;
   bool galerkin = false;                 // coarseGridDiscretization = FEM+Galerkin
+  bool semfem = false;                   // coarseGridDiscretization = SEMFEM
   std::string mgPrecision = "fp64";      // fp64 | fp32
   bool poisson = true;
   double lambda0 = 1.0, lambda1 = 0.0;

@@ -62,6 +62,7 @@ def lib():
         _lib.orc_interp.argtypes = [ctypes.c_int, ctypes.c_int, D]
         vp, ci, cd, cl = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_longlong
         _lib.orc_assemble_galerkin.argtypes = [vp, vp, cd, cd, ci] + [vp] * 5
+        _lib.orc_assemble_semfem.argtypes = [vp, cd] + [vp] * 5
         _lib.orc_block_vgeo.argtypes = [vp, vp]
         _lib.orc_block_ax.argtypes = [vp, ci, ci, ci, cl, vp, vp, cd, cd, vp, vp]
         _lib.orc_block_diag.argtypes = [vp, ci, ci, cl, vp, vp, cd, cd, vp]
@@ -263,6 +264,17 @@ class Elliptic:
         vals = np.zeros(nnz.value)
         lib().orc_assemble_fem(*a, rp.ctypes.data_as(ctypes.c_void_p), cols.ctypes.data_as(ctypes.c_void_p),
                                vals.ctypes.data_as(ctypes.c_void_p))
+        return rp, cols, vals
+
+    def assemble_semfem(self, lambda0=1.0):
+        """SEMFEM operator of this level (linear tetrahedra on its GLL grid), CSR."""
+        nrow, nnz = ctypes.c_longlong(0), ctypes.c_longlong(0)
+        a = (self.h, float(lambda0), ctypes.byref(nrow), ctypes.byref(nnz))
+        lib().orc_assemble_semfem(*a, None, None, None)
+        rp = np.zeros(nrow.value + 1, np.int64)
+        cols = np.zeros(nnz.value, np.int64)
+        vals = np.zeros(nnz.value)
+        lib().orc_assemble_semfem(*a, rp.ctypes.data, cols.ctypes.data, vals.ctypes.data)
         return rp, cols, vals
 
     def assemble_galerkin(self, coarse, lambda0=1.0, lambda1=0.0, poisson=True):

@@ -182,6 +182,20 @@ void orc_assemble_fem(void *h, double lambda0, double lambda1, int poisson, long
   std::memcpy(vals, v.data(), v.size() * sizeof(double));
 }
 
+void orc_assemble_semfem(void *h, double lambda0, long long *nrow, long long *nnz, long long *rowPtr, long long *cols,
+                         double *vals)
+{
+  std::vector<long long> rp, c;
+  std::vector<double> v;
+  assemble_semfem(((Elliptic *)h)->fine, lambda0, rp, c, v);
+  *nrow = (long long)rp.size() - 1;
+  *nnz = (long long)c.size();
+  if (!rowPtr) return;
+  std::memcpy(rowPtr, rp.data(), rp.size() * sizeof(long long));
+  std::memcpy(cols, c.data(), c.size() * sizeof(long long));
+  std::memcpy(vals, v.data(), v.size() * sizeof(double));
+}
+
 void orc_assemble_galerkin(void *hFine, void *hCoarse, double lambda0, double lambda1, int poisson, long long *nrow,
                            long long *nnz, long long *rowPtr, long long *cols, double *vals)
 {

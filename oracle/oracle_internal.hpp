@@ -37,6 +37,8 @@ template <typename T> T wdot(long long n, const T *w, const T *a, const T *b);
 
 void assemble_fem(const Level &L, double lambda0, double lambda1, bool poisson, std::vector<long long> &rowPtr,
                   std::vector<long long> &cols, std::vector<double> &vals);
+void assemble_semfem(const Level &L, double lambda0, std::vector<long long> &rowPtr, std::vector<long long> &cols,
+                     std::vector<double> &vals);
 void assemble_galerkin(const Level &F, const Level &C, double lambda0, double lambda1, bool poisson,
                        std::vector<long long> &rowPtr, std::vector<long long> &cols, std::vector<double> &vals);
 

@@ -1016,7 +1016,7 @@ template <typename T> static void vcycle(MGT<T> &M, int k)
   if (k == base) {
     if (M.o.coarse == "smooth")
       smooth(M, lv, lv.rhs.data(), lv.x.data(), true);
-    else if (M.o.galerkin)
+    else if (M.o.galerkin || M.o.semfem)
       coarse_pcg_csr(M, lv, lv.rhs.data(), lv.x.data());
     else
       coarse_pcg(M, lv, lv.rhs.data(), lv.x.data());
@@ -1163,11 +1163,14 @@ template <typename T> static void build_mg(Elliptic &el, MGT<T> &M, MG &mg)
       for (auto &v : lv.invDiag) v = (T)1 / v;
     }
   }
-  if (o.galerkin) {
+  if (o.galerkin || o.semfem) {
     const Level &C = *M.levels.back().L;
-    if (C.N != 1) throw std::runtime_error("the Galerkin coarse operator needs an order-1 coarsest level");
+    if (C.N != 1) throw std::runtime_error("the Galerkin / SEMFEM coarse operator needs an order-1 coarsest level");
     std::vector<double> vals;
-    assemble_galerkin(el.fine, C, (double)M.lambda0, (double)M.lambda1, M.poisson, M.gRowPtr, M.gCol, vals);
+    if (o.semfem)
+      assemble_semfem(C, (double)M.lambda0, M.gRowPtr, M.gCol, vals);
+    else
+      assemble_galerkin(el.fine, C, (double)M.lambda0, (double)M.lambda1, M.poisson, M.gRowPtr, M.gCol, vals);
     const long long nr = (long long)M.gRowPtr.size() - 1;
     M.gVal.assign(vals.begin(), vals.end());
     M.gInvDiag.assign(nr, T(0));

@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <map>
 #include <cstdio>
 #include <cstring>
 #include <sstream>
@@ -70,7 +71,10 @@ Options parse_options(const std::string &text)
     else if (key == "maxeigenvalueboundfactor") o.maxEigFactor = std::stod(lv);
     else if (key == "pmgschedule") o.schedule = lv;
     else if (key == "coarsesolver") o.coarse = lv;
-    else if (key == "coarsegriddiscretization") o.galerkin = (lv == "fem+galerkin" || lv == "galerkin");
+    else if (key == "coarsegriddiscretization") {
+      o.galerkin = (lv == "fem+galerkin" || lv == "galerkin");
+      o.semfem = (lv == "semfem");
+    }
     else if (key == "galerkincoarseoperator") o.galerkin = (lv == "true" || lv == "1" || lv == "yes");
     else if (key == "coarsetol") o.coarseTol = std::stod(lv);
     else if (key == "coarsemaxiterations") o.coarseMaxIter = std::stoi(lv);
@@ -825,6 +829,100 @@ void assemble_galerkin(const Level &F, const Level &C, double lambda0, double la
     cols.push_back(nz[i].col);
     vals.push_back(nz[i].val);
     rowPtr[nz[i].row + 1]++;
+  }
+  for (long long r = 0; r < ng; ++r) rowPtr[r + 1] += rowPtr[r];
+}
+
+// ---------------------------------------------------------------------------
+// SEMFEM operator, following SEMFEMSolver_t::build / fem_assembly_host
+// (src/solvers/elliptic/SEMFEMSolverBuild.cpp:218-335, 551-700): on every
+// sub-hexahedron of the level's GLL grid the eight corner tetrahedra
+// (mesh_connectivity :859-940), P1 stiffness by the 4-point rule (weights
+// 1/24, :12-34) with the signed determinant of the tetrahedron map,
+// lambda0 * A_loc added in FP32 entry by entry in the loop order element,
+// sub-hex (z, y, x), tetrahedron, i, j; exact zeros dropped (dropTol 0).
+// ---------------------------------------------------------------------------
+void assemble_semfem(const Level &L, double lambda0, std::vector<long long> &rowPtr, std::vector<long long> &cols,
+                     std::vector<double> &vals)
+{
+  const int nq = L.Nq, np = L.Np;
+  const int corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {1, 1, 0}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+  const int tet[8][4] = {{0, 2, 1, 4}, {1, 0, 3, 5}, {2, 6, 3, 0}, {3, 2, 7, 1},
+                         {4, 5, 6, 0}, {5, 7, 4, 1}, {6, 7, 2, 4}, {7, 3, 6, 5}};
+  // reference-tetrahedron basis gradients: r, s, t, 1 - r - s - t
+  const double grad[4][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {-1, -1, -1}};
+  std::vector<long long> num(L.Nlocal, -1);
+  long long ng = (long long)L.gsOff.size() - 1;
+  for (long long g = 0; g < ng; ++g)
+    for (int t = L.gsOff[g]; t < L.gsOff[g + 1]; ++t) num[L.gsIds[t]] = g;
+  // every unmasked node is an unknown (matrix_distribution :337-420 ranks all of them); element-interior
+  // nodes, which no gather group holds, follow the shared ones in E-vector order
+  std::vector<char> isMasked(L.Nlocal, 0);
+  for (int m : L.maskIds) isMasked[m] = 1;
+  for (long long i = 0; i < L.Nlocal; ++i)
+    if (num[i] < 0 && !isMasked[i]) num[i] = ng++;
+  std::map<std::pair<long long, long long>, float> entries;
+  for (long long e = 0; e < L.E; ++e)
+    for (int sz = 0; sz + 1 < nq; ++sz)
+      for (int sy = 0; sy + 1 < nq; ++sy)
+        for (int sx = 0; sx + 1 < nq; ++sx)
+          for (int t = 0; t < 8; ++t) {
+            long long node[4];
+            double X[3][4];
+            for (int k = 0; k < 4; ++k) {
+              const int *c = corner[tet[t][k]];
+              node[k] = e * np + (sx + c[0]) + nq * ((sy + c[1]) + nq * (sz + c[2]));
+              X[0][k] = L.x[node[k]];
+              X[1][k] = L.y[node[k]];
+              X[2][k] = L.zc[node[k]];
+            }
+            double J[3][3];
+            for (int a = 0; a < 3; ++a)
+              for (int b = 0; b < 3; ++b) {
+                J[a][b] = 0;
+                for (int k = 0; k < 4; ++k) J[a][b] += X[a][k] * grad[k][b];
+              }
+            const double det = J[0][0] * (J[1][1] * J[2][2] - J[2][1] * J[1][2]) -
+                               J[0][1] * (J[1][0] * J[2][2] - J[2][0] * J[1][2]) +
+                               J[0][2] * (J[1][0] * J[2][1] - J[2][0] * J[1][1]);
+            const double inv = 1.0 / det;
+            const double Ji[3][3] = {{inv * (J[1][1] * J[2][2] - J[2][1] * J[1][2]), inv * (J[0][2] * J[2][1] - J[2][2] * J[0][1]),
+                                      inv * (J[0][1] * J[1][2] - J[1][1] * J[0][2])},
+                                     {inv * (J[1][2] * J[2][0] - J[2][2] * J[1][0]), inv * (J[0][0] * J[2][2] - J[2][0] * J[0][2]),
+                                      inv * (J[0][2] * J[1][0] - J[1][2] * J[0][0])},
+                                     {inv * (J[1][0] * J[2][1] - J[2][0] * J[1][1]), inv * (J[0][1] * J[2][0] - J[2][1] * J[0][0]),
+                                      inv * (J[0][0] * J[1][1] - J[1][0] * J[0][1])}};
+            double Aloc[4][4] = {};
+            for (int q = 0; q < 4; ++q)
+              for (int i = 0; i < 4; ++i)
+                for (int j = 0; j < 4; ++j) {
+                  double f = 0;
+                  for (int al = 0; al < 3; ++al) {
+                    double a = 0, b = 0;
+                    for (int be = 0; be < 3; ++be) {
+                      a += grad[i][be] * Ji[be][al];
+                      b += grad[j][be] * Ji[be][al];
+                    }
+                    f += a * b;
+                  }
+                  Aloc[i][j] += f * det * (1.0 / 24.0);
+                }
+            for (int i = 0; i < 4; ++i)
+              for (int j = 0; j < 4; ++j) {
+                const long long r = num[node[i]], c = num[node[j]];
+                if (r < 0 || c < 0) continue;
+                float &v = entries[{r, c}];
+                v += lambda0 * Aloc[i][j];
+              }
+          }
+  rowPtr.assign(ng + 1, 0);
+  cols.clear();
+  vals.clear();
+  for (const auto &kv : entries) {
+    if (!(std::fabs((double)kv.second) > 0.0)) continue;
+    cols.push_back(kv.first.second);
+    vals.push_back(kv.second);
+    rowPtr[kv.first.first + 1]++;
   }
   for (long long r = 0; r < ng; ++r) rowPtr[r + 1] += rowPtr[r];
 }

@@ -111,3 +111,37 @@ def test_oracle_mg_with_galerkin_coarse_converges(oracle_mod):
         assert info["status"] == 0 and info["res"] <= 1e-8 * info["res0"]
         its[g] = info["iterations"]
     assert abs(its["fem"] - its["fem+galerkin"]) <= 3, its
+
+
+@pytest.mark.parametrize("N,n,eps", [(1, 4, 0.3), (1, 3, 1.0), (3, 3, 0.5), (7, 2, 1.0)])
+def test_semfem_operator_matches_oracle(product_lib, oracle_mod, N, n, eps):
+    """coarseGridDiscretization = SEMFEM: the library's linear-tetrahedron operator on the GLL grid equals
+    the oracle's restatement of SEMFEMSolver_t::build (FP32 accumulation in the reference's loop order) up to
+    rounding residues of exact zeros (their node coordinates are interpolated by different code)."""
+    VX, EToV, EToB = W.kershaw_box(n, eps=eps)
+    orc = O.Elliptic(N, VX, EToV, EToB, "preconditioner=none")
+    rp, cols, vals = orc.assemble_semfem(1.3)
+    prp, pcols, pvals, ron = G.host_assemble_semfem(N, VX, EToV, EToB, 1.3)
+    A, P = sp.csr_matrix((vals, cols, rp)), sp.csr_matrix((pvals, pcols, prp))
+    assert A.shape == P.shape
+    assert abs(A - P).max() <= 1e-6 * abs(A).max()  # FP32 entries
+    if N == 1:
+        assert np.array_equal(rp, prp) and np.array_equal(cols, pcols) and np.array_equal(vals, pvals)
+    # symmetric with a positive diagonal; without a mask the constants are in its kernel
+    assert abs(A - A.T).max() <= 1e-6 * abs(A).max()
+    assert (P.diagonal() > 0).all()
+    assert ron.shape[0] == orc.Nlocal
+    nrp, ncols, nvals, _ = G.host_assemble_semfem(N, VX, EToV, np.zeros_like(EToB), 1.3)
+    Pn = sp.csr_matrix((nvals, ncols, nrp))
+    assert np.abs(Pn @ np.ones(Pn.shape[0])).max() <= 1e-5 * abs(Pn).max()
+
+
+def test_oracle_mg_with_semfem_coarse_converges(oracle_mod):
+    VX, EToV, EToB = W.kershaw_box(4, eps=0.3)
+    opts = ("solver=pfcg;residualTol=1e-8+relative;maxIterations=200;preconditioner=multigrid;"
+            "smootherType=fourthoptcheby+asm;pMGSchedule=p=5+degree=2,p=3+degree=2,p=1,p=3+degree=2,p=5+degree=2;"
+            "mgPrecision=fp64;coarseGridDiscretization=semfem")
+    el = O.Elliptic(5, VX, EToV, EToB, opts)
+    x, info = el.solve(W.box_rhs(5, 4, 4, 4, 3, el.get("ggeo")))
+    assert info["status"] == 0 and info["res"] <= 1e-8 * info["res0"]
+    assert info["iterations"] <= 15

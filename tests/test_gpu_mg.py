@@ -213,12 +213,14 @@ def test_fdm_entry_point_matches_smoother(product_lib, torch_cuda, N):
     assert np.array_equal(out.astype(np.float64), ref.cpu().numpy())
 
 
+@pytest.mark.parametrize("disc", ["fem+galerkin", "semfem"])
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
-def test_mg_galerkin_coarse_operator_parity(product_lib, oracle_mod, torch_cuda, prec):
-    """coarseGridDiscretization = FEM+Galerkin: the persistent coarse Jacobi-PCG runs on B^T A_fine B
-    (built on the host, bit-identical to the oracle's); the V-cycle solve matches the oracle's."""
+def test_mg_galerkin_coarse_operator_parity(product_lib, oracle_mod, torch_cuda, prec, disc):
+    """coarseGridDiscretization = FEM+Galerkin (B^T A_fine B) or SEMFEM (linear tetrahedra on the order-1
+    grid): the persistent coarse Jacobi-PCG runs on the operator built on the host (equal to the oracle's);
+    the V-cycle solve matches the oracle's."""
     opts = (f"solver=pfcg;preconditioner=multigrid;smootherType=fourthoptcheby+asm;mgPrecision={prec};"
-            f"residualTol=1e-8+relative;maxIterations=200;pMGSchedule={SCHED[5]};coarseGridDiscretization=fem+galerkin")
+            f"residualTol=1e-8+relative;maxIterations=200;pMGSchedule={SCHED[5]};coarseGridDiscretization={disc}")
     orc, el, xo, io, xg, ig, _ = solve_both(torch_cuda, 5, 4, opts)
     assert ig["status"] == 0 and io["status"] == 0
     assert abs(ig["iterations"] - io["iterations"]) <= 1
