@@ -121,7 +121,9 @@ int nrsg_elliptic_set_tolerance(nrsg_elliptic *el, double tol, int relative, int
  * = 1 (with *info filled and the solve's status returned) when the solve has
  * finished.  One solve per handle at a time.  Handles on different streams
  * advance concurrently (nrsg_elliptic_solve_batch, serving loops).  No
- * reference counterpart (ellipticSolve is blocking). */
+ * reference counterpart (ellipticSolve is blocking).  With solution
+ * projection (initialGuess = projection*) the advance() that finishes a solve
+ * waits for the basis update, which reads its Gram-Schmidt coefficients. */
 int nrsg_elliptic_solve_begin(nrsg_elliptic *el, double *d_r, double *d_x);
 int nrsg_elliptic_solve_advance(nrsg_elliptic *el, int *done, nrsg_solve_info *info);
 /* n independent solves, each on its own handle (and stream), stepped together
