@@ -21,6 +21,7 @@ OUT = os.path.join(HERE, "_ref")
 AX_ORDERS = [1, 2, 3, 4, 5, 6, 7, 8, 9]
 TRANSFER_PAIRS = [(2, 1), (3, 1), (5, 3), (7, 3), (7, 5), (9, 5), (5, 1), (4, 2), (6, 3), (9, 7)]
 FDM_ORDERS = [1, 2, 3, 4, 5, 6, 7, 8, 9]
+BLOCK_ORDERS = [1, 3, 5, 7]
 
 
 def _common(dfloat, pfloat):
@@ -37,7 +38,8 @@ def _undef():
     names = ["FUNC", "dlong", "hlong", "dfloat", "pfloat", "p_blockSize", "p_Nq", "p_Np", "p_Nggeo",
              "p_G00ID", "p_G01ID", "p_G02ID", "p_G11ID", "p_G12ID", "p_G22ID", "p_GWJID", "p_lambda",
              "p_poisson", "p_knl", "p_NqFine", "p_NqCoarse", "p_NpFine", "p_NpCoarse", "p_Nq_e",
-             "p_Np_e", "p_restrict", "p_Nfields"]
+             "p_Np_e", "p_restrict", "p_Nfields", "p_Nvgeo", "p_RXID", "p_RYID", "p_RZID", "p_SXID", "p_SYID",
+             "p_SZID", "p_TXID", "p_TYID", "p_TZID", "p_JWID"]
     return [f"#undef {n}" for n in names]
 
 
@@ -88,6 +90,22 @@ def wrappers(ref):
                 units.append("\n".join(base + [f"#define p_restrict {r}",
                                                f"#define FUNC(a) ref_fdm{'r' if r else 'a'}_{prec}_N{N}",
                                                f'#include "{os.path.join(ke, "fusedFDM.c")}"'] + _undef()))
+    # block (3-field) and stress (symmetric-gradient) axhelm, scalar (p_lambda 0) and field coefficients
+    for N in BLOCK_ORDERS:
+        for lam in (0, 1):
+            units.append("\n".join(_common("double", "float") + [
+                f"#define FUNC(a) ref_block_l{lam}_N{N}", "#define p_knl 0",
+                f"#define p_Nq {N + 1}", f"#define p_Np {(N + 1) ** 3}", "#define p_Nggeo 7",
+                "#define p_G00ID 0", "#define p_G01ID 1", "#define p_G11ID 2", "#define p_G12ID 3",
+                "#define p_G02ID 4", "#define p_G22ID 5", "#define p_GWJID 6", f"#define p_lambda {lam}",
+                f'#include "{os.path.join(ke, "ellipticBlockPartialAxCoeffHex3D.c")}"'] + _undef()))
+            units.append("\n".join(_common("double", "float") + [
+                f"#define FUNC(a) ref_stress_l{lam}_N{N}", "#define p_knl 0",
+                f"#define p_Nq {N + 1}", f"#define p_Np {(N + 1) ** 3}", "#define p_Nvgeo 12",
+                "#define p_RXID 0", "#define p_RYID 1", "#define p_RZID 2", "#define p_SXID 3", "#define p_SYID 4",
+                "#define p_SZID 5", "#define p_TXID 6", "#define p_TYID 7", "#define p_TZID 8", "#define p_JWID 10",
+                f"#define p_lambda {lam}",
+                f'#include "{os.path.join(ke, "ellipticStressPartialAxCoeffHex3D.c")}"'] + _undef()))
     # fused PCG residual update
     units.append("\n".join(_common("double", "float") + [
         "#define p_Nfields 1", "#define FUNC(a) ref_update_pcg",

@@ -186,3 +186,45 @@ def test_oracle_all_neumann_null_space(oracle_mod, precon):
     assert np.sqrt((w * r * r).sum() / el.volume) <= 1e-9 * info["res0"] * 10
     dirichlet = O.Elliptic(N, VX, EToV, np.where(EToB > 0, 1, 0).astype(np.int32), opts)
     assert dirichlet.get("allNeumann")[0] == 0
+
+
+def _ref_block(kind, lam, N, E, geo, D, q, l0, l1, loffset):
+    import ctypes
+
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    f = getattr(O.ref_lib(), f"ref_{kind}_l{lam}_N{N}")
+    Nq = N + 1
+    DT = np.ascontiguousarray(D.reshape(Nq, Nq).T).ravel()
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    out = np.zeros_like(q)
+    el = np.arange(E, dtype=np.int32)
+    cE, off, lo = ctypes.c_int(E), ctypes.c_int(E * Nq ** 3), ctypes.c_int(loffset)
+    f(ctypes.byref(cE), ctypes.byref(off), ctypes.byref(lo), P(el), P(np.ascontiguousarray(geo)),
+      P(np.ascontiguousarray(D)), P(DT), P(np.ascontiguousarray(l0)), P(np.ascontiguousarray(l1)), P(q), P(out))
+    return out
+
+
+@pytest.mark.skipif(O.ref_lib() is None or not hasattr(O.ref_lib(), "ref_block_l1_N3"),
+                    reason="reference kernels (oracle/_ref) not built on this host")
+@pytest.mark.parametrize("N", [1, 3, 5, 7])
+@pytest.mark.parametrize("kind", ["block", "stress"])
+def test_oracle_block_operators_bitexact_vs_reference(oracle_mod, N, kind):
+    """The oracle's block and stress axhelm against the reference's own serial kernels
+    (ellipticBlockPartialAxCoeffHex3D.c, ellipticStressPartialAxCoeffHex3D.c), compiled from its sources:
+    per-field coefficient fields (p_lambda 1, loffset = fieldOffset) and scalars (p_lambda 0)."""
+    VX, EToV, EToB = O.box_mesh(2, 2, 1, 0.4)
+    el = O.Elliptic(N, VX, EToV, EToB, "preconditioner=none")
+    n = el.get("invDegree").size
+    rng = np.random.default_rng(N)
+    q = rng.uniform(-1, 1, 3 * n)
+    lam0 = rng.uniform(0.5, 2.0, 3 * n)
+    lam1 = rng.uniform(0.0, 3.0, 3 * n)
+    geo = el.get("ggeo") if kind == "block" else el.block_vgeo()
+    D = el.get("D")
+    stress = kind == "stress"
+    ref = _ref_block(kind, 1, N, VX.shape[0], geo, D, q, lam0, lam1, n)
+    got = el.block_ax(q, nf=3, stress=stress, lam0=lam0, lam1=lam1, loffset=n)
+    assert np.array_equal(got, ref)
+    ref = _ref_block(kind, 0, N, VX.shape[0], geo, D, q, np.array([1.3]), np.array([0.7]), 0)
+    got = el.block_ax(q, nf=3, stress=stress, l0=1.3, l1=0.7)
+    assert np.array_equal(got, ref)
