@@ -90,6 +90,14 @@ def wrappers(ref):
                 units.append("\n".join(base + [f"#define p_restrict {r}",
                                                f"#define FUNC(a) ref_fdm{'r' if r else 'a'}_{prec}_N{N}",
                                                f'#include "{os.path.join(ke, "fusedFDM.c")}"'] + _undef()))
+    # axhelm with coefficient fields (p_lambda 1), Helmholtz
+    for N in BLOCK_ORDERS:
+        units.append("\n".join(_common("double", "float") + [
+            f"#define FUNC(a) ref_axcoef_N{N}", "#define p_knl 0",
+            f"#define p_Nq {N + 1}", f"#define p_Np {(N + 1) ** 3}", "#define p_Nggeo 7",
+            "#define p_G00ID 0", "#define p_G01ID 1", "#define p_G11ID 2", "#define p_G12ID 3",
+            "#define p_G02ID 4", "#define p_G22ID 5", "#define p_GWJID 6", "#define p_lambda 1",
+            f'#include "{os.path.join(ke, "ellipticPartialAxCoeffHex3D.c")}"'] + _undef()))
     # block (3-field) and stress (symmetric-gradient) axhelm, scalar (p_lambda 0) and field coefficients
     for N in BLOCK_ORDERS:
         for lam in (0, 1):

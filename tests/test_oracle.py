@@ -192,7 +192,7 @@ def _ref_block(kind, lam, N, E, geo, D, q, l0, l1, loffset):
     import ctypes
 
     P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
-    f = getattr(O.ref_lib(), f"ref_{kind}_l{lam}_N{N}")
+    f = getattr(O.ref_lib(), f"ref_{kind}_N{N}" if lam is None else f"ref_{kind}_l{lam}_N{N}")
     Nq = N + 1
     DT = np.ascontiguousarray(D.reshape(Nq, Nq).T).ravel()
     q = np.ascontiguousarray(q, dtype=np.float64)
@@ -227,4 +227,20 @@ def test_oracle_block_operators_bitexact_vs_reference(oracle_mod, N, kind):
     assert np.array_equal(got, ref)
     ref = _ref_block(kind, 0, N, VX.shape[0], geo, D, q, np.array([1.3]), np.array([0.7]), 0)
     got = el.block_ax(q, nf=3, stress=stress, l0=1.3, l1=0.7)
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.skipif(O.ref_lib() is None or not hasattr(O.ref_lib(), "ref_axcoef_N3"),
+                    reason="reference kernels (oracle/_ref) not built on this host")
+@pytest.mark.parametrize("N", [1, 3, 5, 7])
+def test_oracle_coefficient_field_axhelm_bitexact_vs_reference(oracle_mod, N):
+    """One field with per-node lambda0 / lambda1 (the p_lambda = 1 build of ellipticPartialAxCoeffHex3D.c,
+    a scalar Helmholtz solve with coefficient fields) against the oracle's block operator with nf = 1."""
+    VX, EToV, EToB = O.box_mesh(2, 1, 2, 0.4)
+    el = O.Elliptic(N, VX, EToV, EToB, "preconditioner=none")
+    n = el.get("invDegree").size
+    rng = np.random.default_rng(10 + N)
+    q, lam0, lam1 = rng.uniform(-1, 1, n), rng.uniform(0.5, 2.0, n), rng.uniform(0.0, 3.0, n)
+    ref = _ref_block("axcoef", None, N, VX.shape[0], el.get("ggeo"), el.get("D"), q, lam0, lam1, 0)
+    got = el.block_ax(q, nf=1, lam0=lam0, lam1=lam1)
     assert np.array_equal(got, ref)
