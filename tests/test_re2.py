@@ -185,3 +185,17 @@ def test_solve_setup_from_re2_matches_generator_mesh(product_lib, oracle_mod, tm
     xb, ib = b.solve(rhs)
     assert ia["iterations"] == ib["iterations"]
     assert np.array_equal(xa, xb)
+
+
+def test_reader_crosses_its_read_chunk(product_lib, tmp_path):
+    """The element section is read in chunks of 65536 records: a file with more elements than one chunk reads
+    back exactly (corners, groups, boundary codes of the last elements)."""
+    nx, ny, nz = 50, 40, 35  # 70000 elements
+    xs, ys, zs = np.linspace(0, 1, nx + 1), np.linspace(0, 2, ny + 1) ** 1.5, np.cumsum(np.arange(nz + 1.0))
+    VX, cbc = R.box(nx, ny, nz, xs, ys, zs, ("v", "O", "W", "W", "SYM", "W"))
+    group = (np.arange(VX.shape[0]) % 7).astype(np.int32)
+    p = tmp_path / "big.re2"
+    R.write_re2(p, VX, cbc, group=group)
+    m = R.read_re2(p)
+    assert m["header"]["nelgt"] == 70000
+    assert np.array_equal(m["VX"], VX) and np.array_equal(m["group"], group) and np.array_equal(m["cbc"], cbc)
