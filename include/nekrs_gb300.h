@@ -98,6 +98,12 @@ int nrsg_elliptic_create(const nrsg_mesh_desc *mesh, const char *options, nrsg_e
  * diagonal (ellipticUpdateJacobi).  Needs preconditioner jacobi or none. */
 int nrsg_elliptic_set_coefficients(nrsg_elliptic *el, const double *d_lambda0, const double *d_lambda1,
                                    long long loffset);
+/* Boundary types per field for the block solver (elliptic->EToB with Nfields
+ * sections, ellipticSetup.cpp:190-199): h_EToB [nFields][E][6] in nekRS face
+ * order, e.g. a symmetry plane normal to x masks only the first component.
+ * Each field gets its own mask and gather groups; the Jacobi diagonal is
+ * rebuilt.  Without this call every field takes the mesh descriptor's EToB. */
+int nrsg_elliptic_set_field_bcs(nrsg_elliptic *el, const int *h_EToB);
 int nrsg_elliptic_destroy(nrsg_elliptic *el);
 /* Run all later work of `el` on `cuda_stream` (a cudaStream_t; NULL = the
  * legacy default stream) instead of the library's own non-blocking stream,

@@ -72,6 +72,7 @@ def lib():
         L.nrsg_elliptic_solve_begin.argtypes = [vp, vp, vp]
         L.nrsg_elliptic_set_tolerance.argtypes = [vp, ctypes.c_double, ctypes.c_int, ctypes.c_int]
         L.nrsg_elliptic_set_coefficients.argtypes = [vp, vp, vp, LL]
+        L.nrsg_elliptic_set_field_bcs.argtypes = [vp, vp]
         L.nrsg_elliptic_solve_advance.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(SolveInfo)]
         L.nrsg_elliptic_solve_batch.argtypes = [ctypes.c_int, ctypes.POINTER(vp), ctypes.POINTER(vp),
                                                 ctypes.POINTER(vp), ctypes.POINTER(SolveInfo)]
@@ -197,6 +198,11 @@ class Elliptic:
         """Per-node coefficient fields (device buffers of E*Np, or nFields*E*Np with loffset = E*Np)."""
         self._order_with(lambda0, lambda1)
         check(lib().nrsg_elliptic_set_coefficients(self.h, _ptr(lambda0), _ptr(lambda1), loffset))
+
+    def set_field_bcs(self, EToB_fields):
+        """Boundary types per field of a block solve: int array [nFields, E, 6] (nekRS face order)."""
+        b = np.ascontiguousarray(EToB_fields, dtype=np.int32)
+        check(lib().nrsg_elliptic_set_field_bcs(self.h, b.ctypes.data))
 
     def set_tolerance(self, tol, relative=True, max_iterations=400):
         check(lib().nrsg_elliptic_set_tolerance(self.h, float(tol), int(relative), int(max_iterations)))

@@ -251,7 +251,57 @@ void Elliptic::op(const double *q, double *Aq)
 
 void Elliptic::gs_mask_fields(double *v)
 {
-  for (int f = 0; f < opt.nfields; ++f) launch_gs_mask<double>(fine.gsPlan, v + (size_t)f * fine.Nlocal, true, stream);
+  for (int f = 0; f < opt.nfields; ++f)
+    launch_gs_mask<double>(fieldPlans.empty() ? fine.gsPlan : fieldPlans[f].plan, v + (size_t)f * fine.Nlocal, true,
+                           stream);
+}
+
+void build_mask_plan(const FieldLevel &L, const int *EToB, FieldMaskPlan &P)
+{
+  dirichlet_nodes(L.N, L.E, EToB, L.um, P.maskIds);
+  std::vector<long long> masked = L.ids;
+  for (int m : P.maskIds) masked[m] = 0;
+  build_gather(masked, P.gm);
+  P.gsOff.upload(P.gm.devOff);
+  P.gsIds.upload(P.gm.devIds);
+  P.mask.upload(P.maskIds);
+  P.ngroups = (long long)P.gm.devOff.size() - 1;
+  std::vector<int2> pairs;
+  std::vector<int> roff(1, 0), rids;
+  for (long long g = 0; g < P.ngroups; ++g) {
+    const int s0 = P.gm.devOff[g], s1 = P.gm.devOff[g + 1];
+    if (s1 - s0 == 2) {
+      pairs.push_back(make_int2(P.gm.devIds[s0], P.gm.devIds[s0 + 1]));
+    } else {
+      rids.insert(rids.end(), P.gm.devIds.begin() + s0, P.gm.devIds.begin() + s1);
+      roff.push_back((int)rids.size());
+    }
+  }
+  P.pairs.upload(pairs);
+  P.restOff.upload(roff);
+  P.restIds.upload(rids);
+  P.plan.npairs = (long long)pairs.size();
+  P.plan.nrest = (long long)roff.size() - 1;
+  P.plan.nmask = (long long)P.maskIds.size();
+  P.plan.pairs = P.pairs.p;
+  P.plan.restOff = P.restOff.p;
+  P.plan.restIds = P.restIds.p;
+  P.plan.mask = P.mask.p;
+}
+
+// boundary types per field ([nfields][E][6], nekRS face order): each field gets
+// its own mask and gather groups; the Jacobi diagonal is rebuilt
+void Elliptic::set_field_bcs(const int *h_EToB)
+{
+  if (!h_EToB) throw Error(NRSG_ERR_INVALID, "EToB of the fields required");
+  if (opt.nfields < 2) throw Error(NRSG_ERR_BAD_CONFIG, "per-field boundary types need the block solver");
+  std::vector<FieldMaskPlan> plans(opt.nfields);
+  for (int f = 0; f < opt.nfields; ++f) build_mask_plan(fine, h_EToB + (size_t)f * fine.E * 6, plans[f]);
+  NRSG_CUDA(cudaStreamSynchronize(stream));
+  graph_release();
+  fieldPlans.swap(plans);
+  if (opt.precon == "jacobi") build_jacobi();
+  NRSG_CUDA(cudaStreamSynchronize(stream));
 }
 
 // Jacobi: diag(A) per field, gather-scatter, reciprocal
@@ -265,8 +315,13 @@ void Elliptic::build_jacobi()
   else
     launch_build_diag<double>(fine.N, fine.E, fine.d_ggeo64.p, fine.d_D64.p, opt.lambda0, opt.lambda1, opt.poisson,
                               invDiag.p, stream);
-  for (int f = 0; f < opt.nfields; ++f)
-    launch_gs<double>(fine.ngroups, fine.d_gsOff.p, fine.d_gsIds.p, invDiag.p + (size_t)f * fine.Nlocal, stream);
+  for (int f = 0; f < opt.nfields; ++f) {
+    if (fieldPlans.empty())
+      launch_gs<double>(fine.ngroups, fine.d_gsOff.p, fine.d_gsIds.p, invDiag.p + (size_t)f * fine.Nlocal, stream);
+    else
+      launch_gs<double>(fieldPlans[f].ngroups, fieldPlans[f].gsOff.p, fieldPlans[f].gsIds.p,
+                        invDiag.p + (size_t)f * fine.Nlocal, stream);
+  }
   launch_recip<double>(nT(), invDiag.p, stream);
 }
 
@@ -1069,6 +1124,12 @@ int nrsg_ax_stored_f32(int N, long long E, const float *ggeo, const float *D, fl
                        const float *q, float *Aq, void *s)
 {
   NRSG_TRY(nrsg::launch_ax_stored<float>(N, E, ggeo, D, l0, l1, poisson != 0, q, Aq, (cudaStream_t)s))
+}
+
+int nrsg_elliptic_set_field_bcs(nrsg_elliptic *el, const int *h_EToB)
+{
+  if (!el) return NRSG_ERR_INVALID;
+  NRSG_TRY(el->impl->set_field_bcs(h_EToB))
 }
 
 int nrsg_elliptic_set_coefficients(nrsg_elliptic *el, const double *d_lambda0, const double *d_lambda1,

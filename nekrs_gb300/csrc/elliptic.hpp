@@ -35,6 +35,20 @@ struct FieldLevel {
   void make_fp32(cudaStream_t s);
 };
 
+// Mask and gather-scatter of one field of a block solve whose boundary types
+// differ from the level's (elliptic->EToB holds Nfields sections in the
+// reference, ellipticSetup.cpp:190-199): its own Dirichlet nodes and the
+// gather groups of its unmasked nodes.
+struct FieldMaskPlan {
+  std::vector<int> maskIds;
+  GatherMap gm;
+  DevBuf<int> gsOff, gsIds, mask, restOff, restIds;
+  DevBuf<int2> pairs;
+  GsPlan plan;
+  long long ngroups = 0;
+};
+void build_mask_plan(const FieldLevel &L, const int *EToB, FieldMaskPlan &P);
+
 struct MGState;   // p-multigrid hierarchy (mg.cu)
 struct MGDeleter {
   void operator()(MGState *m) const;
@@ -72,6 +86,8 @@ struct Elliptic {
   const double *wT() const { return opt.nfields > 1 ? wBlock.p : fine.d_invDegree64.p; }
   bool block_mode() const { return opt.nfields > 1 || coef || opt.stress; }
   void gs_mask_fields(double *v);
+  std::vector<FieldMaskPlan> fieldPlans; // empty: every field uses the level's mask
+  void set_field_bcs(const int *h_EToB);
   // null space of the all-Neumann Poisson operator (ellipticSetup.cpp:187-205):
   // remove the E-vector mean from r, z and x (ellipticZeroMean)
   bool allNeumann = false;

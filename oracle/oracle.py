@@ -66,7 +66,7 @@ def lib():
         _lib.orc_block_vgeo.argtypes = [vp, vp]
         _lib.orc_block_ax.argtypes = [vp, ci, ci, ci, cl, vp, vp, cd, cd, vp, vp]
         _lib.orc_block_diag.argtypes = [vp, ci, ci, cl, vp, vp, cd, cd, vp]
-        _lib.orc_block_solve.argtypes = [vp, ci, ci, ci, cl, vp, vp, cd, cd, ci, cd, ci, ci, vp, vp, vp]
+        _lib.orc_block_solve.argtypes = [vp, ci, ci, ci, cl, vp, vp, cd, cd, ci, cd, ci, ci, vp, vp, vp, vp]
     return _lib
 
 
@@ -177,14 +177,15 @@ class Elliptic:
         return out
 
     def block_solve(self, rhs, nf=3, stress=False, poisson=False, lam0=None, lam1=None, l0=1.0, l1=0.0, loffset=0,
-                    jacobi=True, tol=1e-8, relative=True, maxit=1000, x0=None):
+                    jacobi=True, tol=1e-8, relative=True, maxit=1000, x0=None, EToB_fields=None):
         r = np.array(rhs, dtype=np.float64)
         x = np.zeros_like(r) if x0 is None else np.array(x0, dtype=np.float64)
         info = np.zeros(4)
         a0, a1 = self._lam(lam0), self._lam(lam1)
+        eb = None if EToB_fields is None else np.ascontiguousarray(EToB_fields, dtype=np.int32)
         lib().orc_block_solve(self.h, nf, int(stress), int(poisson), loffset, None if a0 is None else a0.ctypes.data,
                               None if a1 is None else a1.ctypes.data, l0, l1, int(jacobi), tol, int(relative), maxit,
-                              r.ctypes.data, x.ctypes.data, info.ctypes.data)
+                              None if eb is None else eb.ctypes.data, r.ctypes.data, x.ctypes.data, info.ctypes.data)
         return x, {"iterations": int(info[0]), "res0": info[1], "res": info[2], "status": int(info[3]), "r": r}
 
     @property

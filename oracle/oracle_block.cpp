@@ -238,8 +238,17 @@ struct BlockSolver {
   BlockSpec S;
   std::vector<double> vg, invDiag, w;
   bool jacobi;
-  BlockSolver(const Level &L_, const BlockSpec &S_, bool jac) : L(L_), S(S_), jacobi(jac)
+  // per-field boundary types (elliptic->EToB with Nfields sections): the mask and gather groups of field f
+  std::vector<Level> fieldLevels;
+  const Level &FL(int f) const { return fieldLevels.empty() ? L : fieldLevels[f]; }
+  BlockSolver(const Level &L_, const BlockSpec &S_, bool jac, const int *EToBfields = nullptr)
+      : L(L_), S(S_), jacobi(jac)
   {
+    if (EToBfields) {
+      fieldLevels.resize(S.nf);
+      for (int f = 0; f < S.nf; ++f)
+        build_level(fieldLevels[f], L.N, L.E, L.VX.data(), L.EToV.data(), EToBfields + (size_t)f * L.E * 6);
+    }
     if (S.stress) vgeo_factors(L, vg);
     const long long n = L.Nlocal * S.nf;
     w.resize(n);
@@ -248,7 +257,7 @@ struct BlockSolver {
     if (jacobi) {
       invDiag.resize(n);
       block_diag(L, S, invDiag.data());
-      for (int f = 0; f < S.nf; ++f) gs_add(L, invDiag.data() + f * L.Nlocal);
+      for (int f = 0; f < S.nf; ++f) gs_add(FL(f), invDiag.data() + f * L.Nlocal);
       for (long long i = 0; i < n; ++i) invDiag[i] = 1.0 / invDiag[i];
     }
   }
@@ -261,8 +270,8 @@ struct BlockSolver {
   {
     ax(q, Aq);
     for (int f = 0; f < S.nf; ++f) {
-      apply_mask(L, Aq + f * L.Nlocal);
-      gs_add(L, Aq + f * L.Nlocal);
+      apply_mask(FL(f), Aq + f * L.Nlocal);
+      gs_add(FL(f), Aq + f * L.Nlocal);
     }
   }
   double norm(const double *r) const
@@ -277,8 +286,8 @@ struct BlockSolver {
     ax(x, Ax0.data());
     for (long long i = 0; i < n; ++i) r[i] = -Ax0[i] + r[i];
     for (int f = 0; f < S.nf; ++f) {
-      apply_mask(L, r + f * L.Nlocal);
-      gs_add(L, r + f * L.Nlocal);
+      apply_mask(FL(f), r + f * L.Nlocal);
+      gs_add(FL(f), r + f * L.Nlocal);
     }
     for (long long i = 0; i < n; ++i) x[i] = 0;
     res0 = norm(r);
@@ -362,10 +371,10 @@ void orc_block_diag(void *h, int nf, int poisson, long long loffset, const doubl
 // info: iterations, res0, res, status
 void orc_block_solve(void *h, int nf, int stress, int poisson, long long loffset, const double *lam0,
                      const double *lam1, double l0, double l1, int jacobi, double tol, int relative, int maxit,
-                     double *r, double *x, double *info)
+                     const int *EToBfields, double *r, double *x, double *info)
 {
   const Level &L = ((Elliptic *)h)->fine;
-  BlockSolver B(L, make_spec(nf, stress, poisson, loffset, lam0, lam1, l0, l1), jacobi != 0);
+  BlockSolver B(L, make_spec(nf, stress, poisson, loffset, lam0, lam1, l0, l1), jacobi != 0, EToBfields);
   double res0 = 0, res = 0;
   int status = 0;
   const int it = B.solve(r, x, tol, relative != 0, maxit, res0, res, status);

@@ -120,3 +120,37 @@ def test_block_rejects_multigrid_and_bad_field_counts(product_lib, torch_cuda):
         G.Elliptic(3, VX, EToV, EToB, "solver=pcg;nFields=2;stressFormulation=true;preconditioner=jacobi")
     with pytest.raises(G.NrsgError):
         G.Elliptic(3, VX, EToV, EToB, "solver=pcg;nFields=4;preconditioner=jacobi")
+
+
+@pytest.mark.parametrize("stress", [False, True])
+def test_block_solve_with_per_field_boundary_types(product_lib, oracle_mod, torch_cuda, stress):
+    """Boundary types per field (the reference's EToB with Nfields sections): the x-planes are symmetry-like,
+    Dirichlet for the first component and Neumann for the other two; parity with the oracle, and the first
+    component alone vanishes there."""
+    torch = torch_cuda
+    N, n = 5, 3
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    E3 = np.stack([EToB.copy() for _ in range(3)])
+    for f in (1, 2):
+        for face in (2, 4):  # nekRS faces r+ and r-
+            E3[f][:, face] = np.where(EToB[:, face] > 0, 4, 0)
+    opts = BASE + ";lambda1=10.0;residualTol=1e-10+relative" + (";stressFormulation=true" if stress else "")
+    orc = O.Elliptic(N, VX, EToV, EToB, "preconditioner=jacobi")
+    el = G.Elliptic(N, VX, EToV, EToB, opts)
+    el.set_field_bcs(E3)
+    rhs = np.concatenate([W.box_rhs(N, n, n, n, s, orc.get("ggeo")) for s in (11, 12, 13)])
+    xo, io = orc.block_solve(rhs, nf=3, stress=stress, poisson=False, l0=1.0, l1=10.0, tol=1e-10, relative=True,
+                             maxit=3000, EToB_fields=E3)
+    r = torch.from_numpy(rhs.copy()).cuda()
+    x = torch.zeros_like(r)
+    ig = el.solve(r, x)
+    torch.cuda.synchronize()
+    assert io["status"] == 0 and ig["status"] == 0
+    assert abs(ig["res0"] - io["res0"]) <= 1e-12 * io["res0"]
+    assert abs(ig["iterations"] - io["iterations"]) <= max(1, io["iterations"] // 100)
+    xg = x.cpu().numpy()
+    assert rel(xg, xo) < 1e-7
+    xs = orc.get("x")
+    on_x = np.isclose(xs, 0.0) | np.isclose(xs, 1.0)
+    X = xg.reshape(3, -1)
+    assert np.abs(X[0][on_x]).max() == 0.0 and np.abs(X[1][on_x]).max() > 0.0
