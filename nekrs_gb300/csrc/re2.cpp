@@ -55,6 +55,8 @@ struct File {
     std::fseek(fp, 0, SEEK_END);
     size = std::ftell(fp);
   }
+  File(const File &) = delete;
+  File &operator=(const File &) = delete;
   ~File()
   {
     if (fp) std::fclose(fp);
