@@ -404,11 +404,13 @@ bool launch_ax_pipe(int N, long long E, const float *ggeo, const float *D, float
 {
   if (N != 7 || E <= 0) return false;
   if (((uintptr_t)ggeo | (uintptr_t)q) & 15) return false; // bulk copies need 16-byte aligned sources
-  static int sms = 0;
+  int dev = 0;
+  NRSG_CUDA(cudaGetDevice(&dev));
+  static int smsOf[64] = {0}; // SM count per device, looked up once
+  int sms = smsOf[dev & 63];
   if (!sms) {
-    int dev = 0;
-    NRSG_CUDA(cudaGetDevice(&dev));
     NRSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    smsOf[dev & 63] = sms;
   }
   const long long nchunk = (E + kPipeEps - 1) / kPipeEps;
   const unsigned grid = (unsigned)std::min<long long>(nchunk, 2LL * sms);
