@@ -240,6 +240,9 @@ def time_kernel(fn, stream, reps=10):
     return ev0.elapsed_time(ev1) / 1e3 / reps
 
 
+AX_CONST_TIMING = False  # set by --ax-const: also time the constant-memory FP32 axhelm variant
+
+
 def kernel_rooflines(G, el, N, E):
     """Achieved algorithmic GB/s of the fine-level operator kernels, CUDA events on their stream."""
     import torch
@@ -278,6 +281,10 @@ def kernel_rooflines(G, el, N, E):
         t = time_kernel(lambda: G.ax_pipe_f32(N, E, g32, D32, 1.0, 0.0, True, q32, a32, cs), stream)
         out["ax_pipe_f32"] = {"launch_ms": t * 1e3, "achieved": 32.0 * n / t / 1e9, "unit": "GB/s",
                               "algorithmic_bytes": 32.0 * n}
+        if AX_CONST_TIMING:
+            t = time_kernel(lambda: G.ax_const_f32(N, E, g32, D32, 1.0, 0.0, True, q32, a32, cs), stream)
+            out["ax_const_f32"] = {"launch_ms": t * 1e3, "achieved": 32.0 * n / t / 1e9, "unit": "GB/s",
+                                   "algorithmic_bytes": 32.0 * n}
     for v in out.values():
         v["frac_of_hbm"] = v["achieved"] / peak
     return out, peak, src
@@ -589,11 +596,15 @@ def main():
     ap.add_argument("--mesh", default=None,
                     help="read the mesh from a Nek5000 .re2 box file (e.g. the reference's kershaw.re2); the "
                          "workload's order, eps and options apply, the right-hand side is the BPS5 one")
+    ap.add_argument("--ax-const", action="store_true",
+                    help="also time the FP32 order-7 axhelm variant with D in constant memory and registers")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-plain", action="store_true")
     ap.add_argument("--solve-only", action="store_true",
                     help="time the device-resident solves only (no e2e, FP64 comparison or kernel rooflines)")
     args = ap.parse_args()
+    global AX_CONST_TIMING
+    AX_CONST_TIMING = args.ax_const
     args.warmup = max(args.warmup, 3)
     args.workload_name = args.workload
     if args.workload in ("batch", "serve", "velocity", "projection"):

@@ -82,7 +82,7 @@ long long nrsg_kernel_launches(void);
  * projectionAconj | projection: solution projection of
  * ellipticSolutionProjection.cpp, with residualProjectionVectors (8) and
  * residualProjectionStart (5)), cudaGraphs, nFields, stressFormulation,
- * axPipeline, coarseGridDiscretization (fem | fem+galerkin | semfem). */
+ * axPipeline, axConst, coarseGridDiscretization (fem | fem+galerkin | semfem). */
 int nrsg_elliptic_create(const nrsg_mesh_desc *mesh, const char *options, nrsg_elliptic **out);
 /* Block (vector) Helmholtz, the velocity solve (tombo.cpp:224-228): options
  * "solver = pcg+block" (or nFields = 2 | 3) and stressFormulation = true.
@@ -288,6 +288,14 @@ int nrsg_ax_stored_f32(int N, long long E, const float *d_ggeo, const float *d_D
  * NRSG_ERR_INVALID. */
 int nrsg_ax_pipe_f32(int N, long long E, const float *d_ggeo, const float *d_D, float lambda0, float lambda1,
                      int poisson, const float *d_q, float *d_Aq, void *stream);
+/* The same FP32 operator for N = 7 with D held in constant memory (the row
+ * every thread of a plane reads) and registers (the rows and columns a thread
+ * contracts against), so that only the q and G planes pass through shared
+ * memory; bit-identical to nrsg_ax_stored_f32.  D (64 floats on the device) is
+ * copied into one constant bank on `stream` before the launch: launches that
+ * may overlap must pass the same D.  Other N return NRSG_ERR_INVALID. */
+int nrsg_ax_const_f32(int N, long long E, const float *d_ggeo, const float *d_D, float lambda0, float lambda1,
+                      int poisson, const float *d_q, float *d_Aq, void *stream);
 /* ellipticPartialAxTrilinearHex3D: geometry recomputed from d_VX [E][8][3]. */
 int nrsg_ax_trilinear_f64(int N, long long E, const double *d_VX, const double *d_gllz, const double *d_gllw,
                           const double *d_D, double lambda0, double lambda1, int poisson, const double *d_q,

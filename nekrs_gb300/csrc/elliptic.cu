@@ -1126,6 +1126,13 @@ int nrsg_ax_stored_f32(int N, long long E, const float *ggeo, const float *D, fl
   NRSG_TRY(nrsg::launch_ax_stored<float>(N, E, ggeo, D, l0, l1, poisson != 0, q, Aq, (cudaStream_t)s))
 }
 
+int nrsg_ax_const_f32(int N, long long E, const float *ggeo, const float *D, float l0, float l1, int poisson,
+                      const float *q, float *Aq, void *s)
+{
+  if (N != 7 || E < 1 || !ggeo || !D || !q || !Aq) return NRSG_ERR_INVALID;
+  NRSG_TRY(nrsg::launch_ax_const(N, E, ggeo, D, l0, l1, poisson != 0, q, Aq, (cudaStream_t)s))
+}
+
 int nrsg_elliptic_set_field_bcs(nrsg_elliptic *el, const int *h_EToB)
 {
   if (!el) return NRSG_ERR_INVALID;

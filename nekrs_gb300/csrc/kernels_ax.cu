@@ -222,6 +222,120 @@ __global__ void __launch_bounds__(128, 5)
 }
 
 // ---------------------------------------------------------------------------
+// FP32 order-7 axhelm with D out of shared memory.  Same arithmetic as
+// ax8v_kernel (bit-identical), but a 16-byte shared load costs four
+// wavefronts per warp whatever its address pattern, so ax8v still moves
+// about 76 wavefronts per warp and plane through the shared pipe.  Here the
+// broadcast row D[k][*] is read from constant memory (uniform, compile-time
+// offsets: no shared traffic) and the rows D[i][*], D[j][*] and columns
+// D[*][i], D[*][j] each thread contracts against are held in 32 registers for
+// the whole element, leaving only the q and G planes in shared memory.
+// ---------------------------------------------------------------------------
+__constant__ float c_D8[64];
+
+template <bool POISSON>
+__global__ void __launch_bounds__(128, 4)
+    ax8c_kernel(long long E, const float *__restrict__ ggeo, float lambda0, float lambda1,
+                const float *__restrict__ q, float *__restrict__ Aq)
+{
+  constexpr int NQ = 8, NP = 512, EPB = 2, RT = 12;
+  __shared__ __align__(16) float s_q[EPB][NQ][NQ];
+  __shared__ __align__(16) float s_qT[EPB][NQ][RT];
+  __shared__ __align__(16) float s_Gr[EPB][NQ][NQ];
+  __shared__ __align__(16) float s_GsT[EPB][NQ][RT];
+
+  const int t = threadIdx.x;
+  const int i = t % NQ, j = t / NQ;
+  const int el = threadIdx.y;
+  const long long e = (long long)blockIdx.x * EPB + el;
+  const bool active = e < E;
+  float Di[NQ], Dj[NQ], DTi[NQ], DTj[NQ];
+#pragma unroll
+  for (int m = 0; m < NQ; ++m) {
+    Di[m] = c_D8[i * NQ + m];
+    Dj[m] = c_D8[j * NQ + m];
+    DTi[m] = c_D8[m * NQ + i];
+    DTj[m] = c_D8[m * NQ + j];
+  }
+  float r_q[NQ], r_Aq[NQ];
+  const long long base = e * NP + t;
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    r_q[k] = active ? q[base + k * NQ * NQ] : 0.f;
+    r_Aq[k] = 0;
+  }
+  constexpr int NG = POISSON ? 6 : 7;
+  const float *g = ggeo + e * 7 * NP + t;
+  float gpre[NG * NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k)
+#pragma unroll
+    for (int c = 0; c < NG; ++c) gpre[c * NQ + k] = active ? __ldg(g + c * NP + k * NQ * NQ) : 0.f;
+
+  auto row8 = [](const float *p, float (&v)[NQ]) {
+    const float4 a = *reinterpret_cast<const float4 *>(p);
+    const float4 b = *reinterpret_cast<const float4 *>(p + 4);
+    v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+  };
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    const float G00 = gpre[0 * NQ + k], G01 = gpre[1 * NQ + k], G11 = gpre[2 * NQ + k];
+    const float G12 = gpre[3 * NQ + k], G02 = gpre[4 * NQ + k], G22 = gpre[5 * NQ + k];
+    const float GWJ = POISSON ? 0.f : gpre[(NG - 1) * NQ + k];
+    s_q[el][j][i] = r_q[k];
+    s_qT[el][i][j] = r_q[k];
+    float qt = 0;
+#pragma unroll
+    for (int m = 0; m < NQ; ++m) qt += c_D8[k * NQ + m] * r_q[m];
+    __syncthreads();
+    float qrow[NQ], qcol[NQ];
+    row8(&s_q[el][j][0], qrow);
+    row8(&s_qT[el][i][0], qcol);
+    float qr = 0, qs = 0;
+#pragma unroll
+    for (int m = 0; m < NQ; ++m) {
+      qr += Di[m] * qrow[m];
+      qs += Dj[m] * qcol[m];
+    }
+    s_Gr[el][j][i] = lambda0 * (G00 * qr + G01 * qs + G02 * qt);
+    s_GsT[el][i][j] = lambda0 * (G01 * qr + G11 * qs + G12 * qt);
+    const float Gt = lambda0 * (G02 * qr + G12 * qs + G22 * qt);
+    float auk = POISSON ? 0.f : GWJ * lambda1 * r_q[k];
+    __syncthreads();
+    float gsc[NQ], grr[NQ];
+    row8(&s_GsT[el][i][0], gsc);
+    row8(&s_Gr[el][j][0], grr);
+#pragma unroll
+    for (int m = 0; m < NQ; ++m) {
+      auk += DTj[m] * gsc[m];
+      r_Aq[m] += c_D8[k * NQ + m] * Gt;
+      auk += DTi[m] * grr[m];
+    }
+    r_Aq[k] += auk;
+    __syncthreads();
+  }
+  if (active) {
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) Aq[base + k * NQ * NQ] = r_Aq[k];
+  }
+}
+
+bool launch_ax_const(int N, long long E, const float *ggeo, const float *D, float lambda0, float lambda1,
+                     bool poisson, const float *q, float *Aq, cudaStream_t s)
+{
+  if (N != 7 || E <= 0) return false;
+  // D (64 floats, device memory) into the constant bank, ordered on the stream
+  NRSG_CUDA(cudaMemcpyToSymbolAsync(c_D8, D, sizeof(float) * 64, 0, cudaMemcpyDeviceToDevice, s));
+  const unsigned grid = (unsigned)((E + 1) / 2);
+  if (poisson)
+    ax8c_kernel<true><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, lambda0, lambda1, q, Aq);
+  else
+    ax8c_kernel<false><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, lambda0, lambda1, q, Aq);
+  NRSG_CHECK_LAUNCH();
+  return true;
+}
+
+// ---------------------------------------------------------------------------
 // FP32 order-7 axhelm through a bulk-copy pipeline (sm_90+ cp.async.bulk into
 // shared memory, completion counted on an mbarrier).  Persistent CTAs walk
 // chunks of kPipeEps consecutive elements; while the chunk in one stage is

@@ -336,8 +336,10 @@ template <typename T> struct MGImpl : public MGState {
   {
     FieldLevel &L = *v.L;
     bool done = false;
-    if constexpr (std::is_same<T, float>::value)
-      done = el.opt.axPipeline && launch_ax_pipe(L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, q, Aq, s);
+    if constexpr (std::is_same<T, float>::value) {
+      if (el.opt.axConst) done = launch_ax_const(L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, q, Aq, s);
+      if (!done) done = el.opt.axPipeline && launch_ax_pipe(L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, q, Aq, s);
+    }
     if (!done) launch_ax_stored<T>(L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, q, Aq, s);
     launch_gs_mask<T>(L.gsPlan, Aq, true, s);
   }

@@ -105,6 +105,7 @@ struct Options {
   bool coarsePersistent = true;     // order-1 coarse Jacobi-PCG as one cooperative kernel
   bool graphs = true;               // CUDA graphs of the steady-state PCG iteration (non-legacy streams)
   bool axPipeline = false;          // FP32 order-7 levels: bulk-copy pipelined axhelm
+  bool axConst = false;             // FP32 order-7 levels: axhelm with D in constant memory / registers
   int nfields = 1;                  // block solver: fields at fieldOffset = Nlocal ("solver = pcg+block" -> 3)
   bool stress = false;              // stressFormulation: symmetric-gradient operator (nfields = 3)
   int projection = 0;               // initialGuess: 0 none, 1 projection (classic), 2 projectionAconj
@@ -190,6 +191,10 @@ void raise_dynamic_smem(const void *kfn, size_t bytes);
 bool launch_ax_pipe(int N, long long E, const float *ggeo, const float *D, float lambda0, float lambda1, bool poisson,
                     const float *q, float *Aq, cudaStream_t s);
 unsigned ax_pipe_error(cudaStream_t s);
+// FP32 order-7 Poisson / Helmholtz axhelm with D in constant memory and registers (false: not
+// applicable).  D is copied into one constant bank per launch: concurrent launches must pass the same D.
+bool launch_ax_const(int N, long long E, const float *ggeo, const float *D, float lambda0, float lambda1,
+                     bool poisson, const float *q, float *Aq, cudaStream_t s);
 template <typename T> void launch_mask(long long n, const int *ids, T *q, cudaStream_t s);
 template <typename T>
 void launch_build_diag(int N, long long E, const T *ggeo, const T *D, T lambda0, T lambda1, bool poisson, T *diag,

@@ -407,6 +407,7 @@ Options parse_options(const char *text)
       else if (key == "coarsepersistent") o.coarsePersistent = std::stoi(v) != 0;
       else if (key == "cudagraphs") o.graphs = std::stoi(v) != 0;
       else if (key == "axpipeline") o.axPipeline = std::stoi(v) != 0;
+      else if (key == "axconst") o.axConst = std::stoi(v) != 0;
       else if (key == "nfields") o.nfields = std::stoi(v);
       else if (key == "stressformulation") o.stress = (v == "true" || v == "1" || v == "yes");
       else if (key == "initialguess") {

@@ -212,3 +212,23 @@ def test_mg_solve_same_with_and_without_ax_pipeline(product_lib, torch_cuda):
     ia, ib = a.solve(rhs.clone(), xa), b.solve(rhs.clone(), xb)
     assert ia["status"] == 0 and ia["iterations"] == ib["iterations"]
     assert torch.equal(xa, xb)
+
+
+@pytest.mark.parametrize("E", [1, 2, 7, 1000])
+@pytest.mark.parametrize("poisson", [True, False])
+def test_ax_const_f32_bit_identical(product_lib, torch_cuda, E, poisson):
+    """The FP32 order-7 axhelm with D in constant memory and registers equals the default kernel bit for bit
+    (same operands, same operation order)."""
+    torch = torch_cuda
+    N, Np = 7, 512
+    gen = torch.Generator(device="cuda").manual_seed(3 * E + poisson)
+    g = torch.rand(E * 7 * Np, device="cuda", generator=gen, dtype=torch.float32) + 0.5
+    D = torch.from_numpy(O.dmatrix(N).astype(np.float32).ravel()).cuda()
+    q = torch.rand(E * Np, device="cuda", generator=gen, dtype=torch.float32) - 0.5
+    a_ref = torch.full_like(q, float("nan"))
+    a_c = torch.full_like(q, float("nan"))
+    cs = torch.cuda.current_stream().cuda_stream
+    G.ax_stored_f32(N, E, g, D, 1.3, 0.7, poisson, q, a_ref, cs)
+    G.ax_const_f32(N, E, g, D, 1.3, 0.7, poisson, q, a_c, cs)
+    torch.cuda.synchronize()
+    assert torch.equal(a_ref, a_c)
