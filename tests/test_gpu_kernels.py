@@ -198,15 +198,16 @@ def test_ax_pipe_f32_rejects_unaligned_and_other_orders(product_lib, torch_cuda)
         G.ax_pipe_f32(5, E, g[:-1], D, 1.0, 0.0, True, q[:-1], a, cs)
 
 
-def test_mg_solve_same_with_and_without_ax_pipeline(product_lib, torch_cuda):
+@pytest.mark.parametrize("variant", ["axPipeline=1", "axConst=1"])
+def test_mg_solve_same_with_and_without_ax_pipeline(product_lib, torch_cuda, variant):
     torch = torch_cuda
     N, n = 7, 5
     VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
     opts = ("solver=pfcg;residualTol=1e-8+relative;maxIterations=200;preconditioner=multigrid;"
             "smootherType=fourthoptcheby+ras;pMGSchedule=p=7+degree=5,p=3+degree=5,p=1,p=3+degree=5,p=7+degree=5;"
             "mgPrecision=mixed")
-    a = G.Elliptic(N, VX, EToV, EToB, opts + ";axPipeline=1")
-    b = G.Elliptic(N, VX, EToV, EToB, opts + ";axPipeline=0")
+    a = G.Elliptic(N, VX, EToV, EToB, opts + ";" + variant)
+    b = G.Elliptic(N, VX, EToV, EToB, opts)
     rhs = torch.from_numpy(W.box_rhs(N, n, n, n, 3, a.get("ggeo"))).cuda()
     xa, xb = torch.zeros_like(rhs), torch.zeros_like(rhs)
     ia, ib = a.solve(rhs.clone(), xa), b.solve(rhs.clone(), xb)
