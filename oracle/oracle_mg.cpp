@@ -493,7 +493,9 @@ static void ext_gather(const Level &L, std::vector<int> &off, std::vector<int> &
 
 template <typename T> static void gs_groups(const std::vector<int> &off, const std::vector<int> &gid, T *q)
 {
-  for (size_t g = 0; g + 1 < off.size(); ++g) {
+  const long long ng = (long long)off.size() - 1;
+#pragma omp parallel for schedule(static)
+  for (long long g = 0; g < ng; ++g) {
     if (off[g] + 1 == off[g + 1]) continue;
     T v = 0;
     for (int m = off[g]; m < off[g + 1]; ++m) v += q[gid[m]];
@@ -591,6 +593,7 @@ template <typename T> static void smooth_schwarz(MGT<T> &M, MGLevel<T> &lv, cons
   T *w1 = F.work1.data(), *w2 = F.work2.data();
   auto X = [&](int i, int j, int k) { return i + nl * (j + nl * k); };
   // preFDM
+  #pragma omp parallel for schedule(static)
   for (long long e = 0; e < E; ++e) {
     T *we = w1 + e * npe;
     const T *ue = u + e * np;
@@ -614,6 +617,7 @@ template <typename T> static void smooth_schwarz(MGT<T> &M, MGLevel<T> &lv, cons
   gs_groups(F.extOff, F.extIds, w1);
   std::vector<T> Sext(ras ? 0 : (size_t)E * npe);
   std::vector<T> out((size_t)E * np);
+  #pragma omp parallel for schedule(static)
   for (long long e = 0; e < E; ++e) {
     T *we = w1 + e * npe;
     for (int a = 1; a < nl - 1; ++a)
@@ -699,6 +703,7 @@ template <typename T> static void smooth_schwarz(MGT<T> &M, MGLevel<T> &lv, cons
   }
   if (!ras) {
     gs_groups(F.extOff, F.extIds, Sext.data());
+    #pragma omp parallel for schedule(static)
     for (long long e = 0; e < E; ++e) {
       T *s = &Sext[e * npe];
       const T *own = w1 + e * npe;
@@ -739,6 +744,7 @@ template <typename T> static void apply_S(MGT<T> &M, MGLevel<T> &lv, const T *r,
 {
   const long long n = lv.L->Nlocal;
   if (lv.base == "jac") {
+    #pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; ++i) Sr[i] = lv.invDiag[i] * r[i];
   } else {
     smooth_schwarz(M, lv, r, Sr);
@@ -762,11 +768,13 @@ template <typename T> static void smooth_cheby1(MGT<T> &M, MGLevel<T> &lv, const
   if (xIsZero) std::fill(x, x + n, T(0));
   if (!xIsZero) {
     level_op(M, lv, x, res);
+    #pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; ++i) res[i] = (T)1 * r[i] + (T)(-1) * res[i];
   } else {
     std::memcpy(res, r, sizeof(T) * n);
   }
   apply_S(M, lv, res, res);
+  #pragma omp parallel for schedule(static)
   for (long long i = 0; i < n; ++i) d[i] = invTheta * res[i];
   for (int k = 1; k < degree; ++k) {
     level_op(M, lv, d, Ad);
@@ -775,12 +783,14 @@ template <typename T> static void smooth_cheby1(MGT<T> &M, MGLevel<T> &lv, const
     rho_n = (T)1.0 / ((T)2.0 * sigma - rho_n);
     const T rCoeff = (T)2.0 * rho_n / delta;
     const T dCoeff = rho_n * rhoSave;
+    #pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; ++i) {
       x[i] = x[i] + d[i];
       res[i] = res[i] - Ad[i];
       d[i] = dCoeff * d[i] + rCoeff * res[i];
     }
   }
+  #pragma omp parallel for schedule(static)
   for (long long i = 0; i < n; ++i) x[i] = (T)1 * d[i] + (T)1 * x[i];
   apply_mask(*lv.L, x);
 }
@@ -798,14 +808,17 @@ template <typename T> static void smooth_cheby4(MGT<T> &M, MGLevel<T> &lv, const
     std::memcpy(res, r, sizeof(T) * n);
   } else {
     level_op(M, lv, x, res);
+    #pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; ++i) res[i] = r[i] - res[i];
   }
   apply_S(M, lv, res, Ad);
   const T c0 = (T)(4.0 / (3.0 * rho));
+  #pragma omp parallel for schedule(static)
   for (long long i = 0; i < n; ++i) d[i] = c0 * Ad[i];
   for (int k = 1; k < degree; ++k) {
     level_op(M, lv, d, Ad);
     const T beta = (T)betas[k - 1];
+    #pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; ++i) {
       x[i] = x[i] + beta * d[i];
       res[i] = res[i] - Ad[i];
@@ -813,9 +826,11 @@ template <typename T> static void smooth_cheby4(MGT<T> &M, MGLevel<T> &lv, const
     apply_S(M, lv, res, Ad);
     const T dCoeff = (T)((2.0 * k - 1.0) / (2.0 * k + 3.0));
     const T rCoeff = (T)((8.0 * k + 4.0) / ((2.0 * k + 3.0) * rho));
+    #pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; ++i) d[i] = rCoeff * Ad[i] + dCoeff * d[i];
   }
   const T bl = (T)betas.back();
+  #pragma omp parallel for schedule(static)
   for (long long i = 0; i < n; ++i) x[i] = bl * d[i] + x[i];
   apply_mask(*lv.L, x);
 }
@@ -837,7 +852,10 @@ template <typename T> static void coarsen_apply(const MGLevel<T> &lc, const T *q
   const int Nfq = lc.Nf + 1, Ncq = lc.L->Nq;
   const long long E = lc.L->E;
   const long long npf = (long long)Nfq * Nfq * Nfq, npc = (long long)Ncq * Ncq * Ncq;
-  std::vector<double> t1((size_t)Nfq * Nfq * Ncq), t2((size_t)Nfq * Ncq * Ncq);
+#pragma omp parallel
+  {
+  std::vector<double> t1((size_t)Nfq * Nfq * Ncq), t2((size_t)Nfq * Ncq * Ncq); // per-thread scratch
+#pragma omp for schedule(static)
   for (long long e = 0; e < E; ++e) {
     const T *f = qf + e * npf;
     // along k
@@ -864,6 +882,7 @@ template <typename T> static void coarsen_apply(const MGLevel<T> &lc, const T *q
           qc[e * npc + a + Ncq * (b + Ncq * c)] = (T)v;
         }
   }
+  }
 }
 
 // qf += (P x P x P) qc with P = R^T
@@ -872,7 +891,10 @@ template <typename T> static void prolong_apply(const MGLevel<T> &lc, const T *q
   const int Nfq = lc.Nf + 1, Ncq = lc.L->Nq;
   const long long E = lc.L->E;
   const long long npf = (long long)Nfq * Nfq * Nfq, npc = (long long)Ncq * Ncq * Ncq;
-  std::vector<double> t1((size_t)Ncq * Ncq * Nfq), t2((size_t)Ncq * Nfq * Nfq);
+#pragma omp parallel
+  {
+  std::vector<double> t1((size_t)Ncq * Ncq * Nfq), t2((size_t)Ncq * Nfq * Nfq); // per-thread scratch
+#pragma omp for schedule(static)
   for (long long e = 0; e < E; ++e) {
     const T *c = qc + e * npc;
     for (int b = 0; b < Ncq; ++b)
@@ -896,6 +918,7 @@ template <typename T> static void prolong_apply(const MGLevel<T> &lc, const T *q
           for (int a = 0; a < Ncq; ++a) v += (double)lc.R[a * Nfq + i] * t2[a + Ncq * (j + Nfq * k)];
           qf[e * npf + i + Nfq * (j + Nfq * k)] += (T)v;
         }
+  }
   }
 }
 
@@ -939,14 +962,17 @@ template <typename T> static int coarse_pcg(MGT<T> &M, MGLevel<T> &lv, const T *
   double rn = r0;
   while (rn > tol && it < M.o.coarseMaxIter) {
     ++it;
+#pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; ++i) z[i] = lv.invDiag[i] * r[i];
     rdotz2 = rdotz1;
     rdotz1 = (double)wdot<T>(n, w, r, z);
     const double beta = (it == 1) ? 0.0 : rdotz1 / rdotz2;
+#pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; ++i) p[i] = z[i] + (T)beta * p[i];
     level_op(M, lv, p, Ap);
     const double pAp = (double)wdot<T>(n, w, p, Ap);
     const T alpha = (T)(rdotz1 / (pAp + 1e-300));
+#pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; ++i) {
       x[i] += alpha * p[i];
       r[i] -= alpha * Ap[i];
