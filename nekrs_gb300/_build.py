@@ -16,7 +16,10 @@ INC = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(OUT, "libnekrs_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp", "--expt-relaxed-constexpr",
+# Host code is compiled without floating-point contraction (-ffp-contract=off) so
+# that host-side FP64 setup (basis, Givens rotations, projection scalars) rounds
+# the same way on every host architecture.
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp,-ffp-contract=off", "--expt-relaxed-constexpr",
               "-I", INC]
 
 

@@ -169,7 +169,7 @@ Elliptic::Elliptic(const nrsg_mesh_desc *m, const char *options)
   x0.alloc(n);
   d_scal.alloc(1);
   NRSG_CUDA(cudaMallocHost((void **)&h_scal, sizeof(PcgScalars)));
-  red_partials.alloc((size_t)kRedSlots * kRedBlocks);
+  red_partials.alloc((size_t)kRedSlots * kRedSegments);
   red_counters.alloc(kRedSlots);
   NRSG_CUDA(cudaMemsetAsync(red_counters.p, 0, sizeof(unsigned) * kRedSlots, stream));
   NRSG_CUDA(cudaMemsetAsync(d_scal.p, 0, sizeof(PcgScalars), stream));
@@ -642,7 +642,8 @@ bool Elliptic::advance(bool block, nrsg_solve_info *info)
   for (;;) {
     if (st.phase == 1) {
       if (!event_done(evRead, block)) return false;
-      st.res0 = std::sqrt(h_scal->rdotr / fine.volume);
+      // res0Norm = weightedNorm2Many * sqrt(resNormFactor) (ellipticSolve.cpp:130-139)
+      st.res0 = std::sqrt(h_scal->rdotr) * std::sqrt(1.0 / fine.volume);
       if (!std::isfinite(st.res0)) {
         st.phase = 4;
         throw Error(NRSG_ERR_NAN, "unreasonable res0Norm (NaN/Inf right-hand side)");
@@ -665,7 +666,8 @@ bool Elliptic::advance(bool block, nrsg_solve_info *info)
       }
     } else if (st.phase == 2) {
       if (!event_done(evRead, block)) return false;
-      const double rnorm = std::sqrt(h_scal->rdotr) * std::sqrt(1.0 / fine.volume);
+      // rdotr = sqrt(update() * resNormFactor) (PCG.cpp:189)
+      const double rnorm = std::sqrt(h_scal->rdotr * (1.0 / fine.volume));
       history.push_back(rnorm);
       st.res = rnorm;
       if (!std::isfinite(rnorm)) {
@@ -1203,7 +1205,7 @@ KernelScratch &kernel_scratch()
   std::lock_guard<std::mutex> lock(g_ks_mutex);
   KernelScratch &k = ks[dev];
   if (k.device != dev) {
-    k.partials.alloc(nrsg::kRedBlocks);
+    k.partials.alloc(nrsg::kRedSegments);
     k.counters.alloc(1);
     NRSG_CUDA(cudaMemset(k.counters.p, 0, sizeof(unsigned)));
     k.red.partials = k.partials.p;

@@ -16,6 +16,29 @@
 
 namespace nrsg {
 
+// acc += a b.  FP64: one explicit fused multiply-add, so that the compiler's
+// contraction choices cannot change the result (the oracle calls std::fma at
+// the same places and the FP64 solve is bit-identical to it); FP32: the plain
+// expression, contracted as before.
+template <typename T> __device__ __forceinline__ void macc(T &acc, T a, T b) { acc += a * b; }
+template <> __device__ __forceinline__ void macc<double>(double &acc, double a, double b) { acc = __fma_rn(a, b, acc); }
+// lambda0 (Ga qr + Gb qs + Gc qt); FP64 as fma(Gc, qt, fma(Gb, qs, Ga qr)) with every rounding explicit
+template <typename T> __device__ __forceinline__ T gflux(T l0, T Ga, T Gb, T Gc, T qr, T qs, T qt)
+{
+  return l0 * (Ga * qr + Gb * qs + Gc * qt);
+}
+template <>
+__device__ __forceinline__ double gflux<double>(double l0, double Ga, double Gb, double Gc, double qr, double qs,
+                                                double qt)
+{
+  return __dmul_rn(l0, __fma_rn(Gc, qt, __fma_rn(Gb, qs, __dmul_rn(Ga, qr))));
+}
+template <typename T> __device__ __forceinline__ T mul3(T a, T b, T c) { return a * b * c; }
+template <> __device__ __forceinline__ double mul3<double>(double a, double b, double c)
+{
+  return __dmul_rn(__dmul_rn(a, b), c);
+}
+
 template <int NQ> struct AxShape {
   static constexpr int plane = NQ * NQ;
   static constexpr int epb = plane >= 128 ? 1 : (128 + plane - 1) / plane;
@@ -88,24 +111,24 @@ __global__ void __launch_bounds__(NQ *NQ *AxShape<NQ>::epb, (sizeof(T) == 4 && N
     s_q[el][j][i] = r_q[k];
     T qt = 0;
 #pragma unroll
-    for (int m = 0; m < NQ; ++m) qt += s_D[k][m] * r_q[m];
+    for (int m = 0; m < NQ; ++m) macc(qt, s_D[k][m], r_q[m]);
     __syncthreads();
     T qr = 0, qs = 0;
 #pragma unroll
     for (int m = 0; m < NQ; ++m) {
-      qr += s_D[i][m] * s_q[el][j][m];
-      qs += s_D[j][m] * s_q[el][m][i];
+      macc(qr, s_D[i][m], s_q[el][j][m]);
+      macc(qs, s_D[j][m], s_q[el][m][i]);
     }
-    s_Gr[el][j][i] = lambda0 * (G00 * qr + G01 * qs + G02 * qt);
-    s_Gs[el][j][i] = lambda0 * (G01 * qr + G11 * qs + G12 * qt);
-    const T Gt = lambda0 * (G02 * qr + G12 * qs + G22 * qt);
-    T auk = POISSON ? T(0) : GWJ * lambda1 * r_q[k];
+    s_Gr[el][j][i] = gflux(lambda0, G00, G01, G02, qr, qs, qt);
+    s_Gs[el][j][i] = gflux(lambda0, G01, G11, G12, qr, qs, qt);
+    const T Gt = gflux(lambda0, G02, G12, G22, qr, qs, qt);
+    T auk = POISSON ? T(0) : mul3(GWJ, lambda1, r_q[k]);
     __syncthreads();
 #pragma unroll
     for (int m = 0; m < NQ; ++m) {
-      auk += s_D[m][j] * s_Gs[el][m][i];
-      r_Aq[m] += s_D[k][m] * Gt;
-      auk += s_D[m][i] * s_Gr[el][j][m];
+      macc(auk, s_D[m][j], s_Gs[el][m][i]);
+      macc(r_Aq[m], s_D[k][m], Gt);
+      macc(auk, s_D[m][i], s_Gr[el][j][m]);
     }
     r_Aq[k] += auk;
     __syncthreads();
@@ -747,15 +770,32 @@ __global__ void build_diag_kernel(long long E, const T *__restrict__ ggeo, const
   for (int n = threadIdx.x; n < NP; n += blockDim.x) {
     const int i = n % NQ, j = (n / NQ) % NQ, k = n / (NQ * NQ);
     T r = 0;
-    r += T(2) * g[1 * NP + n] * lambda0 * s_D[i][i] * s_D[j][j];
-    r += T(2) * g[4 * NP + n] * lambda0 * s_D[i][i] * s_D[k][k];
-    r += T(2) * g[3 * NP + n] * lambda0 * s_D[j][j] * s_D[k][k];
-    for (int m = 0; m < NQ; ++m) {
-      r += g[0 * NP + m + NQ * (j + NQ * k)] * lambda0 * s_D[m][i] * s_D[m][i];
-      r += g[2 * NP + i + NQ * (m + NQ * k)] * lambda0 * s_D[m][j] * s_D[m][j];
-      r += g[5 * NP + i + NQ * (j + NQ * m)] * lambda0 * s_D[m][k] * s_D[m][k];
+    if constexpr (sizeof(T) == 8) {
+      // FP64: r = fma(((2 g) l0) Da, Db, r) etc., every rounding explicit (mirrored by the oracle)
+      auto cross = [&](double g0, double Da, double Db) {
+        r = __fma_rn(__dmul_rn(__dmul_rn(__dmul_rn(2.0, g0), lambda0), Da), Db, r);
+      };
+      auto line = [&](double g0, double Dm) { r = __fma_rn(__dmul_rn(__dmul_rn(g0, lambda0), Dm), Dm, r); };
+      cross(g[1 * NP + n], s_D[i][i], s_D[j][j]);
+      cross(g[4 * NP + n], s_D[i][i], s_D[k][k]);
+      cross(g[3 * NP + n], s_D[j][j], s_D[k][k]);
+      for (int m = 0; m < NQ; ++m) {
+        line(g[0 * NP + m + NQ * (j + NQ * k)], s_D[m][i]);
+        line(g[2 * NP + i + NQ * (m + NQ * k)], s_D[m][j]);
+        line(g[5 * NP + i + NQ * (j + NQ * m)], s_D[m][k]);
+      }
+      if (!poisson) r = __fma_rn(g[6 * NP + n], lambda1, r);
+    } else {
+      r += T(2) * g[1 * NP + n] * lambda0 * s_D[i][i] * s_D[j][j];
+      r += T(2) * g[4 * NP + n] * lambda0 * s_D[i][i] * s_D[k][k];
+      r += T(2) * g[3 * NP + n] * lambda0 * s_D[j][j] * s_D[k][k];
+      for (int m = 0; m < NQ; ++m) {
+        r += g[0 * NP + m + NQ * (j + NQ * k)] * lambda0 * s_D[m][i] * s_D[m][i];
+        r += g[2 * NP + i + NQ * (m + NQ * k)] * lambda0 * s_D[m][j] * s_D[m][j];
+        r += g[5 * NP + i + NQ * (j + NQ * m)] * lambda0 * s_D[m][k] * s_D[m][k];
+      }
+      if (!poisson) r += g[6 * NP + n] * lambda1;
     }
-    if (!poisson) r += g[6 * NP + n] * lambda1;
     diag[e * NP + n] = r;
   }
 }
@@ -800,8 +840,8 @@ __global__ void geofac_kernel(long long E, const double *__restrict__ VX, const 
     const double c[2] = {0.5 * (1 - s_z[k]), 0.5 * (1 + s_z[k])};
     double X[3] = {0, 0, 0};
     for (int v = 0; v < 8; ++v) {
-      const double wv = a[v & 1] * b[(v >> 1) & 1] * c[v >> 2];
-      for (int d = 0; d < 3; ++d) X[d] += wv * s_v[v * 3 + d];
+      const double wv = __dmul_rn(__dmul_rn(a[v & 1], b[(v >> 1) & 1]), c[v >> 2]);
+      for (int d = 0; d < 3; ++d) X[d] = __fma_rn(wv, s_v[v * 3 + d], X[d]);
     }
     for (int d = 0; d < 3; ++d) s_x[d][n] = X[d];
   }
@@ -812,24 +852,32 @@ __global__ void geofac_kernel(long long E, const double *__restrict__ VX, const 
     double dr[3] = {0, 0, 0}, ds[3] = {0, 0, 0}, dt[3] = {0, 0, 0};
     for (int m = 0; m < NQ; ++m)
       for (int d = 0; d < 3; ++d) {
-        dr[d] += s_D[i][m] * s_x[d][m + NQ * (j + NQ * k)];
-        ds[d] += s_D[j][m] * s_x[d][i + NQ * (m + NQ * k)];
-        dt[d] += s_D[k][m] * s_x[d][i + NQ * (j + NQ * m)];
+        dr[d] = __fma_rn(s_D[i][m], s_x[d][m + NQ * (j + NQ * k)], dr[d]);
+        ds[d] = __fma_rn(s_D[j][m], s_x[d][i + NQ * (m + NQ * k)], ds[d]);
+        dt[d] = __fma_rn(s_D[k][m], s_x[d][i + NQ * (j + NQ * m)], dt[d]);
       }
     const double xr = dr[0], yr = dr[1], zr = dr[2], xs = ds[0], ys = ds[1], zs = ds[2], xt = dt[0], yt = dt[1],
                  zt = dt[2];
-    const double J = xr * (ys * zt - zs * yt) - yr * (xs * zt - zs * xt) + zr * (xs * yt - ys * xt);
+    // 2x2 minors a b - c d as fma(a, b, -(c d)); every rounding explicit (mirrored by the oracle)
+    auto minor2 = [](double a, double b, double c, double d) { return __fma_rn(a, b, -__dmul_rn(c, d)); };
+    const double cx = minor2(ys, zt, zs, yt), cy = minor2(xs, zt, zs, xt), cz = minor2(xs, yt, ys, xt);
+    const double J = __fma_rn(zr, cz, __fma_rn(-yr, cy, __dmul_rn(xr, cx)));
     const double Ji = 1.0 / J;
-    const double JW = J * s_w[i] * s_w[j] * s_w[k];
-    const double rx = (ys * zt - zs * yt) * Ji, ry = -(xs * zt - zs * xt) * Ji, rz = (xs * yt - ys * xt) * Ji;
-    const double sx = -(yr * zt - zr * yt) * Ji, sy = (xr * zt - zr * xt) * Ji, sz = -(xr * yt - yr * xt) * Ji;
-    const double tx = (yr * zs - zr * ys) * Ji, ty = -(xr * zs - zr * xs) * Ji, tz = (xr * ys - yr * xs) * Ji;
-    g[0 * NP + n] = JW * (rx * rx + ry * ry + rz * rz);
-    g[1 * NP + n] = JW * (rx * sx + ry * sy + rz * sz);
-    g[2 * NP + n] = JW * (sx * sx + sy * sy + sz * sz);
-    g[3 * NP + n] = JW * (sx * tx + sy * ty + sz * tz);
-    g[4 * NP + n] = JW * (rx * tx + ry * ty + rz * tz);
-    g[5 * NP + n] = JW * (tx * tx + ty * ty + tz * tz);
+    const double JW = __dmul_rn(__dmul_rn(__dmul_rn(J, s_w[i]), s_w[j]), s_w[k]);
+    const double rx = __dmul_rn(cx, Ji), ry = __dmul_rn(-cy, Ji), rz = __dmul_rn(cz, Ji);
+    const double sx = __dmul_rn(-minor2(yr, zt, zr, yt), Ji), sy = __dmul_rn(minor2(xr, zt, zr, xt), Ji),
+                 sz = __dmul_rn(-minor2(xr, yt, yr, xt), Ji);
+    const double tx = __dmul_rn(minor2(yr, zs, zr, ys), Ji), ty = __dmul_rn(-minor2(xr, zs, zr, xs), Ji),
+                 tz = __dmul_rn(minor2(xr, ys, yr, xs), Ji);
+    auto dot3 = [](double a0, double b0, double a1, double b1, double a2, double b2) {
+      return __fma_rn(a2, b2, __fma_rn(a1, b1, __dmul_rn(a0, b0)));
+    };
+    g[0 * NP + n] = __dmul_rn(JW, dot3(rx, rx, ry, ry, rz, rz));
+    g[1 * NP + n] = __dmul_rn(JW, dot3(rx, sx, ry, sy, rz, sz));
+    g[2 * NP + n] = __dmul_rn(JW, dot3(sx, sx, sy, sy, sz, sz));
+    g[3 * NP + n] = __dmul_rn(JW, dot3(sx, tx, sy, ty, sz, tz));
+    g[4 * NP + n] = __dmul_rn(JW, dot3(rx, tx, ry, ty, rz, tz));
+    g[5 * NP + n] = __dmul_rn(JW, dot3(tx, tx, ty, ty, tz, tz));
     g[6 * NP + n] = JW;
   }
 }

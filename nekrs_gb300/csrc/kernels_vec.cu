@@ -7,12 +7,31 @@
 //   ellipticBlockUpdatePCG   kernels/elliptic/ellipticBlockUpdatePCG.okl:26-111
 //   axpbyMany, axmyzMany, adyMany, fill, copyDfloatToPfloat (kernels/linAlg, kernels/core)
 //
-// Reductions are one launch each: every CTA writes its partial sum, the last
-// CTA to finish (atomic ticket) adds the partials in index order and stores
-// the result on the device.  The partial layout and the order of every sum
-// are fixed, so results are bit-reproducible run to run.  There is no host
-// round trip: Krylov scalars (alpha, beta) are formed on the device by the
-// kernels that consume them.
+// Reductions are one launch each and are bit-reproducible: every FP64 sum
+// is formed in one fixed order that depends only on n, and the oracle's
+// wsum() performs the same additions in the same order.  The order:
+//   term_i    per kernel, with every rounding explicit (e.g. w_i * (a_i * b_i),
+//             both products rounded: the reference's weightedInnerProdMany term);
+//   chunk c   entries [256 c, 256 c + 256), entries past n count as +0.0; its sum
+//             is the pairwise tree s[x] += s[x + o], o = 128, 64, ..., 1, i.e. the
+//             block order of weightedInnerProdMany.okl:27-105, so chunk sums equal
+//             the reference's block partials bit for bit;
+//   result    the chunk sums added by the blocked pairwise tree
+//             ((P0 + P1) + (P2 + P3)) + ..., zero-padded to a power of two.  The
+//             reference adds its block partials one after another on the host
+//             (linAlg.cpp:986-1035); the tree keeps the whole sum on the device
+//             and parallel.
+// A warp sums groups of 4 chunks (1024 entries); each warp owns one aligned,
+// power-of-two run of groups and merges its group sums by the same tree with
+// a small stack; the CTA that finishes last (atomic ticket) adds the warp
+// sums, still by the same tree, and stores the result on the device.  Krylov
+// scalars (alpha, beta) are formed on the device by the kernels that consume
+// them, so there is no host round trip.
+//
+// FP64 element-wise arithmetic on the plain solve path uses explicit
+// roundings (__fma_rn / __dmul_rn / __dadd_rn) so that the compiler's
+// contraction choices cannot change results; the oracle calls std::fma at the
+// same places.
 
 #include "nrsg_internal.hpp"
 
@@ -20,61 +39,159 @@ namespace nrsg {
 
 namespace {
 constexpr int kThreads = kRedThreads;
+constexpr int kWarps = kThreads / 32;
+constexpr int kChunk = 256;    // entries per chunk (the reference's p_blockSize)
+constexpr int kGroup = 4;      // chunks per group (one warp step)
+constexpr int kStack = 24;     // depth of the per-warp merge stack (runs of up to 2^23 groups)
 
-__device__ __forceinline__ double warp_sum(double v)
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+
+// weighted product term w * (a * b) with both products rounded
+__device__ __forceinline__ double wterm(double w, double a, double b) { return dmul(w, dmul(a, b)); }
+
+// Sum of one chunk in lane 0; a[j] holds the term at chunk offset lane + 32 j.
+__device__ __forceinline__ double chunk_tree(double (&a)[8])
 {
+  a[0] = dadd(a[0], a[4]); // o = 128
+  a[1] = dadd(a[1], a[5]);
+  a[2] = dadd(a[2], a[6]);
+  a[3] = dadd(a[3], a[7]);
+  a[0] = dadd(a[0], a[2]); // o = 64
+  a[1] = dadd(a[1], a[3]);
+  double v = dadd(a[0], a[1]); // o = 32
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  for (int o = 16; o > 0; o >>= 1) v = dadd(v, __shfl_down_sync(0xffffffffu, v, o));
   return v;
 }
 
-// Block sum (fixed order), result valid in thread 0.
-__device__ __forceinline__ double block_sum(double v)
+// F: double operator()(long long i) const -- term of entry i < n (and its side effects)
+template <typename F> __device__ __forceinline__ double chunk_sum(long long c, long long n, const F &f)
 {
-  __shared__ double s_w[kThreads / 32];
-  v = warp_sum(v);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) s_w[wid] = v;
-  __syncthreads();
-  double r = 0;
-  if (wid == 0) {
-    r = (lane < kThreads / 32) ? s_w[lane] : 0.0;
-    r = warp_sum(r);
+  const long long i0 = c * kChunk + (threadIdx.x & 31);
+  double a[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const long long i = i0 + 32 * j;
+    a[j] = i < n ? f(i) : 0.0;
   }
+  return chunk_tree(a);
+}
+
+template <typename F> __device__ __forceinline__ double group_sum(long long g, long long n, const F &f)
+{
+  const double p0 = chunk_sum(g * kGroup + 0, n, f);
+  const double p1 = chunk_sum(g * kGroup + 1, n, f);
+  const double p2 = chunk_sum(g * kGroup + 2, n, f);
+  const double p3 = chunk_sum(g * kGroup + 3, n, f);
+  return dadd(dadd(p0, p1), dadd(p2, p3));
+}
+
+// Work split of one reduction: W warp runs of `len` groups each (both powers
+// of two, W <= kRedSegments), CTAs = ceil(W / 8).
+struct RedSplit {
+  long long len;
+  int warps, ctas;
+};
+inline RedSplit red_split(long long n)
+{
+  const long long nc = (n + kChunk - 1) / kChunk;
+  const long long ng = (nc + kGroup - 1) / kGroup;
+  long long M = 1;
+  while (M < ng) M <<= 1;
+  const long long W = M < kRedSegments ? M : kRedSegments;
+  RedSplit r;
+  r.len = M / W;
+  r.warps = (int)W;
+  r.ctas = (int)((W + kWarps - 1) / kWarps);
+  return r;
+}
+
+// The sum of warp run `wid` (groups [wid*len, (wid+1)*len)) by the blocked
+// tree, merged on a per-warp stack in shared memory (lane 0 writes it); the
+// result is returned to every lane.
+template <typename F>
+__device__ __forceinline__ double run_sum(long long wid, long long len, long long n, const F &f)
+{
+  __shared__ double s_stk[kWarps][kStack];
+  double *stk = s_stk[threadIdx.x >> 5];
+  const bool lane0 = (threadIdx.x & 31) == 0;
+  int sp = 0;
+  for (long long q = 0; q < len; ++q) {
+    double v = group_sum(wid * len + q, n, f);
+    for (long long k = q + 1; (k & 1) == 0; k >>= 1) v = dadd(stk[--sp], v);
+    if (lane0) stk[sp] = v;
+    ++sp;
+    __syncwarp();
+  }
+  return stk[0];
+}
+
+// Blocked tree over row[0, W) (zero past W, W <= 8192) by the whole CTA; the
+// result is valid in thread 0.
+__device__ __forceinline__ double final_tree(const double *row, int W)
+{
+  __shared__ double sh[kThreads];
+  const int t = threadIdx.x;
+  const volatile double *vr = row;
+  double st[6];
+  int sp = 0;
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    const int idx = 32 * t + j;
+    double v = idx < W ? vr[idx] : 0.0;
+#pragma unroll
+    for (int k = j + 1; (k & 1) == 0; k >>= 1) v = dadd(st[--sp], v);
+    st[sp++] = v;
+  }
+  sh[t] = st[0];
+  __syncthreads();
+#pragma unroll
+  for (int o = 1; o < kThreads; o <<= 1) {
+    if ((t & (2 * o - 1)) == 0) sh[t] = dadd(sh[t], sh[t + o]);
+    __syncthreads();
+  }
+  const double r = sh[0];
   __syncthreads();
   return r;
 }
 
-// Write this block's partial; the last block reduces all partials into *out.
-// Returns true in the thread that stored *out.
-__device__ __forceinline__ bool finish_reduction(double partial, double *partials, unsigned *counter, double *out)
+// Store this warp's run sum (lane 0), then take the CTA's ticket; true in
+// every thread of the CTA that finished last.
+__device__ __forceinline__ bool store_run_and_ticket(bool storing, double v, double *row, long long wid,
+                                                     unsigned *counter)
 {
-  __shared__ bool s_last;
-  if (threadIdx.x == 0) {
-    partials[blockIdx.x] = partial;
+  if (storing && (threadIdx.x & 31) == 0) {
+    row[wid] = v;
     __threadfence();
-    const unsigned ticket = atomicAdd(counter, 1u);
-    s_last = (ticket == gridDim.x - 1);
   }
+  __shared__ bool s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
   __syncthreads();
   if (!s_last) return false;
   __threadfence();
+  return true;
+}
+
+// One-vector reduction body shared by the kernels below: run sums, ticket,
+// final tree into *out; returns true in the thread that stored *out.
+template <typename F>
+__device__ __forceinline__ bool reduce1(long long n, long long len, int W, const F &f, double *row, unsigned *counter,
+                                        double *out)
+{
+  const long long wid = (long long)blockIdx.x * kWarps + (threadIdx.x >> 5);
   double v = 0;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += kThreads) v += ((volatile double *)partials)[b];
-  v = block_sum(v);
+  if (wid < W) v = run_sum(wid, len, n, f);
+  if (!store_run_and_ticket(wid < W, v, row, wid, counter)) return false;
+  const double r = final_tree(row, W);
   if (threadIdx.x == 0) {
-    *out = v;
+    *out = r;
     *counter = 0; // ready for the next launch on this slot
   }
   return threadIdx.x == 0;
 }
 
-inline unsigned red_grid(long long n)
-{
-  long long b = (n + kThreads - 1) / kThreads;
-  if (b < 1) b = 1;
-  return (unsigned)(b < kRedBlocks ? b : kRedBlocks);
-}
 inline unsigned vec_grid(long long n)
 {
   long long b = (n + kThreads - 1) / kThreads;
@@ -141,8 +258,8 @@ __global__ void accumulate_kernel(long long n, int m, const double *__restrict__
                                   double *__restrict__ y)
 {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    double v = alpha[0] * X[i];
-    for (int k = 1; k < m; ++k) v += alpha[k] * X[(size_t)k * n + i];
+    double v = dmul(alpha[0], X[i]);
+    for (int k = 1; k < m; ++k) v = __fma_rn(alpha[k], X[(size_t)k * n + i], v);
     y[i] = v;
   }
 }
@@ -157,7 +274,7 @@ __global__ void multi_scaled_sub_kernel(long long n, int m, const double *__rest
   double *xm = X + (size_t)(m - 1) * n;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     double v = xm[i];
-    for (int k = 0; k < m - 1; ++k) v = -alpha[k] * X[(size_t)k * n + i] + v;
+    for (int k = 0; k < m - 1; ++k) v = __fma_rn(-alpha[k], X[(size_t)k * n + i], v);
     xm[i] = v;
   }
 }
@@ -214,24 +331,31 @@ template void launch_mask<float>(long long, const int *, float *, cudaStream_t);
 // ---------------------------------------------------------------------------
 // weighted inner product
 // ---------------------------------------------------------------------------
+// Launch geometry of a reduction over n entries and the Reduce row of `slot`.
+#define NRSG_RED_ARGS(n, red, slot)                                                                         \
+  const RedSplit sp_ = red_split(n);                                                                      \
+  double *row_ = red.row(slot);                                                                          \
+  unsigned *cnt_ = red.counters + (slot)
+
 template <typename T>
-__global__ void wdot_kernel(long long n, const T *__restrict__ w, const T *__restrict__ a, const T *__restrict__ b,
-                            double *partials, unsigned *counter, double *out)
+__global__ void __launch_bounds__(kThreads)
+    wdot_kernel(long long n, long long len, int W, const T *__restrict__ w, const T *__restrict__ a,
+                const T *__restrict__ b, double *row, unsigned *counter, double *out)
 {
-  double acc = 0;
-  for (long long i = blockIdx.x * (long long)kThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kThreads) {
-    const double av = (double)a[i];
-    const double bv = b ? (double)b[i] : av;
-    const double wv = w ? (double)w[i] : 1.0;
-    acc += wv * av * bv;
-  }
-  finish_reduction(block_sum(acc), partials, counter, out);
+  reduce1(
+      n, len, W,
+      [&](long long i) {
+        const double av = (double)a[i];
+        const double bv = b ? (double)b[i] : av;
+        return w ? wterm((double)w[i], av, bv) : dmul(av, bv);
+      },
+      row, counter, out);
 }
 template <typename T>
 void launch_wdot(long long n, const T *w, const T *a, const T *b, double *out, Reduce &red, int slot, cudaStream_t s)
 {
-  wdot_kernel<T><<<red_grid(n), kThreads, 0, s>>>(n, w, a, b, red.partials + (size_t)slot * kRedBlocks,
-                                                   red.counters + slot, out);
+  NRSG_RED_ARGS(n, red, slot);
+  wdot_kernel<T><<<sp_.ctas, kThreads, 0, s>>>(n, sp_.len, sp_.warps, w, a, b, row_, cnt_, out);
   NRSG_CHECK_LAUNCH();
 }
 template void launch_wdot<double>(long long, const double *, const double *, const double *, double *, Reduce &, int,
@@ -249,6 +373,12 @@ template <typename T> __global__ void fill_kernel(long long n, T v, T *x) { NRSG
 template <typename T> __global__ void axpby_kernel(long long n, T a, const T *__restrict__ x, T b, T *__restrict__ y)
 {
   NRSG_GRID_LOOP(i, n) y[i] = a * x[i] + b * y[i];
+}
+// FP64: y = fma(a, x, b*y)
+template <> __global__ void axpby_kernel<double>(long long n, double a, const double *__restrict__ x, double b,
+                                                 double *__restrict__ y)
+{
+  NRSG_GRID_LOOP(i, n) y[i] = __fma_rn(a, x[i], dmul(b, y[i]));
 }
 template <typename T> __global__ void axmy_kernel(long long n, const T *__restrict__ w, T *__restrict__ x)
 {
@@ -316,39 +446,43 @@ template void launch_copy_cast<float, float>(long long, const float *, float *, 
 // ---------------------------------------------------------------------------
 // PCG kernels with device-resident scalars
 // ---------------------------------------------------------------------------
-__global__ void jacobi_rdotz_kernel(long long n, const double *__restrict__ w, const double *__restrict__ invDiag,
-                                    const double *__restrict__ r, double *__restrict__ z, PcgScalars *sc,
-                                    double *partials, unsigned *counter)
+__global__ void __launch_bounds__(kThreads)
+    jacobi_rdotz_kernel(long long n, long long len, int W, const double *__restrict__ w,
+                        const double *__restrict__ invDiag, const double *__restrict__ r, double *__restrict__ z,
+                        PcgScalars *sc, double *row, unsigned *counter)
 {
-  double acc = 0;
-  for (long long i = blockIdx.x * (long long)kThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kThreads) {
-    const double ri = r[i];
-    const double zi = ri * invDiag[i];
-    z[i] = zi;
-    acc += w[i] * ri * zi;
-  }
   __shared__ double s_old;
   if (threadIdx.x == 0) s_old = sc->rdotz;
   // every block reads rdotz before the last block overwrites it: the last
   // block only finishes after all tickets are taken, i.e. after every block
   // passed this point.
   __syncthreads();
-  if (finish_reduction(block_sum(acc), partials, counter, &sc->rdotz)) sc->rdotz_old = s_old;
+  const bool last = reduce1(
+      n, len, W,
+      [&](long long i) {
+        const double ri = r[i];
+        const double zi = dmul(ri, invDiag[i]);
+        z[i] = zi;
+        return wterm(w[i], ri, zi);
+      },
+      row, counter, &sc->rdotz);
+  if (last) sc->rdotz_old = s_old;
 }
 void launch_jacobi_rdotz(long long n, const double *w, const double *invDiag, const double *r, double *z,
                          PcgScalars *sc, Reduce &red, int slot, cudaStream_t s)
 {
-  jacobi_rdotz_kernel<<<red_grid(n), kThreads, 0, s>>>(n, w, invDiag, r, z, sc, red.partials + (size_t)slot * kRedBlocks,
-                                                       red.counters + slot);
+  NRSG_RED_ARGS(n, red, slot);
+  jacobi_rdotz_kernel<<<sp_.ctas, kThreads, 0, s>>>(n, sp_.len, sp_.warps, w, invDiag, r, z, sc, row_, cnt_);
   NRSG_CHECK_LAUNCH();
 }
 
+// p = z + beta p as fma(beta, p, z)
 __global__ void update_p_kernel(long long n, const double *__restrict__ z, double *__restrict__ p, const PcgScalars *sc,
                                 bool first, bool flexible)
 {
   double beta = 0;
   if (!first) beta = flexible ? -sc->alpha * sc->zAp / sc->rdotz_old : sc->rdotz / sc->rdotz_old;
-  NRSG_GRID_LOOP(i, n) p[i] = z[i] + beta * p[i];
+  NRSG_GRID_LOOP(i, n) p[i] = __fma_rn(beta, p[i], z[i]);
 }
 void launch_update_p(long long n, const double *z, double *p, const PcgScalars *sc, bool first, bool flexible,
                      cudaStream_t s)
@@ -357,49 +491,54 @@ void launch_update_p(long long n, const double *z, double *p, const PcgScalars *
   NRSG_CHECK_LAUNCH();
 }
 
-__global__ void update_xr_kernel(long long n, const double *__restrict__ w, const double *__restrict__ p,
-                                 const double *__restrict__ Ap, double *__restrict__ x, double *__restrict__ r,
-                                 PcgScalars *sc, double *partials, unsigned *counter)
+// r = fma(-alpha, Ap, r), x = fma(alpha, p, x), term w (r r)
+__global__ void __launch_bounds__(kThreads)
+    update_xr_kernel(long long n, long long len, int W, const double *__restrict__ w, const double *__restrict__ p,
+                     const double *__restrict__ Ap, double *__restrict__ x, double *__restrict__ r, PcgScalars *sc,
+                     double *row, unsigned *counter)
 {
   const double alpha = sc->rdotz / (sc->pAp + 1e-300);
-  double acc = 0;
-  for (long long i = blockIdx.x * (long long)kThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kThreads) {
-    double ri = r[i];
-    ri -= alpha * Ap[i];
-    r[i] = ri;
-    acc += ri * ri * w[i];
-    x[i] += alpha * p[i];
-  }
-  if (finish_reduction(block_sum(acc), partials, counter, &sc->rdotr)) sc->alpha = alpha;
+  const bool last = reduce1(
+      n, len, W,
+      [&](long long i) {
+        const double ri = __fma_rn(-alpha, Ap[i], r[i]);
+        r[i] = ri;
+        x[i] = __fma_rn(alpha, p[i], x[i]);
+        return wterm(w[i], ri, ri);
+      },
+      row, counter, &sc->rdotr);
+  if (last) sc->alpha = alpha;
 }
 void launch_update_xr(long long n, const double *w, const double *p, const double *Ap, double *x, double *r,
                       PcgScalars *sc, Reduce &red, int slot, cudaStream_t s)
 {
-  update_xr_kernel<<<red_grid(n), kThreads, 0, s>>>(n, w, p, Ap, x, r, sc, red.partials + (size_t)slot * kRedBlocks,
-                                                    red.counters + slot);
+  NRSG_RED_ARGS(n, red, slot);
+  update_xr_kernel<<<sp_.ctas, kThreads, 0, s>>>(n, sp_.len, sp_.warps, w, p, Ap, x, r, sc, row_, cnt_);
   NRSG_CHECK_LAUNCH();
 }
 
-__global__ void update_pcg_alpha_kernel(long long n, const double *__restrict__ w, const double *__restrict__ p,
-                                        const double *__restrict__ Ap, double alpha, double *__restrict__ x,
-                                        double *__restrict__ r, double *partials, unsigned *counter, double *out)
+__global__ void __launch_bounds__(kThreads)
+    update_pcg_alpha_kernel(long long n, long long len, int W, const double *__restrict__ w,
+                            const double *__restrict__ p, const double *__restrict__ Ap, double alpha,
+                            double *__restrict__ x, double *__restrict__ r, double *row, unsigned *counter,
+                            double *out)
 {
-  double acc = 0;
-  for (long long i = blockIdx.x * (long long)kThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kThreads) {
-    double ri = r[i];
-    ri -= alpha * Ap[i];
-    r[i] = ri;
-    acc += ri * ri * w[i];
-    x[i] += alpha * p[i];
-  }
-  finish_reduction(block_sum(acc), partials, counter, out);
+  reduce1(
+      n, len, W,
+      [&](long long i) {
+        const double ri = __fma_rn(-alpha, Ap[i], r[i]);
+        r[i] = ri;
+        x[i] = __fma_rn(alpha, p[i], x[i]);
+        return wterm(w[i], ri, ri);
+      },
+      row, counter, out);
 }
 void launch_update_pcg_alpha(long long n, const double *w, const double *p, const double *Ap, double alpha, double *x,
                              double *r, double *rdotr, Reduce &red, int slot, cudaStream_t s)
 {
-  update_pcg_alpha_kernel<<<red_grid(n), kThreads, 0, s>>>(n, w, p, Ap, alpha, x, r,
-                                                           red.partials + (size_t)slot * kRedBlocks,
-                                                           red.counters + slot, rdotr);
+  NRSG_RED_ARGS(n, red, slot);
+  update_pcg_alpha_kernel<<<sp_.ctas, kThreads, 0, s>>>(n, sp_.len, sp_.warps, w, p, Ap, alpha, x, r, row_, cnt_,
+                                                        rdotr);
   NRSG_CHECK_LAUNCH();
 }
 
@@ -429,37 +568,79 @@ namespace {
 constexpr int kMultiVec = 8;
 }
 
-__global__ void multi_wdot_kernel(long long n, const double *__restrict__ w, const double *__restrict__ V, int nvec,
-                                  const double *__restrict__ x, double *partials, unsigned *counter, double *out)
+// One pass over x and w for up to kMultiVec vectors: term w (x V_k); every
+// vector's sums follow the one-vector order exactly.
+__global__ void __launch_bounds__(kThreads)
+    multi_wdot_kernel(long long n, long long len, int W, const double *__restrict__ w, const double *__restrict__ V,
+                      int nvec, const double *__restrict__ x, double *rows, long long stride, unsigned *counter,
+                      double *out)
 {
-  double acc[kMultiVec];
+  __shared__ double s_stk[kWarps][kMultiVec][kStack];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long wid = (long long)blockIdx.x * kWarps + warp;
+  if (wid < W) {
+    int sp = 0;
+    for (long long q = 0; q < len; ++q) {
+      const long long g = wid * len + q;
+      double lo[kMultiVec], hi[kMultiVec];
 #pragma unroll
-  for (int k = 0; k < kMultiVec; ++k) acc[k] = 0;
-  for (long long i = blockIdx.x * (long long)kThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kThreads) {
-    const double wx = w[i] * x[i];
+      for (int cq = 0; cq < kGroup; ++cq) {
+        const long long i0 = (g * kGroup + cq) * kChunk + lane;
+        double wv[8], xv[8];
 #pragma unroll
-    for (int k = 0; k < kMultiVec; ++k)
-      if (k < nvec) acc[k] += wx * V[(size_t)k * n + i];
+        for (int j = 0; j < 8; ++j) {
+          const long long i = i0 + 32 * j;
+          wv[j] = i < n ? w[i] : 0.0;
+          xv[j] = i < n ? x[i] : 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < kMultiVec; ++k) {
+          if (k >= nvec) break;
+          double a[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const long long i = i0 + 32 * j;
+            a[j] = i < n ? wterm(wv[j], xv[j], V[(size_t)k * n + i]) : 0.0;
+          }
+          const double P = chunk_tree(a);
+          if (cq == 0) lo[k] = P;
+          else if (cq == 1) lo[k] = dadd(lo[k], P);
+          else if (cq == 2) hi[k] = P;
+          else hi[k] = dadd(hi[k], P);
+        }
+      }
+      double v[kMultiVec];
+#pragma unroll
+      for (int k = 0; k < kMultiVec; ++k)
+        if (k < nvec) v[k] = dadd(lo[k], hi[k]);
+      for (long long kk = q + 1; (kk & 1) == 0; kk >>= 1) {
+        --sp;
+#pragma unroll
+        for (int k = 0; k < kMultiVec; ++k)
+          if (k < nvec) v[k] = dadd(s_stk[warp][k][sp], v[k]);
+      }
+      if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < kMultiVec; ++k)
+          if (k < nvec) s_stk[warp][k][sp] = v[k];
+      }
+      ++sp;
+      __syncwarp();
+    }
+    if (lane == 0) {
+      for (int k = 0; k < nvec; ++k) rows[(size_t)k * stride + wid] = s_stk[warp][k][0];
+      __threadfence();
+    }
   }
   __shared__ bool s_last;
-#pragma unroll
-  for (int k = 0; k < kMultiVec; ++k) {
-    if (k >= nvec) break;
-    const double v = block_sum(acc[k]);
-    if (threadIdx.x == 0) partials[(size_t)k * kRedBlocks + blockIdx.x] = v;
-  }
-  if (threadIdx.x == 0) {
-    __threadfence();
-    s_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
-  }
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
   __syncthreads();
   if (!s_last) return;
   __threadfence();
   for (int k = 0; k < nvec; ++k) {
-    double v = 0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += kThreads) v += ((volatile double *)partials)[(size_t)k * kRedBlocks + b];
-    v = block_sum(v);
-    if (threadIdx.x == 0) out[k] = v;
+    const double r = final_tree(rows + (size_t)k * stride, W);
+    if (threadIdx.x == 0) out[k] = r;
   }
   if (threadIdx.x == 0) *counter = 0;
 }
@@ -467,41 +648,46 @@ __global__ void multi_wdot_kernel(long long n, const double *__restrict__ w, con
 void launch_multi_wdot(long long n, const double *w, const double *V, int nvec, const double *x, double *out,
                        Reduce &red, int slot, cudaStream_t s)
 {
-  // chunks of kMultiVec vectors; each chunk uses kMultiVec consecutive partial rows of `slot`
+  // chunks of kMultiVec vectors; each chunk uses kMultiVec consecutive rows starting at `slot`
+  if (slot + kMultiVec > red.slots) throw Error(NRSG_ERR_INVALID, "multi-dot needs 8 reduction rows");
+  const RedSplit sp = red_split(n);
   for (int k0 = 0; k0 < nvec; k0 += kMultiVec) {
     const int m = (nvec - k0) < kMultiVec ? (nvec - k0) : kMultiVec;
-    multi_wdot_kernel<<<red_grid(n), kThreads, 0, s>>>(n, w, V + (size_t)k0 * n, m, x,
-                                                      red.partials + (size_t)slot * kRedBlocks, red.counters + slot,
-                                                      out + k0);
+    multi_wdot_kernel<<<sp.ctas, kThreads, 0, s>>>(n, sp.len, sp.warps, w, V + (size_t)k0 * n, m, x, red.row(slot),
+                                                  red.stride, red.counters + slot, out + k0);
     NRSG_CHECK_LAUNCH();
   }
 }
 
-__global__ void gram_schmidt_kernel(long long n, const double *__restrict__ w, const double *__restrict__ V, int nvec,
-                                    const double *__restrict__ y, double *__restrict__ x, double *partials,
-                                    unsigned *counter, double *nrm2)
+// x -= sum_k y_k V_k (fma in k order), nrm2 = (x, x)_w
+__global__ void __launch_bounds__(kThreads)
+    gram_schmidt_kernel(long long n, long long len, int W, const double *__restrict__ w,
+                        const double *__restrict__ V, int nvec, const double *__restrict__ y, double *__restrict__ x,
+                        double *row, unsigned *counter, double *nrm2)
 {
   __shared__ double s_y[64];
   for (int k = threadIdx.x; k < nvec; k += kThreads) s_y[k] = y[k];
   __syncthreads();
-  double acc = 0;
-  for (long long i = blockIdx.x * (long long)kThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kThreads) {
-    double v = x[i];
-    for (int k = 0; k < nvec; ++k) v -= s_y[k] * V[(size_t)k * n + i];
-    x[i] = v;
-    acc += w[i] * v * v;
-  }
-  finish_reduction(block_sum(acc), partials, counter, nrm2);
+  reduce1(
+      n, len, W,
+      [&](long long i) {
+        double v = x[i];
+        for (int k = 0; k < nvec; ++k) v = __fma_rn(-s_y[k], V[(size_t)k * n + i], v);
+        x[i] = v;
+        return wterm(w[i], v, v);
+      },
+      row, counter, nrm2);
 }
 void launch_gram_schmidt(long long n, const double *w, const double *V, int nvec, const double *y, double *x,
                          double *nrm2, Reduce &red, int slot, cudaStream_t s)
 {
   if (nvec > 64) throw Error(NRSG_ERR_BAD_CONFIG, "GMRES restart length above 64");
-  gram_schmidt_kernel<<<red_grid(n), kThreads, 0, s>>>(n, w, V, nvec, y, x, red.partials + (size_t)slot * kRedBlocks,
-                                                       red.counters + slot, nrm2);
+  NRSG_RED_ARGS(n, red, slot);
+  gram_schmidt_kernel<<<sp_.ctas, kThreads, 0, s>>>(n, sp_.len, sp_.warps, w, V, nvec, y, x, row_, cnt_, nrm2);
   NRSG_CHECK_LAUNCH();
 }
 
+// x += sum_k y_k V_k (fma in k order)
 __global__ void gmres_update_kernel(long long n, const double *__restrict__ V, int nvec, const double *__restrict__ y,
                                     double *__restrict__ x)
 {
@@ -511,7 +697,7 @@ __global__ void gmres_update_kernel(long long n, const double *__restrict__ V, i
   NRSG_GRID_LOOP(i, n)
   {
     double v = x[i];
-    for (int k = 0; k < nvec; ++k) v += s_y[k] * V[(size_t)k * n + i];
+    for (int k = 0; k < nvec; ++k) v = __fma_rn(s_y[k], V[(size_t)k * n + i], v);
     x[i] = v;
   }
 }
@@ -521,23 +707,26 @@ void launch_gmres_update(long long n, const double *V, int nvec, const double *y
   NRSG_CHECK_LAUNCH();
 }
 
-__global__ void residual_norm_kernel(long long n, const double *__restrict__ w, const double *__restrict__ b,
-                                     const double *__restrict__ Ax, double *__restrict__ r, double *partials,
-                                     unsigned *counter, double *nrm2)
+// r = b - Ax, nrm2 = (r, r)_w
+__global__ void __launch_bounds__(kThreads)
+    residual_norm_kernel(long long n, long long len, int W, const double *__restrict__ w,
+                         const double *__restrict__ b, const double *__restrict__ Ax, double *__restrict__ r,
+                         double *row, unsigned *counter, double *nrm2)
 {
-  double acc = 0;
-  for (long long i = blockIdx.x * (long long)kThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kThreads) {
-    const double v = b[i] - Ax[i];
-    r[i] = v;
-    acc += w[i] * v * v;
-  }
-  finish_reduction(block_sum(acc), partials, counter, nrm2);
+  reduce1(
+      n, len, W,
+      [&](long long i) {
+        const double v = dadd(b[i], -Ax[i]);
+        r[i] = v;
+        return wterm(w[i], v, v);
+      },
+      row, counter, nrm2);
 }
 void launch_residual_norm(long long n, const double *w, const double *b, const double *Ax, double *r, double *nrm2,
                           Reduce &red, int slot, cudaStream_t s)
 {
-  residual_norm_kernel<<<red_grid(n), kThreads, 0, s>>>(n, w, b, Ax, r, red.partials + (size_t)slot * kRedBlocks,
-                                                        red.counters + slot, nrm2);
+  NRSG_RED_ARGS(n, red, slot);
+  residual_norm_kernel<<<sp_.ctas, kThreads, 0, s>>>(n, sp_.len, sp_.warps, w, b, Ax, r, row_, cnt_, nrm2);
   NRSG_CHECK_LAUNCH();
 }
 
@@ -564,21 +753,23 @@ template void launch_scale_copy<float>(long long, float, const float *, float *,
 namespace nrsg {
 
 template <typename T>
-__global__ void pcgT_rdotz_kernel(long long n, const T *__restrict__ w, const T *__restrict__ invDiag,
-                                  const T *__restrict__ r, T *__restrict__ z, PcgScalars *sc, double *partials,
-                                  unsigned *counter)
+__global__ void __launch_bounds__(kThreads)
+    pcgT_rdotz_kernel(long long n, long long len, int W, const T *__restrict__ w, const T *__restrict__ invDiag,
+                      const T *__restrict__ r, T *__restrict__ z, PcgScalars *sc, double *row, unsigned *counter)
 {
-  double acc = 0;
-  for (long long i = blockIdx.x * (long long)kThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kThreads) {
-    const T ri = r[i];
-    const T zi = invDiag[i] * ri;
-    z[i] = zi;
-    acc += (double)w[i] * (double)ri * (double)zi;
-  }
   __shared__ double s_old;
   if (threadIdx.x == 0) s_old = sc->rdotz;
   __syncthreads();
-  if (finish_reduction(block_sum(acc), partials, counter, &sc->rdotz)) sc->rdotz_old = s_old;
+  const bool last = reduce1(
+      n, len, W,
+      [&](long long i) {
+        const T ri = r[i];
+        const T zi = invDiag[i] * ri;
+        z[i] = zi;
+        return wterm((double)w[i], (double)ri, (double)zi);
+      },
+      row, counter, &sc->rdotz);
+  if (last) sc->rdotz_old = s_old;
 }
 template <typename T>
 __global__ void pcgT_p_kernel(long long n, const T *__restrict__ z, T *__restrict__ p, const PcgScalars *sc, bool first)
@@ -587,27 +778,29 @@ __global__ void pcgT_p_kernel(long long n, const T *__restrict__ z, T *__restric
   NRSG_GRID_LOOP(i, n) p[i] = z[i] + beta * p[i];
 }
 template <typename T>
-__global__ void pcgT_xr_kernel(long long n, const T *__restrict__ w, const T *__restrict__ p, const T *__restrict__ Ap,
-                               T *__restrict__ x, T *__restrict__ r, PcgScalars *sc, double *partials,
-                               unsigned *counter)
+__global__ void __launch_bounds__(kThreads)
+    pcgT_xr_kernel(long long n, long long len, int W, const T *__restrict__ w, const T *__restrict__ p,
+                   const T *__restrict__ Ap, T *__restrict__ x, T *__restrict__ r, PcgScalars *sc, double *row,
+                   unsigned *counter)
 {
   const T alpha = (T)(sc->rdotz / (sc->pAp + 1e-300));
-  double acc = 0;
-  for (long long i = blockIdx.x * (long long)kThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kThreads) {
-    x[i] += alpha * p[i];
-    const T ri = r[i] - alpha * Ap[i];
-    r[i] = ri;
-    acc += (double)w[i] * (double)ri * (double)ri;
-  }
-  finish_reduction(block_sum(acc), partials, counter, &sc->rdotr);
+  reduce1(
+      n, len, W,
+      [&](long long i) {
+        x[i] += alpha * p[i];
+        const T ri = r[i] - alpha * Ap[i];
+        r[i] = ri;
+        return wterm((double)w[i], (double)ri, (double)ri);
+      },
+      row, counter, &sc->rdotr);
 }
 
 template <typename T>
 void launch_pcg_rdotz(long long n, const T *w, const T *invDiag, const T *r, T *z, PcgScalars *sc, Reduce &red, int slot,
                       cudaStream_t s)
 {
-  pcgT_rdotz_kernel<T><<<red_grid(n), kThreads, 0, s>>>(n, w, invDiag, r, z, sc, red.partials + (size_t)slot * kRedBlocks,
-                                                        red.counters + slot);
+  NRSG_RED_ARGS(n, red, slot);
+  pcgT_rdotz_kernel<T><<<sp_.ctas, kThreads, 0, s>>>(n, sp_.len, sp_.warps, w, invDiag, r, z, sc, row_, cnt_);
   NRSG_CHECK_LAUNCH();
 }
 template <typename T> void launch_pcg_p(long long n, const T *z, T *p, const PcgScalars *sc, bool first, cudaStream_t s)
@@ -619,8 +812,8 @@ template <typename T>
 void launch_pcg_xr(long long n, const T *w, const T *p, const T *Ap, T *x, T *r, PcgScalars *sc, Reduce &red, int slot,
                    cudaStream_t s)
 {
-  pcgT_xr_kernel<T><<<red_grid(n), kThreads, 0, s>>>(n, w, p, Ap, x, r, sc, red.partials + (size_t)slot * kRedBlocks,
-                                                     red.counters + slot);
+  NRSG_RED_ARGS(n, red, slot);
+  pcgT_xr_kernel<T><<<sp_.ctas, kThreads, 0, s>>>(n, sp_.len, sp_.warps, w, p, Ap, x, r, sc, row_, cnt_);
   NRSG_CHECK_LAUNCH();
 }
 #define NRSG_INST_PCGT(T)                                                                                  \

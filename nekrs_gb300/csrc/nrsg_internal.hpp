@@ -140,13 +140,15 @@ void trilinear_nodes(int N, long long E, const double *VX, const std::vector<dou
 // ----------------------------------------------------------------------------
 // Device kernels (launchers)
 // ----------------------------------------------------------------------------
+constexpr int kRedThreads = 256;
+constexpr int kRedSegments = 4096; // warp runs per reduction: doubles per Reduce row
 struct Reduce {              // scratch for deterministic one-launch reductions
-  double *partials = nullptr; // [slots][kMaxBlocks]
+  double *partials = nullptr; // [slots][stride] warp-run sums
   unsigned *counters = nullptr;
   int slots = 0;
+  long long stride = kRedSegments;
+  double *row(int slot) const { return partials + (size_t)slot * stride; }
 };
-constexpr int kRedBlocks = 1216;     // 152 SMs x 8
-constexpr int kRedThreads = 256;
 
 template <typename T>
 void launch_ax_stored(int N, long long E, const T *ggeo, const T *D, T lambda0, T lambda1, bool poisson, const T *q,

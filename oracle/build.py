@@ -6,10 +6,30 @@ tree is present, the reference's serial kernels into oracle/_ref.
 """
 import glob
 import os
+import platform
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
+
+
+def _fp_flags():
+    """No floating-point contraction: the oracle rounds the same way on every
+    host, with fused multiply-adds only where the source calls std::fma.  On
+    x86-64 hosts whose CPU has FMA, -mfma lets those calls compile to the
+    instruction instead of a library call (same result, correctly rounded)."""
+    flags = ["-ffp-contract=off"]
+    if platform.machine() in ("x86_64", "AMD64"):
+        try:
+            with open("/proc/cpuinfo") as f:
+                if " fma " in f.read():
+                    flags.append("-mfma")
+        except OSError:
+            pass
+    return flags
+
+
+FP_FLAGS = _fp_flags()
 
 
 def build_oracle(force=False):
@@ -25,7 +45,7 @@ def build_oracle(force=False):
     for s in srcs:
         o = os.path.join(BUILD, os.path.basename(s)[:-4] + ".o")
         objs.append(o)
-        procs.append(subprocess.Popen(["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC", "-c", s, "-o", o]))
+        procs.append(subprocess.Popen(["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC"] + FP_FLAGS + ["-c", s, "-o", o]))
     for p in procs:
         if p.wait() != 0:
             raise RuntimeError("oracle build failed")

@@ -36,7 +36,7 @@ def lib():
         _lib.orc_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p]
         _lib.orc_volume.restype = ctypes.c_double
         _lib.orc_volume.argtypes = [ctypes.c_void_p]
-        for name in ("orc_ax", "orc_operator", "orc_precond"):
+        for name in ("orc_ax", "orc_ax_ref", "orc_operator", "orc_precond"):
             getattr(_lib, name).argtypes = [ctypes.c_void_p, D, D]
         _lib.orc_ax_fp32.argtypes = [ctypes.c_void_p, F, F]
         _lib.orc_gs.argtypes = [ctypes.c_void_p, D]
@@ -58,6 +58,10 @@ def lib():
             [ctypes.c_void_p] * 5
         _lib.orc_global_ids.argtypes = [ctypes.c_int, ctypes.c_longlong, L, L]
         _lib.orc_gll.argtypes = [ctypes.c_int, D, D]
+        _lib.orc_wdot.restype = ctypes.c_double
+        _lib.orc_wdot.argtypes = [ctypes.c_longlong, ctypes.c_void_p, D, D]
+        _lib.orc_update_pcg.restype = ctypes.c_double
+        _lib.orc_update_pcg.argtypes = [ctypes.c_longlong, D, D, D, ctypes.c_double, D, D]
         _lib.orc_dmatrix.argtypes = [ctypes.c_int, D]
         _lib.orc_interp.argtypes = [ctypes.c_int, ctypes.c_int, D]
         vp, ci, cd, cl = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_longlong
@@ -86,6 +90,22 @@ def gll(N):
     w = np.zeros(N + 1)
     lib().orc_gll(N, _p(z, D), _p(w, D))
     return z, w
+
+
+def wdot(w, a, b):
+    """sum_i w_i (a_i b_i) in the device library's reduction order (w None: unweighted)."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    if w is None:
+        return lib().orc_wdot(a.size, None, _p(a, D), _p(b, D))
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    return lib().orc_wdot(a.size, w.ctypes.data_as(ctypes.c_void_p), _p(a, D), _p(b, D))
+
+
+def update_pcg(w, p, Ap, alpha, x, r):
+    """The fused PCG update in place on x and r; returns (r, r)_w."""
+    arrs = [np.ascontiguousarray(v, dtype=np.float64) for v in (w, p, Ap)]
+    return lib().orc_update_pcg(x.size, _p(arrs[0], D), _p(arrs[1], D), _p(arrs[2], D), alpha, _p(x, D), _p(r, D))
 
 
 def dmatrix(N):
@@ -196,6 +216,13 @@ class Elliptic:
         q = np.ascontiguousarray(q, dtype=np.float64)
         out = np.zeros_like(q)
         lib().orc_ax(self.h, _p(q, D), _p(out, D))
+        return out
+
+    def ax_ref(self, q):
+        """FP64 Ax in the operation order of the reference's serial kernel."""
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        out = np.zeros_like(q)
+        lib().orc_ax_ref(self.h, _p(q, D), _p(out, D))
         return out
 
     def ax_fp32(self, q):

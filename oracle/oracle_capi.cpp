@@ -2,6 +2,8 @@
 // Flat C entry points used by oracle/oracle.py (ctypes).
 #include "oracle_internal.hpp"
 
+#include <cmath>
+
 #include <cstdint>
 #include <cstring>
 #include <stdexcept>
@@ -23,6 +25,22 @@ uint64_t splitmix64(uint64_t x)
 extern "C" {
 
 void orc_gll(int N, double *z, double *w) { gll(N, z, w); }
+// weighted inner product sum_i w_i (a_i b_i) in the device's reduction order (w may be null: 1)
+double orc_wdot(long long n, const double *w, const double *a, const double *b)
+{
+  if (!w) return wsum(n, [&](long long i) { return a[i] * b[i]; });
+  return wdot<double>(n, w, a, b);
+}
+// the fused PCG update: r = fma(-alpha, Ap, r), x = fma(alpha, p, x), returns (r, r)_w
+double orc_update_pcg(long long n, const double *w, const double *p, const double *Ap, double alpha, double *x,
+                      double *r)
+{
+  for (long long i = 0; i < n; ++i) {
+    r[i] = std::fma(-alpha, Ap[i], r[i]);
+    x[i] = std::fma(alpha, p[i], x[i]);
+  }
+  return wdot<double>(n, w, r, r);
+}
 void orc_dmatrix(int N, double *D)
 {
   std::vector<double> z(N + 1), w(N + 1);
@@ -120,6 +138,7 @@ int orc_get(void *h, const char *name, void *out)
 double orc_volume(void *h) { return ((Elliptic *)h)->fine.volume; }
 
 void orc_ax(void *h, const double *q, double *Aq) { ((Elliptic *)h)->ax(q, Aq); }
+void orc_ax_ref(void *h, const double *q, double *Aq) { ((Elliptic *)h)->ax_ref(q, Aq); }
 void orc_ax_fp32(void *h, const float *q, float *Aq)
 {
   auto *el = (Elliptic *)h;

@@ -34,6 +34,36 @@ void build_diag(const Level &L, const T *ggeo, const T *D, T lambda0, T lambda1,
 template <typename T> void gs_add(const Level &L, T *q);
 template <typename T> void apply_mask(const Level &L, T *q);
 template <typename T> T wdot(long long n, const T *w, const T *a, const T *b);
+void ax_stored_dev(const Level &L, const double *ggeo, const double *D, double lambda0, double lambda1, bool poisson,
+                   const double *q, double *Aq);
+
+// Sum of term(i), i < n, in the device library's reduction order: 256-entry
+// chunks (entries past n are +0.0), each summed by the tree s[x] += s[x+o],
+// o = 128, 64, ..., 1 (the block order of the reference's
+// weightedInnerProdMany.okl:27-105); then the chunk sums by the blocked
+// pairwise tree ((P0 + P1) + (P2 + P3)) + ..., zero-padded to a power of two.
+template <typename F> double wsum(long long n, const F &term)
+{
+  const long long nc = (n + 255) / 256;
+  if (nc <= 0) return 0.0;
+  long long M = 1;
+  while (M < nc) M <<= 1;
+  std::vector<double> P((size_t)M, 0.0);
+#pragma omp parallel for schedule(static)
+  for (long long c = 0; c < nc; ++c) {
+    double t[256];
+    for (int x = 0; x < 256; ++x) {
+      const long long i = c * 256 + x;
+      t[x] = i < n ? term(i) : 0.0;
+    }
+    for (int o = 128; o >= 1; o >>= 1)
+      for (int x = 0; x < o; ++x) t[x] = t[x] + t[x + o];
+    P[(size_t)c] = t[0];
+  }
+  for (long long len = M; len > 1; len >>= 1)
+    for (long long x = 0; x < len / 2; ++x) P[(size_t)x] = P[(size_t)(2 * x)] + P[(size_t)(2 * x + 1)];
+  return P[0];
+}
 
 void assemble_fem(const Level &L, double lambda0, double lambda1, bool poisson, std::vector<long long> &rowPtr,
                   std::vector<long long> &cols, std::vector<double> &vals);
@@ -55,7 +85,8 @@ struct Elliptic {
   int status = 0;                         // 0 ok, 1 max-iterations, 3 NaN
 
   void setup(int N, long long E, const double *VX, const long long *EToV, const int *EToB, const std::string &opt);
-  void ax(const double *q, double *Aq) const;
+  void ax(const double *q, double *Aq) const;      // FP64 operator in the device's operation order
+  void ax_ref(const double *q, double *Aq) const;  // the reference serial kernel's operation order
   void op(const double *q, double *Aq) const;
   void precond(const double *r, double *z);
   double norm(const double *r) const;

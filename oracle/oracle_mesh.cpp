@@ -27,53 +27,70 @@ namespace orc {
 // ---------------------------------------------------------------------------
 // 1-D basis.  nekRS computes GLL nodes with a Golub-Welsch Jacobi-Gauss
 // solve and D / interpolation through Vandermonde right-solves
-// (src/mesh/meshBasis1D.cpp:99-153,249-280).  The restatement uses the
-// closed forms (Newton on (1-x^2)P_N'(x), barycentric Lagrange weights),
-// which agree to rounding; parity tests compare to 1e-13.
+// (src/mesh/meshBasis1D.cpp:99-153,249-280).  The restatement uses closed
+// forms, which agree with those to rounding: the interior nodes are the
+// roots of P_N'(x) found by Newton's method on f = P_{N-1} - x P_N (a
+// multiple of (1 - x^2) P_N'/N) with f' = -(N+1) P_N at the root, from
+// Chebyshev-Lobatto guesses; weights 2/(N(N+1) P_N^2); D from the node
+// products c_j = prod_{k != j} (z_j - z_k).  The FP64 solve compares the
+// device bit for bit with this oracle, so these are the same operations, in
+// the same order, as the device library's host setup.
 // ---------------------------------------------------------------------------
-static void legendre(int n, double x, double &p, double &dp)
+static void legendre_pair(int n, double x, double &pn, double &pnm1)
 {
-  double p0 = 1.0, p1 = x;
-  if (n == 0) { p = 1.0; dp = 0.0; return; }
+  double a = 1.0, b = x;
+  if (n == 0) { pn = 1.0; pnm1 = 0.0; return; }
   for (int k = 2; k <= n; ++k) {
-    const double pk = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
-    p0 = p1;
-    p1 = pk;
+    const double c = ((2 * k - 1) * x * b - (k - 1) * a) / k;
+    a = b;
+    b = c;
   }
-  p = p1;
-  dp = (std::fabs(x) < 1.0) ? n * (p0 - x * p1) / (1.0 - x * x) : 0.5 * n * (n + 1) * (x > 0 ? 1.0 : (n % 2 ? 1.0 : -1.0));
+  pn = b;
+  pnm1 = a;
 }
 
 void gll(int N, double *z, double *w)
 {
+  for (int i = 0; i <= N; ++i) z[i] = 0.0;
   z[0] = -1.0;
   z[N] = 1.0;
-  for (int i = 1; i < N; ++i) {
-    // Chebyshev-Gauss-Lobatto initial guess, then Newton on q(x) = (1-x^2) P_N'(x)
+  for (int i = 1; i <= N / 2; ++i) {
     double x = -std::cos(M_PI * i / N);
-    for (int it = 0; it < 100; ++it) {
-      double p, dp;
-      legendre(N, x, p, dp);
-      // q = (1-x^2) P', q' = -N(N+1) P
-      const double q = (1.0 - x * x) * dp;
-      const double dq = -N * (N + 1.0) * p;
-      const double dx = q / dq;
+    for (int it = 0; it < 64; ++it) {
+      double pn, pm;
+      legendre_pair(N, x, pn, pm);
+      const double f = pm - x * pn;
+      const double df = -(N + 1.0) * pn;
+      const double dx = f / df;
       x -= dx;
-      if (std::fabs(dx) < 1e-16) break;
+      if (std::fabs(dx) < 1e-17) break;
     }
     z[i] = x;
-  }
-  // symmetrise
-  for (int i = 0; i <= N / 2; ++i) {
-    const double a = 0.5 * (z[N - i] - z[i]);
-    z[i] = -a;
-    z[N - i] = a;
+    z[N - i] = -x;
   }
   if (N % 2 == 0) z[N / 2] = 0.0;
   for (int i = 0; i <= N; ++i) {
-    double p, dp;
-    legendre(N, z[i], p, dp);
-    w[i] = 2.0 / (N * (N + 1.0) * p * p);
+    double pn, pm;
+    legendre_pair(N, z[i], pn, pm);
+    w[i] = 2.0 / (N * (N + 1.0) * pn * pn);
+  }
+}
+
+void dmatrix(int N, const double *z, double *D)
+{
+  const int nq = N + 1;
+  std::vector<double> c(nq, 1.0);
+  for (int j = 0; j < nq; ++j)
+    for (int k = 0; k < nq; ++k)
+      if (k != j) c[j] *= (z[j] - z[k]);
+  for (int i = 0; i < nq; ++i) {
+    double s = 0;
+    for (int j = 0; j < nq; ++j) {
+      if (j == i) continue;
+      D[i * nq + j] = c[i] / (c[j] * (z[i] - z[j]));
+      s += D[i * nq + j];
+    }
+    D[i * nq + i] = -s;
   }
 }
 
@@ -84,23 +101,6 @@ static void bary_weights(int n, const double *z, double *lam)
     for (int k = 0; k < n; ++k)
       if (k != j) prod *= (z[j] - z[k]);
     lam[j] = 1.0 / prod;
-  }
-}
-
-void dmatrix(int N, const double *z, double *D)
-{
-  const int nq = N + 1;
-  std::vector<double> lam(nq);
-  bary_weights(nq, z, lam.data());
-  for (int i = 0; i < nq; ++i) {
-    double diag = 0.0;
-    for (int j = 0; j < nq; ++j) {
-      if (i == j) continue;
-      const double v = (lam[j] / lam[i]) / (z[i] - z[j]);
-      D[i * nq + j] = v;
-      diag -= v;
-    }
-    D[i * nq + i] = diag;
   }
 }
 
@@ -189,7 +189,8 @@ void box_mesh(int nx, int ny, int nz, double eps, double *VX, long long *EToV, i
 }
 
 // Trilinear node coordinates from the 8 vertices (straight-sided hexes, as
-// Nek5000 builds xm1 for elements without curved sides).
+// Nek5000 builds xm1 for elements without curved sides); blending weights
+// (hr hs) ht and fused multiply-adds in vertex order, as the device does.
 void trilinear_coords(int N, long long E, const double *VX, const double *z1, double *x, double *y, double *z)
 {
   const int nq = N + 1, np = nq * nq * nq;
@@ -204,9 +205,9 @@ void trilinear_coords(int N, long long E, const double *VX, const double *z1, do
           double X = 0, Y = 0, Z = 0;
           for (int v = 0; v < 8; ++v) {
             const double wv = hr[v & 1] * hs[(v >> 1) & 1] * ht[(v >> 2) & 1];
-            X += wv * VX[(e * 8 + v) * 3 + 0];
-            Y += wv * VX[(e * 8 + v) * 3 + 1];
-            Z += wv * VX[(e * 8 + v) * 3 + 2];
+            X = std::fma(wv, VX[(e * 8 + v) * 3 + 0], X);
+            Y = std::fma(wv, VX[(e * 8 + v) * 3 + 1], Y);
+            Z = std::fma(wv, VX[(e * 8 + v) * 3 + 2], Z);
           }
           const long long id = e * np + i + nq * (j + nq * k);
           x[id] = X;
@@ -217,6 +218,9 @@ void trilinear_coords(int N, long long E, const double *VX, const double *z1, do
 
 // Geometric factors, restated from kernels/mesh/geometricFactorsHex3D.okl:77-139.
 // ggeo layout [e][7][Np] with G00,G01,G11,G12,G02,G22,GWJ (mesh3D.h:96-102).
+// Every multiply-add is an explicit std::fma or a separately rounded product,
+// in the order of the device kernel (geofac_kernel), so that the FP64
+// factors are bit-identical to the device's.
 void geometric_factors(int N, long long E, const double *D, const double *w, const double *x, const double *y,
                        const double *z, double *ggeo, double *J_out)
 {
@@ -229,30 +233,38 @@ void geometric_factors(int N, long long E, const double *D, const double *w, con
           double xr = 0, xs = 0, xt = 0, yr = 0, ys = 0, yt = 0, zr = 0, zs = 0, zt = 0;
           for (int m = 0; m < nq; ++m) {
             const int ir = m + nq * (j + nq * k), is = i + nq * (m + nq * k), it = i + nq * (j + nq * m);
-            xr += D[i * nq + m] * xe[ir];
-            xs += D[j * nq + m] * xe[is];
-            xt += D[k * nq + m] * xe[it];
-            yr += D[i * nq + m] * ye[ir];
-            ys += D[j * nq + m] * ye[is];
-            yt += D[k * nq + m] * ye[it];
-            zr += D[i * nq + m] * ze[ir];
-            zs += D[j * nq + m] * ze[is];
-            zt += D[k * nq + m] * ze[it];
+            xr = std::fma(D[i * nq + m], xe[ir], xr);
+            xs = std::fma(D[j * nq + m], xe[is], xs);
+            xt = std::fma(D[k * nq + m], xe[it], xt);
+            yr = std::fma(D[i * nq + m], ye[ir], yr);
+            ys = std::fma(D[j * nq + m], ye[is], ys);
+            yt = std::fma(D[k * nq + m], ye[it], yt);
+            zr = std::fma(D[i * nq + m], ze[ir], zr);
+            zs = std::fma(D[j * nq + m], ze[is], zs);
+            zt = std::fma(D[k * nq + m], ze[it], zt);
           }
-          const double J = xr * (ys * zt - zs * yt) - yr * (xs * zt - zs * xt) + zr * (xs * yt - ys * xt);
+          // 2x2 minors a b - c d as fma(a, b, -(c d)) (the device kernel's operation order)
+          auto minor2 = [](double a, double b, double c, double d) { return std::fma(a, b, -(c * d)); };
+          const double cx = minor2(ys, zt, zs, yt), cy = minor2(xs, zt, zs, xt), cz = minor2(xs, yt, ys, xt);
+          const double J = std::fma(zr, cz, std::fma(-yr, cy, xr * cx));
           const double Ji = 1.0 / J;
           const double JW = J * w[i] * w[j] * w[k];
-          const double rx = (ys * zt - zs * yt) * Ji, ry = -(xs * zt - zs * xt) * Ji, rz = (xs * yt - ys * xt) * Ji;
-          const double sx = -(yr * zt - zr * yt) * Ji, sy = (xr * zt - zr * xt) * Ji, sz = -(xr * yt - yr * xt) * Ji;
-          const double tx = (yr * zs - zr * ys) * Ji, ty = -(xr * zs - zr * xs) * Ji, tz = (xr * ys - yr * xs) * Ji;
+          const double rx = cx * Ji, ry = -cy * Ji, rz = cz * Ji;
+          const double sx = -minor2(yr, zt, zr, yt) * Ji, sy = minor2(xr, zt, zr, xt) * Ji,
+                       sz = -minor2(xr, yt, yr, xt) * Ji;
+          const double tx = minor2(yr, zs, zr, ys) * Ji, ty = -minor2(xr, zs, zr, xs) * Ji,
+                       tz = minor2(xr, ys, yr, xs) * Ji;
+          auto dot3 = [](double a0, double b0, double a1, double b1, double a2, double b2) {
+            return std::fma(a2, b2, std::fma(a1, b1, a0 * b0));
+          };
           const int n = i + nq * (j + nq * k);
           double *g = ggeo + e * 7 * np;
-          g[0 * np + n] = JW * (rx * rx + ry * ry + rz * rz);
-          g[1 * np + n] = JW * (rx * sx + ry * sy + rz * sz);
-          g[2 * np + n] = JW * (sx * sx + sy * sy + sz * sz);
-          g[3 * np + n] = JW * (sx * tx + sy * ty + sz * tz);
-          g[4 * np + n] = JW * (rx * tx + ry * ty + rz * tz);
-          g[5 * np + n] = JW * (tx * tx + ty * ty + tz * tz);
+          g[0 * np + n] = JW * dot3(rx, rx, ry, ry, rz, rz);
+          g[1 * np + n] = JW * dot3(rx, sx, ry, sy, rz, sz);
+          g[2 * np + n] = JW * dot3(sx, sx, sy, sy, sz, sz);
+          g[3 * np + n] = JW * dot3(sx, tx, sy, ty, sz, tz);
+          g[4 * np + n] = JW * dot3(rx, tx, ry, ty, rz, tz);
+          g[5 * np + n] = JW * dot3(tx, tx, ty, ty, tz, tz);
           g[6 * np + n] = JW;
           if (J_out) J_out[e * np + n] = J;
         }

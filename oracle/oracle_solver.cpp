@@ -11,6 +11,19 @@
 //   pcg / flexible pcg              src/solvers/elliptic/linearSolver/PCG.cpp:33-203
 //   pgmres / flexible pgmres        src/solvers/elliptic/linearSolver/PGMRES.cpp:31-340
 // The multigrid preconditioner lives in oracle_mg.cpp.
+//
+// Bit-identical FP64 path.  The plain FP64 solve (stored geometry; Jacobi or
+// no preconditioner; PCG, flexible PCG, GMRES, flexible GMRES; solution
+// projection) performs exactly the device library's floating-point
+// operations in the device's order: weighted sums through wsum() (256-entry
+// chunks by the reference's block tree, then a blocked pairwise tree over the
+// chunk sums), std::fma wherever the device uses a fused multiply-add, and
+// separately rounded products elsewhere.  The oracle is compiled without
+// contraction (-ffp-contract=off), so the same source rounds the same way on
+// every host.  The reference-order operator (ax_stored, the order of the
+// reference's serial kernel) is kept and pinned bit for bit against that
+// kernel; the device-order operator (ax_stored_dev) differs from it only by
+// fused rounding.
 
 #include "oracle_internal.hpp"
 
@@ -180,6 +193,56 @@ void ax_stored(const Level &L, const T *ggeo, const T *D, T lambda0, T lambda1, 
   }
 }
 
+// Ax, stored geometric factors, FP64 in the device kernel's operation order
+// (ax_stored_kernel<double>): per k-plane, qt, qr, qs as fused multiply-add
+// chains over m; G q as lambda0 fma(Gc, qt, fma(Gb, qs, Ga qr)); then for m
+// ascending auk += D[m][j] Gs(i,m,k), Aq(i,j,m) += D[k][m] Gt(i,j,k),
+// auk += D[m][i] Gr(m,j,k), all fused; Aq(i,j,k) += auk at the end of plane k.
+void ax_stored_dev(const Level &L, const double *ggeo, const double *D, double lambda0, double lambda1, bool poisson,
+                   const double *q, double *Aq)
+{
+  const int nq = L.Nq, np = L.Np, nq2 = nq * nq;
+  auto gflux = [&](double Ga, double Gb, double Gc, double qr, double qs, double qt) {
+    return lambda0 * std::fma(Gc, qt, std::fma(Gb, qs, Ga * qr));
+  };
+#pragma omp parallel for
+  for (long long e = 0; e < L.E; ++e) {
+    std::vector<double> Gr(nq2), Gs(nq2), Gt(nq2), auk(nq2), rAq(np, 0.0);
+    const double *qe = q + e * np;
+    const double *g = ggeo + (size_t)e * 7 * np;
+    for (int k = 0; k < nq; ++k) {
+      for (int j = 0; j < nq; ++j)
+        for (int i = 0; i < nq; ++i) {
+          const int n = i + nq * (j + nq * k), t = i + nq * j;
+          double qt = 0, qr = 0, qs = 0;
+          for (int m = 0; m < nq; ++m) qt = std::fma(D[k * nq + m], qe[t + nq2 * m], qt);
+          for (int m = 0; m < nq; ++m) {
+            qr = std::fma(D[i * nq + m], qe[m + nq * j + nq2 * k], qr);
+            qs = std::fma(D[j * nq + m], qe[i + nq * m + nq2 * k], qs);
+          }
+          const double G00 = g[0 * np + n], G01 = g[1 * np + n], G11 = g[2 * np + n];
+          const double G12 = g[3 * np + n], G02 = g[4 * np + n], G22 = g[5 * np + n];
+          Gr[t] = gflux(G00, G01, G02, qr, qs, qt);
+          Gs[t] = gflux(G01, G11, G12, qr, qs, qt);
+          Gt[t] = gflux(G02, G12, G22, qr, qs, qt);
+          auk[t] = poisson ? 0.0 : g[6 * np + n] * lambda1 * qe[n];
+        }
+      for (int j = 0; j < nq; ++j)
+        for (int i = 0; i < nq; ++i) {
+          const int t = i + nq * j;
+          double a = auk[t];
+          for (int m = 0; m < nq; ++m) {
+            a = std::fma(D[m * nq + j], Gs[i + nq * m], a);
+            rAq[t + nq2 * m] = std::fma(D[k * nq + m], Gt[t], rAq[t + nq2 * m]);
+            a = std::fma(D[m * nq + i], Gr[m + nq * j], a);
+          }
+          rAq[t + nq2 * k] += a;
+        }
+    }
+    std::copy(rAq.begin(), rAq.end(), Aq + e * np);
+  }
+}
+
 // Ax with geometric factors rebuilt from the 8 trilinear vertices
 // (ellipticPartialAxTrilinearHex3D.okl:50-120).  Vertex input is in
 // hypercube order; lambda0 scales all three fluxes (the reference applies it
@@ -269,6 +332,22 @@ void build_diag(const Level &L, const T *ggeo, const T *D, T lambda0, T lambda1,
           const int n = i + nq * (j + nq * k);
           T r = 0;
           const T grs = g[1 * np + n], grt = g[4 * np + n], gst = g[3 * np + n];
+          if constexpr (sizeof(T) == 8) {
+            // the device kernel's order: fma(((2 g) l0) Da, Db, r), fma((g l0) Dm, Dm, r)
+            auto cross = [&](double g0, double Da, double Db) { r = std::fma(2.0 * g0 * lambda0 * Da, Db, r); };
+            auto line = [&](double g0, double Dm) { r = std::fma(g0 * lambda0 * Dm, Dm, r); };
+            cross(grs, D[i * nq + i], D[j * nq + j]);
+            cross(grt, D[i * nq + i], D[k * nq + k]);
+            cross(gst, D[j * nq + j], D[k * nq + k]);
+            for (int m = 0; m < nq; ++m) {
+              line(g[0 * np + m + nq * (j + nq * k)], D[m * nq + i]);
+              line(g[2 * np + i + nq * (m + nq * k)], D[m * nq + j]);
+              line(g[5 * np + i + nq * (j + nq * m)], D[m * nq + k]);
+            }
+            if (!poisson) r = std::fma(g[6 * np + n], lambda1, r);
+            diag[e * np + n] = r;
+            continue;
+          }
           r += (T)2.0 * grs * lambda0 * D[i * nq + i] * D[j * nq + j];
           r += (T)2.0 * grt * lambda0 * D[i * nq + i] * D[k * nq + k];
           r += (T)2.0 * gst * lambda0 * D[j * nq + j] * D[k * nq + k];
@@ -301,21 +380,10 @@ template <typename T> void apply_mask(const Level &L, T *q)
   for (int m : L.maskIds) q[m] = 0;
 }
 
-// Deterministic: fixed blocks summed in parallel, block sums added in order,
-// so the result does not depend on the thread count or schedule.
+// Weighted inner product in the device's summation order (wsum).
 template <typename T> T wdot(long long n, const T *w, const T *a, const T *b)
 {
-  const long long B = 4096, nb = (n + B - 1) / B;
-  std::vector<double> part(nb);
-#pragma omp parallel for schedule(static)
-  for (long long k = 0; k < nb; ++k) {
-    double s = 0;
-    for (long long i = k * B; i < std::min(n, (k + 1) * B); ++i) s += (double)w[i] * (double)a[i] * (double)b[i];
-    part[k] = s;
-  }
-  double s = 0;
-  for (long long k = 0; k < nb; ++k) s += part[k];
-  return (T)s;
+  return (T)wsum(n, [&](long long i) { return (double)w[i] * ((double)a[i] * (double)b[i]); });
 }
 
 // explicit instantiations used by the MG code
@@ -359,7 +427,12 @@ void Elliptic::ax(const double *q, double *Aq) const
   if (o.trilinear)
     ax_trilinear(fine, o.lambda0, o.lambda1, o.poisson, q, Aq);
   else
-    ax_stored<double>(fine, fine.ggeo.data(), fine.D.data(), o.lambda0, o.lambda1, o.poisson, q, Aq);
+    ax_stored_dev(fine, fine.ggeo.data(), fine.D.data(), o.lambda0, o.lambda1, o.poisson, q, Aq);
+}
+
+void Elliptic::ax_ref(const double *q, double *Aq) const
+{
+  ax_stored<double>(fine, fine.ggeo.data(), fine.D.data(), o.lambda0, o.lambda1, o.poisson, q, Aq);
 }
 
 void Elliptic::op(const double *q, double *Aq) const
@@ -386,15 +459,15 @@ void Elliptic::precond(const double *r, double *z)
 void Elliptic::zero_mean(double *q) const
 {
   const long long n = fine.Nlocal;
-  double s = 0;
-  for (long long i = 0; i < n; ++i) s += q[i];
+  const double s = wsum(n, [&](long long i) { return q[i]; });
   const double mean = s / (double)n;
   for (long long i = 0; i < n; ++i) q[i] += -mean;
 }
 
 double Elliptic::norm(const double *r) const
 {
-  return std::sqrt(wdot<double>(fine.Nlocal, fine.invDegree.data(), r, r) / fine.volume);
+  // res0Norm = weightedNorm2Many * sqrt(resNormFactor) (ellipticSolve.cpp:130-139)
+  return std::sqrt(wdot<double>(fine.Nlocal, fine.invDegree.data(), r, r)) * std::sqrt(1.0 / fine.volume);
 }
 
 // PCG / flexible PCG (PCG.cpp:86-203)
@@ -426,17 +499,17 @@ int Elliptic::pcg(double *r, double *x, double tol, int maxit, double &rnorm)
         beta = -alpha * zdotAp / rdotz2;
       }
     }
-    for (long long i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+    for (long long i = 0; i < n; ++i) p[i] = std::fma(beta, p[i], z[i]);
     op(p.data(), Ap.data());
     const double pAp = wdot<double>(n, w, p.data(), Ap.data());
     alpha = rdotz1 / (pAp + 1e-300);
-    double rdotr = 0;
     for (long long i = 0; i < n; ++i) {
-      r[i] -= alpha * Ap[i];
-      rdotr += r[i] * r[i] * w[i];
+      r[i] = std::fma(-alpha, Ap[i], r[i]);
+      x[i] = std::fma(alpha, p[i], x[i]);
     }
-    for (long long i = 0; i < n; ++i) x[i] += alpha * p[i];
-    rnorm = std::sqrt(rdotr / fine.volume);
+    const double rdotr = wdot<double>(n, w, r, r);
+    // rdotr = sqrt(update() * resNormFactor) (PCG.cpp:189)
+    rnorm = std::sqrt(rdotr * (1.0 / fine.volume));
     history.push_back(rnorm);
     if (std::isnan(rnorm)) { status = 3; break; }
   } while (rnorm > tol && it < maxit);
@@ -468,14 +541,14 @@ void Elliptic::proj_update_space()
   double *xm = &projXX[(size_t)(m - 1) * n];
   for (long long i = 0; i < n; ++i) {
     double v = xm[i];
-    for (int k = 0; k < m - 1; ++k) v = -alpha[k] * projXX[(size_t)k * n + i] + v;
+    for (int k = 0; k < m - 1; ++k) v = std::fma(-alpha[k], projXX[(size_t)k * n + i], v);
     xm[i] = v;
   }
   if (classic) {
     double *bm = &projBB[(size_t)(m - 1) * n];
     for (long long i = 0; i < n; ++i) {
       double v = bm[i];
-      for (int k = 0; k < m - 1; ++k) v = -alpha[k] * projBB[(size_t)k * n + i] + v;
+      for (int k = 0; k < m - 1; ++k) v = std::fma(-alpha[k], projBB[(size_t)k * n + i], v);
       bm[i] = v;
     }
   }
@@ -503,14 +576,14 @@ void Elliptic::proj_pre(double *r)
   for (int k = 0; k < m; ++k) alpha[k] = wdot<double>(n, w, &projXX[(size_t)k * n], r);
   for (long long i = 0; i < n; ++i) {
     double v = alpha[0] * projXX[i];
-    for (int k = 1; k < m; ++k) v += alpha[k] * projXX[(size_t)k * n + i];
+    for (int k = 1; k < m; ++k) v = std::fma(alpha[k], projXX[(size_t)k * n + i], v);
     projXbar[i] = v;
   }
   std::vector<double> t(n);
   if (o.projection == 1) {
     for (long long i = 0; i < n; ++i) {
       double v = alpha[0] * projBB[i];
-      for (int k = 1; k < m; ++k) v += alpha[k] * projBB[(size_t)k * n + i];
+      for (int k = 1; k < m; ++k) v = std::fma(alpha[k], projBB[(size_t)k * n + i], v);
       t[i] = v;
     }
   } else {
@@ -611,13 +684,13 @@ int Elliptic::pgmres(double *r, double *x, double tol, int maxit, double &rdotr)
     if (flexible) {
       for (long long q = 0; q < n; ++q) {
         double v = x[q];
-        for (int k = 0; k < m; ++k) v += y[k] * Z[k][q];
+        for (int k = 0; k < m; ++k) v = std::fma(y[k], Z[k][q], v);
         x[q] = v;
       }
     } else {
       for (long long q = 0; q < n; ++q) {
         double v = 0;
-        for (int k = 0; k < m; ++k) v += y[k] * V[k][q];
+        for (int k = 0; k < m; ++k) v = std::fma(y[k], V[k][q], v);
         ztmp[q] = v;
       }
       precond(ztmp.data(), tmp.data());
@@ -627,23 +700,24 @@ int Elliptic::pgmres(double *r, double *x, double tol, int maxit, double &rdotr)
   int iter = 0;
   for (iter = 0; iter < maxit;) {
     s[0] = nrm;
-    for (long long q = 0; q < n; ++q) V[0][q] = r[q] / nrm;
+    const double inrm = 1.0 / nrm;
+    for (long long q = 0; q < n; ++q) V[0][q] = inrm * r[q];
     for (int i = 0; i < nr; ++i) {
       std::vector<double> &Mv = flexible ? Z[i] : Z[0];
       precond(V[i].data(), Mv.data());
       op(Mv.data(), w.data());
       for (int k = 0; k <= i; ++k) y[k] = wdot<double>(n, wt, V[k].data(), w.data());
-      double nw2 = 0;
       for (long long q = 0; q < n; ++q) {
         double v = w[q];
-        for (int k = 0; k <= i; ++k) v -= y[k] * V[k][q];
+        for (int k = 0; k <= i; ++k) v = std::fma(-y[k], V[k][q], v);
         w[q] = v;
-        nw2 += wt[q] * v * v;
       }
-      const double nw = std::sqrt(nw2);
+      const double nw = std::sqrt(wdot<double>(n, wt, w.data(), w.data()));
       H[i + 1 + i * ld] = nw;
-      if (i < nr - 1)
-        for (long long q = 0; q < n; ++q) V[i + 1][q] = w[q] / nw;
+      if (i < nr - 1) {
+        const double inw = 1.0 / nw;
+        for (long long q = 0; q < n; ++q) V[i + 1][q] = inw * w[q];
+      }
       for (int k = 0; k <= i; ++k) H[k + i * ld] = y[k];
       for (int k = 0; k < i; ++k) {
         const double h1 = H[k + i * ld], h2 = H[k + 1 + i * ld];
@@ -671,12 +745,8 @@ int Elliptic::pgmres(double *r, double *x, double tol, int maxit, double &rdotr)
     if (error < tol || iter == maxit) break;
     update(nr);
     op(x, Ax.data());
-    double nr2 = 0;
-    for (long long q = 0; q < n; ++q) {
-      r[q] = b[q] - Ax[q];
-      nr2 += wt[q] * r[q] * r[q];
-    }
-    nrm = std::sqrt(nr2);
+    for (long long q = 0; q < n; ++q) r[q] = b[q] - Ax[q];
+    nrm = std::sqrt(wdot<double>(n, wt, r, r));
     error = nrm * sqrtFac;
     rdotr = error;
     if (error <= tol) return iter;

@@ -1,6 +1,13 @@
 """End-to-end solve parity: the GPU ellipticSolve against the CPU oracle on the
-same Kershaw boxes and seeded right-hand sides.  Bar (FP64 plain form):
-identical iteration counts and solutions within 1e-10 relative."""
+same Kershaw boxes and seeded right-hand sides.  Bar for the plain FP64 form
+(stored geometry, Jacobi or no preconditioner, every Krylov variant):
+bit-identical -- the same iteration count, the same residual history and the
+same solution, bit for bit.  Finite-precision CG amplifies any rounding
+difference (a 1e-16 change of the right-hand side moves Jacobi-PCG's count by
+one and its solution by ~1e-9 at a 1e-8 tolerance), so only identical
+arithmetic gives the north star's "identical iteration counts, 1e-10"
+reliably; the device and the oracle share the reduction order and the fused
+multiply-add placement for that reason."""
 import numpy as np
 import pytest
 
@@ -28,34 +35,29 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
+def assert_bit_identical(xo, io, xg, ig, el):
+    assert ig["status"] == io["status"]
+    assert ig["iterations"] == io["iterations"]
+    assert ig["res0"] == io["res0"] and ig["res"] == io["res"]
+    assert np.array_equal(el.get("history"), np.asarray(io["history"]))
+    assert np.array_equal(xg, xo)
+
+
 @pytest.mark.parametrize("N,n", [(1, 4), (3, 3), (5, 3), (7, 3), (9, 2)])
 def test_jacobi_pcg_parity(product_lib, oracle_mod, torch_cuda, N, n):
-    """Jacobi-PCG runs 70-150 iterations here; GPU and CPU differ only in rounding (FMA contraction,
-    reduction order), which CG amplifies over many iterations.  Bars: identical residual histories
-    over the first 20 iterations (1e-10 relative), iteration counts within one (the reference's own
-    CI allows +-1, examples/ethier/ci.inc:815), solutions within 1e-8 relative at a 1e-8 tolerance,
-    and identical counts with 1e-10 solutions when solving to 1e-12."""
+    """Jacobi-PCG (70-150 iterations here): bit-identical to the oracle."""
     opts = "preconditioner=jacobi;solver=pcg;residualTol=1e-8+relative;maxIterations=3000"
     xo, io, xg, ig, el, orc = run_pair(torch_cuda, N, n, opts)
-    assert ig["status"] == 0 and io["status"] == 0
-    assert abs(ig["iterations"] - io["iterations"]) <= 1
-    assert abs(ig["res0"] - io["res0"]) <= 1e-12 * io["res0"]
-    hist = el.get("history")
-    k = min(20, len(hist), len(io["history"]))
-    assert np.allclose(hist[:k], io["history"][:k], rtol=1e-10, atol=0)
-    assert rel(xg, xo) < 1e-8
+    assert ig["status"] == 0
+    assert_bit_identical(xo, io, xg, ig, el)
 
 
-@pytest.mark.parametrize("solver", ["pfcg", "pgmres+nVector=10", "pfgmres"])
+@pytest.mark.parametrize("solver", ["pfcg", "pgmres+nVector=10", "pfgmres", "pcg;preconditioner=none"])
 def test_krylov_variants_parity(product_lib, oracle_mod, torch_cuda, solver):
     opts = f"preconditioner=jacobi;solver={solver};residualTol=1e-8+relative;maxIterations=3000"
     xo, io, xg, ig, el, orc = run_pair(torch_cuda, 4, 3, opts)
     assert ig["status"] == 0
-    assert abs(ig["iterations"] - io["iterations"]) <= 1
-    hist = el.get("history")
-    k = min(15, len(hist), len(io["history"]))
-    assert np.allclose(hist[:k], io["history"][:k], rtol=1e-9, atol=0)
-    assert rel(xg, xo) < 1e-8
+    assert_bit_identical(xo, io, xg, ig, el)
 
 
 def test_nonzero_initial_guess_and_helmholtz(product_lib, oracle_mod, torch_cuda):
@@ -64,8 +66,7 @@ def test_nonzero_initial_guess_and_helmholtz(product_lib, oracle_mod, torch_cuda
     rng = np.random.default_rng(5)
     x0 = rng.uniform(-1, 1, n ** 3 * (N + 1) ** 3)
     xo, io, xg, ig, el, orc = run_pair(torch_cuda, N, n, opts, x0=x0)
-    assert abs(ig["iterations"] - io["iterations"]) <= 1
-    assert rel(xg, xo) < 1e-8
+    assert_bit_identical(xo, io, xg, ig, el)
 
 
 def test_trilinear_operator_solve(product_lib, oracle_mod, torch_cuda):
@@ -87,11 +88,9 @@ def test_operator_gs_mask_entry_points(product_lib, oracle_mod, torch_cuda):
     out = torch.zeros_like(qd)
     el.operator(qd, out)
     ref = orc.operator(q)
-    assert np.max(np.abs(out.cpu().numpy() - ref)) < 1e-13 * np.max(np.abs(ref))
-    for k in ("ids", "gsOff", "gsIds", "maskIds", "invDegree"):
+    assert np.array_equal(out.cpu().numpy(), ref)
+    for k in ("ids", "gsOff", "gsIds", "maskIds", "invDegree", "ggeo", "invDiag", "D"):
         assert np.array_equal(el.get(k), orc.get(k)), k
-    assert np.max(np.abs(el.get("ggeo") - orc.get("ggeo"))) < 1e-13 * np.max(np.abs(orc.get("ggeo")))
-    assert np.max(np.abs(el.get("invDiag") - orc.get("invDiag"))) < 1e-13 * np.max(np.abs(orc.get("invDiag")))
 
 
 def test_host_buffer_solve_matches_device_solve(product_lib, torch_cuda):
@@ -159,11 +158,10 @@ def test_fp32x2_operator_solve_parity(product_lib, oracle_mod, torch_cuda, preco
 
 
 def test_jacobi_pcg_parity_tight_tolerance(product_lib, oracle_mod, torch_cuda):
-    """At a 1e-12 tolerance both solutions sit on the discrete solution: 1e-10 relative."""
+    """At a 1e-12 tolerance: still bit-identical."""
     opts = "preconditioner=jacobi;solver=pcg;residualTol=1e-12+relative;maxIterations=3000"
     xo, io, xg, ig, el, orc = run_pair(torch_cuda, 5, 3, opts)
-    assert abs(ig["iterations"] - io["iterations"]) <= 1
-    assert rel(xg, xo) < 1e-10
+    assert_bit_identical(xo, io, xg, ig, el)
 
 
 def test_solve_ordered_with_callers_torch_stream(product_lib, torch_cuda):
@@ -218,7 +216,10 @@ def test_all_neumann_poisson_parity(product_lib, oracle_mod, torch_cuda, precon)
     torch.cuda.synchronize()
     xg = x.cpu().numpy()
     assert ig["status"] == 0 and io["status"] == 0
-    assert abs(ig["res0"] - io["res0"]) <= 1e-12 * io["res0"]
-    assert abs(ig["iterations"] - io["iterations"]) <= max(1, io["iterations"] // 100)
     assert abs(xg.sum()) <= 1e-12 * np.abs(xg).sum()
-    assert rel(xg, xo) < 1e-7
+    if precon == "jacobi":
+        assert_bit_identical(xo, io, xg, ig, el)
+    else:  # FP64 multigrid: same iteration count, 1e-10
+        assert ig["iterations"] == io["iterations"]
+        assert abs(ig["res0"] - io["res0"]) <= 1e-12 * io["res0"]
+        assert rel(xg, xo) < 1e-10

@@ -91,7 +91,10 @@ def test_oracle_ax_bitexact_vs_reference(oracle_mod, N):
     rng = np.random.default_rng(N)
     q = rng.uniform(-1, 1, el.Nlocal)
     ref = ref_ax(O.ref_lib(), N, el.E, el.get("ggeo"), el.get("D"), q, True)
-    assert np.array_equal(el.ax(q), ref)
+    assert np.array_equal(el.ax_ref(q), ref)
+    # the device-order operator (fused multiply-adds) agrees to the reference's own
+    # acceptance bar for Ax variants: 400 eps relative (benchmarkAx.cpp:295)
+    assert np.max(np.abs(el.ax(q) - ref)) <= 400 * np.finfo(np.float64).eps * np.max(np.abs(ref))
 
 
 @pytest.mark.parametrize("solver", ["pcg", "pfcg", "pgmres", "pfgmres"])
@@ -142,7 +145,7 @@ def test_oracle_solution_projection(oracle_mod, form):
 
 def test_oracle_block_helmholtz_sanity(oracle_mod):
     """Block / stress restatement: one field with scalar coefficients is the scalar Helmholtz operator
-    bit for bit; constant coefficient arrays equal the scalars; the stress operator annihilates a rigid
+    (reference operation order) bit for bit; constant coefficient arrays equal the scalars; the stress operator annihilates a rigid
     rotation and is symmetric; its PCG converges."""
     N, n = 4, 3
     VX, EToV, EToB = O.box_mesh(n, n, n, 0.3)
@@ -152,9 +155,10 @@ def test_oracle_block_helmholtz_sanity(oracle_mod):
     rng = np.random.default_rng(0)
     q = rng.standard_normal(Nl)
     b = el.block_ax(q, nf=1, l0=1.3, l1=0.7)
-    assert np.array_equal(b, hel.ax(q))
+    assert np.array_equal(b, hel.ax_ref(q))
     assert np.array_equal(el.block_ax(q, nf=1, lam0=np.full(Nl, 1.3), lam1=np.full(Nl, 0.7)), b)
-    assert np.array_equal(el.block_inv_diag(nf=1, l0=1.3, l1=0.7), hel.get("invDiag"))
+    # the scalar FP64 diagonal is formed in the device's fused order: equal to rounding
+    assert np.allclose(el.block_inv_diag(nf=1, l0=1.3, l1=0.7), hel.get("invDiag"), rtol=1e-14, atol=0)
     x, y = el.get("x"), el.get("y")
     rot = np.concatenate([y, -x, np.zeros_like(x)])
     assert np.abs(el.block_ax(rot, nf=3, stress=True, l0=1.0, l1=0.0)).max() < 1e-12
