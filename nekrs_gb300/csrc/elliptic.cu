@@ -237,7 +237,7 @@ void Elliptic::ax(const double *q, double *Aq)
     launch_ax_fp32x2(fine.N, fine.E, ggeoPairs.p, DPairs.p, opt.lambda0, opt.lambda1, opt.poisson, q, Aq, stream);
   else if (opt.trilinear)
     launch_ax_trilinear<double>(fine.N, fine.E, fine.d_VX64.p, fine.d_z64.p, fine.d_w64.p, fine.d_D64.p, opt.lambda0,
-                                opt.lambda1, opt.poisson, q, Aq, stream);
+                                opt.lambda1, opt.poisson, q, Aq, stream, opt.trilinearLambda0All);
   else
     launch_ax_stored<double>(fine.N, fine.E, fine.d_ggeo64.p, fine.d_D64.p, opt.lambda0, opt.lambda1, opt.poisson, q,
                              Aq, stream);
@@ -610,6 +610,7 @@ void Elliptic::begin(double *r, double *x)
   st = StepState();
   st.r = r;
   st.x = x;
+  mg_clear_error();
   NRSG_CUDA(cudaEventRecord(ev0, stream));
   // r = b - A x0 (local Ax, ellipticSolve.cpp:91-103), mask, gather-scatter
   ax(x, Ap.p);

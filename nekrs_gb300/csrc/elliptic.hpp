@@ -166,6 +166,7 @@ struct Elliptic {
   void mg_apply(const double *r, double *z);
   void mg_release();
   int mg_error();
+  void mg_clear_error(); // clears the coarse kernel's sticky error flag (solve begin)
   std::vector<double> mg_get(const std::string &name);
   long long mg_level_size(int level);
   void mg_schwarz(int level, const double *u, double *Su);

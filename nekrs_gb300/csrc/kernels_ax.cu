@@ -603,11 +603,50 @@ __device__ __forceinline__ void trilinear_G(const T *xe, const T *ye, const T *z
   G22 = sc * (tx * tx + ty * ty + tz * tz);
   GWJ = W * J;
 }
+// FP64: the same factors with every rounding explicit (the oracle performs these operations in this order)
+template <>
+__device__ __forceinline__ void trilinear_G<double>(const double *xe, const double *ye, const double *ze, double rn,
+                                                    double sn, double tn, double W, double &G00, double &G01,
+                                                    double &G02, double &G11, double &G12, double &G22, double &GWJ)
+{
+  const double am = __dmul_rn(1 - tn, 1 - sn), ap = __dmul_rn(1 - tn, 1 + sn), bm = __dmul_rn(1 + tn, 1 - sn),
+               bp = __dmul_rn(1 + tn, 1 + sn);
+  const double cm = __dmul_rn(1 - tn, 1 - rn), cp = __dmul_rn(1 - tn, 1 + rn), dm = __dmul_rn(1 + tn, 1 - rn),
+               dp = __dmul_rn(1 + tn, 1 + rn);
+  const double fm = __dmul_rn(1 - rn, 1 - sn), fp = __dmul_rn(1 + rn, 1 - sn), hp = __dmul_rn(1 + rn, 1 + sn),
+               hm = __dmul_rn(1 - rn, 1 + sn);
+  // 0.125 (a0 d0 + a1 d1 + a2 d2 + a3 d3) as 0.125 fma(a3, d3, fma(a2, d2, fma(a1, d1, a0 d0)))
+  auto comb = [](double a0, double d0, double a1, double d1, double a2, double d2, double a3, double d3) {
+    return __dmul_rn(0.125, __fma_rn(a3, d3, __fma_rn(a2, d2, __fma_rn(a1, d1, __dmul_rn(a0, d0)))));
+  };
+  auto dr = [&](const double *X) { return comb(am, X[1] - X[0], ap, X[2] - X[3], bm, X[5] - X[4], bp, X[6] - X[7]); };
+  auto ds = [&](const double *X) { return comb(cm, X[3] - X[0], cp, X[2] - X[1], dm, X[7] - X[4], dp, X[6] - X[5]); };
+  auto dt = [&](const double *X) { return comb(fm, X[4] - X[0], fp, X[5] - X[1], hp, X[6] - X[2], hm, X[7] - X[3]); };
+  const double xr = dr(xe), xs = ds(xe), xt = dt(xe);
+  const double yr = dr(ye), ys = ds(ye), yt = dt(ye);
+  const double zr = dr(ze), zs = ds(ze), zt = dt(ze);
+  auto minor2 = [](double a, double b, double c, double d) { return __fma_rn(a, b, -__dmul_rn(c, d)); };
+  const double rx = minor2(ys, zt, zs, yt), ry = -minor2(xs, zt, zs, xt), rz = minor2(xs, yt, ys, xt);
+  const double sx = -minor2(yr, zt, zr, yt), sy = minor2(xr, zt, zr, xt), sz = -minor2(xr, yt, yr, xt);
+  const double tx = minor2(yr, zs, zr, ys), ty = -minor2(xr, zs, zr, xs), tz = minor2(xr, ys, yr, xs);
+  const double J = __fma_rn(zr, rz, __fma_rn(yr, ry, __dmul_rn(xr, rx)));
+  const double sc = W / J;
+  auto dot3 = [](double a0, double b0, double a1, double b1, double a2, double b2) {
+    return __fma_rn(a2, b2, __fma_rn(a1, b1, __dmul_rn(a0, b0)));
+  };
+  G00 = __dmul_rn(sc, dot3(rx, rx, ry, ry, rz, rz));
+  G01 = __dmul_rn(sc, dot3(rx, sx, ry, sy, rz, sz));
+  G02 = __dmul_rn(sc, dot3(rx, tx, ry, ty, rz, tz));
+  G11 = __dmul_rn(sc, dot3(sx, sx, sy, sy, sz, sz));
+  G12 = __dmul_rn(sc, dot3(sx, tx, sy, ty, sz, tz));
+  G22 = __dmul_rn(sc, dot3(tx, tx, ty, ty, tz, tz));
+  GWJ = __dmul_rn(W, J);
+}
 
 template <typename T, int NQ, bool POISSON>
 __global__ void __launch_bounds__(NQ *NQ *AxShape<NQ>::epb)
     ax_trilinear_kernel(long long E, const T *__restrict__ VX, const T *__restrict__ gllz,
-                        const T *__restrict__ gllw, const T *__restrict__ D, T lambda0, T lambda1,
+                        const T *__restrict__ gllw, const T *__restrict__ D, T l0rs, T l0t, T lambda1,
                         const T *__restrict__ q, T *__restrict__ Aq)
 {
   constexpr int EPB = AxShape<NQ>::epb;
@@ -651,24 +690,26 @@ __global__ void __launch_bounds__(NQ *NQ *AxShape<NQ>::epb)
     s_q[el][j][i] = r_q[k];
     T qt = 0;
 #pragma unroll
-    for (int m = 0; m < NQ; ++m) qt += s_D[k][m] * r_q[m];
+    for (int m = 0; m < NQ; ++m) macc(qt, s_D[k][m], r_q[m]);
     __syncthreads();
     T qr = 0, qs = 0;
 #pragma unroll
     for (int m = 0; m < NQ; ++m) {
-      qr += s_D[i][m] * s_q[el][j][m];
-      qs += s_D[j][m] * s_q[el][m][i];
+      macc(qr, s_D[i][m], s_q[el][j][m]);
+      macc(qs, s_D[j][m], s_q[el][m][i]);
     }
-    s_Gr[el][j][i] = lambda0 * (G00 * qr + G01 * qs + G02 * qt);
-    s_Gs[el][j][i] = lambda0 * (G01 * qr + G11 * qs + G12 * qt);
-    const T Gt = lambda0 * (G02 * qr + G12 * qs + G22 * qt);
-    T auk = POISSON ? T(0) : GWJ * lambda1 * r_q[k];
+    // the reference scales the t-flux by lambda0 only (ellipticPartialAxTrilinearHex3D.okl:154-157);
+    // l0rs = lambda0 scales all three (option trilinearLambda0 = all), l0rs = 1 is the reference
+    s_Gr[el][j][i] = gflux(l0rs, G00, G01, G02, qr, qs, qt);
+    s_Gs[el][j][i] = gflux(l0rs, G01, G11, G12, qr, qs, qt);
+    const T Gt = gflux(l0t, G02, G12, G22, qr, qs, qt);
+    T auk = POISSON ? T(0) : mul3(GWJ, lambda1, r_q[k]);
     __syncthreads();
 #pragma unroll
     for (int m = 0; m < NQ; ++m) {
-      auk += s_D[m][j] * s_Gs[el][m][i];
-      r_Aq[m] += s_D[k][m] * Gt;
-      auk += s_D[m][i] * s_Gr[el][j][m];
+      macc(auk, s_D[m][j], s_Gs[el][m][i]);
+      macc(r_Aq[m], s_D[k][m], Gt);
+      macc(auk, s_D[m][i], s_Gr[el][j][m]);
     }
     r_Aq[k] += auk;
     __syncthreads();
@@ -726,18 +767,19 @@ void launch_ax_stored(int N, long long E, const T *ggeo, const T *D, T lambda0, 
 
 template <typename T>
 void launch_ax_trilinear(int N, long long E, const T *VX, const T *gllz, const T *gllw, const T *D, T lambda0,
-                         T lambda1, bool poisson, const T *q, T *Aq, cudaStream_t s)
+                         T lambda1, bool poisson, const T *q, T *Aq, cudaStream_t s, bool lambda0All)
 {
   if (E <= 0) return;
+  const T l0rs = lambda0All ? lambda0 : T(1), l0t = lambda0;
 #define NRSG_AXT(NQ)                                                                                       \
   {                                                                                                        \
     constexpr int EPB = AxShape<NQ>::epb;                                                                  \
     dim3 blk(NQ * NQ, EPB);                                                                                \
     const unsigned grid = (unsigned)((E + EPB - 1) / EPB);                                                 \
     if (poisson)                                                                                           \
-      ax_trilinear_kernel<T, NQ, true><<<grid, blk, 0, s>>>(E, VX, gllz, gllw, D, lambda0, lambda1, q, Aq); \
+      ax_trilinear_kernel<T, NQ, true><<<grid, blk, 0, s>>>(E, VX, gllz, gllw, D, l0rs, l0t, lambda1, q, Aq); \
     else                                                                                                   \
-      ax_trilinear_kernel<T, NQ, false><<<grid, blk, 0, s>>>(E, VX, gllz, gllw, D, lambda0, lambda1, q, Aq); \
+      ax_trilinear_kernel<T, NQ, false><<<grid, blk, 0, s>>>(E, VX, gllz, gllw, D, l0rs, l0t, lambda1, q, Aq); \
   }
   NRSG_DISPATCH_NQ(N, NRSG_AXT)
 #undef NRSG_AXT
@@ -750,9 +792,9 @@ template void launch_ax_stored<float>(int, long long, const float *, const float
                                       float *, cudaStream_t);
 template void launch_ax_trilinear<double>(int, long long, const double *, const double *, const double *,
                                           const double *, double, double, bool, const double *, double *,
-                                          cudaStream_t);
+                                          cudaStream_t, bool);
 template void launch_ax_trilinear<float>(int, long long, const float *, const float *, const float *, const float *,
-                                         float, float, bool, const float *, float *, cudaStream_t);
+                                         float, float, bool, const float *, float *, cudaStream_t, bool);
 
 // ---------------------------------------------------------------------------
 // diag(A_L) per node (ellipticBlockBuildDiagonalHex3D.okl:61-107), one field.

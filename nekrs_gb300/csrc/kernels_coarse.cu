@@ -47,7 +47,6 @@ namespace nrsg {
 
 namespace {
 constexpr int kCT = 1024;              // most threads per CTA (one CTA per SM; a row block of fewer rows uses fewer)
-constexpr long long kSpinLimit = 1LL << 22;
 constexpr int kMinRowsPerCta = 128;
 constexpr long long kOneCtaRows = 4096; // 10 FP32 row vectors = 160 KB of shared memory
 
@@ -179,21 +178,24 @@ template <typename T> __device__ __forceinline__ void grid_sum3(const T *part, T
 }
 
 // Grid barrier number `nb` (1, 2, ...).  Returns false in every thread of the
-// CTA if the wait timed out or another CTA reported an error.
-__device__ __forceinline__ bool grid_barrier(CoarseState *st, unsigned nb)
+// CTA if the wait timed out (more than spinLimit polls) or another CTA
+// reported an error.  `extra` arrivals are added to the target: 0 in
+// ordinary use; a nonzero value makes the target unreachable, which is how
+// the test of the bounded wait makes every wait run out.
+__device__ __forceinline__ bool grid_barrier(CoarseState *st, unsigned nb, long long spinLimit, unsigned extra)
 {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     red_release_add_u32(&st->arrive, 1u);
-    const unsigned target = nb * gridDim.x;
+    const unsigned target = nb * gridDim.x + extra;
     int ok = 1;
     long long spins = 0;
     while ((int)(ld_acquire_u32(&st->arrive) - target) < 0) {
       ++spins;
       if ((spins & 63) == 0) {
         if (*(volatile int *)&st->err) { ok = 0; break; }
-        if (spins > kSpinLimit) {
+        if (spins > spinLimit) {
           atomicExch(&st->err, 1);
           ok = 0;
           break;
@@ -248,6 +250,8 @@ template <typename T> struct CoarseArgs {
   CoarseState *st;
   double tol;                 // relative
   int maxit;
+  unsigned barrierExtra;      // added to every grid barrier's target (0; nonzero only to test the bounded wait)
+  long long spinLimit;        // polls before a grid barrier wait gives up
 };
 
 template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_pcg_kernel(CoarseArgs<T> a)
@@ -299,7 +303,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_pcg_kerne
     rz = fma_t<T>(ru, zu, rz);
   }
   cta_partial2<T>(rr, rz, sh, a.partials + blockIdx.x, a.partials + gridDim.x + blockIdx.x);
-  if (!grid_barrier(a.st, 1)) return;
+  if (!grid_barrier(a.st, 1, a.spinLimit, a.barrierExtra)) return;
   unsigned nb = 1;
   // scalars, kept by thread 0 of each CTA (identical in every CTA)
   double r0 = 0, rn = 0, tol = 0, rdotz = 0;
@@ -334,7 +338,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_pcg_kerne
       pap = fma_t<T>(pu, apu, pap);
     }
     cta_partial<T>(pap, sh, a.partials + 2 * gridDim.x + blockIdx.x);
-    if (!grid_barrier(a.st, ++nb)) return;
+    if (!grid_barrier(a.st, ++nb, a.spinLimit, a.barrierExtra)) return;
     if (threadIdx.x < 32) {
       const double spap = grid_sum(a.partials + 2 * gridDim.x);
       if (threadIdx.x == 0) s_alpha = (T)(rdotz / (spap + 1e-300));
@@ -355,7 +359,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_pcg_kerne
       rz = fma_t<T>(ru, zu, rz);
     }
     cta_partial2<T>(rr, rz, sh, a.partials + blockIdx.x, a.partials + gridDim.x + blockIdx.x);
-    if (!grid_barrier(a.st, ++nb)) return;
+    if (!grid_barrier(a.st, ++nb, a.spinLimit, a.barrierExtra)) return;
     if (threadIdx.x < 32) {
       const double srr = grid_sum(a.partials);
       const double srz = grid_sum(a.partials + gridDim.x);
@@ -372,7 +376,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_pcg_kerne
   }
   // E-vector solution: every copy of a row takes its value, masked nodes 0
   for (int t = threadIdx.x; t < cnt; t += blockDim.x) a.x[start + t] = xs[t];
-  if (!grid_barrier(a.st, ++nb)) return;
+  if (!grid_barrier(a.st, ++nb, a.spinLimit, a.barrierExtra)) return;
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x, nth = (long long)gridDim.x * blockDim.x;
   for (long long i = tid; i < a.nE; i += nth) {
     const int u = __ldg(a.rowOf + i);
@@ -446,7 +450,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_ppcg_kern
     ms[t] = uu;
     a.z[start + t] = uu;
   }
-  if (!grid_barrier(a.st, 1)) return;
+  if (!grid_barrier(a.st, 1, a.spinLimit, a.barrierExtra)) return;
   unsigned nb = 1;
   // w0 = A u0
 #pragma unroll 4
@@ -477,7 +481,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_ppcg_kern
       mg[start + t] = mm;
     }
     cta_partial3<T>(g, d, rr, sh, part + blockIdx.x, part + gridDim.x + blockIdx.x, part + 2 * gridDim.x + blockIdx.x);
-    if (!grid_barrier(a.st, ++nb)) return;
+    if (!grid_barrier(a.st, ++nb, a.spinLimit, a.barrierExtra)) return;
     if (threadIdx.x < 32) {
       T sgT, sdT, srrT;
       grid_sum3<T>(part, sgT, sdT, srrT);
@@ -530,7 +534,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_ppcg_kern
   }
   // E-vector solution: every copy of a row takes its value, masked nodes 0
   for (int t = threadIdx.x; t < cnt; t += blockDim.x) a.x[start + t] = xs[t];
-  if (!grid_barrier(a.st, ++nb)) return;
+  if (!grid_barrier(a.st, ++nb, a.spinLimit, a.barrierExtra)) return;
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x, nth = (long long)gridDim.x * blockDim.x;
   for (long long i = tid; i < a.nE; i += nth) {
     const int u = __ldg(a.rowOf + i);
@@ -678,7 +682,8 @@ CoarseGate &coarse_gate()
 
 template <typename T>
 int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *z, T *z2, double *partials,
-                          void *state, int gridMax, double tol, int maxit, cudaStream_t s)
+                          void *state, int gridMax, double tol, int maxit, cudaStream_t s, long long spinLimit,
+                          unsigned barrierExtra)
 {
   if (A.grid > gridMax) throw Error(NRSG_ERR_CUDA, "coarse solver: partial-sum buffer too small");
   int dev = 0;
@@ -692,7 +697,9 @@ int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *
     if (!gate.ev[dev]) NRSG_CUDA(cudaEventCreateWithFlags(&gate.ev[dev], cudaEventDisableTiming));
     NRSG_CUDA(cudaStreamWaitEvent(s, gate.ev[dev], 0));
   }
-  NRSG_CUDA(cudaMemsetAsync(state, 0, sizeof(CoarseState), s));
+  // the arrival counter starts at zero for every launch; the error flag is kept (sticky for the
+  // outer solve, cleared by coarse_state_clear when the solve begins)
+  NRSG_CUDA(cudaMemsetAsync(state, 0, sizeof(unsigned), s));
   CoarseArgs<T> a;
   a.nrow = A.nrow;
   a.nE = A.nE;
@@ -716,6 +723,8 @@ int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *
   a.st = (CoarseState *)state;
   a.tol = tol;
   a.maxit = maxit;
+  a.barrierExtra = barrierExtra;
+  a.spinLimit = spinLimit;
   void *args[] = {&a};
   const void *kfn = A.pipelined ? (const void *)coarse_ppcg_kernel<T> : (const void *)coarse_pcg_kernel<T>;
   if (cooperative) {
@@ -730,6 +739,7 @@ int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *
 }
 
 size_t coarse_state_bytes() { return sizeof(CoarseState); }
+void coarse_state_clear(void *state, cudaStream_t s) { NRSG_CUDA(cudaMemsetAsync(state, 0, sizeof(CoarseState), s)); }
 int coarse_state_read(const void *state_host, int *iters, double *res0, double *res)
 {
   const CoarseState *st = (const CoarseState *)state_host;
@@ -744,8 +754,10 @@ template void coarse_matrix_setup<double>(long long, const long long *, const lo
 template void coarse_matrix_setup<float>(long long, const long long *, const long long *, const double *, long long,
                                          const long long *, const int *, CoarseMatrix<float> &);
 template int coarse_pcg_persistent<double>(const CoarseMatrix<double> &, const double *, double *, double *, double *,
-                                           double *, double *, void *, int, double, int, cudaStream_t);
+                                           double *, double *, void *, int, double, int, cudaStream_t, long long,
+                                           unsigned);
 template int coarse_pcg_persistent<float>(const CoarseMatrix<float> &, const float *, float *, float *, float *,
-                                          float *, double *, void *, int, double, int, cudaStream_t);
+                                          float *, double *, void *, int, double, int, cudaStream_t, long long,
+                                          unsigned);
 
 } // namespace nrsg

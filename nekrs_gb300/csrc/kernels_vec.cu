@@ -9,24 +9,27 @@
 //
 // Reductions are one launch each and are bit-reproducible: every FP64 sum
 // is formed in one fixed order that depends only on n, and the oracle's
-// wsum() performs the same additions in the same order.  The order:
-//   term_i    per kernel, with every rounding explicit (e.g. w_i * (a_i * b_i),
-//             both products rounded: the reference's weightedInnerProdMany term);
-//   chunk c   entries [256 c, 256 c + 256), entries past n count as +0.0; its sum
-//             is the pairwise tree s[x] += s[x + o], o = 128, 64, ..., 1, i.e. the
-//             block order of weightedInnerProdMany.okl:27-105, so chunk sums equal
-//             the reference's block partials bit for bit;
+// wsum() performs the same operations in the same order:
+//   term      each entry contributes through one fused multiply-add,
+//             s = fma(x_i, y_i, s), with the factors defined per kernel (a
+//             weighted inner product: x_i = w_i a_i rounded, y_i = b_i);
+//   chunk c   entries [1024 c, 1024 c + 1024): lane l of the warp accumulates
+//             entries 1024 c + l + 32 j, j = 0..31 ascending, from 0 (entries
+//             past n are skipped); the 32 lane sums are added by the tree
+//             s[l] += s[l + o], o = 16, 8, 4, 2, 1;
 //   result    the chunk sums added by the blocked pairwise tree
-//             ((P0 + P1) + (P2 + P3)) + ..., zero-padded to a power of two.  The
-//             reference adds its block partials one after another on the host
-//             (linAlg.cpp:986-1035); the tree keeps the whole sum on the device
-//             and parallel.
-// A warp sums groups of 4 chunks (1024 entries); each warp owns one aligned,
-// power-of-two run of groups and merges its group sums by the same tree with
-// a small stack; the CTA that finishes last (atomic ticket) adds the warp
-// sums, still by the same tree, and stores the result on the device.  Krylov
-// scalars (alpha, beta) are formed on the device by the kernels that consume
-// them, so there is no host round trip.
+//             ((P0 + P1) + (P2 + P3)) + ..., zero-padded to a power of two.
+// The reference forms w (a b) per entry, adds 256-entry blocks by a tree and
+// the block sums one after another on the host (weightedInnerProdMany.okl:
+// 27-105, linAlg.cpp:986-1035).  On GB300 the FP64 pipe issues one warp
+// instruction per ~16 clocks per SM, so that order (about 3.5 FP64
+// operations per entry) is FP64-bound at a third of the HBM rate; this one
+// takes about 2.2 per entry and runs at the memory bound.  Each warp owns an
+// aligned, power-of-two run of chunks and merges its chunk sums by the
+// blocked tree on a small stack; the CTA that finishes last (atomic ticket)
+// adds the warp sums, still by the same tree, and stores the result on the
+// device.  Krylov scalars (alpha, beta) are formed on the device by the
+// kernels that consume them, so there is no host round trip.
 //
 // FP64 element-wise arithmetic on the plain solve path uses explicit
 // roundings (__fma_rn / __dmul_rn / __dadd_rn) so that the compiler's
@@ -40,54 +43,41 @@ namespace nrsg {
 namespace {
 constexpr int kThreads = kRedThreads;
 constexpr int kWarps = kThreads / 32;
-constexpr int kChunk = 256;    // entries per chunk (the reference's p_blockSize)
-constexpr int kGroup = 4;      // chunks per group (one warp step)
-constexpr int kStack = 24;     // depth of the per-warp merge stack (runs of up to 2^23 groups)
+constexpr int kChunk = 1024;   // entries per chunk: 32 lanes x 32 entries
+constexpr int kStack = 24;     // depth of the per-warp merge stack (runs of up to 2^23 chunks)
 
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 
-// weighted product term w * (a * b) with both products rounded
-__device__ __forceinline__ double wterm(double w, double a, double b) { return dmul(w, dmul(a, b)); }
-
-// Sum of one chunk in lane 0; a[j] holds the term at chunk offset lane + 32 j.
-__device__ __forceinline__ double chunk_tree(double (&a)[8])
-{
-  a[0] = dadd(a[0], a[4]); // o = 128
-  a[1] = dadd(a[1], a[5]);
-  a[2] = dadd(a[2], a[6]);
-  a[3] = dadd(a[3], a[7]);
-  a[0] = dadd(a[0], a[2]); // o = 64
-  a[1] = dadd(a[1], a[3]);
-  double v = dadd(a[0], a[1]); // o = 32
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = dadd(v, __shfl_down_sync(0xffffffffu, v, o));
-  return v;
-}
-
-// F: double operator()(long long i) const -- term of entry i < n (and its side effects)
+// Sum of chunk c in lane 0.  F: void operator()(long long i, double &x, double &y) const gives
+// the factors of entry i < n (and performs the entry's side effects).
 template <typename F> __device__ __forceinline__ double chunk_sum(long long c, long long n, const F &f)
 {
   const long long i0 = c * kChunk + (threadIdx.x & 31);
-  double a[8];
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const long long i = i0 + 32 * j;
-    a[j] = i < n ? f(i) : 0.0;
+  double s = 0.0;
+  if ((c + 1) * kChunk <= n) {
+#pragma unroll 8
+    for (int j = 0; j < 32; ++j) {
+      double x, y;
+      f(i0 + 32 * j, x, y);
+      s = __fma_rn(x, y, s);
+    }
+  } else {
+    for (int j = 0; j < 32; ++j) {
+      const long long i = i0 + 32 * j;
+      if (i < n) {
+        double x, y;
+        f(i, x, y);
+        s = __fma_rn(x, y, s);
+      }
+    }
   }
-  return chunk_tree(a);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s = dadd(s, __shfl_down_sync(0xffffffffu, s, o));
+  return s;
 }
 
-template <typename F> __device__ __forceinline__ double group_sum(long long g, long long n, const F &f)
-{
-  const double p0 = chunk_sum(g * kGroup + 0, n, f);
-  const double p1 = chunk_sum(g * kGroup + 1, n, f);
-  const double p2 = chunk_sum(g * kGroup + 2, n, f);
-  const double p3 = chunk_sum(g * kGroup + 3, n, f);
-  return dadd(dadd(p0, p1), dadd(p2, p3));
-}
-
-// Work split of one reduction: W warp runs of `len` groups each (both powers
+// Work split of one reduction: W warp runs of `len` chunks each (both powers
 // of two, W <= kRedSegments), CTAs = ceil(W / 8).
 struct RedSplit {
   long long len;
@@ -96,9 +86,8 @@ struct RedSplit {
 inline RedSplit red_split(long long n)
 {
   const long long nc = (n + kChunk - 1) / kChunk;
-  const long long ng = (nc + kGroup - 1) / kGroup;
   long long M = 1;
-  while (M < ng) M <<= 1;
+  while (M < nc) M <<= 1;
   const long long W = M < kRedSegments ? M : kRedSegments;
   RedSplit r;
   r.len = M / W;
@@ -107,7 +96,7 @@ inline RedSplit red_split(long long n)
   return r;
 }
 
-// The sum of warp run `wid` (groups [wid*len, (wid+1)*len)) by the blocked
+// The sum of warp run `wid` (chunks [wid*len, (wid+1)*len)) by the blocked
 // tree, merged on a per-warp stack in shared memory (lane 0 writes it); the
 // result is returned to every lane.
 template <typename F>
@@ -118,7 +107,7 @@ __device__ __forceinline__ double run_sum(long long wid, long long len, long lon
   const bool lane0 = (threadIdx.x & 31) == 0;
   int sp = 0;
   for (long long q = 0; q < len; ++q) {
-    double v = group_sum(wid * len + q, n, f);
+    double v = chunk_sum(wid * len + q, n, f);
     for (long long k = q + 1; (k & 1) == 0; k >>= 1) v = dadd(stk[--sp], v);
     if (lane0) stk[sp] = v;
     ++sp;
@@ -344,10 +333,10 @@ __global__ void __launch_bounds__(kThreads)
 {
   reduce1(
       n, len, W,
-      [&](long long i) {
+      [&](long long i, double &x, double &y) {
         const double av = (double)a[i];
-        const double bv = b ? (double)b[i] : av;
-        return w ? wterm((double)w[i], av, bv) : dmul(av, bv);
+        y = b ? (double)b[i] : av;
+        x = w ? dmul((double)w[i], av) : av;
       },
       row, counter, out);
 }
@@ -459,11 +448,12 @@ __global__ void __launch_bounds__(kThreads)
   __syncthreads();
   const bool last = reduce1(
       n, len, W,
-      [&](long long i) {
+      [&](long long i, double &x, double &y) {
         const double ri = r[i];
         const double zi = dmul(ri, invDiag[i]);
         z[i] = zi;
-        return wterm(w[i], ri, zi);
+        x = dmul(w[i], ri);
+        y = zi;
       },
       row, counter, &sc->rdotz);
   if (last) sc->rdotz_old = s_old;
@@ -500,11 +490,12 @@ __global__ void __launch_bounds__(kThreads)
   const double alpha = sc->rdotz / (sc->pAp + 1e-300);
   const bool last = reduce1(
       n, len, W,
-      [&](long long i) {
+      [&](long long i, double &fx, double &fy) {
         const double ri = __fma_rn(-alpha, Ap[i], r[i]);
         r[i] = ri;
         x[i] = __fma_rn(alpha, p[i], x[i]);
-        return wterm(w[i], ri, ri);
+        fx = dmul(w[i], ri);
+        fy = ri;
       },
       row, counter, &sc->rdotr);
   if (last) sc->alpha = alpha;
@@ -525,11 +516,12 @@ __global__ void __launch_bounds__(kThreads)
 {
   reduce1(
       n, len, W,
-      [&](long long i) {
+      [&](long long i, double &fx, double &fy) {
         const double ri = __fma_rn(-alpha, Ap[i], r[i]);
         r[i] = ri;
         x[i] = __fma_rn(alpha, p[i], x[i]);
-        return wterm(w[i], ri, ri);
+        fx = dmul(w[i], ri);
+        fy = ri;
       },
       row, counter, out);
 }
@@ -568,8 +560,9 @@ namespace {
 constexpr int kMultiVec = 8;
 }
 
-// One pass over x and w for up to kMultiVec vectors: term w (x V_k); every
-// vector's sums follow the one-vector order exactly.
+// One pass over x and w for up to kMultiVec vectors: entry factors (w x, V_k),
+// w x rounded once and shared by the vectors; every vector's sum follows the
+// one-vector order exactly.
 __global__ void __launch_bounds__(kThreads)
     multi_wdot_kernel(long long n, long long len, int W, const double *__restrict__ w, const double *__restrict__ V,
                       int nvec, const double *__restrict__ x, double *rows, long long stride, unsigned *counter,
@@ -581,38 +574,26 @@ __global__ void __launch_bounds__(kThreads)
   if (wid < W) {
     int sp = 0;
     for (long long q = 0; q < len; ++q) {
-      const long long g = wid * len + q;
-      double lo[kMultiVec], hi[kMultiVec];
-#pragma unroll
-      for (int cq = 0; cq < kGroup; ++cq) {
-        const long long i0 = (g * kGroup + cq) * kChunk + lane;
-        double wv[8], xv[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const long long i = i0 + 32 * j;
-          wv[j] = i < n ? w[i] : 0.0;
-          xv[j] = i < n ? x[i] : 0.0;
-        }
-#pragma unroll
-        for (int k = 0; k < kMultiVec; ++k) {
-          if (k >= nvec) break;
-          double a[8];
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const long long i = i0 + 32 * j;
-            a[j] = i < n ? wterm(wv[j], xv[j], V[(size_t)k * n + i]) : 0.0;
-          }
-          const double P = chunk_tree(a);
-          if (cq == 0) lo[k] = P;
-          else if (cq == 1) lo[k] = dadd(lo[k], P);
-          else if (cq == 2) hi[k] = P;
-          else hi[k] = dadd(hi[k], P);
-        }
-      }
+      const long long c = wid * len + q;
+      const long long i0 = c * kChunk + lane;
       double v[kMultiVec];
 #pragma unroll
-      for (int k = 0; k < kMultiVec; ++k)
-        if (k < nvec) v[k] = dadd(lo[k], hi[k]);
+      for (int k = 0; k < kMultiVec; ++k) v[k] = 0.0;
+      for (int j = 0; j < 32; ++j) {
+        const long long i = i0 + 32 * j;
+        if (i < n) {
+          const double wx = dmul(w[i], x[i]);
+#pragma unroll
+          for (int k = 0; k < kMultiVec; ++k)
+            if (k < nvec) v[k] = __fma_rn(wx, V[(size_t)k * n + i], v[k]);
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kMultiVec; ++k) {
+        if (k >= nvec) break;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] = dadd(v[k], __shfl_down_sync(0xffffffffu, v[k], o));
+      }
       for (long long kk = q + 1; (kk & 1) == 0; kk >>= 1) {
         --sp;
 #pragma unroll
@@ -670,11 +651,12 @@ __global__ void __launch_bounds__(kThreads)
   __syncthreads();
   reduce1(
       n, len, W,
-      [&](long long i) {
+      [&](long long i, double &fx, double &fy) {
         double v = x[i];
         for (int k = 0; k < nvec; ++k) v = __fma_rn(-s_y[k], V[(size_t)k * n + i], v);
         x[i] = v;
-        return wterm(w[i], v, v);
+        fx = dmul(w[i], v);
+        fy = v;
       },
       row, counter, nrm2);
 }
@@ -715,10 +697,11 @@ __global__ void __launch_bounds__(kThreads)
 {
   reduce1(
       n, len, W,
-      [&](long long i) {
+      [&](long long i, double &fx, double &fy) {
         const double v = dadd(b[i], -Ax[i]);
         r[i] = v;
-        return wterm(w[i], v, v);
+        fx = dmul(w[i], v);
+        fy = v;
       },
       row, counter, nrm2);
 }
@@ -762,11 +745,12 @@ __global__ void __launch_bounds__(kThreads)
   __syncthreads();
   const bool last = reduce1(
       n, len, W,
-      [&](long long i) {
+      [&](long long i, double &fx, double &fy) {
         const T ri = r[i];
         const T zi = invDiag[i] * ri;
         z[i] = zi;
-        return wterm((double)w[i], (double)ri, (double)zi);
+        fx = dmul((double)w[i], (double)ri);
+        fy = (double)zi;
       },
       row, counter, &sc->rdotz);
   if (last) sc->rdotz_old = s_old;
@@ -786,11 +770,12 @@ __global__ void __launch_bounds__(kThreads)
   const T alpha = (T)(sc->rdotz / (sc->pAp + 1e-300));
   reduce1(
       n, len, W,
-      [&](long long i) {
+      [&](long long i, double &fx, double &fy) {
         x[i] += alpha * p[i];
         const T ri = r[i] - alpha * Ap[i];
         r[i] = ri;
-        return wterm((double)w[i], (double)ri, (double)ri);
+        fx = dmul((double)w[i], (double)ri);
+        fy = (double)ri;
       },
       row, counter, &sc->rdotr);
 }

@@ -29,6 +29,7 @@ struct MGState {
   virtual bool graph_capturable() = 0;
   virtual long long level_size(int level) = 0;
   virtual int error() = 0;
+  virtual void clear_error() = 0;
 };
 void MGDeleter::operator()(MGState *m) const { delete m; }
 
@@ -472,7 +473,8 @@ template <typename T> struct MGImpl : public MGState {
       }
       if (el.allNeumann) project_coarse_rhs(v, const_cast<T *>(b));
       coarse_pcg_persistent<T>(cA, b, x, cx.p, cz2.p, cz3.p, cPartials.p, cState.p, kCoarseGridMax,
-                               el.opt.coarseTol, el.opt.coarseMaxIter, s);
+                               el.opt.coarseTol, el.opt.coarseMaxIter, s, el.opt.coarseSpinLimit,
+                               (unsigned)el.opt.coarseBarrierExtra);
       return 0;
     }
     const long long n = L.Nlocal;
@@ -591,6 +593,10 @@ template <typename T> struct MGImpl : public MGState {
 
   long long level_size(int level) override { return lv.at(level).L->Nlocal; }
 
+  void clear_error() override
+  {
+    if (persistentCoarse) coarse_state_clear(cState.p, s);
+  }
   int error() override
   {
     if (std::is_same<T, float>::value && el.opt.axPipeline && ax_pipe_error(s)) return 2;
@@ -647,6 +653,10 @@ void Elliptic::mg_apply(const double *r, double *zz)
 }
 void Elliptic::mg_release() { mg.reset(); }
 int Elliptic::mg_error() { return mg ? mg->error() : 0; }
+void Elliptic::mg_clear_error()
+{
+  if (mg) mg->clear_error();
+}
 std::vector<double> Elliptic::mg_get(const std::string &name)
 {
   if (!mg) throw Error(NRSG_ERR_INVALID, "no multigrid preconditioner");

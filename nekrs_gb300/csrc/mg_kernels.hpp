@@ -53,10 +53,15 @@ void coarse_matrix_setup(long long n, const long long *rowPtr, const long long *
 // are E-vectors, x, z and z2 row vectors (solution rows, two exchange
 // buffers); returns the grid size used.  `state` holds coarse_state_bytes()
 // bytes, `partials` 6 * gridMax doubles.
+// Every grid-barrier wait gives up after spinLimit polls and sets the state's
+// error flag; barrierExtra (0 in use) is added to every barrier's target.
 template <typename T>
 int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *z, T *z2, double *partials,
-                          void *state, int gridMax, double tol, int maxit, cudaStream_t s);
+                          void *state, int gridMax, double tol, int maxit, cudaStream_t s,
+                          long long spinLimit = 1LL << 22, unsigned barrierExtra = 0);
 size_t coarse_state_bytes();
+// zero the whole state, error flag included (once per outer solve)
+void coarse_state_clear(void *state, cudaStream_t s);
 // decode a host copy of the state; returns the error flag (0 = ok)
 int coarse_state_read(const void *state_host, int *iters, double *res0, double *res);
 

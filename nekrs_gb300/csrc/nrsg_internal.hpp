@@ -103,6 +103,8 @@ struct Options {
   double coarseTol = 1e-4;
   int coarseMaxIter = 200;
   bool coarsePersistent = true;     // order-1 coarse Jacobi-PCG as one cooperative kernel
+  long long coarseSpinLimit = 1LL << 22; // polls before a grid-barrier wait of that kernel gives up
+  int coarseBarrierExtra = 0;       // arrivals added to every barrier target: nonzero only to test the bounded wait
   bool graphs = true;               // CUDA graphs of the steady-state PCG iteration (non-legacy streams)
   bool axPipeline = false;          // FP32 order-7 levels: bulk-copy pipelined axhelm
   bool axConst = false;             // FP32 order-7 levels: axhelm with D in constant memory / registers
@@ -116,6 +118,7 @@ struct Options {
   bool poisson = true;
   double lambda0 = 1.0, lambda1 = 0.0;
   bool trilinear = false;
+  bool trilinearLambda0All = false; // trilinearLambda0 = all: lambda0 scales every flux (reference: the t-flux only)
   unsigned long long seed = 0x5eed;
 };
 Options parse_options(const char *text);
@@ -153,9 +156,10 @@ struct Reduce {              // scratch for deterministic one-launch reductions
 template <typename T>
 void launch_ax_stored(int N, long long E, const T *ggeo, const T *D, T lambda0, T lambda1, bool poisson, const T *q,
                       T *Aq, cudaStream_t s);
+// lambda0 scales the t-flux only, as the reference's trilinear kernel does; lambda0All: all three fluxes
 template <typename T>
 void launch_ax_trilinear(int N, long long E, const T *VX, const T *gllz, const T *gllw, const T *D, T lambda0,
-                         T lambda1, bool poisson, const T *q, T *Aq, cudaStream_t s);
+                         T lambda1, bool poisson, const T *q, T *Aq, cudaStream_t s, bool lambda0All = false);
 template <typename T> void launch_gs(long long ngroups, const int *off, const int *ids, T *q, cudaStream_t s);
 // Gather-scatter plan of one level: the groups of exactly two members as
 // index pairs (most of them: face-interior nodes), the other groups (>= 3

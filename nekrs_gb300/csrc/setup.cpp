@@ -405,6 +405,14 @@ Options parse_options(const char *text)
       else if (key == "coarsetol") o.coarseTol = std::stod(v);
       else if (key == "coarsemaxiterations") o.coarseMaxIter = std::stoi(v);
       else if (key == "coarsepersistent") o.coarsePersistent = std::stoi(v) != 0;
+      else if (key == "coarsespinlimit") {
+        o.coarseSpinLimit = std::stoll(v);
+        if (o.coarseSpinLimit < 64) throw Error(NRSG_ERR_BAD_CONFIG, "coarseSpinLimit must be >= 64");
+      }
+      else if (key == "coarsebarrierextra") {
+        o.coarseBarrierExtra = std::stoi(v);
+        if (o.coarseBarrierExtra < 0) throw Error(NRSG_ERR_BAD_CONFIG, "coarseBarrierExtra must be >= 0");
+      }
       else if (key == "cudagraphs") o.graphs = std::stoi(v) != 0;
       else if (key == "axpipeline") o.axPipeline = std::stoi(v) != 0;
       else if (key == "axconst") o.axConst = std::stoi(v) != 0;
@@ -427,6 +435,10 @@ Options parse_options(const char *text)
       else if (key == "lambda0") o.lambda0 = std::stod(v);
       else if (key == "lambda1") o.lambda1 = std::stod(v);
       else if (key == "elementmap") o.trilinear = (v == "trilinear");
+      else if (key == "trilinearlambda0") {
+        if (v != "all" && v != "t") throw Error(NRSG_ERR_BAD_CONFIG, "trilinearLambda0 must be t or all");
+        o.trilinearLambda0All = (v == "all");
+      }
       else if (key == "seed") o.seed = std::stoull(v);
       else throw Error(NRSG_ERR_BAD_CONFIG, "unknown option '" + key + "'");
     } catch (const std::invalid_argument &) {

@@ -45,7 +45,7 @@ def build_oracle(force=False):
     for s in srcs:
         o = os.path.join(BUILD, os.path.basename(s)[:-4] + ".o")
         objs.append(o)
-        procs.append(subprocess.Popen(["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC"] + FP_FLAGS + ["-c", s, "-o", o]))
+        procs.append(subprocess.Popen(["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC"] + FP_FLAGS + ["-c", s, "-o", o]))
     for p in procs:
         if p.wait() != 0:
             raise RuntimeError("oracle build failed")
@@ -53,12 +53,13 @@ def build_oracle(force=False):
     return lib
 
 
-def build_all(reference_root="/root/reference"):
+def build_all(reference_root=None):
+    from . import build_ref  # noqa: E402
+
     lib = build_oracle()
     ref = None
+    reference_root = reference_root or build_ref.reference_root()
     if os.path.isdir(reference_root):
-        from . import build_ref  # noqa: E402
-
         ref = build_ref.build(reference_root)
     return lib, ref
 

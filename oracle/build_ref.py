@@ -9,7 +9,7 @@ repository; the wrappers and the library live in the git-ignored
 oracle/_ref/ folder.  When the reference tree is absent (the GPU host) this
 script does nothing and the parity tests that need it are skipped.
 
-Usage: python oracle/build_ref.py [reference_root]
+Usage: python oracle/build_ref.py [reference_root]   (default: $NEKRS_REFERENCE_ROOT)
 """
 import os
 import subprocess
@@ -121,7 +121,14 @@ def wrappers(ref):
     return units
 
 
-def build(ref="/root/reference"):
+def reference_root():
+    """Root of the reference source tree: $NEKRS_REFERENCE_ROOT, else where this
+    build environment mounts it."""
+    return os.environ.get("NEKRS_REFERENCE_ROOT", "/root/reference")
+
+
+def build(ref=None):
+    ref = ref or reference_root()
     if not os.path.isdir(os.path.join(ref, "kernels", "elliptic")):
         print("build_ref: reference tree not found, skipping")
         return None
@@ -154,4 +161,4 @@ def build(ref="/root/reference"):
 
 
 if __name__ == "__main__":
-    print(build(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    print(build(sys.argv[1] if len(sys.argv) > 1 else None))

@@ -41,6 +41,7 @@ struct Options {
   bool poisson = true;
   double lambda0 = 1.0, lambda1 = 0.0;
   bool trilinear = false;                // ELEMENT MAP = TRILINEAR
+  bool trilinearLambda0All = false;      // lambda0 on every flux (the reference: the t-flux only)
   unsigned long long seed = 0x5eed;      // Arnoldi start vector seed
   int projection = 0;                    // INITIAL GUESS: 0 none, 1 PROJECTION (classic), 2 PROJECTION-ACONJ
   int projVecs = 8;                      // RESIDUAL PROJECTION VECTORS

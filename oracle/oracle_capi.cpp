@@ -28,7 +28,11 @@ void orc_gll(int N, double *z, double *w) { gll(N, z, w); }
 // weighted inner product sum_i w_i (a_i b_i) in the device's reduction order (w may be null: 1)
 double orc_wdot(long long n, const double *w, const double *a, const double *b)
 {
-  if (!w) return wsum(n, [&](long long i) { return a[i] * b[i]; });
+  if (!w)
+    return wsum(n, [&](long long i, double &x, double &y) {
+      x = a[i];
+      y = b[i];
+    });
   return wdot<double>(n, w, a, b);
 }
 // the fused PCG update: r = fma(-alpha, Ap, r), x = fma(alpha, p, x), returns (r, r)_w

@@ -2,6 +2,7 @@
 #pragma once
 #include "oracle.hpp"
 
+#include <cmath>
 #include <memory>
 #include <vector>
 
@@ -28,7 +29,8 @@ void build_level(Level &L, int N, long long E, const double *VX, const long long
 
 template <typename T>
 void ax_stored(const Level &L, const T *ggeo, const T *D, T lambda0, T lambda1, bool poisson, const T *q, T *Aq);
-void ax_trilinear(const Level &L, double lambda0, double lambda1, bool poisson, const double *q, double *Aq);
+void ax_trilinear(const Level &L, double lambda0, double lambda1, bool poisson, bool lambda0All, const double *q,
+                  double *Aq);
 template <typename T>
 void build_diag(const Level &L, const T *ggeo, const T *D, T lambda0, T lambda1, bool poisson, T *diag);
 template <typename T> void gs_add(const Level &L, T *q);
@@ -37,28 +39,38 @@ template <typename T> T wdot(long long n, const T *w, const T *a, const T *b);
 void ax_stored_dev(const Level &L, const double *ggeo, const double *D, double lambda0, double lambda1, bool poisson,
                    const double *q, double *Aq);
 
-// Sum of term(i), i < n, in the device library's reduction order: 256-entry
-// chunks (entries past n are +0.0), each summed by the tree s[x] += s[x+o],
-// o = 128, 64, ..., 1 (the block order of the reference's
-// weightedInnerProdMany.okl:27-105); then the chunk sums by the blocked
-// pairwise tree ((P0 + P1) + (P2 + P3)) + ..., zero-padded to a power of two.
-template <typename F> double wsum(long long n, const F &term)
+// Sum over i < n in the device library's reduction order: entry i
+// contributes s = fma(x_i, y_i, s), f(i, x, y) giving the factors.  Chunk c
+// = entries [1024 c, 1024 c + 1024); lane l (0..31) accumulates entries
+// 1024 c + l + 32 j for j ascending from s = 0 (entries past n skipped); the
+// 32 lane sums are added by the tree s[l] += s[l + o], o = 16, 8, 4, 2, 1;
+// the chunk sums by the blocked pairwise tree ((P0 + P1) + (P2 + P3)) + ...,
+// zero-padded to a power of two.
+template <typename F> double wsum(long long n, const F &f)
 {
-  const long long nc = (n + 255) / 256;
+  const long long nc = (n + 1023) / 1024;
   if (nc <= 0) return 0.0;
   long long M = 1;
   while (M < nc) M <<= 1;
   std::vector<double> P((size_t)M, 0.0);
 #pragma omp parallel for schedule(static)
   for (long long c = 0; c < nc; ++c) {
-    double t[256];
-    for (int x = 0; x < 256; ++x) {
-      const long long i = c * 256 + x;
-      t[x] = i < n ? term(i) : 0.0;
+    double s[32];
+    for (int l = 0; l < 32; ++l) {
+      double acc = 0.0;
+      for (int j = 0; j < 32; ++j) {
+        const long long i = c * 1024 + l + 32 * j;
+        if (i < n) {
+          double x, y;
+          f(i, x, y);
+          acc = std::fma(x, y, acc);
+        }
+      }
+      s[l] = acc;
     }
-    for (int o = 128; o >= 1; o >>= 1)
-      for (int x = 0; x < o; ++x) t[x] = t[x] + t[x + o];
-    P[(size_t)c] = t[0];
+    for (int o = 16; o >= 1; o >>= 1)
+      for (int l = 0; l < o; ++l) s[l] = s[l] + s[l + o];
+    P[(size_t)c] = s[0];
   }
   for (long long len = M; len > 1; len >>= 1)
     for (long long x = 0; x < len / 2; ++x) P[(size_t)x] = P[(size_t)(2 * x)] + P[(size_t)(2 * x + 1)];

@@ -194,6 +194,7 @@ void box_mesh(int nx, int ny, int nz, double eps, double *VX, long long *EToV, i
 void trilinear_coords(int N, long long E, const double *VX, const double *z1, double *x, double *y, double *z)
 {
   const int nq = N + 1, np = nq * nq * nq;
+#pragma omp parallel for schedule(static)
   for (long long e = 0; e < E; ++e)
     for (int k = 0; k < nq; ++k)
       for (int j = 0; j < nq; ++j)
@@ -225,6 +226,7 @@ void geometric_factors(int N, long long E, const double *D, const double *w, con
                        const double *z, double *ggeo, double *J_out)
 {
   const int nq = N + 1, np = nq * nq * nq;
+#pragma omp parallel for schedule(static)
   for (long long e = 0; e < E; ++e) {
     const double *xe = x + e * np, *ye = y + e * np, *ze = z + e * np;
     for (int k = 0; k < nq; ++k)

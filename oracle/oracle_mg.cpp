@@ -230,6 +230,7 @@ template <typename T> struct FDMData {
   std::vector<T> Sx, Sy, Sz, invL, wts;
   std::vector<int> extOff, extIds;   // masked extended-mesh gather groups
   std::vector<T> work1, work2;
+  std::vector<T> Sext, out;          // per-call result buffers, kept between calls
 };
 
 template <typename T> struct MGLevel {
@@ -583,6 +584,7 @@ template <typename T> static void fdm_setup(MGLevel<T> &lv, const Level &fineL)
 
 // Schwarz smoother Su = S(u) (pMGLevel::smoothSchwarz): preFDM -> ext gs ->
 // fusedFDM -> [ASM: ext gs -> postFDM] -> gs -> mask.  u and Su may alias.
+constexpr int kMaxNpe = 12 * 12 * 12; // (N+3)^3 for N <= 9
 template <typename T> static void smooth_schwarz(MGT<T> &M, MGLevel<T> &lv, const T *u, T *Su)
 {
   const Level &L = *lv.L;
@@ -615,8 +617,9 @@ template <typename T> static void smooth_schwarz(MGT<T> &M, MGLevel<T> &lv, cons
       }
   }
   gs_groups(F.extOff, F.extIds, w1);
-  std::vector<T> Sext(ras ? 0 : (size_t)E * npe);
-  std::vector<T> out((size_t)E * np);
+  if (!ras && F.Sext.size() != (size_t)E * npe) F.Sext.resize((size_t)E * npe);
+  if (F.out.size() != (size_t)E * np) F.out.resize((size_t)E * np);
+  std::vector<T> &Sext = F.Sext, &out = F.out; // every entry is written below before it is read
   #pragma omp parallel for schedule(static)
   for (long long e = 0; e < E; ++e) {
     T *we = w1 + e * npe;
@@ -634,50 +637,64 @@ template <typename T> static void smooth_schwarz(MGT<T> &M, MGLevel<T> &lv, cons
     auto SX = [&](int r, int c) { return sx[c + r * nl]; };
     auto SY = [&](int r, int c) { return sy[c + r * nl]; };
     auto SZ = [&](int r, int c) { return sz[c + r * nl]; };
-    std::vector<T> t1(npe), t2(npe);
-    // forward: S^T along x, y, z; scale by invL; back: S along x, y, z
+    T t1[kMaxNpe], t2[kMaxNpe];
+    // forward: S^T along x, y, z; scale by invL; back: S along x, y, z.  Each
+    // output is sum_l S(.,.) v(l) accumulated for l ascending from 0 (the
+    // order of fusedFDM.c); the loops run the outputs innermost so that they
+    // vectorise without changing any output's summation order.
+    const int nl2 = nl * nl;
+    for (int q = 0; q < npe; ++q) t1[q] = 0;
     for (int k = 0; k < nl; ++k)
       for (int j = 0; j < nl; ++j)
-        for (int i = 0; i < nl; ++i) {
-          T v = 0;
-          for (int l = 0; l < nl; ++l) v += SX(l, i) * we[X(l, j, k)];
-          t1[X(i, j, k)] = v;
+        for (int l = 0; l < nl; ++l) {
+          const T w = we[X(l, j, k)];
+          T *o = t1 + X(0, j, k);
+          const T *srow = sx + l * nl; // SX(l, i) = sx[i + l nl]
+          for (int i = 0; i < nl; ++i) o[i] += srow[i] * w;
         }
+    for (int q = 0; q < npe; ++q) t2[q] = 0;
     for (int k = 0; k < nl; ++k)
       for (int j = 0; j < nl; ++j)
-        for (int i = 0; i < nl; ++i) {
-          T v = 0;
-          for (int l = 0; l < nl; ++l) v += SY(l, j) * t1[X(i, l, k)];
-          t2[X(i, j, k)] = v;
+        for (int l = 0; l < nl; ++l) {
+          const T c = SY(l, j);
+          T *o = t2 + X(0, j, k);
+          const T *v = t1 + X(0, l, k);
+          for (int i = 0; i < nl; ++i) o[i] += c * v[i];
         }
+    for (int q = 0; q < npe; ++q) t1[q] = 0;
+    for (int k = 0; k < nl; ++k)
+      for (int l = 0; l < nl; ++l) {
+        const T c = SZ(l, k);
+        T *o = t1 + k * nl2;
+        const T *v = t2 + l * nl2;
+        for (int ij = 0; ij < nl2; ++ij) o[ij] += c * v[ij];
+      }
+    for (int q = 0; q < npe; ++q) t1[q] = t1[q] * F.invL[e * npe + q];
+    for (int q = 0; q < npe; ++q) t2[q] = 0;
     for (int k = 0; k < nl; ++k)
       for (int j = 0; j < nl; ++j)
-        for (int i = 0; i < nl; ++i) {
-          T v = 0;
-          for (int l = 0; l < nl; ++l) v += SZ(l, k) * t2[X(i, j, l)];
-          t1[X(i, j, k)] = v * F.invL[e * npe + X(i, j, k)];
+        for (int l = 0; l < nl; ++l) {
+          const T w = t1[X(l, j, k)];
+          T *o = t2 + X(0, j, k);
+          for (int i = 0; i < nl; ++i) o[i] += SX(i, l) * w;
         }
+    for (int q = 0; q < npe; ++q) t1[q] = 0;
     for (int k = 0; k < nl; ++k)
       for (int j = 0; j < nl; ++j)
-        for (int i = 0; i < nl; ++i) {
-          T v = 0;
-          for (int l = 0; l < nl; ++l) v += SX(i, l) * t1[X(l, j, k)];
-          t2[X(i, j, k)] = v;
+        for (int l = 0; l < nl; ++l) {
+          const T c = SY(j, l);
+          T *o = t1 + X(0, j, k);
+          const T *v = t2 + X(0, l, k);
+          for (int i = 0; i < nl; ++i) o[i] += c * v[i];
         }
+    for (int q = 0; q < npe; ++q) t2[q] = 0;
     for (int k = 0; k < nl; ++k)
-      for (int j = 0; j < nl; ++j)
-        for (int i = 0; i < nl; ++i) {
-          T v = 0;
-          for (int l = 0; l < nl; ++l) v += SY(j, l) * t2[X(i, l, k)];
-          t1[X(i, j, k)] = v;
-        }
-    for (int k = 0; k < nl; ++k)
-      for (int j = 0; j < nl; ++j)
-        for (int i = 0; i < nl; ++i) {
-          T v = 0;
-          for (int l = 0; l < nl; ++l) v += SZ(k, l) * t1[X(i, j, l)];
-          t2[X(i, j, k)] = v;
-        }
+      for (int l = 0; l < nl; ++l) {
+        const T c = SZ(k, l);
+        T *o = t2 + k * nl2;
+        const T *v = t1 + l * nl2;
+        for (int ij = 0; ij < nl2; ++ij) o[ij] += c * v[ij];
+      }
     if (ras) {
       // restrict with the level's inverse degree (the weights argument of
       // fusedFDM, elliptic->o_invDegree: ellipticMultiGridSchwarz.cpp:1069-1077,
@@ -689,7 +706,7 @@ template <typename T> static void smooth_schwarz(MGT<T> &M, MGLevel<T> &lv, cons
             out[id] = t2[X(i + 1, j + 1, k + 1)] * lv.invDegree[id];
           }
     } else {
-      std::memcpy(&Sext[e * npe], t2.data(), sizeof(T) * npe);
+      std::memcpy(&Sext[e * npe], t2, sizeof(T) * npe);
       // keep this element's own face-layer results for the overlap combine
       for (int a = 1; a < nl - 1; ++a)
         for (int b = 1; b < nl - 1; ++b)
@@ -1053,6 +1070,7 @@ template <typename T> static void vcycle(MGT<T> &M, int k)
   // residual: res = rhs - A x
   level_op(M, lv, lv.x.data(), lv.res.data());
   const long long n = lv.L->Nlocal;
+#pragma omp parallel for schedule(static)
   for (long long i = 0; i < n; ++i) lv.res[i] = (T)1 * lv.rhs[i] + (T)(-1) * lv.res[i];
   level_coarsen(M, lc, lv.res.data(), lc.rhs.data());
   vcycle(M, k + 1);
@@ -1265,11 +1283,13 @@ void mg_setup(Elliptic &el)
 template <typename T> static void run_mg(MGT<T> &M, const double *r, double *z, long long n)
 {
   auto &l0 = M.levels[0];
+#pragma omp parallel for schedule(static)
   for (long long i = 0; i < n; ++i) {
     l0.rhs[i] = (T)r[i];
     l0.x[i] = 0;
   }
   vcycle(M, 0);
+#pragma omp parallel for schedule(static)
   for (long long i = 0; i < n; ++i) z[i] = (double)l0.x[i];
 }
 

@@ -15,9 +15,10 @@
 // Bit-identical FP64 path.  The plain FP64 solve (stored geometry; Jacobi or
 // no preconditioner; PCG, flexible PCG, GMRES, flexible GMRES; solution
 // projection) performs exactly the device library's floating-point
-// operations in the device's order: weighted sums through wsum() (256-entry
-// chunks by the reference's block tree, then a blocked pairwise tree over the
-// chunk sums), std::fma wherever the device uses a fused multiply-add, and
+// operations in the device's order: weighted sums through wsum() (one fused
+// multiply-add per entry on 32 interleaved lanes of 1024-entry chunks, a lane
+// tree, then a blocked pairwise tree over the chunk sums), std::fma wherever
+// the device uses a fused multiply-add, and
 // separately rounded products elsewhere.  The oracle is compiled without
 // contraction (-ffp-contract=off), so the same source rounds the same way on
 // every host.  The reference-order operator (ax_stored, the order of the
@@ -96,6 +97,7 @@ Options parse_options(const std::string &text)
     else if (key == "lambda0") o.lambda0 = std::stod(lv);
     else if (key == "lambda1") o.lambda1 = std::stod(lv);
     else if (key == "elementmap") o.trilinear = (lv == "trilinear");
+    else if (key == "trilinearlambda0") o.trilinearLambda0All = (lv == "all");
     else if (key == "seed") o.seed = std::stoull(lv);
     else if (key == "initialguess")
       o.projection = (lv == "projectionaconj" || lv == "projection-aconj") ? 2 : (lv == "projection" ? 1 : 0);
@@ -154,7 +156,7 @@ void ax_stored(const Level &L, const T *ggeo, const T *D, T lambda0, T lambda1, 
   const int nq = L.Nq, np = L.Np;
 #pragma omp parallel for
   for (long long e = 0; e < L.E; ++e) {
-    std::vector<T> Gr(np), Gs(np), Gt(np);
+    T Gr[1000], Gs[1000], Gt[1000]; // Np <= 10^3
     const T *qe = q + e * np;
     const T *g = ggeo + (size_t)e * 7 * np;
     for (int k = 0; k < nq; ++k)
@@ -193,23 +195,26 @@ void ax_stored(const Level &L, const T *ggeo, const T *D, T lambda0, T lambda1, 
   }
 }
 
-// Ax, stored geometric factors, FP64 in the device kernel's operation order
-// (ax_stored_kernel<double>): per k-plane, qt, qr, qs as fused multiply-add
-// chains over m; G q as lambda0 fma(Gc, qt, fma(Gb, qs, Ga qr)); then for m
-// ascending auk += D[m][j] Gs(i,m,k), Aq(i,j,m) += D[k][m] Gt(i,j,k),
+// Ax in FP64 in the device kernel's operation order (ax_stored_kernel<double>
+// and ax_trilinear_kernel<double>): per k-plane, qt, qr, qs as fused
+// multiply-add chains over m; G q as l0 fma(Gc, qt, fma(Gb, qs, Ga qr)); then
+// for m ascending auk += D[m][j] Gs(i,m,k), Aq(i,j,m) += D[k][m] Gt(i,j,k),
 // auk += D[m][i] Gr(m,j,k), all fused; Aq(i,j,k) += auk at the end of plane k.
-void ax_stored_dev(const Level &L, const double *ggeo, const double *D, double lambda0, double lambda1, bool poisson,
-                   const double *q, double *Aq)
+// gf(e, i, j, k, G[7]) supplies G00, G01, G11, G12, G02, G22, GWJ of a node;
+// l0rs scales the r and s fluxes, l0t the t flux.
+template <typename GF>
+static void ax_dev(const Level &L, const double *D, double l0rs, double l0t, double lambda1, bool poisson,
+                   const double *q, double *Aq, const GF &gf)
 {
   const int nq = L.Nq, np = L.Np, nq2 = nq * nq;
-  auto gflux = [&](double Ga, double Gb, double Gc, double qr, double qs, double qt) {
-    return lambda0 * std::fma(Gc, qt, std::fma(Gb, qs, Ga * qr));
+  auto gflux = [&](double l0, double Ga, double Gb, double Gc, double qr, double qs, double qt) {
+    return l0 * std::fma(Gc, qt, std::fma(Gb, qs, Ga * qr));
   };
 #pragma omp parallel for
   for (long long e = 0; e < L.E; ++e) {
-    std::vector<double> Gr(nq2), Gs(nq2), Gt(nq2), auk(nq2), rAq(np, 0.0);
+    double Gr[100], Gs[100], Gt[100], auk[100], rAq[1000]; // Nq <= 10
+    for (int t = 0; t < np; ++t) rAq[t] = 0.0;
     const double *qe = q + e * np;
-    const double *g = ggeo + (size_t)e * 7 * np;
     for (int k = 0; k < nq; ++k) {
       for (int j = 0; j < nq; ++j)
         for (int i = 0; i < nq; ++i) {
@@ -220,12 +225,13 @@ void ax_stored_dev(const Level &L, const double *ggeo, const double *D, double l
             qr = std::fma(D[i * nq + m], qe[m + nq * j + nq2 * k], qr);
             qs = std::fma(D[j * nq + m], qe[i + nq * m + nq2 * k], qs);
           }
-          const double G00 = g[0 * np + n], G01 = g[1 * np + n], G11 = g[2 * np + n];
-          const double G12 = g[3 * np + n], G02 = g[4 * np + n], G22 = g[5 * np + n];
-          Gr[t] = gflux(G00, G01, G02, qr, qs, qt);
-          Gs[t] = gflux(G01, G11, G12, qr, qs, qt);
-          Gt[t] = gflux(G02, G12, G22, qr, qs, qt);
-          auk[t] = poisson ? 0.0 : g[6 * np + n] * lambda1 * qe[n];
+          double G[7];
+          gf(e, i, j, k, G);
+          const double G00 = G[0], G01 = G[1], G11 = G[2], G12 = G[3], G02 = G[4], G22 = G[5];
+          Gr[t] = gflux(l0rs, G00, G01, G02, qr, qs, qt);
+          Gs[t] = gflux(l0rs, G01, G11, G12, qr, qs, qt);
+          Gt[t] = gflux(l0t, G02, G12, G22, qr, qs, qt);
+          auk[t] = poisson ? 0.0 : G[6] * lambda1 * qe[n];
         }
       for (int j = 0; j < nq; ++j)
         for (int i = 0; i < nq; ++i) {
@@ -239,83 +245,70 @@ void ax_stored_dev(const Level &L, const double *ggeo, const double *D, double l
           rAq[t + nq2 * k] += a;
         }
     }
-    std::copy(rAq.begin(), rAq.end(), Aq + e * np);
+    std::copy(rAq, rAq + np, Aq + e * np);
   }
 }
 
-// Ax with geometric factors rebuilt from the 8 trilinear vertices
-// (ellipticPartialAxTrilinearHex3D.okl:50-120).  Vertex input is in
-// hypercube order; lambda0 scales all three fluxes (the reference applies it
-// to the t-flux only, which is identical for the constant lambda0 = 1 case).
-void ax_trilinear(const Level &L, double lambda0, double lambda1, bool poisson, const double *q, double *Aq)
+void ax_stored_dev(const Level &L, const double *ggeo, const double *D, double lambda0, double lambda1, bool poisson,
+                   const double *q, double *Aq)
 {
   const int nq = L.Nq, np = L.Np;
-  const double *D = L.D.data();
-#pragma omp parallel for
-  for (long long e = 0; e < L.E; ++e) {
-    std::vector<double> Gr(np), Gs(np), Gt(np), G6(np);
-    // CCW vertex order used by the reference kernel: 0:(-,-,-) 1:(+,-,-) 2:(+,+,-) 3:(-,+,-), 4..7 at t=+1
-    static const int ccw[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+  ax_dev(L, D, lambda0, lambda0, lambda1, poisson, q, Aq, [&](long long e, int i, int j, int k, double *G) {
+    const double *g = ggeo + (size_t)e * 7 * np;
+    const int n = i + nq * (j + nq * k);
+    for (int c = 0; c < 7; ++c) G[c] = g[c * np + n];
+  });
+}
+
+// Ax with geometric factors rebuilt from the 8 trilinear vertices
+// (ellipticPartialAxTrilinearHex3D.okl:50-120), in the device kernel's
+// operation order.  Vertex input is in hypercube order.  The reference
+// scales the t-flux alone by lambda0 (lines 154-157), which is the default
+// here; option trilinearLambda0 = all scales all three fluxes.
+void ax_trilinear(const Level &L, double lambda0, double lambda1, bool poisson, bool lambda0All, const double *q,
+                  double *Aq)
+{
+  // CCW vertex order used by the reference kernel: 0:(-,-,-) 1:(+,-,-) 2:(+,+,-) 3:(-,+,-), 4..7 at t=+1
+  static const int ccw[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+  auto gf = [&](long long e, int i, int j, int k, double *G) {
     double xe[8], ye[8], ze[8];
     for (int v = 0; v < 8; ++v) {
       xe[v] = L.VX[(e * 8 + ccw[v]) * 3 + 0];
       ye[v] = L.VX[(e * 8 + ccw[v]) * 3 + 1];
       ze[v] = L.VX[(e * 8 + ccw[v]) * 3 + 2];
     }
-    const double *qe = q + e * np;
-    for (int k = 0; k < nq; ++k)
-      for (int j = 0; j < nq; ++j)
-        for (int i = 0; i < nq; ++i) {
-          const double rn = L.z[i], sn = L.z[j], tn = L.z[k];
-          auto dr = [&](const double *X) {
-            return 0.125 * ((1 - tn) * (1 - sn) * (X[1] - X[0]) + (1 - tn) * (1 + sn) * (X[2] - X[3]) +
-                            (1 + tn) * (1 - sn) * (X[5] - X[4]) + (1 + tn) * (1 + sn) * (X[6] - X[7]));
-          };
-          auto ds = [&](const double *X) {
-            return 0.125 * ((1 - tn) * (1 - rn) * (X[3] - X[0]) + (1 - tn) * (1 + rn) * (X[2] - X[1]) +
-                            (1 + tn) * (1 - rn) * (X[7] - X[4]) + (1 + tn) * (1 + rn) * (X[6] - X[5]));
-          };
-          auto dt = [&](const double *X) {
-            return 0.125 * ((1 - rn) * (1 - sn) * (X[4] - X[0]) + (1 + rn) * (1 - sn) * (X[5] - X[1]) +
-                            (1 + rn) * (1 + sn) * (X[6] - X[2]) + (1 - rn) * (1 + sn) * (X[7] - X[3]));
-          };
-          const double xr = dr(xe), xs = ds(xe), xt = dt(xe);
-          const double yr = dr(ye), ys = ds(ye), yt = dt(ye);
-          const double zr = dr(ze), zs = ds(ze), zt = dt(ze);
-          const double J = xr * (ys * zt - zs * yt) - yr * (xs * zt - zs * xt) + zr * (xs * yt - ys * xt);
-          const double rx = (ys * zt - zs * yt), ry = -(xs * zt - zs * xt), rz = (xs * yt - ys * xt);
-          const double sx = -(yr * zt - zr * yt), sy = (xr * zt - zr * xt), sz = -(xr * yt - yr * xt);
-          const double tx = (yr * zs - zr * ys), ty = -(xr * zs - zr * xs), tz = (xr * ys - yr * xs);
-          const double W = L.w[i] * L.w[j] * L.w[k];
-          const double sc = W / J;
-          const double G00 = sc * (rx * rx + ry * ry + rz * rz), G01 = sc * (rx * sx + ry * sy + rz * sz);
-          const double G02 = sc * (rx * tx + ry * ty + rz * tz), G11 = sc * (sx * sx + sy * sy + sz * sz);
-          const double G12 = sc * (sx * tx + sy * ty + sz * tz), G22 = sc * (tx * tx + ty * ty + tz * tz);
-          double qr = 0, qs = 0, qt = 0;
-          for (int m = 0; m < nq; ++m) {
-            qr += D[i * nq + m] * qe[m + nq * (j + nq * k)];
-            qs += D[j * nq + m] * qe[i + nq * (m + nq * k)];
-            qt += D[k * nq + m] * qe[i + nq * (j + nq * m)];
-          }
-          const int n = i + nq * (j + nq * k);
-          Gr[n] = lambda0 * (G00 * qr + G01 * qs + G02 * qt);
-          Gs[n] = lambda0 * (G01 * qr + G11 * qs + G12 * qt);
-          Gt[n] = lambda0 * (G02 * qr + G12 * qs + G22 * qt);
-          G6[n] = poisson ? 0.0 : W * J * lambda1 * qe[n];
-        }
-    for (int k = 0; k < nq; ++k)
-      for (int j = 0; j < nq; ++j)
-        for (int i = 0; i < nq; ++i) {
-          const int n = i + nq * (j + nq * k);
-          double ar = 0, as = 0, at = 0;
-          for (int m = 0; m < nq; ++m) {
-            ar += D[m * nq + i] * Gr[m + nq * (j + nq * k)];
-            as += D[m * nq + j] * Gs[i + nq * (m + nq * k)];
-            at += D[m * nq + k] * Gt[i + nq * (j + nq * m)];
-          }
-          Aq[e * np + n] = ar + as + at + G6[n];
-        }
-  }
+    const double rn = L.z[i], sn = L.z[j], tn = L.z[k];
+    const double am = (1 - tn) * (1 - sn), ap = (1 - tn) * (1 + sn), bm = (1 + tn) * (1 - sn), bp = (1 + tn) * (1 + sn);
+    const double cm = (1 - tn) * (1 - rn), cp = (1 - tn) * (1 + rn), dm = (1 + tn) * (1 - rn), dp = (1 + tn) * (1 + rn);
+    const double fm = (1 - rn) * (1 - sn), fp = (1 + rn) * (1 - sn), hp = (1 + rn) * (1 + sn), hm = (1 - rn) * (1 + sn);
+    auto comb = [](double a0, double d0, double a1, double d1, double a2, double d2, double a3, double d3) {
+      return 0.125 * std::fma(a3, d3, std::fma(a2, d2, std::fma(a1, d1, a0 * d0)));
+    };
+    auto dr = [&](const double *X) { return comb(am, X[1] - X[0], ap, X[2] - X[3], bm, X[5] - X[4], bp, X[6] - X[7]); };
+    auto ds = [&](const double *X) { return comb(cm, X[3] - X[0], cp, X[2] - X[1], dm, X[7] - X[4], dp, X[6] - X[5]); };
+    auto dt = [&](const double *X) { return comb(fm, X[4] - X[0], fp, X[5] - X[1], hp, X[6] - X[2], hm, X[7] - X[3]); };
+    const double xr = dr(xe), xs = ds(xe), xt = dt(xe);
+    const double yr = dr(ye), ys = ds(ye), yt = dt(ye);
+    const double zr = dr(ze), zs = ds(ze), zt = dt(ze);
+    auto minor2 = [](double a, double b, double c, double d) { return std::fma(a, b, -(c * d)); };
+    const double rx = minor2(ys, zt, zs, yt), ry = -minor2(xs, zt, zs, xt), rz = minor2(xs, yt, ys, xt);
+    const double sx = -minor2(yr, zt, zr, yt), sy = minor2(xr, zt, zr, xt), sz = -minor2(xr, yt, yr, xt);
+    const double tx = minor2(yr, zs, zr, ys), ty = -minor2(xr, zs, zr, xs), tz = minor2(xr, ys, yr, xs);
+    const double J = std::fma(zr, rz, std::fma(yr, ry, xr * rx));
+    const double W = L.w[i] * L.w[j] * L.w[k];
+    const double sc = W / J;
+    auto dot3 = [](double a0, double b0, double a1, double b1, double a2, double b2) {
+      return std::fma(a2, b2, std::fma(a1, b1, a0 * b0));
+    };
+    G[0] = sc * dot3(rx, rx, ry, ry, rz, rz);
+    G[1] = sc * dot3(rx, sx, ry, sy, rz, sz);
+    G[2] = sc * dot3(sx, sx, sy, sy, sz, sz);
+    G[3] = sc * dot3(sx, tx, sy, ty, sz, tz);
+    G[4] = sc * dot3(rx, tx, ry, ty, rz, tz);
+    G[5] = sc * dot3(tx, tx, ty, ty, tz, tz);
+    G[6] = W * J;
+  };
+  ax_dev(L, L.D.data(), lambda0All ? lambda0 : 1.0, lambda0, lambda1, poisson, q, Aq, gf);
 }
 
 // diag(A_L) per element (ellipticBlockBuildDiagonalHex3D.okl:61-107), single field.
@@ -377,13 +370,19 @@ template <typename T> void gs_add(const Level &L, T *q)
 
 template <typename T> void apply_mask(const Level &L, T *q)
 {
-  for (int m : L.maskIds) q[m] = 0;
+  const long long nm = (long long)L.maskIds.size();
+#pragma omp parallel for schedule(static)
+  for (long long k = 0; k < nm; ++k) q[L.maskIds[k]] = 0;
 }
 
-// Weighted inner product in the device's summation order (wsum).
+// Weighted inner product in the device's summation order (wsum): entry
+// factors (w_i a_i rounded, b_i), so the argument order matters.
 template <typename T> T wdot(long long n, const T *w, const T *a, const T *b)
 {
-  return (T)wsum(n, [&](long long i) { return (double)w[i] * ((double)a[i] * (double)b[i]); });
+  return (T)wsum(n, [&](long long i, double &x, double &y) {
+    x = (double)w[i] * (double)a[i];
+    y = (double)b[i];
+  });
 }
 
 // explicit instantiations used by the MG code
@@ -425,7 +424,7 @@ void Elliptic::setup(int N, long long E, const double *VX, const long long *EToV
 void Elliptic::ax(const double *q, double *Aq) const
 {
   if (o.trilinear)
-    ax_trilinear(fine, o.lambda0, o.lambda1, o.poisson, q, Aq);
+    ax_trilinear(fine, o.lambda0, o.lambda1, o.poisson, o.trilinearLambda0All, q, Aq);
   else
     ax_stored_dev(fine, fine.ggeo.data(), fine.D.data(), o.lambda0, o.lambda1, o.poisson, q, Aq);
 }
@@ -446,6 +445,7 @@ void Elliptic::precond(const double *r, double *z)
 {
   const long long n = fine.Nlocal;
   if (o.precon == "jacobi") {
+    #pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; ++i) z[i] = r[i] * invDiag[i];
   } else if (o.precon == "multigrid") {
     mg_apply(*this, r, z);
@@ -459,8 +459,12 @@ void Elliptic::precond(const double *r, double *z)
 void Elliptic::zero_mean(double *q) const
 {
   const long long n = fine.Nlocal;
-  const double s = wsum(n, [&](long long i) { return q[i]; });
+  const double s = wsum(n, [&](long long i, double &x, double &y) {
+    x = q[i];
+    y = 1.0;
+  });
   const double mean = s / (double)n;
+  #pragma omp parallel for schedule(static)
   for (long long i = 0; i < n; ++i) q[i] += -mean;
 }
 
@@ -499,10 +503,12 @@ int Elliptic::pcg(double *r, double *x, double tol, int maxit, double &rnorm)
         beta = -alpha * zdotAp / rdotz2;
       }
     }
+    #pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; ++i) p[i] = std::fma(beta, p[i], z[i]);
     op(p.data(), Ap.data());
     const double pAp = wdot<double>(n, w, p.data(), Ap.data());
     alpha = rdotz1 / (pAp + 1e-300);
+    #pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; ++i) {
       r[i] = std::fma(-alpha, Ap[i], r[i]);
       x[i] = std::fma(alpha, p[i], x[i]);
@@ -536,9 +542,10 @@ void Elliptic::proj_update_space()
   const double *w = fine.invDegree.data();
   const double *b = &projBB[(size_t)(classic ? m - 1 : 0) * n];
   std::vector<double> alpha(m);
-  for (int k = 0; k < m; ++k) alpha[k] = wdot<double>(n, w, &projXX[(size_t)k * n], b);
+  for (int k = 0; k < m; ++k) alpha[k] = wdot<double>(n, w, b, &projXX[(size_t)k * n]);
   const double normOrig = alpha[m - 1];
   double *xm = &projXX[(size_t)(m - 1) * n];
+  #pragma omp parallel for schedule(static)
   for (long long i = 0; i < n; ++i) {
     double v = xm[i];
     for (int k = 0; k < m - 1; ++k) v = std::fma(-alpha[k], projXX[(size_t)k * n + i], v);
@@ -546,6 +553,7 @@ void Elliptic::proj_update_space()
   }
   if (classic) {
     double *bm = &projBB[(size_t)(m - 1) * n];
+    #pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; ++i) {
       double v = bm[i];
       for (int k = 0; k < m - 1; ++k) v = std::fma(-alpha[k], projBB[(size_t)k * n + i], v);
@@ -557,8 +565,10 @@ void Elliptic::proj_update_space()
   const double normNew = std::sqrt(normOrig - sumAlpha);
   if (normNew / normOrig > 1e-7) {
     const double sc = 1.0 / normNew;
+    #pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; ++i) xm[i] *= sc;
     if (classic)
+      #pragma omp parallel for schedule(static)
       for (long long i = 0; i < n; ++i) projBB[(size_t)(m - 1) * n + i] *= sc;
   } else {
     --projM; // linearly dependent: discard
@@ -573,7 +583,8 @@ void Elliptic::proj_pre(double *r)
   const double *w = fine.invDegree.data();
   const int m = projM;
   std::vector<double> alpha(m);
-  for (int k = 0; k < m; ++k) alpha[k] = wdot<double>(n, w, &projXX[(size_t)k * n], r);
+  for (int k = 0; k < m; ++k) alpha[k] = wdot<double>(n, w, r, &projXX[(size_t)k * n]);
+  #pragma omp parallel for schedule(static)
   for (long long i = 0; i < n; ++i) {
     double v = alpha[0] * projXX[i];
     for (int k = 1; k < m; ++k) v = std::fma(alpha[k], projXX[(size_t)k * n + i], v);
@@ -581,6 +592,7 @@ void Elliptic::proj_pre(double *r)
   }
   std::vector<double> t(n);
   if (o.projection == 1) {
+    #pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; ++i) {
       double v = alpha[0] * projBB[i];
       for (int k = 1; k < m; ++k) v = std::fma(alpha[k], projBB[(size_t)k * n + i], v);
@@ -589,6 +601,7 @@ void Elliptic::proj_pre(double *r)
   } else {
     op(projXbar.data(), t.data());
   }
+  #pragma omp parallel for schedule(static)
   for (long long i = 0; i < n; ++i) r[i] = -1.0 * t[i] + 1.0 * r[i];
 }
 
@@ -602,11 +615,13 @@ void Elliptic::proj_post(double *x)
     std::copy(x, x + n, projXX.begin());
   } else if (projM == maxv) {
     projM = 1;
+    #pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; ++i) x[i] = 1.0 * projXbar[i] + 1.0 * x[i];
     std::copy(x, x + n, projXX.begin());
   } else {
     ++projM;
     std::copy(x, x + n, projXX.begin() + (size_t)(projM - 1) * n);
+    #pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; ++i) x[i] = 1.0 * projXbar[i] + 1.0 * x[i];
   }
   const int prev = projM;
@@ -626,10 +641,12 @@ int Elliptic::solve(double *r, double *x, double &res0, double &res)
   const long long n = fine.Nlocal;
   std::vector<double> Ax0(n), x0(x, x + n);
   ax(x, Ax0.data());
+  #pragma omp parallel for schedule(static)
   for (long long i = 0; i < n; ++i) r[i] = -Ax0[i] + r[i];
   if (allNeumann) zero_mean(r); // ellipticSolve.cpp:101
   apply_mask(fine, r);
   gs_add(fine, r);
+  #pragma omp parallel for schedule(static)
   for (long long i = 0; i < n; ++i) x[i] = 0;
   if (o.projection) {
     if (projXX.empty()) {
@@ -651,6 +668,7 @@ int Elliptic::solve(double *r, double *x, double &res0, double &res)
   else
     iters = pgmres(r, x, tol, o.maxIter, res);
   if (o.projection) proj_post(x);
+  #pragma omp parallel for schedule(static)
   for (long long i = 0; i < n; ++i) x[i] += x0[i];
   if (allNeumann) zero_mean(x); // ellipticSolve.cpp:188-189
   if (std::isnan(res)) status = 3;
@@ -706,7 +724,7 @@ int Elliptic::pgmres(double *r, double *x, double tol, int maxit, double &rdotr)
       std::vector<double> &Mv = flexible ? Z[i] : Z[0];
       precond(V[i].data(), Mv.data());
       op(Mv.data(), w.data());
-      for (int k = 0; k <= i; ++k) y[k] = wdot<double>(n, wt, V[k].data(), w.data());
+      for (int k = 0; k <= i; ++k) y[k] = wdot<double>(n, wt, w.data(), V[k].data());
       for (long long q = 0; q < n; ++q) {
         double v = w[q];
         for (int k = 0; k <= i; ++k) v = std::fma(-y[k], V[k][q], v);

@@ -14,7 +14,8 @@ import sys
 
 import numpy as np
 
-SRC = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/examples/kershaw/kershaw.re2"
+SRC = sys.argv[1] if len(sys.argv) > 1 else os.path.join(
+    os.environ.get("NEKRS_REFERENCE_ROOT", "/root/reference"), "examples", "kershaw", "kershaw.re2")
 b = open(SRC, "rb").read()
 hdr = b[:80].decode()
 E = int(hdr[5:14])

@@ -69,11 +69,15 @@ def test_nonzero_initial_guess_and_helmholtz(product_lib, oracle_mod, torch_cuda
     assert_bit_identical(xo, io, xg, ig, el)
 
 
-def test_trilinear_operator_solve(product_lib, oracle_mod, torch_cuda):
-    opts = "preconditioner=jacobi;solver=pcg;residualTol=1e-8+relative;elementMap=trilinear"
+@pytest.mark.parametrize("lam", ["", ";trilinearLambda0=all"])
+def test_trilinear_operator_solve(product_lib, oracle_mod, torch_cuda, lam):
+    """Recomputed (trilinear) geometry, Helmholtz with lambda0 != 1 on the reference's t-flux-only scaling and
+    on the all-flux option: bit-identical to the oracle."""
+    opts = ("preconditioner=jacobi;solver=pcg;residualTol=1e-8+relative;elementMap=trilinear;poisson=0;"
+            "lambda0=1.4;lambda1=0.3" + lam)
     xo, io, xg, ig, el, orc = run_pair(torch_cuda, 5, 3, opts, eps=1.0)
-    assert abs(ig["iterations"] - io["iterations"]) <= 1
-    assert rel(xg, xo) < 1e-8
+    assert ig["status"] == 0
+    assert_bit_identical(xo, io, xg, ig, el)
 
 
 def test_operator_gs_mask_entry_points(product_lib, oracle_mod, torch_cuda):

@@ -248,3 +248,43 @@ def test_oracle_coefficient_field_axhelm_bitexact_vs_reference(oracle_mod, N):
     ref = _ref_block("axcoef", None, N, VX.shape[0], el.get("ggeo"), el.get("D"), q, lam0, lam1, 0)
     got = el.block_ax(q, nf=1, lam0=lam0, lam1=lam1)
     assert np.array_equal(got, ref)
+
+
+def test_oracle_trilinear_lambda0_on_t_flux_only(oracle_mod):
+    """The reference's trilinear kernel scales the t-flux alone by lambda0 (ellipticPartialAxTrilinearHex3D.okl:
+    154-157); option trilinearLambda0=all scales all three.  On an undeformed box a field that does not vary in
+    z has no t-flux, so the default operator ignores lambda0 there, while the all-flux form scales by it."""
+    N, n = 4, 2
+    VX, EToV, EToB = O.box_mesh(n, n, n, 1.0)  # Kershaw eps = 1: the undeformed box
+    base = "preconditioner=jacobi;elementMap=trilinear"
+    a1 = O.Elliptic(N, VX, EToV, EToB, base)
+    a2 = O.Elliptic(N, VX, EToV, EToB, base + ";lambda0=2.5")
+    a3 = O.Elliptic(N, VX, EToV, EToB, base + ";lambda0=2.5;trilinearLambda0=all")
+    x, y = a1.get("x"), a1.get("y")
+    q = np.sin(2.0 * x) * np.cos(3.0 * y)
+    r1, r2, r3 = a1.ax(q), a2.ax(q), a3.ax(q)
+    scale = np.max(np.abs(r1))
+    assert np.max(np.abs(r2 - r1)) <= 1e-13 * scale
+    assert np.max(np.abs(r3 - 2.5 * r1)) <= 1e-13 * scale
+    # a field varying in z only: the t-flux is all there is, both forms scale it
+    zc = a1.get("z")
+    qz = np.cos(2.0 * zc)
+    assert np.max(np.abs(a2.ax(qz) - 2.5 * a1.ax(qz))) <= 1e-13 * np.max(np.abs(a1.ax(qz)))
+
+
+def test_oracle_config0_matches_fixture(oracle_mod):
+    """The oracle's E=8^3 Jacobi-PCG solve reproduces the committed fixture (iterations, history, solution)."""
+    import hashlib
+    import json
+
+    from nekrs_gb300 import workloads as W
+
+    with open(os.path.join(os.path.dirname(__file__), "golden", "config_parity.json")) as f:
+        cfg = json.load(f)["c0"]
+    VX, EToV, EToB = W.kershaw_box(cfg["nel"], eps=cfg["eps"])
+    orc = O.Elliptic(cfg["N"], VX, EToV, EToB, cfg["options"])
+    x, io = orc.solve(W.box_rhs(cfg["N"], cfg["nel"], cfg["nel"], cfg["nel"], cfg["seed"], orc.get("ggeo")))
+    assert io["iterations"] == cfg["iterations"]
+    assert np.allclose(io["history"], cfg["history"], rtol=1e-10, atol=0)
+    assert abs(np.linalg.norm(x) - cfg["x_norm"]) <= 1e-12 * cfg["x_norm"]
+    assert hashlib.sha256(x.tobytes()).hexdigest() == cfg["x_sha256"]

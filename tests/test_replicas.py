@@ -57,3 +57,20 @@ def test_reference_arm_runs_on_rank_zero_only():
                           "--warmup", "3"], env=env, capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stderr
     assert out.stdout.strip() == ""
+
+
+def test_reference_arm_times_complete_solves():
+    """The reference arm runs complete oracle solves of the workload (here the E=8^3 Jacobi-PCG one) with the
+    oracle's own iteration count, and reports the number of solves it ran."""
+    with open(os.path.join(ROOT, "tests", "golden", "config_parity.json")) as f:
+        c0 = json.load(f)["c0"]
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0", NRSG_REF_BUDGET_S="30")
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload",
+                          "kershaw8-n7-jacobi", "--steps", "2", "--warmup", "3"], env=env, capture_output=True,
+                         text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["config"]["iterations"] == c0["iterations"]
+    assert 1 <= line["steps"] <= 2 and line["warmup"] == 0
+    assert line["value"] == pytest.approx(8 ** 3 * 7 ** 3 / (line["ms_per_step"] / 1e3))
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1

@@ -38,6 +38,31 @@ def test_noalloc_matches_allocating_entry_point(product_lib, torch_cuda):
         assert abs(out_na.item() - ref) <= 1e-12 * abs(ref), (call, out_na.item(), ref)
 
 
+def test_noalloc_full_width(product_lib, torch_cuda):
+    """n at the scratch limit (8192 x 8192 entries): every one of the 8192 partial-sum slots is written and the
+    final reduction runs over all of them; one below the limit leaves the last slot partly filled."""
+    torch = torch_cuda
+    L = product_lib
+    vp = ctypes.c_void_p
+    L.nrsg_weighted_inner_prod_f64_noalloc.argtypes = [ctypes.c_longlong, vp, vp, vp, vp, vp]
+    L.nrsg_weighted_inner_prod_f64.argtypes = [ctypes.c_longlong, vp, vp, vp, vp, vp]
+    g = torch.Generator(device="cuda")
+    g.manual_seed(8192)
+    w, a, b = (torch.rand(MAX_N, dtype=torch.float64, device="cuda", generator=g) for _ in range(3))
+    for n in (MAX_N, MAX_N - 1):
+        out_na = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
+        out_ref = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
+        assert L.nrsg_weighted_inner_prod_f64_noalloc(n, w.data_ptr(), a.data_ptr(), b.data_ptr(),
+                                                      out_na.data_ptr(), None) == 0
+        assert L.nrsg_weighted_inner_prod_f64(n, w.data_ptr(), a.data_ptr(), b.data_ptr(), out_ref.data_ptr(),
+                                              None) == 0
+        torch.cuda.synchronize()
+        ref = out_ref.item()
+        assert abs(out_na.item() - ref) <= 1e-12 * abs(ref), (n, out_na.item(), ref)
+    del w, a, b
+    torch.cuda.empty_cache()
+
+
 def test_noalloc_small_and_unweighted(product_lib, torch_cuda):
     torch = torch_cuda
     L = product_lib
