@@ -20,6 +20,8 @@
 
 #include "mg_kernels.hpp"
 
+#include <cuda_fp16.h>
+
 #include <type_traits>
 
 namespace nrsg {
@@ -667,6 +669,267 @@ __global__ void __launch_bounds__(32 * fdm8::EPC, 5)
       ho[q] = w[fdm8_ext(f, pp % 8, pp / 8)];
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Order-7 RAS FDM in FP16 on the tensor cores, per-element max-abs scaling.
+//
+// One warp per element.  The (N+3)^3 = 10^3 extended tile lives in shared
+// memory as FP16 "lines": line L = u + 10 v (the two coordinates other than
+// the one contracted), its 10 entries along the contracted coordinate
+// contiguous, padded to 16 (zeros) and strided by 24 halfs so that the B
+// fragment loads are bank-conflict free.  Each of the six 1-D transforms
+// (S^T along x, y, z, then S along x, y, z) is a 16x16 (padded 10x10)
+// matrix times the 16 x 104 line block: 13 mma.sync.m16n8k16 (FP16 inputs,
+// FP32 accumulation).  The output of a pass, row r (the new coordinate) of
+// line L = u + 10 v, is stored for the next pass at line v + 10 r, entry u:
+// the coordinates rotate (x, y, z) -> (y, z, x) every pass, so that every
+// pass contracts over contiguous entries.  Scaling: the input tile is divided
+// by max |u_ext| of the element, each direction's S by its max |S|, and each
+// pass's FP32 result by its max before it is rounded to FP16 again; the scale
+// factors multiply up in FP32 and are applied to the final FP32 result.  The
+// z-forward pass multiplies by 1/(lx + ly + lz) (0 where <= 1e-5) in FP32.
+// ---------------------------------------------------------------------------
+namespace fdm8h {
+constexpr int LS = 24;        // halfs per line (16 used)
+constexpr int TN = 104 * LS;  // halfs per tile (104 lines: 13 blocks of 8)
+constexpr int EPC = 4;        // elements (warps) per CTA
+} // namespace fdm8h
+
+__device__ __forceinline__ unsigned pack_h2(float lo, float hi)
+{
+  const __half2 h = __floats2half2_rn(lo, hi);
+  return *reinterpret_cast<const unsigned *>(&h);
+}
+
+__device__ __forceinline__ void mma16816(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1)
+{
+  asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+               "{%0,%1,%2,%3};"
+               : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ float warp_max(float v)
+{
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// A fragment of the 16x16 matrix M[o][i] (o, i < 10; zero elsewhere) scaled by inv:
+// forward (S^T) M[o][i] = S(i, o) = Sd[i + 10 o]; backward (S) M[o][i] = S(o, i) = Sd[o + 10 i]
+__device__ __forceinline__ void fdm8h_afrag(const float *Sd, bool fwd, float inv, int g, int t, unsigned (&a)[4])
+{
+  auto m = [&](int o, int i) -> float {
+    if (o >= 10 || i >= 10) return 0.f;
+    return (fwd ? __ldg(Sd + i + 10 * o) : __ldg(Sd + o + 10 * i)) * inv;
+  };
+  a[0] = pack_h2(m(g, 2 * t), m(g, 2 * t + 1));
+  a[1] = pack_h2(m(g + 8, 2 * t), m(g + 8, 2 * t + 1));
+  a[2] = pack_h2(m(g, 2 * t + 8), m(g, 2 * t + 9));
+  a[3] = pack_h2(m(g + 8, 2 * t + 8), m(g + 8, 2 * t + 9));
+}
+
+// fragment element q (0..3) of block nb: row r, line L
+__device__ __forceinline__ void fdm8h_rl(int nb, int q, int g, int t, int &r, int &L)
+{
+  r = g + ((q & 2) ? 8 : 0);
+  L = 8 * nb + 2 * t + (q & 1);
+}
+
+// One pass: D = A x tile_in, block by block (8 lines each); each result is
+// multiplied by f (and, on the z-forward pass, by 1/(lx + ly + lz)) and stored
+// rotated into tout: row r of line L = u + 10 v -> line v + 10 r, entry u.
+template <bool INVL>
+__device__ __forceinline__ void fdm8h_pass(const __half *tin, __half *tout, const unsigned (&a)[4], int g, int t,
+                                           float f, const float *lm)
+{
+  using namespace fdm8h;
+#pragma unroll
+  for (int nb = 0; nb < 13; ++nb) {
+    const __half *line = tin + (8 * nb + g) * LS + 2 * t;
+    const unsigned b0 = *reinterpret_cast<const unsigned *>(line);
+    const unsigned b1 = *reinterpret_cast<const unsigned *>(line + 8);
+    float d[4] = {0.f, 0.f, 0.f, 0.f};
+    mma16816(d, a, b0, b1);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int r, L;
+      fdm8h_rl(nb, q, g, t, r, L);
+      if (r < 10 && L < 100) {
+        const int uu = L % 10, vv = L / 10;
+        float v = d[q] * f;
+        if (INVL) {
+          const float den = (lm[uu] + lm[10 + vv]) + lm[20 + r];
+          v *= den > 1e-5f ? __frcp_rn(den) : 0.f;
+        }
+        tout[(vv + 10 * r) * LS + uu] = __float2half_rn(v);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(32 * fdm8h::EPC)
+    fdm8h_kernel(long long E, const float *__restrict__ u, const int *__restrict__ haloSrc,
+                 const float *__restrict__ Sx, const float *__restrict__ Sy, const float *__restrict__ Sz,
+                 const float *__restrict__ lam, const float *__restrict__ wts, float *__restrict__ Su)
+{
+  using namespace fdm8h;
+  constexpr int NP = 512, NF = 64;
+  __shared__ __align__(16) __half s_t[EPC][2][TN];
+  __shared__ float s_lam[EPC][32];
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const long long e = (long long)blockIdx.x * EPC + wp;
+  if (e >= E) return; // whole warp; warp-level synchronisation only
+  __half *T0 = s_t[wp][0], *T1 = s_t[wp][1];
+  float *lm = s_lam[wp];
+  // global loads first: own nodes, halo indices and values, lambda, S
+  const float4 *ue4 = (const float4 *)(u + e * NP);
+  float4 uv[4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m) uv[m] = __ldg(ue4 + lane + 32 * m);
+  const int *hs = haloSrc + e * 6 * NF;
+  float hv[12];
+#pragma unroll
+  for (int m = 0; m < 12; ++m) {
+    const int src = __ldg(hs + lane + 32 * m);
+    hv[m] = src >= 0 ? __ldg(u + src) : 0.f;
+  }
+  const float lmv = lane < 30 ? __ldg(lam + e * 30 + lane) : 0.f;
+  const float *Sxe = Sx + e * 100, *Sye = Sy + e * 100, *Sze = Sz + e * 100;
+  float smx = 0.f, smy = 0.f, smz = 0.f;
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const int q = lane + 32 * m;
+    if (q < 100) {
+      smx = fmaxf(smx, fabsf(__ldg(Sxe + q)));
+      smy = fmaxf(smy, fabsf(__ldg(Sye + q)));
+      smz = fmaxf(smz, fabsf(__ldg(Sze + q)));
+    }
+  }
+  if (lane < 30) lm[lane] = lmv;
+  // per-element scales: max |u_ext|, max |S_d|, max 1/(lx + ly + lz)
+  float mx = 0.f;
+#pragma unroll
+  for (int m = 0; m < 4; ++m)
+    mx = fmaxf(mx, fmaxf(fmaxf(fabsf(uv[m].x), fabsf(uv[m].y)), fmaxf(fabsf(uv[m].z), fabsf(uv[m].w))));
+#pragma unroll
+  for (int m = 0; m < 12; ++m) mx = fmaxf(mx, fabsf(hv[m]));
+  mx = warp_max(mx);
+  smx = warp_max(smx);
+  smy = warp_max(smy);
+  smz = warp_max(smz);
+  if (!(mx > 0.f)) mx = 1.f;
+  if (!(smx > 0.f)) smx = 1.f;
+  if (!(smy > 0.f)) smy = 1.f;
+  if (!(smz > 0.f)) smz = 1.f;
+  __syncwarp();
+  float ilmax = 0.f;
+  for (int q = lane; q < 1000; q += 32) {
+    const float den = (lm[q % 10] + lm[10 + (q / 10) % 10]) + lm[20 + q / 100];
+    if (den > 1e-5f) ilmax = fmaxf(ilmax, __frcp_rn(den));
+  }
+  ilmax = warp_max(ilmax);
+  if (!(ilmax > 0.f)) ilmax = 1.f;
+  const float inv = 1.f / mx;
+  // zero both tiles (pads and the uncovered edges of the extended cube stay zero)
+  for (int q = lane; q < TN / 2; q += 32) {
+    reinterpret_cast<unsigned *>(T0)[q] = 0u;
+    reinterpret_cast<unsigned *>(T1)[q] = 0u;
+  }
+  __syncwarp();
+  // tile 0: line y + 10 z, entry x (extended coordinates 0..9; own nodes at 1..8)
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const int q = lane + 32 * m;
+    const int i = (4 * q) & 7, j = (q >> 1) & 7, k = q >> 4;
+    __half *dst = T0 + ((j + 1) + 10 * (k + 1)) * LS + (i + 1);
+    dst[0] = __float2half_rn(uv[m].x * inv);
+    dst[1] = __float2half_rn(uv[m].y * inv);
+    dst[2] = __float2half_rn(uv[m].z * inv);
+    dst[3] = __float2half_rn(uv[m].w * inv);
+  }
+#pragma unroll
+  for (int m = 0; m < 12; ++m) {
+    const int q = lane + 32 * m;
+    const int f = q / NF, pp = q % NF, a = pp % 8 + 1, b = pp / 8 + 1;
+    int x, y, z;
+    switch (f) {
+    case 0: x = 0; y = a; z = b; break;
+    case 1: x = 9; y = a; z = b; break;
+    case 2: x = a; y = 0; z = b; break;
+    case 3: x = a; y = 9; z = b; break;
+    case 4: x = a; y = b; z = 0; break;
+    default: x = a; y = b; z = 9; break;
+    }
+    T0[(y + 10 * z) * LS + x] = __float2half_rn(hv[m] * inv);
+  }
+  __syncwarp();
+  // |S/max| <= 1 and |stored input| <= 1, so a pass result is at most 10 in
+  // magnitude: stored passes are multiplied by 1/10 (the z-forward pass by
+  // 1/(10 max invL) and by invL itself); scale collects the true magnitude
+  constexpr float kF = 0.1f;
+  float scale = mx * (smx * smx) * (smy * smy) * (smz * smz) * 1e4f * (10.f * ilmax);
+  unsigned a[4];
+  fdm8h_afrag(Sxe, true, 1.f / smx, g, t, a);
+  fdm8h_pass<false>(T0, T1, a, g, t, kF, lm);
+  __syncwarp();
+  fdm8h_afrag(Sye, true, 1.f / smy, g, t, a);
+  fdm8h_pass<false>(T1, T0, a, g, t, kF, lm);
+  __syncwarp();
+  fdm8h_afrag(Sze, true, 1.f / smz, g, t, a);
+  fdm8h_pass<true>(T0, T1, a, g, t, kF / ilmax, lm);
+  __syncwarp();
+  fdm8h_afrag(Sxe, false, 1.f / smx, g, t, a);
+  fdm8h_pass<false>(T1, T0, a, g, t, kF, lm);
+  __syncwarp();
+  fdm8h_afrag(Sye, false, 1.f / smy, g, t, a);
+  fdm8h_pass<false>(T0, T1, a, g, t, kF, lm);
+  __syncwarp();
+  // final pass (S_z) in FP32: rows r = z'', lines (x'', y''); own nodes at
+  // 1..8, staged in T0 (not read by this pass) for coalesced stores
+  fdm8h_afrag(Sze, false, 1.f / smz, g, t, a);
+  float *stage = reinterpret_cast<float *>(T0);
+#pragma unroll
+  for (int nb = 0; nb < 13; ++nb) {
+    const __half *line = T1 + (8 * nb + g) * LS + 2 * t;
+    const unsigned b0 = *reinterpret_cast<const unsigned *>(line);
+    const unsigned b1 = *reinterpret_cast<const unsigned *>(line + 8);
+    float d[4] = {0.f, 0.f, 0.f, 0.f};
+    mma16816(d, a, b0, b1);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int r, L;
+      fdm8h_rl(nb, q, g, t, r, L);
+      const int x = L % 10, y = L / 10;
+      if (r >= 1 && r <= 8 && L < 100 && x >= 1 && x <= 8 && y >= 1 && y <= 8)
+        stage[(x - 1) + 8 * (y - 1) + 64 * (r - 1)] = d[q] * scale;
+    }
+  }
+  __syncwarp();
+  float *se = Su + e * NP;
+  for (int q = lane; q < NP / 4; q += 32) {
+    float4 v = reinterpret_cast<const float4 *>(stage)[q];
+    const float4 wt = __ldg((const float4 *)(wts + e * NP) + q);
+    v.x *= wt.x;
+    v.y *= wt.y;
+    v.z *= wt.z;
+    v.w *= wt.w;
+    ((float4 *)se)[q] = v;
+  }
+}
+
+bool launch_fdm8h(long long E, const float *u, const int *haloSrc, const float *Sx, const float *Sy, const float *Sz,
+                  const float *lam, const float *wts, float *Su, cudaStream_t s)
+{
+  if (E <= 0) return true;
+  if (!lam) return false;
+  const unsigned grid = (unsigned)((E + fdm8h::EPC - 1) / fdm8h::EPC);
+  fdm8h_kernel<<<grid, 32 * fdm8h::EPC, 0, s>>>(E, u, haloSrc, Sx, Sy, Sz, lam, wts, Su);
+  NRSG_CHECK_LAUNCH();
+  return true;
 }
 
 template <typename T>

@@ -345,13 +345,27 @@ template <typename T> struct MGImpl : public MGState {
     launch_gs_mask<T>(L.gsPlan, Aq, true, s);
   }
 
+  // the fused FDM of one level: FP16 tensor-core transforms (option fdmPrecision = fp16) where they
+  // apply (FP32 multigrid, order 7, RAS), the FP32 kernels otherwise
+  void run_fdm(MGLevelDev<T> &v, const T *u, T *Su)
+  {
+    FieldLevel &L = *v.L;
+    const bool ras = plan.base == 2;
+    if constexpr (std::is_same<T, float>::value) {
+      if (el.opt.fdmFp16 && ras && L.N == 7 &&
+          launch_fdm8h(L.E, u, v.haloSrc.p, v.Sx.p, v.Sy.p, v.Sz.p, v.lam.p, v.wts.p, Su, s))
+        return;
+    }
+    launch_fdm<T>(L.N, L.E, ras, u, v.haloSrc.p, v.Sx.p, v.Sy.p, v.Sz.p, v.invL.p, v.lam.p, v.wts.p, Su, v.haloOut.p,
+                  s);
+  }
+
   // Schwarz: FDM (+ ASM combine) -> gs -> mask; u and Su must not alias
   void schwarz_apply(MGLevelDev<T> &v, const T *u, T *Su)
   {
     FieldLevel &L = *v.L;
     const bool ras = plan.base == 2;
-    launch_fdm<T>(L.N, L.E, ras, u, v.haloSrc.p, v.Sx.p, v.Sy.p, v.Sz.p, v.invL.p, v.lam.p, v.wts.p, Su, v.haloOut.p,
-                  s);
+    run_fdm(v, u, Su);
     if (!ras) launch_asm_combine<T>(L.N, L.E, v.haloPartner.p, v.haloOut.p, v.wts.p, Su, s);
     launch_gs_mask<T>(L.gsPlan, Su, true, s);
   }
@@ -613,9 +627,7 @@ template <typename T> struct MGImpl : public MGState {
   {
     auto &v = lv.at(level);
     if (plan.base == 0 || !v.smoothed) throw Error(NRSG_ERR_INVALID, "level has no Schwarz smoother");
-    const FieldLevel &L = *v.L;
-    launch_fdm<T>(L.N, L.E, plan.base == 2, (const T *)u, v.haloSrc.p, v.Sx.p, v.Sy.p, v.Sz.p, v.invL.p, v.lam.p,
-                  v.wts.p, (T *)Su, v.haloOut.p, s);
+    run_fdm(v, (const T *)u, (T *)Su);
   }
 
   void coarse_launch() override

@@ -15,6 +15,9 @@ void launch_cheby4_update(long long n, T beta, const T *Ad, const T *d, const T 
 template <typename T>
 void launch_fdm(int N, long long E, bool ras, const T *u, const int *haloSrc, const T *Sx, const T *Sy, const T *Sz,
                 const T *invL, const T *lam, const T *wts, T *Su, T *haloOut, cudaStream_t s);
+// order-7 RAS FDM in FP16 on the tensor cores (per-element max-abs scaling); false if not applicable
+bool launch_fdm8h(long long E, const float *u, const int *haloSrc, const float *Sx, const float *Sy, const float *Sz,
+                  const float *lam, const float *wts, float *Su, cudaStream_t s);
 template <typename T>
 void launch_asm_combine(int N, long long E, const int *haloPartner, const T *haloOut, const T *wts, T *Su,
                         cudaStream_t s);

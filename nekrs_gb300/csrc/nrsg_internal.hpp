@@ -114,6 +114,7 @@ struct Options {
   int projVecs = 8;                 // residualProjectionVectors
   int projStart = 5;                // residualProjectionStart
   std::string mgPrecision = "fp64"; // fp64 | fp32 | mixed
+  bool fdmFp16 = false;             // fdmPrecision = fp16: order-7 RAS FDM transforms in FP16 on the tensor cores
   std::string axPrecision = "fp64"; // fine-level operator: fp64 | fp32x2 (FP64-accurate FP32-pair arithmetic)
   bool poisson = true;
   double lambda0 = 1.0, lambda1 = 0.0;

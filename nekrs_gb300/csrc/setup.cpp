@@ -426,6 +426,10 @@ Options parse_options(const char *text)
       } else if (key == "residualprojectionvectors") o.projVecs = std::stoi(v);
       else if (key == "residualprojectionstart") o.projStart = std::stoi(v);
       else if (key == "mgprecision") o.mgPrecision = v;
+      else if (key == "fdmprecision") {
+        if (v != "fp32" && v != "fp16") throw Error(NRSG_ERR_BAD_CONFIG, "fdmPrecision must be fp32 or fp16");
+        o.fdmFp16 = (v == "fp16");
+      }
       else if (key == "axprecision") {
         if (v != "fp64" && v != "fp32x2") throw Error(NRSG_ERR_BAD_CONFIG, "axPrecision must be fp64 or fp32x2");
         o.axPrecision = v;
