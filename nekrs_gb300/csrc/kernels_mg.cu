@@ -738,6 +738,38 @@ __device__ __forceinline__ void fdm8h_rl(int nb, int q, int g, int t, int &r, in
   L = 8 * nb + 2 * t + (q & 1);
 }
 
+// 1/(lx + ly + lz) of mode (u, v, r) of the z-forward pass (0 where the sum is <= 1e-5)
+__device__ __forceinline__ float fdm8h_invl(const float *lm, int uu, int vv, int r)
+{
+  const float den = (lm[uu] + lm[10 + vv]) + lm[20 + r];
+  return den > 1e-5f ? __frcp_rn(den) : 0.f;
+}
+
+// max |(A x tile_in) / (lx + ly + lz)| over the element (the z-forward pass's
+// result, whose modes span many decades: it is scaled by its own maximum)
+__device__ __forceinline__ float fdm8h_invl_max(const __half *tin, const unsigned (&a)[4], int g, int t,
+                                                const float *lm)
+{
+  using namespace fdm8h;
+  float mx = 0.f;
+#pragma unroll
+  for (int nb = 0; nb < 13; ++nb) {
+    const __half *line = tin + (8 * nb + g) * LS + 2 * t;
+    const unsigned b0 = *reinterpret_cast<const unsigned *>(line);
+    const unsigned b1 = *reinterpret_cast<const unsigned *>(line + 8);
+    float d[4] = {0.f, 0.f, 0.f, 0.f};
+    mma16816(d, a, b0, b1);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int r, L;
+      fdm8h_rl(nb, q, g, t, r, L);
+      if (r < 10 && L < 100) mx = fmaxf(mx, fabsf(d[q] * fdm8h_invl(lm, L % 10, L / 10, r)));
+    }
+  }
+  mx = warp_max(mx);
+  return mx > 0.f ? mx : 1.f;
+}
+
 // One pass: D = A x tile_in, block by block (8 lines each); each result is
 // multiplied by f (and, on the z-forward pass, by 1/(lx + ly + lz)) and stored
 // rotated into tout: row r of line L = u + 10 v -> line v + 10 r, entry u.
@@ -760,10 +792,7 @@ __device__ __forceinline__ void fdm8h_pass(const __half *tin, __half *tout, cons
       if (r < 10 && L < 100) {
         const int uu = L % 10, vv = L / 10;
         float v = d[q] * f;
-        if (INVL) {
-          const float den = (lm[uu] + lm[10 + vv]) + lm[20 + r];
-          v *= den > 1e-5f ? __frcp_rn(den) : 0.f;
-        }
+        if (INVL) v *= fdm8h_invl(lm, uu, vv, r);
         tout[(vv + 10 * r) * LS + uu] = __float2half_rn(v);
       }
     }
@@ -825,14 +854,6 @@ __global__ void __launch_bounds__(32 * fdm8h::EPC)
   if (!(smx > 0.f)) smx = 1.f;
   if (!(smy > 0.f)) smy = 1.f;
   if (!(smz > 0.f)) smz = 1.f;
-  __syncwarp();
-  float ilmax = 0.f;
-  for (int q = lane; q < 1000; q += 32) {
-    const float den = (lm[q % 10] + lm[10 + (q / 10) % 10]) + lm[20 + q / 100];
-    if (den > 1e-5f) ilmax = fmaxf(ilmax, __frcp_rn(den));
-  }
-  ilmax = warp_max(ilmax);
-  if (!(ilmax > 0.f)) ilmax = 1.f;
   const float inv = 1.f / mx;
   // zero both tiles (pads and the uncovered edges of the extended cube stay zero)
   for (int q = lane; q < TN / 2; q += 32) {
@@ -868,10 +889,11 @@ __global__ void __launch_bounds__(32 * fdm8h::EPC)
   }
   __syncwarp();
   // |S/max| <= 1 and |stored input| <= 1, so a pass result is at most 10 in
-  // magnitude: stored passes are multiplied by 1/10 (the z-forward pass by
-  // 1/(10 max invL) and by invL itself); scale collects the true magnitude
+  // magnitude: stored passes are multiplied by 1/10, except the z-forward
+  // pass, whose result times 1/(lx + ly + lz) is divided by its own maximum;
+  // scale collects the true magnitude
   constexpr float kF = 0.1f;
-  float scale = mx * (smx * smx) * (smy * smy) * (smz * smz) * 1e4f * (10.f * ilmax);
+  float scale = mx * (smx * smx) * (smy * smy) * (smz * smz) * 1e4f;
   unsigned a[4];
   fdm8h_afrag(Sxe, true, 1.f / smx, g, t, a);
   fdm8h_pass<false>(T0, T1, a, g, t, kF, lm);
@@ -880,7 +902,9 @@ __global__ void __launch_bounds__(32 * fdm8h::EPC)
   fdm8h_pass<false>(T1, T0, a, g, t, kF, lm);
   __syncwarp();
   fdm8h_afrag(Sze, true, 1.f / smz, g, t, a);
-  fdm8h_pass<true>(T0, T1, a, g, t, kF / ilmax, lm);
+  const float m2 = fdm8h_invl_max(T0, a, g, t, lm);
+  scale *= m2;
+  fdm8h_pass<true>(T0, T1, a, g, t, 1.f / m2, lm);
   __syncwarp();
   fdm8h_afrag(Sxe, false, 1.f / smx, g, t, a);
   fdm8h_pass<false>(T1, T0, a, g, t, kF, lm);
