@@ -785,21 +785,28 @@ __device__ __forceinline__ void fdm8h_pass(const __half *tin, __half *tout, cons
     const unsigned b1 = *reinterpret_cast<const unsigned *>(line + 8);
     float d[4] = {0.f, 0.f, 0.f, 0.f};
     mma16816(d, a, b0, b1);
+    // d0, d1: row g, lines L and L + 1 (L even, so entries u and u + 1 of one
+    // line of the next tile); d2, d3: row g + 8
+    const int L = 8 * nb + 2 * t;
+    if (L < 100) {
+      const int uu = L % 10, vv = L / 10;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      int r, L;
-      fdm8h_rl(nb, q, g, t, r, L);
-      if (r < 10 && L < 100) {
-        const int uu = L % 10, vv = L / 10;
-        float v = d[q] * f;
-        if (INVL) v *= fdm8h_invl(lm, uu, vv, r);
-        tout[(vv + 10 * r) * LS + uu] = __float2half_rn(v);
+      for (int h = 0; h < 2; ++h) {
+        const int r = g + 8 * h;
+        if (r < 10) {
+          float v0 = d[2 * h] * f, v1 = d[2 * h + 1] * f;
+          if (INVL) {
+            v0 *= fdm8h_invl(lm, uu, vv, r);
+            v1 *= fdm8h_invl(lm, uu + 1, vv, r);
+          }
+          *reinterpret_cast<__half2 *>(tout + (vv + 10 * r) * LS + uu) = __floats2half2_rn(v0, v1);
+        }
       }
     }
   }
 }
 
-__global__ void __launch_bounds__(32 * fdm8h::EPC)
+__global__ void __launch_bounds__(32 * fdm8h::EPC, 4)
     fdm8h_kernel(long long E, const float *__restrict__ u, const int *__restrict__ haloSrc,
                  const float *__restrict__ Sx, const float *__restrict__ Sy, const float *__restrict__ Sz,
                  const float *__restrict__ lam, const float *__restrict__ wts, float *__restrict__ Su)
@@ -810,10 +817,17 @@ __global__ void __launch_bounds__(32 * fdm8h::EPC)
   __shared__ float s_lam[EPC][32];
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   const int g = lane >> 2, t = lane & 3;
-  const long long e = (long long)blockIdx.x * EPC + wp;
-  if (e >= E) return; // whole warp; warp-level synchronisation only
   __half *T0 = s_t[wp][0], *T1 = s_t[wp][1];
   float *lm = s_lam[wp];
+  // both tiles zeroed once: the K pads (entries 10..15) and lines 100..103
+  // are never written afterwards
+  for (int q = lane; q < TN / 2; q += 32) {
+    reinterpret_cast<unsigned *>(T0)[q] = 0u;
+    reinterpret_cast<unsigned *>(T1)[q] = 0u;
+  }
+  __syncwarp();
+  // persistent warps: element after element (warp-uniform loop, warp-level synchronisation only)
+  for (long long e = (long long)blockIdx.x * EPC + wp; e < E; e += (long long)gridDim.x * EPC) {
   // global loads first: own nodes, halo indices and values, lambda, S
   const float4 *ue4 = (const float4 *)(u + e * NP);
   float4 uv[4];
@@ -855,10 +869,12 @@ __global__ void __launch_bounds__(32 * fdm8h::EPC)
   if (!(smy > 0.f)) smy = 1.f;
   if (!(smz > 0.f)) smz = 1.f;
   const float inv = 1.f / mx;
-  // zero both tiles (pads and the uncovered edges of the extended cube stay zero)
-  for (int q = lane; q < TN / 2; q += 32) {
-    reinterpret_cast<unsigned *>(T0)[q] = 0u;
-    reinterpret_cast<unsigned *>(T1)[q] = 0u;
+  // the 104 points of the extended cube that neither own nodes nor the halo
+  // cover (two or three coordinates in {0, 9}) are zero: earlier passes of the
+  // previous element wrote them
+  for (int q = lane; q < 1000; q += 32) {
+    const int x = q % 10, y = (q / 10) % 10, z = q / 100;
+    if ((x == 0 || x == 9) + (y == 0 || y == 9) + (z == 0 || z == 9) >= 2) T0[(y + 10 * z) * LS + x] = __float2half_rn(0.f);
   }
   __syncwarp();
   // tile 0: line y + 10 z, entry x (extended coordinates 0..9; own nodes at 1..8)
@@ -943,6 +959,13 @@ __global__ void __launch_bounds__(32 * fdm8h::EPC)
     v.w *= wt.w;
     ((float4 *)se)[q] = v;
   }
+  __syncwarp();
+  // the FP32 stage covered the first 2048 bytes of T0 (lines 0..42): their K
+  // pads are zeroed again; every entry 0..9 is rewritten by the next element
+  for (int q = lane; q < 43 * 3; q += 32)
+    reinterpret_cast<unsigned *>(T0)[(q / 3) * (LS / 2) + 5 + q % 3] = 0u;
+  __syncwarp();
+  }
 }
 
 bool launch_fdm8h(long long E, const float *u, const int *haloSrc, const float *Sx, const float *Sy, const float *Sz,
@@ -950,7 +973,17 @@ bool launch_fdm8h(long long E, const float *u, const int *haloSrc, const float *
 {
   if (E <= 0) return true;
   if (!lam) return false;
-  const unsigned grid = (unsigned)((E + fdm8h::EPC - 1) / fdm8h::EPC);
+  // persistent CTAs: as many as are resident at once (occupancy of this kernel, all SMs)
+  static int perSM = 0, sms = 0;
+  if (perSM == 0) {
+    int dev = 0;
+    NRSG_CUDA(cudaGetDevice(&dev));
+    NRSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    NRSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fdm8h_kernel, 32 * fdm8h::EPC, 0));
+    if (perSM < 1) perSM = 1;
+  }
+  const long long need = (E + fdm8h::EPC - 1) / fdm8h::EPC;
+  const unsigned grid = (unsigned)(need < (long long)sms * perSM ? need : (long long)sms * perSM);
   fdm8h_kernel<<<grid, 32 * fdm8h::EPC, 0, s>>>(E, u, haloSrc, Sx, Sy, Sz, lam, wts, Su);
   NRSG_CHECK_LAUNCH();
   return true;
