@@ -806,7 +806,7 @@ __device__ __forceinline__ void fdm8h_pass(const __half *tin, __half *tout, cons
   }
 }
 
-__global__ void __launch_bounds__(32 * fdm8h::EPC, 4)
+__global__ void __launch_bounds__(32 * fdm8h::EPC)
     fdm8h_kernel(long long E, const float *__restrict__ u, const int *__restrict__ haloSrc,
                  const float *__restrict__ Sx, const float *__restrict__ Sy, const float *__restrict__ Sz,
                  const float *__restrict__ lam, const float *__restrict__ wts, float *__restrict__ Su)
@@ -819,15 +819,19 @@ __global__ void __launch_bounds__(32 * fdm8h::EPC, 4)
   const int g = lane >> 2, t = lane & 3;
   __half *T0 = s_t[wp][0], *T1 = s_t[wp][1];
   float *lm = s_lam[wp];
-  // both tiles zeroed once: the K pads (entries 10..15) and lines 100..103
-  // are never written afterwards
-  for (int q = lane; q < TN / 2; q += 32) {
-    reinterpret_cast<unsigned *>(T0)[q] = 0u;
-    reinterpret_cast<unsigned *>(T1)[q] = 0u;
+  const long long e = (long long)blockIdx.x * EPC + wp;
+  if (e >= E) return; // whole warp; warp-level synchronisation only
+  // the K pads (entries 10..15, words 5..7 of a line) and lines 100..103 of
+  // both tiles are zero; no pass writes them
+  for (int q = lane; q < 104 * 3; q += 32) {
+    const int w = (q / 3) * (LS / 2) + 5 + q % 3;
+    reinterpret_cast<unsigned *>(T0)[w] = 0u;
+    reinterpret_cast<unsigned *>(T1)[w] = 0u;
   }
-  __syncwarp();
-  // persistent warps: element after element (warp-uniform loop, warp-level synchronisation only)
-  for (long long e = (long long)blockIdx.x * EPC + wp; e < E; e += (long long)gridDim.x * EPC) {
+  for (int q = lane; q < 4 * (LS / 2); q += 32) {
+    reinterpret_cast<unsigned *>(T0)[100 * (LS / 2) + q] = 0u;
+    reinterpret_cast<unsigned *>(T1)[100 * (LS / 2) + q] = 0u;
+  }
   // global loads first: own nodes, halo indices and values, lambda, S
   const float4 *ue4 = (const float4 *)(u + e * NP);
   float4 uv[4];
@@ -870,8 +874,7 @@ __global__ void __launch_bounds__(32 * fdm8h::EPC, 4)
   if (!(smz > 0.f)) smz = 1.f;
   const float inv = 1.f / mx;
   // the 104 points of the extended cube that neither own nodes nor the halo
-  // cover (two or three coordinates in {0, 9}) are zero: earlier passes of the
-  // previous element wrote them
+  // cover (two or three coordinates in {0, 9}) are zero
   for (int q = lane; q < 1000; q += 32) {
     const int x = q % 10, y = (q / 10) % 10, z = q / 100;
     if ((x == 0 || x == 9) + (y == 0 || y == 9) + (z == 0 || z == 9) >= 2) T0[(y + 10 * z) * LS + x] = __float2half_rn(0.f);
@@ -959,13 +962,6 @@ __global__ void __launch_bounds__(32 * fdm8h::EPC, 4)
     v.w *= wt.w;
     ((float4 *)se)[q] = v;
   }
-  __syncwarp();
-  // the FP32 stage covered the first 2048 bytes of T0 (lines 0..42): their K
-  // pads are zeroed again; every entry 0..9 is rewritten by the next element
-  for (int q = lane; q < 43 * 3; q += 32)
-    reinterpret_cast<unsigned *>(T0)[(q / 3) * (LS / 2) + 5 + q % 3] = 0u;
-  __syncwarp();
-  }
 }
 
 bool launch_fdm8h(long long E, const float *u, const int *haloSrc, const float *Sx, const float *Sy, const float *Sz,
@@ -973,17 +969,7 @@ bool launch_fdm8h(long long E, const float *u, const int *haloSrc, const float *
 {
   if (E <= 0) return true;
   if (!lam) return false;
-  // persistent CTAs: as many as are resident at once (occupancy of this kernel, all SMs)
-  static int perSM = 0, sms = 0;
-  if (perSM == 0) {
-    int dev = 0;
-    NRSG_CUDA(cudaGetDevice(&dev));
-    NRSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    NRSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fdm8h_kernel, 32 * fdm8h::EPC, 0));
-    if (perSM < 1) perSM = 1;
-  }
-  const long long need = (E + fdm8h::EPC - 1) / fdm8h::EPC;
-  const unsigned grid = (unsigned)(need < (long long)sms * perSM ? need : (long long)sms * perSM);
+  const unsigned grid = (unsigned)((E + fdm8h::EPC - 1) / fdm8h::EPC);
   fdm8h_kernel<<<grid, 32 * fdm8h::EPC, 0, s>>>(E, u, haloSrc, Sx, Sy, Sz, lam, wts, Su);
   NRSG_CHECK_LAUNCH();
   return true;
