@@ -742,7 +742,7 @@ __device__ __forceinline__ void fdm8h_rl(int nb, int q, int g, int t, int &r, in
 __device__ __forceinline__ float fdm8h_invl(const float *lm, int uu, int vv, int r)
 {
   const float den = (lm[uu] + lm[10 + vv]) + lm[20 + r];
-  return den > 1e-5f ? __frcp_rn(den) : 0.f;
+  return den > 1e-5f ? __fdividef(1.f, den) : 0.f; // approximate: the value is rounded to FP16 next
 }
 
 // max |(A x tile_in) / (lx + ly + lz)| over the element (the z-forward pass's
@@ -775,9 +775,10 @@ __device__ __forceinline__ float fdm8h_invl_max(const __half *tin, const unsigne
 // rotated into tout: row r of line L = u + 10 v -> line v + 10 r, entry u.
 template <bool INVL>
 __device__ __forceinline__ void fdm8h_pass(const __half *tin, __half *tout, const unsigned (&a)[4], int g, int t,
-                                           float f, const float *lm)
+                                           float f, const float *lm, const short *offs)
 {
   using namespace fdm8h;
+  const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int nb = 0; nb < 13; ++nb) {
     const __half *line = tin + (8 * nb + g) * LS + 2 * t;
@@ -786,20 +787,19 @@ __device__ __forceinline__ void fdm8h_pass(const __half *tin, __half *tout, cons
     float d[4] = {0.f, 0.f, 0.f, 0.f};
     mma16816(d, a, b0, b1);
     // d0, d1: row g, lines L and L + 1 (L even, so entries u and u + 1 of one
-    // line of the next tile); d2, d3: row g + 8
-    const int L = 8 * nb + 2 * t;
-    if (L < 100) {
-      const int uu = L % 10, vv = L / 10;
+    // line of the next tile); d2, d3: row g + 8 (offset + 80 lines)
+    const int off = offs[nb * 32 + lane];
+    if (off >= 0) {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        const int r = g + 8 * h;
-        if (r < 10) {
+        if (h == 0 || g < 2) {
           float v0 = d[2 * h] * f, v1 = d[2 * h + 1] * f;
           if (INVL) {
+            const int L = 8 * nb + 2 * t, uu = L % 10, vv = L / 10, r = g + 8 * h;
             v0 *= fdm8h_invl(lm, uu, vv, r);
             v1 *= fdm8h_invl(lm, uu + 1, vv, r);
           }
-          *reinterpret_cast<__half2 *>(tout + (vv + 10 * r) * LS + uu) = __floats2half2_rn(v0, v1);
+          *reinterpret_cast<__half2 *>(tout + off + h * 80 * LS) = __floats2half2_rn(v0, v1);
         }
       }
     }
@@ -815,22 +815,24 @@ __global__ void __launch_bounds__(32 * fdm8h::EPC)
   constexpr int NP = 512, NF = 64;
   __shared__ __align__(16) __half s_t[EPC][2][TN];
   __shared__ float s_lam[EPC][32];
+  __shared__ short s_off[13 * 32]; // store offset of lane's row-g results of block nb, -1 past line 99
+  for (int q = threadIdx.x; q < 13 * 32; q += blockDim.x) {
+    const int nb = q / 32, ln = q % 32, L = 8 * nb + 2 * (ln & 3);
+    s_off[q] = L < 100 ? (short)(((L / 10) + 10 * (ln >> 2)) * fdm8h::LS + L % 10) : (short)-1;
+  }
+  __syncthreads();
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   const int g = lane >> 2, t = lane & 3;
   __half *T0 = s_t[wp][0], *T1 = s_t[wp][1];
   float *lm = s_lam[wp];
   const long long e = (long long)blockIdx.x * EPC + wp;
   if (e >= E) return; // whole warp; warp-level synchronisation only
-  // the K pads (entries 10..15, words 5..7 of a line) and lines 100..103 of
-  // both tiles are zero; no pass writes them
-  for (int q = lane; q < 104 * 3; q += 32) {
-    const int w = (q / 3) * (LS / 2) + 5 + q % 3;
-    reinterpret_cast<unsigned *>(T0)[w] = 0u;
-    reinterpret_cast<unsigned *>(T1)[w] = 0u;
-  }
-  for (int q = lane; q < 4 * (LS / 2); q += 32) {
-    reinterpret_cast<unsigned *>(T0)[100 * (LS / 2) + q] = 0u;
-    reinterpret_cast<unsigned *>(T1)[100 * (LS / 2) + q] = 0u;
+  // both tiles zero (16-byte stores): the K pads (entries 10..15), lines
+  // 100..103 and the 104 points of the extended cube that neither own nodes
+  // nor the halo cover stay zero; no pass writes the pads
+  for (int q = lane; q < TN / 8; q += 32) {
+    reinterpret_cast<uint4 *>(T0)[q] = make_uint4(0u, 0u, 0u, 0u);
+    reinterpret_cast<uint4 *>(T1)[q] = make_uint4(0u, 0u, 0u, 0u);
   }
   // global loads first: own nodes, halo indices and values, lambda, S
   const float4 *ue4 = (const float4 *)(u + e * NP);
@@ -873,12 +875,6 @@ __global__ void __launch_bounds__(32 * fdm8h::EPC)
   if (!(smy > 0.f)) smy = 1.f;
   if (!(smz > 0.f)) smz = 1.f;
   const float inv = 1.f / mx;
-  // the 104 points of the extended cube that neither own nodes nor the halo
-  // cover (two or three coordinates in {0, 9}) are zero
-  for (int q = lane; q < 1000; q += 32) {
-    const int x = q % 10, y = (q / 10) % 10, z = q / 100;
-    if ((x == 0 || x == 9) + (y == 0 || y == 9) + (z == 0 || z == 9) >= 2) T0[(y + 10 * z) * LS + x] = __float2half_rn(0.f);
-  }
   __syncwarp();
   // tile 0: line y + 10 z, entry x (extended coordinates 0..9; own nodes at 1..8)
 #pragma unroll
@@ -915,21 +911,21 @@ __global__ void __launch_bounds__(32 * fdm8h::EPC)
   float scale = mx * (smx * smx) * (smy * smy) * (smz * smz) * 1e4f;
   unsigned a[4];
   fdm8h_afrag(Sxe, true, 1.f / smx, g, t, a);
-  fdm8h_pass<false>(T0, T1, a, g, t, kF, lm);
+  fdm8h_pass<false>(T0, T1, a, g, t, kF, lm, s_off);
   __syncwarp();
   fdm8h_afrag(Sye, true, 1.f / smy, g, t, a);
-  fdm8h_pass<false>(T1, T0, a, g, t, kF, lm);
+  fdm8h_pass<false>(T1, T0, a, g, t, kF, lm, s_off);
   __syncwarp();
   fdm8h_afrag(Sze, true, 1.f / smz, g, t, a);
   const float m2 = fdm8h_invl_max(T0, a, g, t, lm);
   scale *= m2;
-  fdm8h_pass<true>(T0, T1, a, g, t, 1.f / m2, lm);
+  fdm8h_pass<true>(T0, T1, a, g, t, 1.f / m2, lm, s_off);
   __syncwarp();
   fdm8h_afrag(Sxe, false, 1.f / smx, g, t, a);
-  fdm8h_pass<false>(T1, T0, a, g, t, kF, lm);
+  fdm8h_pass<false>(T1, T0, a, g, t, kF, lm, s_off);
   __syncwarp();
   fdm8h_afrag(Sye, false, 1.f / smy, g, t, a);
-  fdm8h_pass<false>(T0, T1, a, g, t, kF, lm);
+  fdm8h_pass<false>(T0, T1, a, g, t, kF, lm, s_off);
   __syncwarp();
   // final pass (S_z) in FP32: rows r = z'', lines (x'', y''); own nodes at
   // 1..8, staged in T0 (not read by this pass) for coalesced stores
