@@ -44,6 +44,10 @@ WORKLOADS = {
                            "Kershaw box E=48^3 N=7 eps=0.3: FP64 flexible PCG, FP32 pMG 7/3/1 (optimal 4th-kind "
                            "Chebyshev(5)+RAS FDM, coarse Jacobi-PCG 1e-4 on the assembled order-1 operator), "
                            "FP64-accurate FP32-pair fine operator, to 1e-8 relative"),
+    "kershaw48-n7-mixed-fp16": (48, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
+                                ";mgPrecision=mixed;fdmPrecision=fp16",
+                                "the kershaw48-n7-mixed solve with the fine-level FDM transforms in FP16 on the tensor "
+                                "cores (mma.sync m16n8k16, FP32 accumulation, per-element max-abs scaling)"),
     "kershaw32-n7-mixed": (32, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
                            ";mgPrecision=mixed", "the kershaw48-n7-mixed solve on E=32^3 (profiling size)"),
     "kershaw16-n7-mixed": (16, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
@@ -794,10 +798,11 @@ def main():
     if el is None:
         el = G.Elliptic(N, VX, EToV, EToB, "preconditioner=jacobi")
     kr, peak, psrc = kernel_rooflines(G, el, N, E)
+    fdm_name = "fdm_f16" if "fdmPrecision=fp16" in opts else "fdm_f32"
     if fdm is not None:
-        kr["fdm_f32"] = fdm
+        kr[fdm_name] = fdm
     # the dominant kernel of the solve by share of device time (ncu launch list of this workload)
-    dominant = "fdm_f32" if fdm is not None else ("ax_fp32x2" if "mixed" in opts else "ax_stored_f64")
+    dominant = fdm_name if fdm is not None else ("ax_fp32x2" if "mixed" in opts else "ax_stored_f64")
     d = kr[dominant]
     roof = {"bound": "hbm", "kernel": dominant, "achieved": d["achieved"], "peak": peak, "unit": "GB/s",
             "frac": d["achieved"] / peak, "traffic": TRAFFIC.get((args.workload, dominant)),
