@@ -49,6 +49,7 @@ namespace {
 constexpr int kCT = 1024;              // most threads per CTA (one CTA per SM; a row block of fewer rows uses fewer)
 constexpr int kMinRowsPerCta = 128;
 constexpr long long kOneCtaRows = 4096; // 10 FP32 row vectors = 160 KB of shared memory
+constexpr int kMaxCluster = 8;          // portable thread-block cluster size
 
 struct CoarseState {
   unsigned arrive;
@@ -182,8 +183,16 @@ template <typename T> __device__ __forceinline__ void grid_sum3(const T *part, T
 // reported an error.  `extra` arrivals are added to the target: 0 in
 // ordinary use; a nonzero value makes the target unreachable, which is how
 // the test of the bounded wait makes every wait run out.
-__device__ __forceinline__ bool grid_barrier(CoarseState *st, unsigned nb, long long spinLimit, unsigned extra)
+__device__ __forceinline__ bool grid_barrier(CoarseState *st, unsigned nb, long long spinLimit, unsigned extra,
+                                             int cluster)
 {
+  if (cluster) {
+    // the grid is one thread-block cluster, co-scheduled by the hardware: its
+    // barrier (release / acquire at cluster scope, global memory included)
+    // never spins and cannot be left waiting
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+    return true;
+  }
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -251,6 +260,7 @@ template <typename T> struct CoarseArgs {
   double tol;                 // relative
   int maxit;
   unsigned barrierExtra;      // added to every grid barrier's target (0; nonzero only to test the bounded wait)
+  int cluster;                // the grid is one cluster: hardware cluster barrier in place of the counter
   long long spinLimit;        // polls before a grid barrier wait gives up
 };
 
@@ -303,7 +313,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_pcg_kerne
     rz = fma_t<T>(ru, zu, rz);
   }
   cta_partial2<T>(rr, rz, sh, a.partials + blockIdx.x, a.partials + gridDim.x + blockIdx.x);
-  if (!grid_barrier(a.st, 1, a.spinLimit, a.barrierExtra)) return;
+  if (!grid_barrier(a.st, 1, a.spinLimit, a.barrierExtra, a.cluster)) return;
   unsigned nb = 1;
   // scalars, kept by thread 0 of each CTA (identical in every CTA)
   double r0 = 0, rn = 0, tol = 0, rdotz = 0;
@@ -338,7 +348,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_pcg_kerne
       pap = fma_t<T>(pu, apu, pap);
     }
     cta_partial<T>(pap, sh, a.partials + 2 * gridDim.x + blockIdx.x);
-    if (!grid_barrier(a.st, ++nb, a.spinLimit, a.barrierExtra)) return;
+    if (!grid_barrier(a.st, ++nb, a.spinLimit, a.barrierExtra, a.cluster)) return;
     if (threadIdx.x < 32) {
       const double spap = grid_sum(a.partials + 2 * gridDim.x);
       if (threadIdx.x == 0) s_alpha = (T)(rdotz / (spap + 1e-300));
@@ -359,7 +369,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_pcg_kerne
       rz = fma_t<T>(ru, zu, rz);
     }
     cta_partial2<T>(rr, rz, sh, a.partials + blockIdx.x, a.partials + gridDim.x + blockIdx.x);
-    if (!grid_barrier(a.st, ++nb, a.spinLimit, a.barrierExtra)) return;
+    if (!grid_barrier(a.st, ++nb, a.spinLimit, a.barrierExtra, a.cluster)) return;
     if (threadIdx.x < 32) {
       const double srr = grid_sum(a.partials);
       const double srz = grid_sum(a.partials + gridDim.x);
@@ -376,7 +386,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_pcg_kerne
   }
   // E-vector solution: every copy of a row takes its value, masked nodes 0
   for (int t = threadIdx.x; t < cnt; t += blockDim.x) a.x[start + t] = xs[t];
-  if (!grid_barrier(a.st, ++nb, a.spinLimit, a.barrierExtra)) return;
+  if (!grid_barrier(a.st, ++nb, a.spinLimit, a.barrierExtra, a.cluster)) return;
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x, nth = (long long)gridDim.x * blockDim.x;
   for (long long i = tid; i < a.nE; i += nth) {
     const int u = __ldg(a.rowOf + i);
@@ -450,7 +460,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_ppcg_kern
     ms[t] = uu;
     a.z[start + t] = uu;
   }
-  if (!grid_barrier(a.st, 1, a.spinLimit, a.barrierExtra)) return;
+  if (!grid_barrier(a.st, 1, a.spinLimit, a.barrierExtra, a.cluster)) return;
   unsigned nb = 1;
   // w0 = A u0
 #pragma unroll 4
@@ -481,7 +491,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_ppcg_kern
       mg[start + t] = mm;
     }
     cta_partial3<T>(g, d, rr, sh, part + blockIdx.x, part + gridDim.x + blockIdx.x, part + 2 * gridDim.x + blockIdx.x);
-    if (!grid_barrier(a.st, ++nb, a.spinLimit, a.barrierExtra)) return;
+    if (!grid_barrier(a.st, ++nb, a.spinLimit, a.barrierExtra, a.cluster)) return;
     if (threadIdx.x < 32) {
       T sgT, sdT, srrT;
       grid_sum3<T>(part, sgT, sdT, srrT);
@@ -534,7 +544,7 @@ template <typename T> __global__ void __launch_bounds__(kCT, 1) coarse_ppcg_kern
   }
   // E-vector solution: every copy of a row takes its value, masked nodes 0
   for (int t = threadIdx.x; t < cnt; t += blockDim.x) a.x[start + t] = xs[t];
-  if (!grid_barrier(a.st, ++nb, a.spinLimit, a.barrierExtra)) return;
+  if (!grid_barrier(a.st, ++nb, a.spinLimit, a.barrierExtra, a.cluster)) return;
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x, nth = (long long)gridDim.x * blockDim.x;
   for (long long i = tid; i < a.nE; i += nth) {
     const int u = __ldg(a.rowOf + i);
@@ -574,7 +584,7 @@ void raise_dynamic_smem(const void *kfn, size_t bytes)
 // the shared-memory plan.
 template <typename T>
 void coarse_matrix_setup(long long n, const long long *rowPtr, const long long *col, const double *val, long long nE,
-                         const long long *rowOfNode, const int *rep, CoarseMatrix<T> &M)
+                         const long long *rowOfNode, const int *rep, CoarseMatrix<T> &M, bool noCluster)
 {
   int dev = 0, sms = 0, optin = 0;
   NRSG_CUDA(cudaGetDevice(&dev));
@@ -585,10 +595,19 @@ void coarse_matrix_setup(long long n, const long long *rowPtr, const long long *
   for (long long r = 0; r < n; ++r) width = std::max(width, (int)(rowPtr[r + 1] - rowPtr[r]));
   long long grid = std::min<long long>(sms, std::max<long long>(1, (n + kMinRowsPerCta - 1) / kMinRowsPerCta));
   // a level whose row vectors fit one CTA's shared memory is solved by one CTA: no grid barrier ever
-  // waits, so it is an ordinary launch (no cooperative launch, no ordering against other solvers)
-  if (n <= kOneCtaRows) grid = 1;
+  // waits, so it is an ordinary launch (no cooperative launch, no ordering against other solvers);
+  // one that fits kMaxCluster such CTAs runs as one thread-block cluster (hardware barrier, co-scheduled,
+  // again an ordinary launch), when the device can hold such a cluster
+  M.cluster = 0;
+  if (n <= kOneCtaRows) {
+    grid = 1;
+  } else if (!noCluster && n <= kMaxCluster * kOneCtaRows) {
+    grid = (n + kOneCtaRows - 1) / kOneCtaRows;
+    M.cluster = 1;
+  }
   const long long chunk = std::max<long long>(1, (n + grid - 1) / grid);
   grid = std::max<long long>(1, (n + chunk - 1) / chunk);
+  if (M.cluster) M.cluster = (int)grid;
   std::vector<int> haloOff(grid + 1, 0), haloIds;
   std::vector<unsigned short> lcol((size_t)grid * width * chunk, 0);
   std::vector<T> v((size_t)grid * width * chunk, T(0));
@@ -637,6 +656,8 @@ void coarse_matrix_setup(long long n, const long long *rowPtr, const long long *
   const size_t vBytes = M.pipelined ? vec_bytes_pipe<T>((int)chunk, maxHalo) : vec_bytes<T>((int)chunk, maxHalo);
   const size_t mBytes = mat_bytes<T>((int)chunk, width);
   const size_t limit = (size_t)optin > 2048 ? (size_t)optin - 2048 : 0; // static shared memory of the kernel
+  if (vBytes > limit && M.cluster) // the cluster's row blocks and halos do not fit: many smaller blocks instead
+    return coarse_matrix_setup<T>(n, rowPtr, col, val, nE, rowOfNode, rep, M, true);
   if (vBytes > limit) throw Error(NRSG_ERR_BAD_CONFIG, "coarse level: row block too large for shared memory");
   M.matInSmem = vBytes + mBytes <= limit;
   M.smem = vBytes + (M.matInSmem ? mBytes : 0);
@@ -644,6 +665,24 @@ void coarse_matrix_setup(long long n, const long long *rowPtr, const long long *
   int perSM = 0;
   NRSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kfn, std::min<long long>(kCT, std::max<long long>(32, (chunk + 31) / 32 * 32)), M.smem));
   if (perSM < 1) throw Error(NRSG_ERR_CUDA, "coarse solver: kernel cannot be resident");
+  if (M.cluster) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = (unsigned)grid;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)std::min<long long>(kCT, std::max<long long>(32, (chunk + 31) / 32 * 32)));
+    cfg.dynamicSmemBytes = M.smem;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, kfn, &cfg) != cudaSuccess || clusters < 1) {
+      (void)cudaGetLastError();
+      M.cluster = 0; // not schedulable as one cluster: the cooperative launch of the same row blocks
+    }
+  }
   M.threads = (int)std::min<long long>(kCT, std::max<long long>(32, (chunk + 31) / 32 * 32));
   M.nrow = n;
   M.nE = nE;
@@ -689,7 +728,10 @@ int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *
   int dev = 0;
   NRSG_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) throw Error(NRSG_ERR_CUDA, "coarse solver: device index out of range");
-  const bool cooperative = A.grid > 1;
+  // a cluster-sized level runs as one cluster (no cross-solver ordering); the test knob barrierExtra
+  // needs the counting barrier, so it takes the cooperative launch
+  const bool useCluster = A.cluster > 0 && barrierExtra == 0;
+  const bool cooperative = A.grid > 1 && !useCluster;
   CoarseGate &gate = coarse_gate();
   std::unique_lock<std::mutex> lock(gate.m, std::defer_lock);
   if (cooperative) {
@@ -725,9 +767,26 @@ int coarse_pcg_persistent(const CoarseMatrix<T> &A, const T *b, T *xE, T *x, T *
   a.maxit = maxit;
   a.barrierExtra = barrierExtra;
   a.spinLimit = spinLimit;
+  a.cluster = 0;
   void *args[] = {&a};
   const void *kfn = A.pipelined ? (const void *)coarse_ppcg_kernel<T> : (const void *)coarse_pcg_kernel<T>;
-  if (cooperative) {
+  if (useCluster) {
+    a.cluster = 1;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = (unsigned)A.grid;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.gridDim = dim3(A.grid);
+    cfg.blockDim = dim3(A.threads);
+    cfg.dynamicSmemBytes = A.smem;
+    cfg.stream = s;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    NRSG_CUDA(cudaLaunchKernelExC(&cfg, kfn, args));
+    count_launch();
+  } else if (cooperative) {
     NRSG_CUDA(cudaLaunchCooperativeKernel(kfn, dim3(A.grid), dim3(A.threads), args, A.smem, s));
     count_launch();
     NRSG_CUDA(cudaEventRecord(gate.ev[dev], s));
@@ -750,9 +809,9 @@ int coarse_state_read(const void *state_host, int *iters, double *res0, double *
 }
 
 template void coarse_matrix_setup<double>(long long, const long long *, const long long *, const double *, long long,
-                                          const long long *, const int *, CoarseMatrix<double> &);
+                                          const long long *, const int *, CoarseMatrix<double> &, bool);
 template void coarse_matrix_setup<float>(long long, const long long *, const long long *, const double *, long long,
-                                         const long long *, const int *, CoarseMatrix<float> &);
+                                         const long long *, const int *, CoarseMatrix<float> &, bool);
 template int coarse_pcg_persistent<double>(const CoarseMatrix<double> &, const double *, double *, double *, double *,
                                            double *, double *, void *, int, double, int, cudaStream_t, long long,
                                            unsigned);

@@ -596,10 +596,11 @@ template <typename T> struct MGImpl : public MGState {
     else if (what == "mg.bytes")
       out.push_back((double)sizeof(T)); // multigrid precision
     else if (what == "mg.coarseMatrix") {
-      // rows, ELL width, stored nonzeros, row blocks (CTAs), rows per block, matrix in shared memory
+      // rows, ELL width, stored nonzeros, row blocks (CTAs), rows per block, matrix in shared memory,
+      // thread-block cluster size (0: one CTA or a cooperative launch)
       if (persistentCoarse)
         out = {(double)cA.nrow, (double)cA.width, (double)cA.nnz, (double)cA.grid, (double)cA.chunk,
-               cA.matInSmem ? 1.0 : 0.0};
+               cA.matInSmem ? 1.0 : 0.0, (double)cA.cluster};
     } else
       throw Error(NRSG_ERR_INVALID, "unknown array '" + what + "'");
     return out;

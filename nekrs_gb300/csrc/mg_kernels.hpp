@@ -40,6 +40,7 @@ template <typename T> struct CoarseMatrix {
   int threads = 1024;            // threads per CTA: the row block rounded up to a warp, at most 1024
   bool matInSmem = false;
   bool pipelined = false;        // one-barrier pipelined PCG (FP32)
+  int cluster = 0;               // > 0: the grid is one thread-block cluster of this many CTAs (hardware barrier)
   size_t smem = 0;               // dynamic shared memory per CTA
   DevBuf<unsigned short> lcol;   // [grid][width][chunk] local column: own row, or chunk + halo slot
   DevBuf<T> val;                 // [grid][width][chunk], padding 0
@@ -48,9 +49,10 @@ template <typename T> struct CoarseMatrix {
   DevBuf<int> rep;               // [nrow] an E-vector node of each row
   DevBuf<int> rowOf;             // [nE] row of each E-vector node, -1 where masked
 };
+// noCluster: the many-CTA cooperative layout even where one thread-block cluster would hold the level
 template <typename T>
 void coarse_matrix_setup(long long n, const long long *rowPtr, const long long *col, const double *val, long long nE,
-                         const long long *rowOfNode, const int *rep, CoarseMatrix<T> &M);
+                         const long long *rowOfNode, const int *rep, CoarseMatrix<T> &M, bool noCluster = false);
 
 // persistent cooperative Jacobi-PCG on the assembled coarse operator: b and xE
 // are E-vectors, x, z and z2 row vectors (solution rows, two exchange

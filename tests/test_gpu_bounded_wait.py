@@ -17,7 +17,9 @@ pytestmark = pytest.mark.gpu
 SCHED3 = "p=3+degree=2,p=1,p=3+degree=2"
 
 
-@pytest.mark.parametrize("n", [4, 20])  # coarse level of 27 rows (one CTA) / 6859 rows (many CTAs)
+# coarse level of 27 rows (one CTA), 6859 rows (two CTAs: the cluster layout, launched cooperatively with the
+# counting barrier under the test knob) and 42875 rows (many CTAs of a cooperative launch)
+@pytest.mark.parametrize("n", [4, 20, 36])
 def test_coarse_grid_barrier_wait_runs_out(product_lib, torch_cuda, n):
     torch = torch_cuda
     N = 3
@@ -25,9 +27,9 @@ def test_coarse_grid_barrier_wait_runs_out(product_lib, torch_cuda, n):
     base = ("solver=pfcg;preconditioner=multigrid;smootherType=cheby+asm;mgPrecision=fp64;"
             f"residualTol=1e-9+relative;maxIterations=20;pMGSchedule={SCHED3};coarsePersistent=1")
     el = G.Elliptic(N, VX, EToV, EToB, base + ";coarseSpinLimit=4096;coarseBarrierExtra=1")
-    if n == 20:
+    if n > 4:
         grid = el.get("mg.coarseMatrix")[3]
-        assert grid >= 8  # a cooperative launch over many CTAs
+        assert grid >= (2 if n == 20 else 8)  # several CTAs, all waiting at every barrier
     rhs = W.box_rhs(N, n, n, n, 5, el.get("ggeo"))
     r = torch.from_numpy(rhs.copy()).cuda()
     x = torch.zeros_like(r)

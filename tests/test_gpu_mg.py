@@ -118,7 +118,7 @@ def test_persistent_coarse_matches_host_driven(product_lib, torch_cuda):
         assert el.get("mg.coarseError")[0] == 0
         if pers:
             # the persistent solve runs on the assembled order-1 operator: one row per unmasked unique node
-            rows, width, nnz, grid, chunk, in_smem = el.get("mg.coarseMatrix")
+            rows, width, nnz, grid, chunk, in_smem, cluster = el.get("mg.coarseMatrix")
             assert rows == (n - 1) ** 3 and 7 <= width <= 27 and rows <= nnz <= rows * width
             assert grid * chunk >= rows and in_smem == 1
         else:
@@ -128,11 +128,14 @@ def test_persistent_coarse_matches_host_driven(product_lib, torch_cuda):
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
-def test_persistent_coarse_many_row_blocks(product_lib, torch_cuda, prec):
-    """A coarse level spread over many CTAs (row blocks with halos, grid barriers between them) gives the
-    same preconditioner as the host-driven coarse loop on the E-vector level operator."""
+@pytest.mark.parametrize("n", [20, 36])
+def test_persistent_coarse_many_row_blocks(product_lib, torch_cuda, prec, n):
+    """A coarse level spread over several CTAs (row blocks with halos, grid barriers between them) gives the
+    same preconditioner as the host-driven coarse loop on the E-vector level operator: 19^3 = 6859 rows as
+    one thread-block cluster of 2 CTAs (hardware cluster barrier), 35^3 = 42875 rows over many CTAs of a
+    cooperative launch (counting grid barrier)."""
     torch = torch_cuda
-    N, n = 3, 20  # 19^3 = 6859 coarse rows: more than one CTA holds
+    N = 3
     VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
     base = (f"solver=pfcg;preconditioner=multigrid;smootherType=cheby+asm;mgPrecision={prec};"
             f"residualTol=1e-9+relative;maxIterations=200;pMGSchedule={SCHED[3]}")
@@ -140,8 +143,12 @@ def test_persistent_coarse_many_row_blocks(product_lib, torch_cuda, prec):
     for pers in (1, 0):
         el = G.Elliptic(N, VX, EToV, EToB, base + f";coarsePersistent={pers}")
         if pers:
-            rows, width, nnz, grid, chunk, in_smem = el.get("mg.coarseMatrix")
-            assert rows == (n - 1) ** 3 and grid >= 8 and in_smem == 1
+            rows, width, nnz, grid, chunk, in_smem, cluster = el.get("mg.coarseMatrix")
+            assert rows == (n - 1) ** 3
+            if n == 20:
+                assert grid == 2 and cluster == 2
+            else:
+                assert grid >= 8 and cluster == 0
         rhs = W.box_rhs(N, n, n, n, 11, el.get("ggeo"))
         r = torch.from_numpy(rhs).cuda()
         x = torch.zeros_like(r)
