@@ -46,12 +46,12 @@ template <int NQ> struct AxShape {
 
 // FP32 order 7: at most 80 registers so that 6 CTAs (24 warps) fit per SM
 // (measured 2.7% faster at E=48^3 than the unbounded 100-register build)
-template <typename T, int NQ, bool POISSON>
-__global__ void __launch_bounds__(NQ *NQ *AxShape<NQ>::epb, (sizeof(T) == 4 && NQ == 8) ? 6 : 1)
+// EPB elements per CTA (default: enough for 128 threads); the arithmetic of an element does not depend on it
+template <typename T, int NQ, bool POISSON, int EPB = AxShape<NQ>::epb>
+__global__ void __launch_bounds__(NQ *NQ *EPB, (sizeof(T) == 4 && NQ == 8 && EPB == AxShape<NQ>::epb) ? 6 : 1)
     ax_stored_kernel(long long E, const T *__restrict__ ggeo, const T *__restrict__ D, T lambda0, T lambda1,
                      const T *__restrict__ q, T *__restrict__ Aq)
 {
-  constexpr int EPB = AxShape<NQ>::epb;
   constexpr int NP = NQ * NQ * NQ;
   __shared__ T s_D[NQ][NQ + 1];
   __shared__ T s_q[EPB][NQ][NQ];
@@ -763,6 +763,49 @@ void launch_ax_stored(int N, long long E, const T *ggeo, const T *D, T lambda0, 
   NRSG_DISPATCH_NQ(N, NRSG_AX)
 #undef NRSG_AX
   NRSG_CHECK_LAUNCH();
+}
+
+// One named FP32 axhelm variant (the multigrid autotuner's candidates; all give the same bits):
+// kAxVec   the default dispatch (order 7: the 16-byte shared-memory row-load kernel; else the plain kernel)
+// kAxPlain the plain kernel at its default elements per CTA
+// kAxEpb2  the plain kernel at twice the elements per CTA
+// kAxPipe  the bulk-copy pipelined kernel (order 7 Poisson only)
+// kAxConst D in constant memory and registers (order 7 only)
+// Returns false where the variant does not apply.
+bool launch_ax_f32_variant(int variant, int N, long long E, const float *ggeo, const float *D, float lambda0,
+                           float lambda1, bool poisson, const float *q, float *Aq, cudaStream_t s)
+{
+  if (E <= 0) return true;
+  switch (variant) {
+  case kAxVec: launch_ax_stored<float>(N, E, ggeo, D, lambda0, lambda1, poisson, q, Aq, s); return true;
+  case kAxPipe: return launch_ax_pipe(N, E, ggeo, D, lambda0, lambda1, poisson, q, Aq, s);
+  case kAxConst: return launch_ax_const(N, E, ggeo, D, lambda0, lambda1, poisson, q, Aq, s);
+  case kAxPlain:
+  case kAxEpb2: break;
+  default: return false;
+  }
+  const bool two = variant == kAxEpb2;
+#define NRSG_AXV(NQ)                                                                                       \
+  {                                                                                                        \
+    constexpr int B1 = AxShape<NQ>::epb, B2 = 2 * AxShape<NQ>::epb;                                        \
+    if (two) {                                                                                             \
+      const unsigned grid = (unsigned)((E + B2 - 1) / B2);                                                 \
+      if (poisson)                                                                                         \
+        ax_stored_kernel<float, NQ, true, B2><<<grid, dim3(NQ * NQ, B2), 0, s>>>(E, ggeo, D, lambda0, lambda1, q, Aq); \
+      else                                                                                                 \
+        ax_stored_kernel<float, NQ, false, B2><<<grid, dim3(NQ * NQ, B2), 0, s>>>(E, ggeo, D, lambda0, lambda1, q, Aq); \
+    } else {                                                                                               \
+      const unsigned grid = (unsigned)((E + B1 - 1) / B1);                                                 \
+      if (poisson)                                                                                         \
+        ax_stored_kernel<float, NQ, true, B1><<<grid, dim3(NQ * NQ, B1), 0, s>>>(E, ggeo, D, lambda0, lambda1, q, Aq); \
+      else                                                                                                 \
+        ax_stored_kernel<float, NQ, false, B1><<<grid, dim3(NQ * NQ, B1), 0, s>>>(E, ggeo, D, lambda0, lambda1, q, Aq); \
+    }                                                                                                      \
+  }
+  NRSG_DISPATCH_NQ(N, NRSG_AXV)
+#undef NRSG_AXV
+  NRSG_CHECK_LAUNCH();
+  return true;
 }
 
 template <typename T>

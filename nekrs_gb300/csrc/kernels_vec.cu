@@ -181,6 +181,8 @@ __device__ __forceinline__ bool reduce1(long long n, long long len, int W, const
   return threadIdx.x == 0;
 }
 
+#define NRSG_GRID_LOOP_VEC(i, n)                                                                           \
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (n); i += (long long)gridDim.x * blockDim.x)
 inline unsigned vec_grid(long long n)
 {
   long long b = (n + kThreads - 1) / kThreads;
@@ -302,6 +304,39 @@ void launch_scale_inplace(long long n, double a, double *x, cudaStream_t s)
   NRSG_CHECK_LAUNCH();
 }
 template void launch_gs_mask<float>(const GsPlan &, float *, bool, cudaStream_t);
+
+// q[i] = a hash of (seed, i) mapped to [-1, 1) (a reproducible test vector)
+__global__ void hash_fill_kernel(long long n, unsigned long long seed, float *q)
+{
+  NRSG_GRID_LOOP_VEC(i, n)
+  {
+    unsigned long long h = (unsigned long long)i * 0x9E3779B97F4A7C15ull + seed;
+    h ^= h >> 31;
+    h *= 0xBF58476D1CE4E5B9ull;
+    h ^= h >> 29;
+    q[i] = (float)((double)(h >> 11) * (1.0 / 4503599627370496.0) - 1.0);
+  }
+}
+void launch_hash_fill(long long n, unsigned long long seed, float *q, cudaStream_t s)
+{
+  if (n <= 0) return;
+  hash_fill_kernel<<<vec_grid(n), kThreads, 0, s>>>(n, seed, q);
+  NRSG_CHECK_LAUNCH();
+}
+// counter += number of i with a[i], b[i] of different bits
+__global__ void count_mismatch_kernel(long long n, const float *__restrict__ a, const float *__restrict__ b,
+                                      unsigned *counter)
+{
+  unsigned c = 0;
+  NRSG_GRID_LOOP_VEC(i, n) c += (__float_as_uint(a[i]) != __float_as_uint(b[i])) ? 1u : 0u;
+  if (c) atomicAdd(counter, c);
+}
+void launch_count_mismatch(long long n, const float *a, const float *b, unsigned *counter, cudaStream_t s)
+{
+  if (n <= 0) return;
+  count_mismatch_kernel<<<vec_grid(n), kThreads, 0, s>>>(n, a, b, counter);
+  NRSG_CHECK_LAUNCH();
+}
 
 template <typename T> __global__ void mask_kernel(long long n, const int *__restrict__ ids, T *__restrict__ q)
 {

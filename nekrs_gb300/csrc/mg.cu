@@ -12,6 +12,10 @@
 // is solved by Jacobi-PCG in T to `coarseTol` (default 1e-4) or smoothed.
 
 #include "mg_host.hpp"
+
+#include <map>
+#include <mutex>
+#include <tuple>
 #include "mg_kernels.hpp"
 
 #include <cmath>
@@ -47,7 +51,22 @@ template <typename T> struct MGLevelDev {
   DevBuf<T> Sx, Sy, Sz, invL, lam, wts, haloOut;  // invL (FP64 multigrid) or lam (FP32: 1/(lx+ly+lz) rebuilt)
   DevBuf<int> haloSrc, haloPartner;
   DevBuf<T> x, rhs, res;
+  int axVariant = kAxVec;                      // FP32 axhelm variant (autotuner)
+  std::vector<double> axMs;                    // autotuner: ms per launch of each variant, -1 not applicable / rejected
 };
+
+// Autotuner results shared by every solver of the process: (device, order, Poisson, elements) -> variant
+namespace {
+struct AxTuneCache {
+  std::mutex m;
+  std::map<std::tuple<int, int, int, long long>, std::pair<int, std::vector<double>>> best;
+};
+AxTuneCache &ax_tune_cache()
+{
+  static AxTuneCache c;
+  return c;
+}
+} // namespace
 
 template <typename T> struct MGImpl : public MGState {
   Elliptic &el;
@@ -159,6 +178,7 @@ template <typename T> struct MGImpl : public MGState {
       auto &v = lv[l];
       if (!v.smoothed) continue;
       if (plan.base != 0) build_fdm(v);
+      autotune_ax(v);
       v.rho = max_eig(v, o.seed + (unsigned long long)l);
       v.lambda1 = o.maxEigFactor * v.rho;
       v.lambda0 = o.minEigFactor * v.rho;
@@ -341,8 +361,80 @@ template <typename T> struct MGImpl : public MGState {
       if (el.opt.axConst) done = launch_ax_const(L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, q, Aq, s);
       if (!done) done = el.opt.axPipeline && launch_ax_pipe(L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, q, Aq, s);
     }
+    if constexpr (std::is_same<T, float>::value) {
+      if (!done) done = launch_ax_f32_variant(v.axVariant, L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, q, Aq, s);
+    }
     if (!done) launch_ax_stored<T>(L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, q, Aq, s);
     launch_gs_mask<T>(L.gsPlan, Aq, true, s);
+  }
+
+  // Autotuner (FP32 levels): the interchangeable axhelm variants are run on this level's geometric
+  // factors and a reproducible test vector; a variant whose output differs from the default kernel's
+  // in any bit is rejected (the reference's benchmarker accepts 400 eps: kernelBenchmarker.cpp:68-119,
+  // benchmarkAx.cpp:268-307); the others are timed with CUDA events (2 warm-up, 5 timed launches) and
+  // the fastest is kept.  Results are cached per (device, order, Poisson, elements).
+  void autotune_ax(MGLevelDev<T> &v)
+  {
+    if constexpr (std::is_same<T, float>::value) {
+      FieldLevel &L = *v.L;
+      const std::string &want = el.opt.axKernel;
+      if (el.opt.axConst) v.axVariant = kAxConst; // the older switches force a variant
+      else if (el.opt.axPipeline) v.axVariant = kAxPipe;
+      else if (want == "vec") v.axVariant = kAxVec;
+      else if (want == "plain") v.axVariant = kAxPlain;
+      else if (want == "epb2") v.axVariant = kAxEpb2;
+      else if (want == "pipe") v.axVariant = kAxPipe;
+      else if (want == "const") v.axVariant = kAxConst;
+      if (want != "auto" || el.opt.axConst || el.opt.axPipeline) return;
+      int dev = 0;
+      NRSG_CUDA(cudaGetDevice(&dev));
+      const auto key = std::make_tuple(dev, L.N, poisson ? 1 : 0, L.E);
+      auto &cache = ax_tune_cache();
+      {
+        std::lock_guard<std::mutex> lock(cache.m);
+        auto it = cache.best.find(key);
+        if (it != cache.best.end()) {
+          v.axVariant = it->second.first;
+          v.axMs = it->second.second;
+          return;
+        }
+      }
+      const long long n = L.Nlocal;
+      float *q = v.x.p, *ref = v.res.p, *out = v.rhs.p;
+      launch_hash_fill(n, 0x5eedull + (unsigned long long)L.N, q, s);
+      launch_ax_f32_variant(kAxVec, L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, q, ref, s);
+      DevBuf<unsigned> bad(1);
+      cudaEvent_t e0, e1;
+      NRSG_CUDA(cudaEventCreate(&e0));
+      NRSG_CUDA(cudaEventCreate(&e1));
+      std::vector<double> ms(kAxVariants, -1.0);
+      int best = kAxVec;
+      for (int c = 0; c < kAxVariants; ++c) {
+        NRSG_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(unsigned), s));
+        if (!launch_ax_f32_variant(c, L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, q, out, s)) continue;
+        launch_count_mismatch(n, ref, out, bad.p, s);
+        unsigned h = 0;
+        NRSG_CUDA(cudaMemcpyAsync(&h, bad.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+        NRSG_CUDA(cudaStreamSynchronize(s));
+        if (h != 0) continue; // not bit-identical: rejected
+        for (int w = 0; w < 2; ++w) launch_ax_f32_variant(c, L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, q, out, s);
+        NRSG_CUDA(cudaEventRecord(e0, s));
+        for (int w = 0; w < 5; ++w) launch_ax_f32_variant(c, L.N, L.E, v.ggeo.p, v.D.p, l0, l1, poisson, q, out, s);
+        NRSG_CUDA(cudaEventRecord(e1, s));
+        NRSG_CUDA(cudaEventSynchronize(e1));
+        float t = 0;
+        NRSG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+        ms[c] = t / 5.0;
+        if (ms[c] < ms[best] || ms[best] < 0) best = c;
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      if (ax_pipe_error(s)) best = kAxVec; // a bulk copy of the pipelined variant did not complete in time
+      v.axVariant = best;
+      v.axMs = ms;
+      std::lock_guard<std::mutex> lock(cache.m);
+      cache.best[key] = {best, ms};
+    }
   }
 
   // the fused FDM of one level: FP16 tensor-core transforms (option fdmPrecision = fp16) where they
@@ -595,7 +687,16 @@ template <typename T> struct MGImpl : public MGState {
       }
     else if (what == "mg.bytes")
       out.push_back((double)sizeof(T)); // multigrid precision
-    else if (what == "mg.coarseMatrix") {
+    else if (what == "mg.axKernel") {
+      // per smoothed level: the axhelm variant in use (0 vec, 1 plain, 2 epb2, 3 pipe, 4 const)
+      for (auto &v : lv)
+        if (v.smoothed) out.push_back((double)v.axVariant);
+    } else if (what == "mg.axTimes") {
+      // per smoothed level and variant: autotuner ms per launch (-1: not applicable or rejected)
+      for (auto &v : lv)
+        if (v.smoothed)
+          for (int c = 0; c < kAxVariants; ++c) out.push_back(c < (int)v.axMs.size() ? v.axMs[c] : -1.0);
+    } else if (what == "mg.coarseMatrix") {
       // rows, ELL width, stored nonzeros, row blocks (CTAs), rows per block, matrix in shared memory,
       // thread-block cluster size (0: one CTA or a cooperative launch)
       if (persistentCoarse)

@@ -108,6 +108,7 @@ struct Options {
   bool graphs = true;               // CUDA graphs of the steady-state PCG iteration (non-legacy streams)
   bool axPipeline = false;          // FP32 order-7 levels: bulk-copy pipelined axhelm
   bool axConst = false;             // FP32 order-7 levels: axhelm with D in constant memory / registers
+  std::string axKernel = "auto";    // FP32 level axhelm: auto (timed at setup) | vec | plain | epb2 | pipe | const
   int nfields = 1;                  // block solver: fields at fieldOffset = Nlocal ("solver = pcg+block" -> 3)
   bool stress = false;              // stressFormulation: symmetric-gradient operator (nfields = 3)
   int projection = 0;               // initialGuess: 0 none, 1 projection (classic), 2 projectionAconj
@@ -203,6 +204,13 @@ unsigned ax_pipe_error(cudaStream_t s);
 bool launch_ax_const(int N, long long E, const float *ggeo, const float *D, float lambda0, float lambda1,
                      bool poisson, const float *q, float *Aq, cudaStream_t s);
 template <typename T> void launch_mask(long long n, const int *ids, T *q, cudaStream_t s);
+// FP32 axhelm variants the multigrid autotuner chooses between (identical results)
+enum AxVariant { kAxVec = 0, kAxPlain = 1, kAxEpb2 = 2, kAxPipe = 3, kAxConst = 4, kAxVariants = 5 };
+bool launch_ax_f32_variant(int variant, int N, long long E, const float *ggeo, const float *D, float lambda0,
+                           float lambda1, bool poisson, const float *q, float *Aq, cudaStream_t s);
+// autotuner helpers: a reproducible [-1, 1) test vector; count entries whose bits differ
+void launch_hash_fill(long long n, unsigned long long seed, float *q, cudaStream_t s);
+void launch_count_mismatch(long long n, const float *a, const float *b, unsigned *counter, cudaStream_t s);
 template <typename T>
 void launch_build_diag(int N, long long E, const T *ggeo, const T *D, T lambda0, T lambda1, bool poisson, T *diag,
                        cudaStream_t s);

@@ -426,6 +426,11 @@ Options parse_options(const char *text)
       } else if (key == "residualprojectionvectors") o.projVecs = std::stoi(v);
       else if (key == "residualprojectionstart") o.projStart = std::stoi(v);
       else if (key == "mgprecision") o.mgPrecision = v;
+      else if (key == "axkernel") {
+        if (v != "auto" && v != "vec" && v != "plain" && v != "epb2" && v != "pipe" && v != "const")
+          throw Error(NRSG_ERR_BAD_CONFIG, "axKernel must be auto, vec, plain, epb2, pipe or const");
+        o.axKernel = v;
+      }
       else if (key == "fdmprecision") {
         if (v != "fp32" && v != "fp16") throw Error(NRSG_ERR_BAD_CONFIG, "fdmPrecision must be fp32 or fp16");
         o.fdmFp16 = (v == "fp16");

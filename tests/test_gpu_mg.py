@@ -233,3 +233,36 @@ def test_mg_galerkin_coarse_operator_parity(product_lib, oracle_mod, torch_cuda,
     assert abs(ig["iterations"] - io["iterations"]) <= 1
     assert ig["res"] <= 1e-8 * ig["res0"]
     assert rel(xg, xo) < (1e-8 if prec == "fp64" else 1e-6)
+
+
+@pytest.mark.parametrize("N", [5, 7])
+def test_axhelm_autotuner(product_lib, torch_cuda, N):
+    """The setup-time autotuner times the interchangeable FP32 axhelm variants of every smoothed level on the
+    level's own data, keeps only those bit-identical to the default kernel, and picks the fastest; the solve
+    with the tuned choice is bit-identical to the solve with the default kernel forced."""
+    torch = torch_cuda
+    n = 5
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    sched = f"p={N}+degree=3,p=3+degree=3,p=1,p=3+degree=3,p={N}+degree=3"
+    base = ("solver=pfcg;preconditioner=multigrid;smootherType=fourthoptcheby+ras;mgPrecision=mixed;"
+            f"residualTol=1e-9+relative;maxIterations=100;pMGSchedule={sched}")
+    sols = []
+    for kern in ("auto", "vec"):
+        el = G.Elliptic(N, VX, EToV, EToB, base + f";axKernel={kern}")
+        chosen = el.get("mg.axKernel")
+        times = el.get("mg.axTimes").reshape(len(chosen), 5)
+        if kern == "auto":
+            assert (times[:, 0] > 0).all() and (times[:, 1] > 0).all()  # default and plain always apply
+            if N == 7:
+                assert (times[0] > 0).sum() >= 4                          # vec, plain, epb2 and const on order 7
+            for lvl, c in enumerate(chosen.astype(int)):
+                ok = times[lvl] > 0
+                assert ok[c] and times[lvl, c] == times[lvl][ok].min()
+        else:
+            assert (chosen == 0).all()
+        rhs = W.box_rhs(N, n, n, n, 9, el.get("ggeo"))
+        r = torch.from_numpy(rhs).cuda()
+        x = torch.zeros_like(r)
+        assert el.solve(r, x)["status"] == 0
+        sols.append(x.cpu().numpy())
+    assert np.array_equal(sols[0], sols[1])
