@@ -138,6 +138,38 @@ int nrsg_elliptic_solve_advance(nrsg_elliptic *el, int *done, nrsg_solve_info *i
  * NRSG_ERR_MAXIT, else NRSG_OK. */
 int nrsg_elliptic_solve_batch(int n, nrsg_elliptic *const *els, double *const *d_r, double *const *d_x,
                               nrsg_solve_info *info);
+
+/* Serving: a request scheduler over resident operator handles.  The
+ * reference has no counterpart (its ellipticSolve is blocking,
+ * src/solvers/elliptic/ellipticSolve.cpp:32-190); these calls sequence the
+ * resumable solve above for many requests.
+ *   create   hbm_budget_bytes: the most device memory the handles of requests
+ *            in flight may hold together (a request always starts when none
+ *            is in flight).
+ *   submit   queue a solve on a resident handle: d_r (right-hand side,
+ *            overwritten by the residual) and d_x (initial guess, then the
+ *            solution) stay the caller's and must not be touched until the
+ *            request is polled; tol / relative / maxIterations as
+ *            nrsg_elliptic_set_tolerance; footprint_bytes is the handle's
+ *            device memory (nrsg_elliptic_get "deviceBytes").  Returns the
+ *            request id.
+ *   step     admit queued requests in arrival order (a request whose handle
+ *            is busy waits without blocking the ones behind it; the budget
+ *            stops admission), then advance every request in flight by at
+ *            most one Krylov iteration without waiting on the device.  Returns
+ *            the numbers in flight and queued.
+ *   poll     take one finished request (*got = 1): its id and solve info; the
+ *            return value is the solve's hard error, if any (an exhausted
+ *            iteration budget shows as info->status = NRSG_ERR_MAXIT).
+ *   destroy  fails with NRSG_ERR_INVALID while requests are in flight.
+ * One thread at a time per server (calls are serialised by a mutex). */
+typedef struct nrsg_server nrsg_server;
+int nrsg_server_create(long long hbm_budget_bytes, nrsg_server **out);
+int nrsg_server_destroy(nrsg_server *s);
+int nrsg_server_submit(nrsg_server *s, nrsg_elliptic *el, double *d_r, double *d_x, double tol, int relative,
+                       int maxIterations, long long footprint_bytes, long long *request_id);
+int nrsg_server_step(nrsg_server *s, int *in_flight, int *queued);
+int nrsg_server_poll(nrsg_server *s, long long *request_id, nrsg_solve_info *info, int *got);
 /* Same solve on host buffers: copies in, solves, copies back. */
 int nrsg_elliptic_solve_host(nrsg_elliptic *el, double *h_r, double *h_x, nrsg_solve_info *info);
 

@@ -74,6 +74,12 @@ def lib():
         L.nrsg_elliptic_set_coefficients.argtypes = [vp, vp, vp, LL]
         L.nrsg_elliptic_set_field_bcs.argtypes = [vp, vp]
         L.nrsg_elliptic_solve_advance.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(SolveInfo)]
+        L.nrsg_server_create.argtypes = [LL, ctypes.POINTER(vp)]
+        L.nrsg_server_destroy.argtypes = [vp]
+        L.nrsg_server_submit.argtypes = [vp, vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, LL,
+                                         ctypes.POINTER(LL)]
+        L.nrsg_server_step.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+        L.nrsg_server_poll.argtypes = [vp, ctypes.POINTER(LL), ctypes.POINTER(SolveInfo), ctypes.POINTER(ctypes.c_int)]
         L.nrsg_elliptic_solve_batch.argtypes = [ctypes.c_int, ctypes.POINTER(vp), ctypes.POINTER(vp),
                                                 ctypes.POINTER(vp), ctypes.POINTER(SolveInfo)]
         for f in ("nrsg_elliptic_operator", "nrsg_elliptic_ax", "nrsg_elliptic_precondition"):
@@ -439,3 +445,50 @@ def weighted_inner_prod_f64(n, w, a, b, out, stream=0):
 
 def geometric_factors_f64(N, E, VX, ggeo, stream=0):
     check(lib().nrsg_geometric_factors_f64(N, E, _ptr(VX), _ptr(ggeo), stream))
+
+
+class Server:
+    """Request scheduler over resident operator handles (nrsg_server_*): submit() queues a solve, step()
+    admits requests by arrival order and HBM budget and advances every request in flight by at most one
+    Krylov iteration, poll() returns finished requests as (request id, info dict)."""
+
+    def __init__(self, hbm_budget_bytes):
+        h = ctypes.c_void_p()
+        check(lib().nrsg_server_create(int(hbm_budget_bytes), ctypes.byref(h)))
+        self.h = h.value
+        self._keep = {}
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().nrsg_server_destroy(self.h)
+            self.h = None
+
+    def submit(self, el, r, x, tol, relative=True, max_iterations=400, footprint_bytes=None):
+        """Queue a solve of handle `el` on device E-vectors r (overwritten) and x (initial guess / solution)."""
+        el._own_stream()  # the handle's own stream; buffers the caller's torch stream wrote are in place
+        if footprint_bytes is None:
+            footprint_bytes = int(el.get("deviceBytes")[0])
+        rid = LL(0)
+        check(lib().nrsg_server_submit(self.h, el.h, _ptr(r), _ptr(x), float(tol), int(relative),
+                                       int(max_iterations), int(footprint_bytes), ctypes.byref(rid)))
+        self._keep[rid.value] = (el, r, x)
+        return rid.value
+
+    def step(self):
+        """One scheduling step; returns (in flight, queued)."""
+        a, q = ctypes.c_int(0), ctypes.c_int(0)
+        check(lib().nrsg_server_step(self.h, ctypes.byref(a), ctypes.byref(q)))
+        return a.value, q.value
+
+    def poll(self):
+        """All finished requests so far: a list of (request id, info dict)."""
+        out = []
+        while True:
+            rid, info, got = LL(0), SolveInfo(), ctypes.c_int(0)
+            code = lib().nrsg_server_poll(self.h, ctypes.byref(rid), ctypes.byref(info), ctypes.byref(got))
+            if not got.value:
+                return out
+            self._keep.pop(rid.value, None)
+            if code != NRSG_OK:
+                raise NrsgError(code, lib().nrsg_last_error().decode(errors="replace"))
+            out.append((rid.value, info.as_dict()))

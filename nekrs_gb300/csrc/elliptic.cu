@@ -754,12 +754,18 @@ int nrsg_elliptic_create(const nrsg_mesh_desc *mesh, const char *options, nrsg_e
   *out = nullptr;
   NRSG_TRY({
     auto h = new nrsg_elliptic();
+    size_t free0 = 0, free1 = 0, total = 0;
+    NRSG_CUDA(cudaDeviceSynchronize());
+    NRSG_CUDA(cudaMemGetInfo(&free0, &total));
     try {
       h->impl.reset(new Elliptic(mesh, options));
     } catch (...) {
       delete h;
       throw;
     }
+    NRSG_CUDA(cudaDeviceSynchronize());
+    NRSG_CUDA(cudaMemGetInfo(&free1, &total));
+    h->impl->deviceBytes = free0 > free1 ? (long long)(free0 - free1) : 0;
     *out = h;
   })
 }
@@ -951,6 +957,7 @@ int nrsg_elliptic_get(nrsg_elliptic *el, const char *name, void *h_out, long lon
     else if (s == "invDegree") put(L.gm.invDegree);
     else if (s == "D") put(L.Dh);
     else if (s == "history") put(E.history);
+    else if (s == "deviceBytes") put(std::vector<double>{(double)E.deviceBytes});
     else if (s == "allNeumann") put(std::vector<double>{E.allNeumann ? 1.0 : 0.0});
     else if (s == "proj.vectors") put(std::vector<double>{(double)E.projM, (double)E.projStep});
     else if (s == "graph.segments") {

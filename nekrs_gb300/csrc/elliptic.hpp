@@ -100,6 +100,7 @@ struct Elliptic {
   std::vector<double> history;
   int status = NRSG_OK;
   int lastIters = 0;
+  long long deviceBytes = 0; // device memory the handle took at creation (admission estimate for serving)
 
   Elliptic(const nrsg_mesh_desc *mesh, const char *options);
   ~Elliptic();

@@ -86,3 +86,56 @@ def test_batch_reports_iteration_limit(product_lib, torch_cuda):
     b = torch.from_numpy(W.box_rhs(5, 3, 3, 3, 7, ok.get("ggeo"))).cuda()
     infos = G.solve_batch([ok, lim], [b.clone(), b.clone()], [torch.zeros_like(b), torch.zeros_like(b)])
     assert infos[0]["status"] == 0 and infos[1]["status"] == 1 and infos[1]["iterations"] == 5
+
+
+@pytest.mark.parametrize("budget", ["all", "one"])
+def test_library_server_alone_vs_in_mix(product_lib, torch_cuda, budget):
+    """The library's request scheduler (nrsg_server_*): requests on resident handles, several per handle, with
+    tolerances 1e-6 / 1e-8 / 1e-10, stepped together one Krylov iteration at a time; every result is bit
+    for bit the result of the same request solved alone.  With a budget below two handles' device
+    footprint at most one request is in flight at any step."""
+    torch = torch_cuda
+    els, rhs = setup_all(torch)
+    foot = [int(el.get("deviceBytes")[0]) for el in els]
+    assert all(f > 0 for f in foot)
+    tols = [1e-6, 1e-8, 1e-10]
+    reqs = []  # (handle index, tolerance, seed scale)
+    for k in range(9):
+        reqs.append((k % len(els), tols[k % 3], 1.0 + 0.25 * k))
+    # alone
+    alone = []
+    for h, tol, sc in reqs:
+        el = els[h]
+        el.set_tolerance(tol)
+        r = rhs[h] * sc
+        x = torch.zeros_like(r)
+        info = el.solve(r, x)
+        alone.append((x.cpu().numpy(), info["iterations"]))
+    # in the mix, through the library scheduler
+    srv = G.Server(sum(foot) * 2 if budget == "all" else min(foot) + 1)
+    bufs, ids = [], []
+    for h, tol, sc in reqs:
+        r = rhs[h] * sc
+        x = torch.zeros_like(r)
+        bufs.append((r, x))
+        ids.append(srv.submit(els[h], r, x, tol))
+    results, max_inflight = {}, 0
+    for _ in range(200000):
+        a, q = srv.step()
+        max_inflight = max(max_inflight, a)
+        for rid, info in srv.poll():
+            results[rid] = info
+        if a == 0 and q == 0:
+            break
+    for rid, info in srv.poll():
+        results[rid] = info
+    assert len(results) == len(reqs)
+    if budget == "one":
+        assert max_inflight == 1
+    else:
+        assert max_inflight >= 2
+    torch.cuda.synchronize()
+    for k, rid in enumerate(ids):
+        assert results[rid]["status"] == 0
+        assert results[rid]["iterations"] == alone[k][1]
+        assert np.array_equal(bufs[k][1].cpu().numpy(), alone[k][0])
