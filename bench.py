@@ -565,9 +565,10 @@ def run_serve(args):
 
     def serve(concurrent):
         lat = []
-        busy = {}  # op -> request
+        busy = {}  # op -> request handed to the library scheduler
         queue = []
         nxt = 0
+        srv = G.Server(budget) if concurrent else None
         start = time.perf_counter()
         while nxt < len(reqs) or queue or busy:
             now = time.perf_counter() - start
@@ -575,22 +576,22 @@ def run_serve(args):
                 queue.append(reqs[nxt])
                 nxt += 1
             if concurrent:
+                # requests go to the library (nrsg_server_*) in arrival order once their operator is free
+                # (its buffers are reused); the library admits by HBM footprint and steps all in flight
                 rest = []
-                inflight = sum(pool[op]["bytes"] for op in busy)
                 for q in queue:
-                    need = pool[q["op"]]["bytes"]
-                    if q["op"] in busy or (busy and inflight + need > budget):
+                    if q["op"] in busy:
                         rest.append(q)
                         continue
-                    inflight += need
                     prepare(q)
-                    pool[q["op"]]["el"].solve_begin(pool[q["op"]]["r"], pool[q["op"]]["x"])
-                    busy[q["op"]] = q
+                    o = pool[q["op"]]
+                    rid = srv.submit(o["el"], o["r"], o["x"], q["tol"], footprint_bytes=o["bytes"])
+                    busy[q["op"]] = (rid, q)
                 queue = rest
-                for op in list(busy):
-                    info = pool[op]["el"].solve_advance()
-                    if info is not None:
-                        lat.append(time.perf_counter() - start - busy.pop(op)["t"])
+                srv.step()
+                done = {rid for rid, _ in srv.poll()}
+                for op in [op for op, (rid, _) in busy.items() if rid in done]:
+                    lat.append(time.perf_counter() - start - busy.pop(op)[1]["t"])
             elif queue:
                 q = queue.pop(0)
                 prepare(q)
