@@ -542,7 +542,8 @@ def run_serve(args):
     # set is hot) may hold at most this many bytes together
     budget = args.serve_hbm_fraction * torch.cuda.mem_get_info()[1]
     # request trace
-    gaps = rng.exponential(2e-3, size=int(args.serve_seconds / 2e-3 * 2) + 16)
+    mean_gap = args.serve_interarrival_ms / 1e3
+    gaps = rng.exponential(mean_gap, size=int(args.serve_seconds / mean_gap * 2) + 16)
     arr = np.cumsum(gaps)
     arr = arr[arr < args.serve_seconds]
     reqs = [{"t": float(t), "op": int(rng.integers(P)), "tol": float(rng.choice([1e-6, 1e-8, 1e-10])),
@@ -611,7 +612,7 @@ def run_serve(args):
                       "n_gpus": 1, "higher_is_better": False, "dtype": "f64",
                       "data": "synthetic (seeded Kershaw boxes and RHS, exponential arrivals)",
                       "config": {"workload": "serve", "arrivals_s": args.serve_seconds, "requests": len(reqs),
-                                 "pool": P, "setup_s": setup_s, "mean_interarrival_ms": 2.0,
+                                 "pool": P, "setup_s": setup_s, "mean_interarrival_ms": args.serve_interarrival_ms,
                                  "pool_bytes": int(sum(o["bytes"] for o in pool)), "inflight_budget_bytes": int(budget)},
                       "concurrent": conc, "sequential": seq,
                       "solves_per_s_vs_sequential": conc["solves_per_s"] / seq["solves_per_s"]}))
@@ -625,9 +626,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
                     choices=sorted(WORKLOADS) + ["batch", "serve", "velocity", "projection"])
-    ap.add_argument("--batch-problems", type=int, default=64, help="problems in the batch workload (config: 256)")
+    ap.add_argument("--batch-problems", type=int, default=256, help="problems in the batch workload")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window of the serve workload (config: 60)")
     ap.add_argument("--serve-pool", type=int, default=24, help="resident operators of the serve workload")
+    ap.add_argument("--serve-interarrival-ms", type=float, default=2.0,
+                    help="mean of the exponential inter-arrival times (config: 2 ms, far above one GPU's capacity "
+                         "for this request mix; a larger mean measures latency at a load the GPU sustains)")
     ap.add_argument("--serve-hbm-fraction", type=float, default=0.5,
                     help="HBM share the operators of in-flight requests may hold together (admission)")
     ap.add_argument("--mesh", default=None,
