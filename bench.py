@@ -276,9 +276,6 @@ def time_kernel(fn, stream, reps=10):
     return ev0.elapsed_time(ev1) / 1e3 / reps
 
 
-AX_CONST_TIMING = False  # set by --ax-const: also time the constant-memory FP32 axhelm variant
-
-
 def kernel_rooflines(G, el, N, E):
     """Achieved algorithmic GB/s of the fine-level operator kernels, CUDA events on their stream."""
     import torch
@@ -317,10 +314,9 @@ def kernel_rooflines(G, el, N, E):
         t = time_kernel(lambda: G.ax_pipe_f32(N, E, g32, D32, 1.0, 0.0, True, q32, a32, cs), stream)
         out["ax_pipe_f32"] = {"launch_ms": t * 1e3, "achieved": 32.0 * n / t / 1e9, "unit": "GB/s",
                               "algorithmic_bytes": 32.0 * n}
-        if AX_CONST_TIMING:
-            t = time_kernel(lambda: G.ax_const_f32(N, E, g32, D32, 1.0, 0.0, True, q32, a32, cs), stream)
-            out["ax_const_f32"] = {"launch_ms": t * 1e3, "achieved": 32.0 * n / t / 1e9, "unit": "GB/s",
-                                   "algorithmic_bytes": 32.0 * n}
+        t = time_kernel(lambda: G.ax_const_f32(N, E, g32, D32, 1.0, 0.0, True, q32, a32, cs), stream)
+        out["ax_const_f32"] = {"launch_ms": t * 1e3, "achieved": 32.0 * n / t / 1e9, "unit": "GB/s",
+                               "algorithmic_bytes": 32.0 * n}
     for v in out.values():
         v["frac_of_hbm"] = v["achieved"] / peak
     return out, peak, src
@@ -637,15 +633,14 @@ def main():
     ap.add_argument("--mesh", default=None,
                     help="read the mesh from a Nek5000 .re2 box file (e.g. the reference's kershaw.re2); the "
                          "workload's order, eps and options apply, the right-hand side is the BPS5 one")
-    ap.add_argument("--ax-const", action="store_true",
-                    help="also time the FP32 order-7 axhelm variant with D in constant memory and registers")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--oracle-error", action="store_true",
+                    help="also solve the same right-hand side with the CPU oracle in FP64 throughout (FP64 "
+                         "multigrid, minutes on the host) and report the GPU solution's error against it")
     ap.add_argument("--no-fp64-plain", action="store_true")
     ap.add_argument("--solve-only", action="store_true",
                     help="time the device-resident solves only (no e2e, FP64 comparison or kernel rooflines)")
     args = ap.parse_args()
-    global AX_CONST_TIMING
-    AX_CONST_TIMING = args.ax_const
     args.warmup = max(args.warmup, 3)
     args.workload_name = args.workload
     if args.workload in ("batch", "serve", "velocity", "projection"):
@@ -750,6 +745,14 @@ def main():
     del rh, xh
 
     peak, psrc = load_peaks()
+    tuned = None
+    if "multigrid" in opts:
+        names = ["vec", "plain", "epb2", "pipe", "const"]
+        ch = el.get("mg.axKernel").astype(int).tolist()
+        tm = el.get("mg.axTimes").reshape(len(ch), 5) if ch else []
+        tuned = [{"level_order": int(o), "chosen": names[c], "ms": {names[k]: (round(float(v), 4) if v > 0 else None)
+                                                                    for k, v in enumerate(row)}}
+                 for o, c, row in zip(el.get("mg.levels").astype(int).tolist(), ch, tm)]
     fdm = (fdm_roofline(G, el, N, E, peak, "ras" in opts)
            if "multigrid" in opts and ("asm" in opts or "ras" in opts) else None)
     extra = {}
@@ -826,8 +829,21 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single"},
             "e2e": {"value": dofs / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": 2 * rhs.nbytes,
                     "d2h_bytes_per_step": 2 * rhs.nbytes},
-            "roofline": roof, "gpu_launches": int(launches), "clocks": clk}
+            "roofline": roof, "gpu_launches": int(launches), "clocks": clk, "axhelm_autotuner": tuned}
     line.update(extra)
+    if rank == 0 and args.oracle_error:
+        from oracle import oracle as O
+
+        t0 = time.perf_counter()
+        fopts = plain_fp64_options(opts)
+        orc = O.Elliptic(N, VX, EToV, EToB, fopts)
+        xo, io = orc.solve(rhs.copy())
+        line["error_vs_fp64_oracle"] = {
+            "value": float(np.linalg.norm(x_mixed - xo) / np.linalg.norm(xo)), "oracle_iterations": int(io["iterations"]),
+            "oracle_options": fopts, "oracle_seconds": time.perf_counter() - t0,
+            "note": "relative 2-norm difference between the GPU solution of this workload and the CPU oracle's "
+                    "FP64-throughout solve (FP64 multigrid) of the same right-hand side at the same tolerance"}
+        del orc
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(nel, N, eps, opts)
     if rank == 0:
