@@ -48,6 +48,10 @@ WORKLOADS = {
                                 ";mgPrecision=mixed;fdmPrecision=fp16",
                                 "the kershaw48-n7-mixed solve with the fine-level FDM transforms in FP16 on the tensor "
                                 "cores (mma.sync m16n8k16, FP32 accumulation, per-element max-abs scaling)"),
+    "kershaw48-n7-mixed-tf32": (48, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
+                                ";mgPrecision=mixed;fdmPrecision=tf32",
+                                "the kershaw48-n7-mixed solve with the multigrid FDM transforms (orders 7 and 3) in "
+                                "TF32 on the tensor cores (mma.sync m16n8k8, FP32 accumulation)"),
     "kershaw32-n7-mixed": (32, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
                            ";mgPrecision=mixed", "the kershaw48-n7-mixed solve on E=32^3 (profiling size)"),
     "kershaw16-n7-mixed": (16, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
@@ -806,7 +810,8 @@ def main():
     if el is None:
         el = G.Elliptic(N, VX, EToV, EToB, "preconditioner=jacobi")
     kr, peak, psrc = kernel_rooflines(G, el, N, E)
-    fdm_name = "fdm_f16" if "fdmPrecision=fp16" in opts else "fdm_f32"
+    fdm_name = ("fdm_f16" if "fdmPrecision=fp16" in opts else "fdm_tf32" if "fdmPrecision=tf32" in opts
+                else "fdm_f32")
     if fdm is not None:
         kr[fdm_name] = fdm
     # the dominant kernel of the solve by share of device time (ncu launch list of this workload)

@@ -173,14 +173,19 @@ __global__ void cheby1_kernel(long long n, T dc, T rc, const T *__restrict__ SAd
     d[i] = dc * dn + rc * r1;
   }
 }
-// rout = rin - Ad (rin may be rout), x = x + beta d (x = beta d when xzero)
+// explicit roundings, shared with the fused gather-scatter updates
+__device__ __forceinline__ float mg_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double mg_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float mg_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mg_mul(double a, double b) { return __dmul_rn(a, b); }
+// rout = rin - Ad (rin may be rout), x = fma(beta, d, x) (x = beta d when xzero)
 template <typename T>
 __global__ void cheby4_kernel(long long n, T beta, const T *__restrict__ Ad, const T *__restrict__ d, const T *rin,
                               T *rout, T *__restrict__ x, bool xzero)
 {
   MG_LOOP(i, n)
   {
-    x[i] = xzero ? beta * d[i] : x[i] + beta * d[i];
+    x[i] = xzero ? mg_mul(beta, d[i]) : mg_fma(beta, d[i], x[i]);
     rout[i] = rin[i] - Ad[i];
   }
 }
@@ -958,6 +963,221 @@ __global__ void __launch_bounds__(32 * fdm8h::EPC)
     v.w *= wt.w;
     ((float4 *)se)[q] = v;
   }
+}
+
+// ---------------------------------------------------------------------------
+// FDM (Schwarz local solve) on the tensor cores in TF32 (fdmPrecision = tf32).
+// Each 1-D transform of the extended element is the product of the element's
+// NX x NX eigenvector matrix (NX = N + 3) with its NX^2 lines, done as
+// mma.sync m16n8k8 with TF32 inputs and FP32 accumulation: M = the NX output
+// points (padded to 16), N = the lines in tiles of 8, K = the NX input points
+// in steps of 8.  TF32 has FP16's 11-bit significand but FP32's exponent
+// range, so, unlike the FP16 form, it needs no scaling.  One warp per element.
+// The element lives in shared memory as lines of LS floats (line n, point k at
+// n LS + k); every pass writes its result rotated, point (k; b, c) of the
+// input becoming point b of line c + NX m of the output, so that the next
+// direction is again the contiguous one and three passes restore the layout.
+// With LS = 12 (= 4 mod 8) the 8 lines a fragment load touches start in
+// distinct 4-bank groups, and the paired 64-bit result stores of a half-warp
+// are free of bank conflicts.  Inputs of every pass are rounded to TF32
+// (cvt.rna) when they are stored; the last pass keeps FP32.
+// ---------------------------------------------------------------------------
+namespace fdmtc {
+constexpr int LS = 12;
+constexpr int EPC = 4; // elements (warps) per CTA
+template <int NQ> struct Shape {
+  static constexpr int NX = NQ + 2, lines = NX * NX, nt = (lines + 7) / 8, ks = (NX + 7) / 8;
+  static constexpr int buf = nt * 8 * LS; // floats per tile buffer (whole tiles of 8 lines)
+  static_assert(NX % 2 == 0 && NX <= LS, "even extended size of at most 12 points");
+};
+} // namespace fdmtc
+
+__device__ __forceinline__ uint32_t f2tf32(float x)
+{
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float round_tf32(float x) { return __uint_as_float(f2tf32(x)); }
+
+__device__ __forceinline__ void mma_tf32(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1)
+{
+  asm("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// A fragments (m16n8k8, row major) of one direction: forward M(i, l) = S(l, i), backward M(i, l) = S(i, l),
+// S(r, c) = Sd[r + NX c]; a0..a3 = M(g, k), M(g + 8, k), M(g, k + 4), M(g + 8, k + 4) with k = 8 s + t
+template <int NX, int KS>
+__device__ __forceinline__ void fdmtc_afrag(const float *__restrict__ Sd, bool fwd, int g, int t, uint32_t A[KS][4])
+{
+#pragma unroll
+  for (int s = 0; s < KS; ++s)
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      const int row = g + 8 * (h & 1), col = 8 * s + t + 4 * (h >> 1);
+      const float v = (row < NX && col < NX) ? __ldg(Sd + (fwd ? col + NX * row : row + NX * col)) : 0.f;
+      A[s][h] = f2tf32(v);
+    }
+}
+
+// one direction: out(m; line c + NX m, point b) = sum_k M(m, k) in(line b + NX c, point k).  MODE 0 rounds the
+// result to TF32, MODE 1 first scales it by 1/(lxy[n] + lz[m]) (n = b + NX c), MODE 2 keeps FP32.
+template <int NX, int KS, int NT, int MODE>
+__device__ __forceinline__ void fdmtc_pass(const float *in, float *out, const uint32_t A[KS][4], int g, int t,
+                                           const float *lxy, float lz0, float lz1)
+{
+  constexpr int LS = fdmtc::LS, LINES = NX * NX;
+#pragma unroll
+  for (int j = 0; j < NT; ++j) {
+    const float *src = in + (8 * j + g) * LS;
+    float c[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int s = 0; s < KS; ++s) {
+      const int k0 = 8 * s + t, k1 = k0 + 4;
+      uint32_t b0 = 0u, b1 = 0u;
+      if (8 * s < NX) {
+        const float v = src[k0]; // k0 < LS: inside the line; points past NX are taken as 0
+        b0 = k0 < NX ? __float_as_uint(v) : 0u;
+      }
+      if (8 * s + 4 < NX) {
+        const float v = src[k1];
+        b1 = k1 < NX ? __float_as_uint(v) : 0u;
+      }
+      mma_tf32(c, A[s], b0, b1);
+    }
+    const int n0 = 8 * j + 2 * t; // this lane's result columns n0, n0 + 1 (same c: NX and n0 are even)
+    if (n0 < LINES) {
+      const int cc = n0 / NX, b = n0 - NX * cc;
+      if (MODE == 1) {
+        const float2 xy = *(const float2 *)(lxy + n0);
+        const float d0 = xy.x + lz0, d1 = xy.y + lz0, d2 = xy.x + lz1, d3 = xy.y + lz1;
+        c[0] *= d0 > 1e-5f ? __fdividef(1.f, d0) : 0.f;
+        c[1] *= d1 > 1e-5f ? __fdividef(1.f, d1) : 0.f;
+        c[2] *= d2 > 1e-5f ? __fdividef(1.f, d2) : 0.f;
+        c[3] *= d3 > 1e-5f ? __fdividef(1.f, d3) : 0.f;
+      }
+      if (MODE != 2) {
+#pragma unroll
+        for (int h = 0; h < 4; ++h) c[h] = round_tf32(c[h]);
+      }
+      if (g < NX) *(float2 *)(out + (cc + NX * g) * LS + b) = make_float2(c[0], c[1]);
+      if (g + 8 < NX) *(float2 *)(out + (cc + NX * (g + 8)) * LS + b) = make_float2(c[2], c[3]);
+    }
+  }
+}
+
+// extended-element point of halo node (a, b) of face f, in the lines-of-x layout
+template <int NX> __device__ __forceinline__ int fdmtc_ext(int f, int a, int b)
+{
+  constexpr int LS = fdmtc::LS;
+  int x, y, z;
+  switch (f) {
+  case 0: x = 0, y = a + 1, z = b + 1; break;
+  case 1: x = NX - 1, y = a + 1, z = b + 1; break;
+  case 2: x = a + 1, y = 0, z = b + 1; break;
+  case 3: x = a + 1, y = NX - 1, z = b + 1; break;
+  case 4: x = a + 1, y = b + 1, z = 0; break;
+  default: x = a + 1, y = b + 1, z = NX - 1; break;
+  }
+  return (y + NX * z) * LS + x;
+}
+
+template <int NQ, bool RAS>
+__global__ void __launch_bounds__(32 * fdmtc::EPC, 4)
+    fdmtc_kernel(long long E, const float *__restrict__ u, const int *__restrict__ haloSrc,
+                 const float *__restrict__ Sx, const float *__restrict__ Sy, const float *__restrict__ Sz,
+                 const float *__restrict__ lam, const float *__restrict__ wts, float *__restrict__ Su,
+                 float *__restrict__ haloOut)
+{
+  using Sh = fdmtc::Shape<NQ>;
+  constexpr int NX = Sh::NX, KS = Sh::ks, NT = Sh::nt, LS = fdmtc::LS, BUF = Sh::buf;
+  constexpr int NP = NQ * NQ * NQ, NF = NQ * NQ, LN = NX * NX;
+  __shared__ __align__(16) float s_t[fdmtc::EPC][2][BUF];
+  __shared__ __align__(16) float s_xy[fdmtc::EPC][(LN + 3) / 4 * 4];
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
+  const long long e = (long long)blockIdx.x * fdmtc::EPC + wp;
+  if (e >= E) return; // whole warp; warp-level synchronisation only
+  float *T0 = s_t[wp][0], *T1 = s_t[wp][1], *lxy = s_xy[wp];
+  const float *le = lam + e * 3 * NX;
+  // tile: zero (edges and corners of the extended element stay 0), own nodes, halo; lx + ly per line
+  for (int q = lane; q < BUF / 4; q += 32) ((float4 *)T0)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int q = lane; q < LN; q += 32) lxy[q] = __ldg(le + q % NX) + __ldg(le + NX + q / NX);
+  const float lz0 = g < NX ? __ldg(le + 2 * NX + g) : 0.f;
+  const float lz1 = g + 8 < NX ? __ldg(le + 2 * NX + g + 8) : 0.f;
+  __syncwarp();
+  const float *ue = u + e * NP;
+  for (int q = lane; q < NP; q += 32) {
+    const int x = q % NQ, y = (q / NQ) % NQ, z = q / NF;
+    T0[((y + 1) + NX * (z + 1)) * LS + (x + 1)] = round_tf32(__ldg(ue + q));
+  }
+  const int *hs = haloSrc + e * 6 * NF;
+  for (int q = lane; q < 6 * NF; q += 32) {
+    const int src = __ldg(hs + q);
+    const int f = q / NF, pp = q % NF;
+    T0[fdmtc_ext<NX>(f, pp % NQ, pp / NQ)] = src >= 0 ? round_tf32(__ldg(u + src)) : 0.f;
+  }
+  __syncwarp();
+  const float *S3[3] = {Sx + e * LN, Sy + e * LN, Sz + e * LN};
+  uint32_t A[KS][4];
+  // forward S^T along x, y, z (scaling by 1/(lx + ly + lz) after z), then backward S along x, y, z
+  fdmtc_afrag<NX, KS>(S3[0], true, g, t, A);
+  fdmtc_pass<NX, KS, NT, 0>(T0, T1, A, g, t, lxy, lz0, lz1);
+  __syncwarp();
+  fdmtc_afrag<NX, KS>(S3[1], true, g, t, A);
+  fdmtc_pass<NX, KS, NT, 0>(T1, T0, A, g, t, lxy, lz0, lz1);
+  __syncwarp();
+  fdmtc_afrag<NX, KS>(S3[2], true, g, t, A);
+  fdmtc_pass<NX, KS, NT, 1>(T0, T1, A, g, t, lxy, lz0, lz1);
+  __syncwarp();
+  fdmtc_afrag<NX, KS>(S3[0], false, g, t, A);
+  fdmtc_pass<NX, KS, NT, 0>(T1, T0, A, g, t, lxy, lz0, lz1);
+  __syncwarp();
+  fdmtc_afrag<NX, KS>(S3[1], false, g, t, A);
+  fdmtc_pass<NX, KS, NT, 0>(T0, T1, A, g, t, lxy, lz0, lz1);
+  __syncwarp();
+  fdmtc_afrag<NX, KS>(S3[2], false, g, t, A);
+  fdmtc_pass<NX, KS, NT, 2>(T1, T0, A, g, t, lxy, lz0, lz1);
+  __syncwarp();
+  float *se = Su + e * NP;
+  for (int q = lane; q < NP; q += 32) {
+    const int x = q % NQ, y = (q / NQ) % NQ, z = q / NF;
+    float v = T0[((y + 1) + NX * (z + 1)) * LS + (x + 1)];
+    if (RAS) v *= __ldg(wts + e * NP + q);
+    se[q] = v;
+  }
+  if (!RAS) {
+    float *ho = haloOut + e * 6 * NF;
+    for (int q = lane; q < 6 * NF; q += 32) {
+      const int f = q / NF, pp = q % NF;
+      ho[q] = T0[fdmtc_ext<NX>(f, pp % NQ, pp / NQ)];
+    }
+  }
+}
+
+bool launch_fdm_tf32(int N, long long E, bool ras, const float *u, const int *haloSrc, const float *Sx,
+                     const float *Sy, const float *Sz, const float *lam, const float *wts, float *Su, float *haloOut,
+                     cudaStream_t s)
+{
+  if (E <= 0) return true;
+  if (!lam) return false;
+  const unsigned grid = (unsigned)((E + fdmtc::EPC - 1) / fdmtc::EPC);
+  const unsigned blk = 32 * fdmtc::EPC;
+#define NRSG_FDMTC(NQ)                                                                                     \
+  if (ras)                                                                                                 \
+    fdmtc_kernel<NQ, true><<<grid, blk, 0, s>>>(E, u, haloSrc, Sx, Sy, Sz, lam, wts, Su, haloOut);        \
+  else                                                                                                     \
+    fdmtc_kernel<NQ, false><<<grid, blk, 0, s>>>(E, u, haloSrc, Sx, Sy, Sz, lam, wts, Su, haloOut);
+  switch (N) {
+  case 3: NRSG_FDMTC(4) break;
+  case 5: NRSG_FDMTC(6) break;
+  case 7: NRSG_FDMTC(8) break;
+  default: return false;
+  }
+#undef NRSG_FDMTC
+  NRSG_CHECK_LAUNCH();
+  return true;
 }
 
 bool launch_fdm8h(long long E, const float *u, const int *haloSrc, const float *Sx, const float *Sy, const float *Sz,

@@ -404,6 +404,12 @@ template <> __global__ void axpby_kernel<double>(long long n, double a, const do
 {
   NRSG_GRID_LOOP(i, n) y[i] = __fma_rn(a, x[i], dmul(b, y[i]));
 }
+// FP32: y = fma(a, x, b*y), the same explicit rounding
+template <> __global__ void axpby_kernel<float>(long long n, float a, const float *__restrict__ x, float b,
+                                                float *__restrict__ y)
+{
+  NRSG_GRID_LOOP(i, n) y[i] = __fmaf_rn(a, x[i], __fmul_rn(b, y[i]));
+}
 template <typename T> __global__ void axmy_kernel(long long n, const T *__restrict__ w, T *__restrict__ x)
 {
   NRSG_GRID_LOOP(i, n) x[i] = w[i] * x[i];

@@ -438,7 +438,8 @@ template <typename T> struct MGImpl : public MGState {
   }
 
   // the fused FDM of one level: FP16 tensor-core transforms (option fdmPrecision = fp16) where they
-  // apply (FP32 multigrid, order 7, RAS), the FP32 kernels otherwise
+  // apply (FP32 multigrid, order 7, RAS), TF32 tensor-core transforms (fdmPrecision = tf32; FP32
+  // multigrid, orders 3, 5, 7), the FP32 kernels otherwise
   void run_fdm(MGLevelDev<T> &v, const T *u, T *Su)
   {
     FieldLevel &L = *v.L;
@@ -446,6 +447,9 @@ template <typename T> struct MGImpl : public MGState {
     if constexpr (std::is_same<T, float>::value) {
       if (el.opt.fdmFp16 && ras && L.N == 7 &&
           launch_fdm8h(L.E, u, v.haloSrc.p, v.Sx.p, v.Sy.p, v.Sz.p, v.lam.p, v.wts.p, Su, s))
+        return;
+      if (el.opt.fdmTf32 && launch_fdm_tf32(L.N, L.E, ras, u, v.haloSrc.p, v.Sx.p, v.Sy.p, v.Sz.p, v.lam.p,
+                                            v.wts.p, Su, v.haloOut.p, s))
         return;
     }
     launch_fdm<T>(L.N, L.E, ras, u, v.haloSrc.p, v.Sx.p, v.Sy.p, v.Sz.p, v.invL.p, v.lam.p, v.wts.p, Su, v.haloOut.p,

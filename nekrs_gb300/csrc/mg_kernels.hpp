@@ -18,6 +18,11 @@ void launch_fdm(int N, long long E, bool ras, const T *u, const int *haloSrc, co
 // order-7 RAS FDM in FP16 on the tensor cores (per-element max-abs scaling); false if not applicable
 bool launch_fdm8h(long long E, const float *u, const int *haloSrc, const float *Sx, const float *Sy, const float *Sz,
                   const float *lam, const float *wts, float *Su, cudaStream_t s);
+// the FDM in TF32 on the tensor cores (orders 3, 5, 7; RAS or ASM; needs the 1-D eigenvalues); false when
+// the level is not covered
+bool launch_fdm_tf32(int N, long long E, bool ras, const float *u, const int *haloSrc, const float *Sx,
+                     const float *Sy, const float *Sz, const float *lam, const float *wts, float *Su, float *haloOut,
+                     cudaStream_t s);
 template <typename T>
 void launch_asm_combine(int N, long long E, const int *haloPartner, const T *haloOut, const T *wts, T *Su,
                         cudaStream_t s);

@@ -432,8 +432,10 @@ Options parse_options(const char *text)
         o.axKernel = v;
       }
       else if (key == "fdmprecision") {
-        if (v != "fp32" && v != "fp16") throw Error(NRSG_ERR_BAD_CONFIG, "fdmPrecision must be fp32 or fp16");
+        if (v != "fp32" && v != "fp16" && v != "tf32")
+          throw Error(NRSG_ERR_BAD_CONFIG, "fdmPrecision must be fp32, fp16 or tf32");
         o.fdmFp16 = (v == "fp16");
+        o.fdmTf32 = (v == "tf32");
       }
       else if (key == "axprecision") {
         if (v != "fp64" && v != "fp32x2") throw Error(NRSG_ERR_BAD_CONFIG, "axPrecision must be fp64 or fp32x2");
