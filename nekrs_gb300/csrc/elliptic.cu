@@ -687,8 +687,9 @@ bool Elliptic::advance(bool block, nrsg_solve_info *info)
       if (status == NRSG_OK && st.it >= opt.maxIter && st.res > st.tol) status = NRSG_ERR_MAXIT;
       if (const int me = mg_error()) {
         status = NRSG_ERR_CUDA;
-        set_last_error(me == 2 ? "pipelined axhelm: a bulk copy did not complete within its wait limit"
-                               : "coarse-level solver: grid barrier wait exceeded its limit");
+        set_last_error(me == 2   ? "pipelined axhelm: a bulk copy did not complete within its wait limit"
+                       : me == 3 ? "tensor-core FDM: an MMA completion wait exceeded its limit"
+                                 : "coarse-level solver: grid barrier wait exceeded its limit");
       }
       lastIters = st.it;
       st.info.iterations = st.it;

@@ -439,7 +439,8 @@ template <typename T> struct MGImpl : public MGState {
 
   // the fused FDM of one level: FP16 tensor-core transforms (option fdmPrecision = fp16) where they
   // apply (FP32 multigrid, order 7, RAS), TF32 tensor-core transforms (fdmPrecision = tf32; FP32
-  // multigrid, orders 3, 5, 7), the FP32 kernels otherwise
+  // multigrid, orders 3, 5, 7; tcgen05.mma for order-7 RAS unless fdmMma = sync, mma.sync otherwise),
+  // the FP32 kernels otherwise
   void run_fdm(MGLevelDev<T> &v, const T *u, T *Su)
   {
     FieldLevel &L = *v.L;
@@ -447,6 +448,9 @@ template <typename T> struct MGImpl : public MGState {
     if constexpr (std::is_same<T, float>::value) {
       if (el.opt.fdmFp16 && ras && L.N == 7 &&
           launch_fdm8h(L.E, u, v.haloSrc.p, v.Sx.p, v.Sy.p, v.Sz.p, v.lam.p, v.wts.p, Su, s))
+        return;
+      if (el.opt.fdmTf32 && el.opt.fdmTcgen05 && ras && L.N == 7 &&
+          launch_fdm_tc(L.E, u, v.haloSrc.p, v.Sx.p, v.Sy.p, v.Sz.p, v.lam.p, v.wts.p, Su, s))
         return;
       if (el.opt.fdmTf32 && launch_fdm_tf32(L.N, L.E, ras, u, v.haloSrc.p, v.Sx.p, v.Sy.p, v.Sz.p, v.lam.p,
                                             v.wts.p, Su, v.haloOut.p, s))
@@ -720,6 +724,7 @@ template <typename T> struct MGImpl : public MGState {
   int error() override
   {
     if (std::is_same<T, float>::value && el.opt.axPipeline && ax_pipe_error(s)) return 2;
+    if (std::is_same<T, float>::value && el.opt.fdmTf32 && el.opt.fdmTcgen05 && fdm_tc_error(s)) return 3;
     if (!persistentCoarse) return 0;
     std::vector<unsigned char> h(coarse_state_bytes());
     NRSG_CUDA(cudaMemcpyAsync(h.data(), cState.p, h.size(), cudaMemcpyDeviceToHost, s));

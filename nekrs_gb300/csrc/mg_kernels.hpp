@@ -23,6 +23,11 @@ bool launch_fdm8h(long long E, const float *u, const int *haloSrc, const float *
 bool launch_fdm_tf32(int N, long long E, bool ras, const float *u, const int *haloSrc, const float *Sx,
                      const float *Sy, const float *Sz, const float *lam, const float *wts, float *Su, float *haloOut,
                      cudaStream_t s);
+// the order-7 RAS FDM in TF32 on the 5th-generation tensor cores (tcgen05.mma, accumulator in tensor
+// memory); false when not applicable.  fdm_tc_error reads and clears its bounded-wait error flag.
+bool launch_fdm_tc(long long E, const float *u, const int *haloSrc, const float *Sx, const float *Sy, const float *Sz,
+                   const float *lam, const float *wts, float *Su, cudaStream_t s);
+unsigned fdm_tc_error(cudaStream_t s);
 template <typename T>
 void launch_asm_combine(int N, long long E, const int *haloPartner, const T *haloOut, const T *wts, T *Su,
                         cudaStream_t s);

@@ -437,6 +437,10 @@ Options parse_options(const char *text)
         o.fdmFp16 = (v == "fp16");
         o.fdmTf32 = (v == "tf32");
       }
+      else if (key == "fdmmma") {
+        if (v != "tcgen05" && v != "sync") throw Error(NRSG_ERR_BAD_CONFIG, "fdmMma must be tcgen05 or sync");
+        o.fdmTcgen05 = (v == "tcgen05");
+      }
       else if (key == "axprecision") {
         if (v != "fp64" && v != "fp32x2") throw Error(NRSG_ERR_BAD_CONFIG, "axPrecision must be fp64 or fp32x2");
         o.axPrecision = v;

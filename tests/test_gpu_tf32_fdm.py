@@ -48,6 +48,39 @@ def test_fdm_tf32_matches_fp32(product_lib, torch_cuda, N, level, schwarz, eps):
     assert err < 1e-2
 
 
+@pytest.mark.parametrize("eps", [0.3, 1.0])
+def test_fdm_tcgen05_matches_mma_sync(product_lib, torch_cuda, eps):
+    """The order-7 RAS FDM on tcgen05.mma (the default for fdmPrecision = tf32) against the mma.sync form of the
+    same TF32 transforms and against the FP32 kernel; E = 5^3 elements, so every persistent CTA (grid = SMs x
+    resident CTAs, larger than E here) takes at most one element, and E = 12^3 below for several per CTA."""
+    torch = torch_cuda
+    N = 7
+    for n in (5, 12):
+        VX, EToV, EToB = W.kershaw_box(n, eps=eps)
+        base = (f"solver=pfcg;preconditioner=multigrid;smootherType=fourthoptcheby+ras;maxIterations=200;"
+                f"pMGSchedule={SCHED[N]};coarseSolver=jpcg;coarseTol=1e-4;mgPrecision=mixed")
+        out = {}
+        for name, o in (("fp32", ";fdmPrecision=fp32"), ("sync", ";fdmPrecision=tf32;fdmMma=sync"),
+                        ("tcgen05", ";fdmPrecision=tf32;fdmMma=tcgen05")):
+            el = G.Elliptic(N, VX, EToV, EToB, base + o)
+            m = el.mg_level_size(0)
+            u = torch.from_numpy(np.random.default_rng(9).uniform(-1, 1, m).astype(np.float32)).cuda()
+            su = torch.full_like(u, float("nan"))
+            el.mg_fdm(0, u, su)
+            torch.cuda.synchronize()
+            out[name] = su.cpu().numpy().astype(np.float64)
+            del el
+        a = out["fp32"]
+        for name in ("sync", "tcgen05"):
+            err = np.max(np.abs(out[name] - a)) / np.max(np.abs(a))
+            print(f"E={n}^3 eps={eps}: {name} TF32 FDM vs FP32: max error {err:.2e} of max |Su|")
+            assert np.isfinite(out[name]).all()
+            assert err < 1e-2
+        d = np.max(np.abs(out["tcgen05"] - out["sync"])) / np.max(np.abs(a))
+        print(f"E={n}^3 eps={eps}: tcgen05 vs mma.sync: {d:.2e}")
+        assert d < 2e-3
+
+
 @pytest.mark.parametrize("schwarz", ["ras", "asm"])
 def test_mixed_tf32_smoother_solve(product_lib, oracle_mod, torch_cuda, schwarz):
     torch = torch_cuda
