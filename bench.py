@@ -52,6 +52,9 @@ WORKLOADS = {
                                 ";mgPrecision=mixed;fdmPrecision=tf32",
                                 "the kershaw48-n7-mixed solve with the multigrid FDM transforms (orders 7 and 3) in "
                                 "TF32 on the tensor cores (mma.sync m16n8k8, FP32 accumulation)"),
+    "kershaw24-n7-mixed-tf32": (24, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
+                                ";mgPrecision=mixed;fdmPrecision=tf32",
+                                "the kershaw48-n7-mixed-tf32 solve on E=24^3 (profiling size)"),
     "kershaw32-n7-mixed": (32, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
                            ";mgPrecision=mixed", "the kershaw48-n7-mixed solve on E=32^3 (profiling size)"),
     "kershaw16-n7-mixed": (16, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
