@@ -43,6 +43,7 @@ extern "C" {
 /* Face boundary types (elliptic.h:46-49); lower id wins at shared nodes. */
 #define NRSG_BC_NONE 0
 #define NRSG_BC_DIRICHLET 1
+#define NRSG_BC_ZERO_NORMAL 2 /* symmetry on a boundary of any orientation (three-field block solve) */
 #define NRSG_BC_NEUMANN 4
 
 typedef struct nrsg_elliptic nrsg_elliptic;
@@ -102,7 +103,14 @@ int nrsg_elliptic_set_coefficients(nrsg_elliptic *el, const double *d_lambda0, c
  * sections, ellipticSetup.cpp:190-199): h_EToB [nFields][E][6] in nekRS face
  * order, e.g. a symmetry plane normal to x masks only the first component.
  * Each field gets its own mask and gather groups; the Jacobi diagonal is
- * rebuilt.  Without this call every field takes the mesh descriptor's EToB. */
+ * rebuilt.  Without this call every field takes the mesh descriptor's EToB.
+ * NRSG_BC_ZERO_NORMAL faces of the first field (three fields only) remove the
+ * normal component of the velocity on boundaries of any orientation: the
+ * node's normal is the average of its zero-normal faces' normals and every
+ * application of the mask projects (u, v, w) onto its tangent plane before
+ * the Dirichlet mask and the gather-scatter (ellipticApplyMask.cpp:19-23,
+ * applyZeroNormalMask.okl, createZeroNormalMask in applyDirichlet.cpp:7-33).
+ * Type 3 (zero-tangential) is rejected with NRSG_ERR_BAD_CONFIG. */
 int nrsg_elliptic_set_field_bcs(nrsg_elliptic *el, const int *h_EToB);
 int nrsg_elliptic_destroy(nrsg_elliptic *el);
 /* Run all later work of `el` on `cuda_stream` (a cudaStream_t; NULL = the

@@ -251,6 +251,9 @@ void Elliptic::op(const double *q, double *Aq)
 
 void Elliptic::gs_mask_fields(double *v)
 {
+  // zero-normal boundaries first, as ellipticApplyMask (ellipticApplyMask.cpp:19-23)
+  if (znNode.n)
+    launch_zero_normal((long long)znNode.n, znNode.p, znReps.p, znFrame.p, znMask.p, fine.Nlocal, v, stream);
   for (int f = 0; f < opt.nfields; ++f)
     launch_gs_mask<double>(fieldPlans.empty() ? fine.gsPlan : fieldPlans[f].plan, v + (size_t)f * fine.Nlocal, true,
                            stream);
@@ -295,11 +298,32 @@ void Elliptic::set_field_bcs(const int *h_EToB)
 {
   if (!h_EToB) throw Error(NRSG_ERR_INVALID, "EToB of the fields required");
   if (opt.nfields < 2) throw Error(NRSG_ERR_BAD_CONFIG, "per-field boundary types need the block solver");
+  bool zeroNormal = false;
+  for (long long q = 0; q < (long long)opt.nfields * fine.E * 6; ++q) {
+    if (h_EToB[q] == 3) throw Error(NRSG_ERR_BAD_CONFIG, "zero-tangential boundaries (type 3) are not supported");
+    zeroNormal = zeroNormal || h_EToB[q] == 2;
+  }
+  // the reference takes unaligned boundaries with the three-component block solver only
+  // (ellipticSetup.cpp:94-110) and reads their faces from the first field's types (setup.cpp:810-817)
+  if (zeroNormal && opt.nfields != 3)
+    throw Error(NRSG_ERR_BAD_CONFIG, "zero-normal boundaries (type 2) need the three-field block solver");
   std::vector<FieldMaskPlan> plans(opt.nfields);
   for (int f = 0; f < opt.nfields; ++f) build_mask_plan(fine, h_EToB + (size_t)f * fine.E * 6, plans[f]);
+  ZeroNormalPlan zn;
+  if (zeroNormal) build_zero_normal(fine, h_EToB, zn);
   NRSG_CUDA(cudaStreamSynchronize(stream));
   graph_release();
   fieldPlans.swap(plans);
+  znNode = DevBuf<int>();
+  znReps = DevBuf<unsigned char>();
+  znFrame = DevBuf<double>();
+  znMask = DevBuf<double>();
+  if (!zn.node.empty()) {
+    znNode.upload(zn.node);
+    znReps.upload(zn.reps);
+    znFrame.upload(zn.frame);
+    znMask.upload(zn.mask);
+  }
   if (opt.precon == "jacobi") build_jacobi();
   NRSG_CUDA(cudaStreamSynchronize(stream));
 }

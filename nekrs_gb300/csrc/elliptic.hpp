@@ -49,6 +49,16 @@ struct FieldMaskPlan {
 };
 void build_mask_plan(const FieldLevel &L, const int *EToB, FieldMaskPlan &P);
 
+// zero-normal (symmetry) boundaries of any orientation, face type 2 of the first field (three fields):
+// one entry per node of an element on the element's zero-normal faces
+struct ZeroNormalPlan {
+  std::vector<int> node;           // E-vector index
+  std::vector<unsigned char> reps; // zero-normal faces of the element through the node
+  std::vector<double> frame;       // n, t1, t2 per entry
+  std::vector<double> mask;        // maskN, maskT1, maskT2 per entry
+};
+void build_zero_normal(const FieldLevel &L, const int *EToB0, ZeroNormalPlan &P);
+
 struct MGState;   // p-multigrid hierarchy (mg.cu)
 struct MGDeleter {
   void operator()(MGState *m) const;
@@ -87,6 +97,9 @@ struct Elliptic {
   bool block_mode() const { return opt.nfields > 1 || coef || opt.stress; }
   void gs_mask_fields(double *v);
   std::vector<FieldMaskPlan> fieldPlans; // empty: every field uses the level's mask
+  DevBuf<int> znNode;                    // zero-normal entries (empty: none)
+  DevBuf<unsigned char> znReps;
+  DevBuf<double> znFrame, znMask;
   void set_field_bcs(const int *h_EToB);
   // null space of the all-Neumann Poisson operator (ellipticSetup.cpp:187-205):
   // remove the E-vector mean from r, z and x (ellipticZeroMean)

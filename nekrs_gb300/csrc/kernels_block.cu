@@ -327,3 +327,44 @@ void launch_block_diag(int N, long long E, int nf, long long offset, long long l
 }
 
 } // namespace nrsg
+
+namespace nrsg {
+
+// zero-normal projection (applyZeroNormalMask.okl): per entry, reps times,
+// R = (U.n) maskN, (U.t1) maskT1, (U.t2) maskT2 and U = R_n n + R_1 t1 + R_2 t2,
+// every product and sum rounded separately in the reference kernel's order
+__global__ void zero_normal_kernel(long long n, const int *__restrict__ node, const unsigned char *__restrict__ reps,
+                                   const double *__restrict__ frame, const double *__restrict__ mask, long long offset,
+                                   double *__restrict__ U)
+{
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const long long id = node[t];
+    const double *fr = frame + 9 * t, *mk = mask + 3 * t;
+    double u = U[id], v = U[id + offset], w = U[id + 2 * offset];
+    for (int r = 0; r < reps[t]; ++r) {
+      const double Rn = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(u, fr[0]), __dmul_rn(v, fr[1])), __dmul_rn(w, fr[2])),
+                                  mk[0]);
+      const double R1 = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(u, fr[3]), __dmul_rn(v, fr[4])), __dmul_rn(w, fr[5])),
+                                  mk[1]);
+      const double R2 = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(u, fr[6]), __dmul_rn(v, fr[7])), __dmul_rn(w, fr[8])),
+                                  mk[2]);
+      u = __dadd_rn(__dadd_rn(__dmul_rn(Rn, fr[0]), __dmul_rn(R1, fr[3])), __dmul_rn(R2, fr[6]));
+      v = __dadd_rn(__dadd_rn(__dmul_rn(Rn, fr[1]), __dmul_rn(R1, fr[4])), __dmul_rn(R2, fr[7]));
+      w = __dadd_rn(__dadd_rn(__dmul_rn(Rn, fr[2]), __dmul_rn(R1, fr[5])), __dmul_rn(R2, fr[8]));
+    }
+    U[id] = u;
+    U[id + offset] = v;
+    U[id + 2 * offset] = w;
+  }
+}
+
+void launch_zero_normal(long long n, const int *node, const unsigned char *reps, const double *frame,
+                        const double *mask, long long offset, double *U, cudaStream_t s)
+{
+  if (n <= 0) return;
+  const long long blocks = (n + 255) / 256;
+  zero_normal_kernel<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, s>>>(n, node, reps, frame, mask, offset, U);
+  NRSG_CHECK_LAUNCH();
+}
+
+} // namespace nrsg

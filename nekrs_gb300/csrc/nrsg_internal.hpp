@@ -191,6 +191,10 @@ void launch_block_ax(int N, long long E, int nf, long long offset, long long lof
 void launch_stress_ax(int N, long long E, long long offset, long long loffset, const double *vgeo, const double *D,
                       const double *lam0, const double *lam1, double l0, double l1, const double *q, double *Aq,
                       cudaStream_t s);
+// zero-normal projection of three fields at offset `offset` on the n entries (U = (U.n) maskN n + (U.t1) maskT1 t1
+// + (U.t2) maskT2 t2, reps times per entry)
+void launch_zero_normal(long long n, const int *node, const unsigned char *reps, const double *frame,
+                        const double *mask, long long offset, double *U, cudaStream_t s);
 void launch_block_diag(int N, long long E, int nf, long long offset, long long loffset, const double *ggeo,
                        const double *D, const double *lam0, const double *lam1, double l0, double l1, bool poisson,
                        double *diag, cudaStream_t s);

@@ -71,6 +71,9 @@ def lib():
         _lib.orc_block_ax.argtypes = [vp, ci, ci, ci, cl, vp, vp, cd, cd, vp, vp]
         _lib.orc_block_diag.argtypes = [vp, ci, ci, cl, vp, vp, cd, cd, vp]
         _lib.orc_block_solve.argtypes = [vp, ci, ci, ci, cl, vp, vp, cd, cd, ci, cd, ci, ci, vp, vp, vp, vp]
+        _lib.orc_zero_normal.argtypes = [vp, vp, vp, vp]
+        _lib.orc_zero_normal.restype = ci
+        _lib.orc_apply_zero_normal.argtypes = [vp, vp, vp]
     return _lib
 
 
@@ -207,6 +210,25 @@ class Elliptic:
                               None if a1 is None else a1.ctypes.data, l0, l1, int(jacobi), tol, int(relative), maxit,
                               None if eb is None else eb.ctypes.data, r.ctypes.data, x.ctypes.data, info.ctypes.data)
         return x, {"iterations": int(info[0]), "res0": info[1], "res": info[2], "status": int(info[3]), "r": r}
+
+    def zero_normal(self, EToB0):
+        """Frames of the zero-normal faces (type 2) of EToB0 [E][6]: sgeo [E][6][Nq^2][9] (n, t1, t2) and the
+        mask [3][Nlocal]; None when no face is zero-normal."""
+        eb = np.ascontiguousarray(EToB0, dtype=np.int32)
+        E = eb.shape[0]
+        nl = self.get("invDegree").size
+        nq = round((nl // E) ** (1 / 3))
+        sgeo = np.zeros((E, 6, nq * nq, 9))
+        mask = np.zeros(3 * nl)
+        if not lib().orc_zero_normal(self.h, eb.ctypes.data, sgeo.ctypes.data, mask.ctypes.data):
+            return None
+        return sgeo, mask
+
+    def apply_zero_normal(self, EToB0, U):
+        eb = np.ascontiguousarray(EToB0, dtype=np.int32)
+        out = np.array(U, dtype=np.float64)
+        lib().orc_apply_zero_normal(self.h, eb.ctypes.data, out.ctypes.data)
+        return out
 
     @property
     def volume(self):

@@ -11,7 +11,8 @@
 //                  (also the stress form's Jacobi, ellipticUpdateJacobi.cpp:63)
 //   solve          ellipticSolve.cpp:32-190 with PCG.cpp:86-203 and
 //                  ellipticBlockUpdatePCG.c over Nfields fields, norms
-//                  weightedNorm2Many (sum over fields, invDegree per node).
+//                  weightedNorm2Many (sum over fields, invDegree per node);
+//                  zero-normal boundaries below (BlockSolver's op and residual).
 #include "oracle_internal.hpp"
 
 #include <cmath>
@@ -233,6 +234,220 @@ void block_diag(const Level &L, const BlockSpec &S, double *diag)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Zero-normal (symmetry) condition on boundaries of any orientation, face type
+// ZERO_NORMAL = 2 (elliptic.h:44-49; only the block solver takes it,
+// ellipticSetup.cpp:94-110), restated from
+//   face normals   kernels/mesh/surfaceGeometricFactorsHex3D.okl: the normal
+//                  of faces t-, s-, r+, s+, r-, t+ is -grad t, -grad s,
+//                  +grad r, +grad s, -grad r, +grad t, normalised
+//   node types     src/bdry/createEToBV.cpp: min over the faces through a
+//                  node (face types > 0), ogsMin, "none" -> 0; taken from the
+//                  first field's types (setup.cpp:810-817)
+//   mask           kernels/nrs/initializeZeroNormalMask.okl: (0, 1, 1) at
+//                  zero-normal nodes, (1, 1, 1) elsewhere
+//   normals        applyDirichlet.cpp:7-33 createZeroNormalMask:
+//                  averageNormalBcType.okl (sum of the zero-normal faces'
+//                  normals and their count per node, per element in face
+//                  order) + ogsAdd, then fixZeroNormalMask.okl (the averaged
+//                  normal, its tangents t1 = (-ny, nx, 0) / |.| or (1, 0, 0)
+//                  when |nz| ~ 1, t2 = n x t1 normalised; its tolerance 1
+//                  makes this branch the only one taken)
+//   application    kernels/nrs/applyZeroNormalMask.okl (per element, face by
+//                  face, each face node: U = (U.n) maskN n + (U.t1) maskT1 t1 +
+//                  (U.t2) maskT2 t2), called first in ellipticApplyMask
+//                  (ellipticApplyMask.cpp:19-23), i.e. before the Dirichlet
+//                  mask and the gather-scatter
+// ---------------------------------------------------------------------------
+struct ZeroNormal {
+  bool active = false;
+  int nq = 0, np = 0;
+  long long E = 0, Nlocal = 0;
+  std::vector<int> EToB0;    // [e][6]
+  std::vector<double> sgeo;  // [e][f][nq * nq][9]: n, t1, t2 of zero-normal faces
+  std::vector<double> mask;  // [3][Nlocal]
+};
+
+static int face_volume_node(int nq, int f, int a, int b)
+{
+  int i, j, k;
+  switch (f) {
+  case 0: i = a; j = b; k = 0; break;
+  case 1: i = a; j = 0; k = b; break;
+  case 2: i = nq - 1; j = a; k = b; break;
+  case 3: i = a; j = nq - 1; k = b; break;
+  case 4: i = 0; j = a; k = b; break;
+  default: i = a; j = b; k = nq - 1; break;
+  }
+  return i + nq * (j + nq * k);
+}
+
+// unit outward normal of face f at volume node n of element e (the reference's surface factors)
+static void face_normal(const Level &L, long long e, int f, int n, double out[3])
+{
+  const int nq = L.Nq, np = L.Np;
+  const int i = n % nq, j = (n / nq) % nq, k = n / (nq * nq);
+  const double *xe = &L.x[e * np], *ye = &L.y[e * np], *ze = &L.zc[e * np], *D = L.D.data();
+  double xr = 0, xs = 0, xt = 0, yr = 0, ys = 0, yt = 0, zr = 0, zs = 0, zt = 0;
+  for (int m = 0; m < nq; ++m) {
+    const int ir = m + nq * (j + nq * k), is = i + nq * (m + nq * k), it = i + nq * (j + nq * m);
+    xr = std::fma(D[i * nq + m], xe[ir], xr);
+    xs = std::fma(D[j * nq + m], xe[is], xs);
+    xt = std::fma(D[k * nq + m], xe[it], xt);
+    yr = std::fma(D[i * nq + m], ye[ir], yr);
+    ys = std::fma(D[j * nq + m], ye[is], ys);
+    yt = std::fma(D[k * nq + m], ye[it], yt);
+    zr = std::fma(D[i * nq + m], ze[ir], zr);
+    zs = std::fma(D[j * nq + m], ze[is], zs);
+    zt = std::fma(D[k * nq + m], ze[it], zt);
+  }
+  auto minor2 = [](double a, double b, double c, double d) { return std::fma(a, b, -(c * d)); };
+  const double cx = minor2(ys, zt, zs, yt), cy = minor2(xs, zt, zs, xt), cz = minor2(xs, yt, ys, xt);
+  const double J = std::fma(zr, cz, std::fma(-yr, cy, xr * cx));
+  const double Ji = 1.0 / J;
+  double g[3];
+  switch (f) {
+  case 0:
+  case 5: // t
+    g[0] = minor2(yr, zs, zr, ys) * Ji, g[1] = -minor2(xr, zs, zr, xs) * Ji, g[2] = minor2(xr, ys, yr, xs) * Ji;
+    break;
+  case 1:
+  case 3: // s
+    g[0] = -minor2(yr, zt, zr, yt) * Ji, g[1] = minor2(xr, zt, zr, xt) * Ji, g[2] = -minor2(xr, yt, yr, xt) * Ji;
+    break;
+  default: // r
+    g[0] = cx * Ji, g[1] = -cy * Ji, g[2] = cz * Ji;
+    break;
+  }
+  const double sgn = (f == 0 || f == 1 || f == 4) ? -1.0 : 1.0;
+  double nx = sgn * g[0], ny = sgn * g[1], nz = sgn * g[2];
+  const double sJ = std::sqrt(nx * nx + ny * ny + nz * nz);
+  const double invSJ = 1.0 / sJ;
+  out[0] = nx * invSJ;
+  out[1] = ny * invSJ;
+  out[2] = nz * invSJ;
+}
+
+void build_zero_normal(const Level &L, const int *EToB0, ZeroNormal &Z)
+{
+  const int nq = L.Nq, np = L.Np, nfp = nq * nq;
+  Z = ZeroNormal();
+  Z.nq = nq;
+  Z.np = np;
+  Z.E = L.E;
+  Z.Nlocal = L.Nlocal;
+  Z.EToB0.assign(EToB0, EToB0 + L.E * 6);
+  for (long long q = 0; q < L.E * 6; ++q)
+    if (EToB0[q] == 2) Z.active = true;
+  if (!Z.active) return;
+  std::vector<int> off, gid;
+  std::vector<double> invd;
+  ogs_setup(L.Nlocal, L.ids.data(), off, gid, invd);
+  // createEToBV
+  const int large = 1 << 20;
+  std::vector<int> bv((size_t)L.Nlocal, large);
+  for (long long e = 0; e < L.E; ++e)
+    for (int f = 0; f < 6; ++f) {
+      const int bc = EToB0[e * 6 + f];
+      if (bc <= 0) continue;
+      for (int n = 0; n < nfp; ++n) {
+        int &v = bv[e * np + face_volume_node(nq, f, n % nq, n / nq)];
+        v = std::min(v, bc);
+      }
+    }
+  for (size_t g = 0; g + 1 < off.size(); ++g) {
+    int v = large;
+    for (int q = off[g]; q < off[g + 1]; ++q) v = std::min(v, bv[gid[q]]);
+    for (int q = off[g]; q < off[g + 1]; ++q) bv[gid[q]] = v;
+  }
+  for (auto &v : bv)
+    if (v == large) v = 0;
+  // initializeZeroNormalMask
+  Z.mask.assign((size_t)3 * L.Nlocal, 1.0);
+  for (long long id = 0; id < L.Nlocal; ++id)
+    if (bv[id] == 2) Z.mask[id] = 0.0;
+  // averageNormalBcType + ogsAdd over the four fields
+  std::vector<double> nrm((size_t)4 * L.Nlocal, 0.0);
+  const long long off4 = L.Nlocal;
+  for (long long e = 0; e < L.E; ++e)
+    for (int f = 0; f < 6; ++f) {
+      if (EToB0[e * 6 + f] != 2) continue;
+      for (int n = 0; n < nfp; ++n) {
+        const int vn = face_volume_node(nq, f, n % nq, n / nq);
+        const long long id = e * np + vn;
+        double fnv[3];
+        face_normal(L, e, f, vn, fnv);
+        nrm[id + 0 * off4] += fnv[0];
+        nrm[id + 1 * off4] += fnv[1];
+        nrm[id + 2 * off4] += fnv[2];
+        nrm[id + 3 * off4] += 1;
+      }
+    }
+  for (int c = 0; c < 4; ++c)
+    for (size_t g = 0; g + 1 < off.size(); ++g) {
+      double v = 0;
+      for (int q = off[g]; q < off[g + 1]; ++q) v += nrm[gid[q] + c * off4];
+      for (int q = off[g]; q < off[g + 1]; ++q) nrm[gid[q] + c * off4] = v;
+    }
+  // fixZeroNormalMask
+  Z.sgeo.assign((size_t)L.E * 6 * nfp * 9, 0.0);
+  for (long long e = 0; e < L.E; ++e)
+    for (int f = 0; f < 6; ++f) {
+      if (EToB0[e * 6 + f] != 2) continue;
+      for (int n = 0; n < nfp; ++n) {
+        const long long id = e * np + face_volume_node(nq, f, n % nq, n / nq);
+        double vx = nrm[id], vy = nrm[id + off4], vz = nrm[id + 2 * off4];
+        const double invCount = 1.0 / nrm[id + 3 * off4];
+        vx *= invCount;
+        vy *= invCount;
+        vz *= invCount;
+        const double mag = std::sqrt(vx * vx + vy * vy + vz * vz);
+        const double invMag = 1.0 / mag;
+        const double nx = vx * invMag, ny = vy * invMag, nz = vz * invMag;
+        double t1x, t1y, t1z;
+        if (std::fabs(std::fabs(nz) - 1.0) < 1e-4) {
+          t1x = 1.0, t1y = 0.0, t1z = 0.0;
+        } else {
+          const double m2 = std::sqrt(nx * nx + ny * ny);
+          t1x = -ny / m2, t1y = nx / m2, t1z = 0.0;
+        }
+        double t2x = ny * t1z - nz * t1y, t2y = nz * t1x - nx * t1z, t2z = nx * t1y - ny * t1x;
+        const double inv2 = 1.0 / std::sqrt(t2x * t2x + t2y * t2y + t2z * t2z);
+        t2x *= inv2;
+        t2y *= inv2;
+        t2z *= inv2;
+        double *sg = &Z.sgeo[(((size_t)e * 6 + f) * nfp + n) * 9];
+        sg[0] = nx, sg[1] = ny, sg[2] = nz;
+        sg[3] = t1x, sg[4] = t1y, sg[5] = t1z;
+        sg[6] = t2x, sg[7] = t2y, sg[8] = t2z;
+      }
+    }
+}
+
+// applyZeroNormalMask on three fields at offset Nlocal
+void apply_zero_normal(const ZeroNormal &Z, double *U)
+{
+  if (!Z.active) return;
+  const int nfp = Z.nq * Z.nq;
+  const long long off = Z.Nlocal;
+  for (long long e = 0; e < Z.E; ++e)
+    for (int f = 0; f < 6; ++f) {
+      if (Z.EToB0[e * 6 + f] != 2) continue;
+      for (int n = 0; n < nfp; ++n) {
+        const long long id = e * Z.np + face_volume_node(Z.nq, f, n % Z.nq, n / Z.nq);
+        const double *sg = &Z.sgeo[(((size_t)e * 6 + f) * nfp + n) * 9];
+        const double mN = Z.mask[id], mT1 = Z.mask[id + off], mT2 = Z.mask[id + 2 * off];
+        const double u = U[id], v = U[id + off], w = U[id + 2 * off];
+        const double Rn = (u * sg[0] + v * sg[1] + w * sg[2]) * mN;
+        const double R1 = (u * sg[3] + v * sg[4] + w * sg[5]) * mT1;
+        const double R2 = (u * sg[6] + v * sg[7] + w * sg[8]) * mT2;
+        U[id] = Rn * sg[0] + R1 * sg[3] + R2 * sg[6];
+        U[id + off] = Rn * sg[1] + R1 * sg[4] + R2 * sg[7];
+        U[id + 2 * off] = Rn * sg[2] + R1 * sg[5] + R2 * sg[8];
+      }
+    }
+}
+
 struct BlockSolver {
   const Level &L;
   BlockSpec S;
@@ -240,6 +455,7 @@ struct BlockSolver {
   bool jacobi;
   // per-field boundary types (elliptic->EToB with Nfields sections): the mask and gather groups of field f
   std::vector<Level> fieldLevels;
+  ZeroNormal zn; // zero-normal faces among the first field's types (three fields)
   const Level &FL(int f) const { return fieldLevels.empty() ? L : fieldLevels[f]; }
   BlockSolver(const Level &L_, const BlockSpec &S_, bool jac, const int *EToBfields = nullptr)
       : L(L_), S(S_), jacobi(jac)
@@ -248,6 +464,7 @@ struct BlockSolver {
       fieldLevels.resize(S.nf);
       for (int f = 0; f < S.nf; ++f)
         build_level(fieldLevels[f], L.N, L.E, L.VX.data(), L.EToV.data(), EToBfields + (size_t)f * L.E * 6);
+      if (S.nf == 3) build_zero_normal(L, EToBfields, zn);
     }
     if (S.stress) vgeo_factors(L, vg);
     const long long n = L.Nlocal * S.nf;
@@ -269,6 +486,7 @@ struct BlockSolver {
   void op(const double *q, double *Aq) const
   {
     ax(q, Aq);
+    apply_zero_normal(zn, Aq);
     for (int f = 0; f < S.nf; ++f) {
       apply_mask(FL(f), Aq + f * L.Nlocal);
       gs_add(FL(f), Aq + f * L.Nlocal);
@@ -285,6 +503,7 @@ struct BlockSolver {
     std::vector<double> x0(x, x + n), Ax0(n), p(n, 0.0), z(n), Ap(n);
     ax(x, Ax0.data());
     for (long long i = 0; i < n; ++i) r[i] = -Ax0[i] + r[i];
+    apply_zero_normal(zn, r);
     for (int f = 0; f < S.nf; ++f) {
       apply_mask(FL(f), r + f * L.Nlocal);
       gs_add(FL(f), r + f * L.Nlocal);
@@ -366,6 +585,28 @@ void orc_block_diag(void *h, int nf, int poisson, long long loffset, const doubl
   const Level &L = ((Elliptic *)h)->fine;
   BlockSolver B(L, make_spec(nf, 0, poisson, loffset, lam0, lam1, l0, l1), true);
   std::memcpy(invDiag, B.invDiag.data(), B.invDiag.size() * sizeof(double));
+}
+
+// zero-normal frames of the first field's types EToB0 ([E][6]): sgeo [E][6][Nq^2][9] (n, t1, t2 on zero-normal
+// faces, 0 elsewhere) and the mask [3][Nlocal]; returns 1 when some face is zero-normal
+int orc_zero_normal(void *h, const int *EToB0, double *sgeo, double *mask)
+{
+  const Level &L = ((Elliptic *)h)->fine;
+  ZeroNormal Z;
+  build_zero_normal(L, EToB0, Z);
+  if (!Z.active) return 0;
+  std::memcpy(sgeo, Z.sgeo.data(), Z.sgeo.size() * sizeof(double));
+  std::memcpy(mask, Z.mask.data(), Z.mask.size() * sizeof(double));
+  return 1;
+}
+
+// applyZeroNormalMask with the frames of EToB0 on three fields U [3][Nlocal]
+void orc_apply_zero_normal(void *h, const int *EToB0, double *U)
+{
+  const Level &L = ((Elliptic *)h)->fine;
+  ZeroNormal Z;
+  build_zero_normal(L, EToB0, Z);
+  apply_zero_normal(Z, U);
 }
 
 // info: iterations, res0, res, status

@@ -154,3 +154,78 @@ def test_block_solve_with_per_field_boundary_types(product_lib, oracle_mod, torc
     on_x = np.isclose(xs, 0.0) | np.isclose(xs, 1.0)
     X = xg.reshape(3, -1)
     assert np.abs(X[0][on_x]).max() == 0.0 and np.abs(X[1][on_x]).max() > 0.0
+
+
+def _rotation():
+    a, b, c = 0.4, -0.7, 1.1
+    Rx = np.array([[1, 0, 0], [0, np.cos(a), -np.sin(a)], [0, np.sin(a), np.cos(a)]])
+    Ry = np.array([[np.cos(b), 0, np.sin(b)], [0, 1, 0], [-np.sin(b), 0, np.cos(b)]])
+    Rz = np.array([[np.cos(c), -np.sin(c), 0], [np.sin(c), np.cos(c), 0], [0, 0, 1]])
+    return Rz @ Ry @ Rx
+
+
+def _zero_normal_x_planes(EToB):
+    E3 = np.stack([EToB.copy() for _ in range(3)])
+    for face in (2, 4):
+        E3[:, :, face] = np.where(EToB[:, face] > 0, 2, 0)
+    return E3
+
+
+def _aligned_symmetry(EToB):
+    E3 = np.stack([EToB.copy() for _ in range(3)])
+    for f in (1, 2):
+        for face in (2, 4):
+            E3[f][:, face] = np.where(EToB[:, face] > 0, 4, 0)
+    return E3
+
+
+@pytest.mark.parametrize("N", [3, 5])
+def test_zero_normal_block_solve(product_lib, oracle_mod, torch_cuda, N):
+    """Zero-normal (symmetry) x-planes on a rotated Kershaw box (face type 2, ellipticApplyMask's
+    applyZeroNormalMask): parity with the oracle's restatement, and the solution is R times the GPU solution of
+    the unrotated problem with aligned symmetry planes (x-component Dirichlet, y and z Neumann)."""
+    torch = torch_cuda
+    n = 3
+    R = _rotation()
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    opts = BASE + ";lambda1=10.0;residualTol=1e-12+relative;maxIterations=5000"
+    ali = G.Elliptic(N, VX, EToV, EToB, opts)
+    rot = G.Elliptic(N, VX @ R.T, EToV, EToB, opts)
+    orc = O.Elliptic(N, VX @ R.T, EToV, EToB, "preconditioner=jacobi")
+    ali.set_field_bcs(_aligned_symmetry(EToB))
+    rot.set_field_bcs(_zero_normal_x_planes(EToB))
+    nl = orc.get("invDegree").size
+    rhs = np.concatenate([W.box_rhs(N, n, n, n, s, orc.get("ggeo")) for s in (21, 22, 23)])
+    rhs_rot = (R @ rhs.reshape(3, nl)).reshape(-1)
+    out = {}
+    for name, el, b in (("aligned", ali, rhs), ("rotated", rot, rhs_rot)):
+        r = torch.from_numpy(b.copy()).cuda()
+        x = torch.zeros_like(r)
+        info = el.solve(r, x)
+        torch.cuda.synchronize()
+        assert info["status"] == 0
+        out[name] = (info, x.cpu().numpy())
+    xo, io = orc.block_solve(rhs_rot, nf=3, stress=False, poisson=False, l0=1.0, l1=10.0, tol=1e-12, relative=True,
+                             maxit=5000, EToB_fields=_zero_normal_x_planes(EToB))
+    ig, xg = out["rotated"]
+    assert io["status"] == 0
+    assert abs(ig["res0"] - io["res0"]) <= 1e-12 * io["res0"]
+    assert abs(ig["iterations"] - io["iterations"]) <= max(1, io["iterations"] // 100)
+    assert rel(xg, xo) < 1e-9
+    want = (R @ out["aligned"][1].reshape(3, nl)).reshape(-1)
+    err = rel(xg, want)
+    print(f"N={N}: rotated zero-normal solve vs rotated aligned solve {err:.2e}; iterations GPU {ig['iterations']}, "
+          f"oracle {io['iterations']}, aligned {out['aligned'][0]['iterations']}")
+    assert err < 1e-9
+
+
+def test_zero_normal_rejections(product_lib, torch_cuda):
+    VX, EToV, EToB = W.kershaw_box(2, eps=0.3)
+    el2 = G.Elliptic(3, VX, EToV, EToB, BASE.replace("pcg+block", "pcg") + ";nFields=2")
+    with pytest.raises(G.NrsgError):
+        el2.set_field_bcs(_zero_normal_x_planes(EToB)[:2])
+    el3 = G.Elliptic(3, VX, EToV, EToB, BASE)
+    E3 = _zero_normal_x_planes(EToB)
+    E3[:, :, 0] = np.where(EToB[:, 0] > 0, 3, 0)  # zero-tangential
+    with pytest.raises(G.NrsgError):
+        el3.set_field_bcs(E3)
