@@ -17,6 +17,7 @@ no data-path collective); `value` sums the ranks' DOFs over the max time.
 """
 import argparse
 import json
+import re
 import os
 import subprocess
 import sys
@@ -32,18 +33,28 @@ SCHED7 = "p=7+degree=2,p=3+degree=2,p=1,p=3+degree=2,p=7+degree=2"
 PMG = "preconditioner=multigrid;smootherType=cheby+asm;pMGSchedule=" + SCHED7 + ";coarseSolver=jpcg;coarseTol=1e-4"
 # mixed-precision headline: optimal 4th-kind Chebyshev (degree 5) over RAS; at E=48^3 it reaches 1e-8 in 26
 # iterations in 0.73 s, against 32 / 0.81 s for optimal 4th-kind (4) + ASM and 76 / 1.54 s for Chebyshev(2) + ASM
-# (measured on the GB300)
+# (measured on the GB300).  Coarse solve: three V-cycles of the algebraic multigrid (the reference's BoomerAMG
+# configuration) on the assembled order-1 operator: 26 iterations, 0.700 s, against 0.714 s with Jacobi-PCG to
+# 1e-4 and 27 iterations / 0.718 s with one V-cycle
 SCHED7_5 = "p=7+degree=5,p=3+degree=5,p=1,p=3+degree=5,p=7+degree=5"
-PMG4 = ("preconditioner=multigrid;smootherType=fourthoptcheby+ras;pMGSchedule=" + SCHED7_5 +
-        ";coarseSolver=jpcg;coarseTol=1e-4")
+PMG4_JPCG = ("preconditioner=multigrid;smootherType=fourthoptcheby+ras;pMGSchedule=" + SCHED7_5 +
+             ";coarseSolver=jpcg;coarseTol=1e-4")
+PMG4 = PMG4_JPCG.replace("coarseSolver=jpcg;coarseTol=1e-4", "coarseSolver=amg;amgIterations=3")
+BPS5 = ("solver=pfgmres+nVector=15;residualTol=1e-8+relative;maxIterations=400;preconditioner=multigrid;"
+        "smootherType=fourthoptcheby+ras;pMGSchedule=p=7+degree=3,p=3+degree=3,p=1,p=3+degree=3,p=7+degree=3;"
+        "mgPrecision=mixed")
+FGMRES_NOTE = "the pressure solver's default flexible GMRES(15)"
 
 # name: (elements per side, N, eps, options, description)
 WORKLOADS = {
     "kershaw48-n7-mixed": (48, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
                            ";mgPrecision=mixed",
                            "Kershaw box E=48^3 N=7 eps=0.3: FP64 flexible PCG, FP32 pMG 7/3/1 (optimal 4th-kind "
-                           "Chebyshev(5)+RAS FDM, coarse Jacobi-PCG 1e-4 on the assembled order-1 operator), "
-                           "FP64-accurate FP32-pair fine operator, to 1e-8 relative"),
+                           "Chebyshev(5)+RAS FDM, coarse solve three algebraic-multigrid V-cycles on the assembled "
+                           "order-1 operator), FP64-accurate FP32-pair fine operator, to 1e-8 relative"),
+    "kershaw48-n7-mixed-jpcg": (48, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4_JPCG +
+                                ";mgPrecision=mixed",
+                                "the kershaw48-n7-mixed solve with the coarse level solved by Jacobi-PCG to 1e-4"),
     "kershaw48-n7-mixed-fp16": (48, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
                                 ";mgPrecision=mixed;fdmPrecision=fp16",
                                 "the kershaw48-n7-mixed solve with the fine-level FDM transforms in FP16 on the tensor "
@@ -51,7 +62,7 @@ WORKLOADS = {
     "kershaw48-n7-mixed-tf32": (48, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
                                 ";mgPrecision=mixed;fdmPrecision=tf32",
                                 "the kershaw48-n7-mixed solve with the multigrid FDM transforms (orders 7 and 3) in "
-                                "TF32 on the tensor cores (mma.sync m16n8k8, FP32 accumulation)"),
+                                "TF32 on the tensor cores (order 7 on tcgen05.mma, order 3 on mma.sync m16n8k8)"),
     "kershaw24-n7-mixed-tf32": (24, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
                                 ";mgPrecision=mixed;fdmPrecision=tf32",
                                 "the kershaw48-n7-mixed-tf32 solve on E=24^3 (profiling size)"),
@@ -59,14 +70,13 @@ WORKLOADS = {
                            ";mgPrecision=mixed", "the kershaw48-n7-mixed solve on E=32^3 (profiling size)"),
     "kershaw16-n7-mixed": (16, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
                            ";mgPrecision=mixed", "the kershaw48-n7-mixed solve on E=16^3 (profiling size)"),
-    "kershaw20-n7-bps5": (20, 7, 0.3, "solver=pfgmres+nVector=15;residualTol=1e-8+relative;maxIterations=400;"
-                          "preconditioner=multigrid;"
-                          "smootherType=fourthoptcheby+ras;pMGSchedule=p=7+degree=3,p=3+degree=3,p=1,p=3+degree=3,"
-                          "p=7+degree=3;coarseSolver=jpcg;coarseTol=1e-4;mgPrecision=mixed",
-                          "the reference's BPS5 case (examples/kershaw: E=20^3, N=7, eps=0.3, the pressure solver's "
-                          "default flexible GMRES(15), RAS + optimal 4th-kind Chebyshev(3), levels 7/3/1, RHS "
-                          "3 pi^2 sin(pi x) sin(pi y) sin(pi z) on [-0.5,0.5]^3, 1e-8), coarse Jacobi-PCG 1e-4 in "
-                          "place of BoomerAMG; the reference reports 28 iterations"),
+    "kershaw20-n7-bps5": (20, 7, 0.3, BPS5 + ";coarseSolver=amg;amgIterations=2",
+                          "the reference's BPS5 case (examples/kershaw: E=20^3, N=7, eps=0.3, " + FGMRES_NOTE +
+                          ", RAS + optimal 4th-kind Chebyshev(3), levels 7/3/1, RHS 3 pi^2 sin(pi x) sin(pi y) "
+                          "sin(pi z) on [-0.5,0.5]^3, 1e-8), coarse solve two algebraic-multigrid V-cycles (the "
+                          "reference: one BoomerAMG V-cycle); the reference reports 28 iterations"),
+    "kershaw20-n7-bps5-jpcg": (20, 7, 0.3, BPS5 + ";coarseSolver=jpcg;coarseTol=1e-4",
+                               "the kershaw20-n7-bps5 solve with the coarse level solved by Jacobi-PCG to 1e-4"),
     "kershaw32-n7-fp64": (32, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG +
                           ";mgPrecision=fp64;axPrecision=fp64",
                           "Kershaw box E=32^3 N=7 eps=0.3: plain FP64 pMG-PCG (flexible), Chebyshev(2)+ASM, "
@@ -199,6 +209,13 @@ def host_cpu():
     return model or "unknown", threads
 
 
+def oracle_options(opts):
+    """Options for the CPU oracle: its coarse level is always solved by Jacobi-PCG (default 1e-4); the library's
+    algebraic-multigrid coarse solve is not restated in the C++ oracle (the reference's own CPU path would run
+    BoomerAMG there)."""
+    return re.sub(r"coarseSolver=amg(;amgIterations=\d+)?", "coarseSolver=jpcg;coarseTol=1e-4", opts)
+
+
 def oracle_solves(nel, N, eps, opts, seed, max_solves, budget_s):
     """Complete CPU-oracle solves (all host threads) of the Kershaw-box workload with `nel`^3 elements: setup
     once (not timed), then solves from x = 0 to the workload's tolerance, each with the oracle's own iteration
@@ -209,7 +226,7 @@ def oracle_solves(nel, N, eps, opts, seed, max_solves, budget_s):
 
     t0 = time.perf_counter()
     VX, EToV, EToB = W.kershaw_box(nel, eps=eps)
-    o = O.Elliptic(N, VX, EToV, EToB, opts)
+    o = O.Elliptic(N, VX, EToV, EToB, oracle_options(opts))
     rhs = W.box_rhs(N, nel, nel, nel, seed, o.get("ggeo"))
     setup_s = time.perf_counter() - t0
     times, info = [], None
@@ -236,7 +253,8 @@ def cpu_sample(nel, N, eps, opts, budget_s=30.0):
             "sample": (f"{len(times)} complete solve(s) of the same solver and options on the {nel_s}^3-element "
                        f"Kershaw box (1/8 of the workload's elements), {info['iterations']} iterations each (the "
                        f"oracle's own count), {t:.1f} s per solve on {threads} host threads; unscaled DOF/s.  "
-                       f"The complete {nel}^3 solve is the reference arm's line"),
+                       f"The complete {nel}^3 solve is the reference arm's line.  Coarse level: the oracle's "
+                       f"Jacobi-PCG to 1e-4"),
             "iterations": int(info["iterations"]), "seconds_per_solve": t, "setup_s": setup_s}
 
 
@@ -265,7 +283,8 @@ def run_reference(args, nel, N, eps, opts, desc):
                                "budget (NRSG_REF_BUDGET_S, default 240 s); no warm-up on the CPU path"},
             "cpu_baseline": {"value": value, "unit": "DOF/s", "cores": threads, "kind": "port", "cpu_model": model,
                              "sample": f"{len(times)} complete solve(s) of the {nel}^3-element workload to its "
-                                       f"tolerance, {info['iterations']} iterations (the oracle's own count)"},
+                                       f"tolerance, {info['iterations']} iterations (the oracle's own count; "
+                                       f"its coarse level by Jacobi-PCG to 1e-4)"},
             "e2e": {"value": value, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -689,7 +708,7 @@ def main():
     t0 = time.perf_counter()
     el = G.Elliptic(N, VX, EToV, EToB, opts)
     setup_s = time.perf_counter() - t0
-    if args.workload.endswith("bps5") or args.mesh:
+    if "bps5" in args.workload or args.mesh:
         # kershaw.udf: P0 = 3 pi^2 sin(pi x) sin(pi y) sin(pi z) at every node of the mesh on [-0.5, 0.5]^3
         xs, ys, zs = (el.get(c) - 0.5 for c in ("x", "y", "z"))
         rhs = 3 * np.pi ** 2 * np.sin(np.pi * xs) * np.sin(np.pi * ys) * np.sin(np.pi * zs)
@@ -845,7 +864,7 @@ def main():
         from oracle import oracle as O
 
         t0 = time.perf_counter()
-        fopts = plain_fp64_options(opts)
+        fopts = oracle_options(plain_fp64_options(opts))
         orc = O.Elliptic(N, VX, EToV, EToB, fopts)
         xo, io = orc.solve(rhs.copy())
         line["error_vs_fp64_oracle"] = {

@@ -237,6 +237,28 @@ double nrsg_host_hessenberg_rho(int n, const double *h_H);
  * h_rowPtr == NULL to get *nrow and *nnz; then capacities are nrow+1
  * (h_rowPtr), nnz (h_cols, h_vals) and E*Np (h_rowOfNode: row of each E-vector
  * node, -1 where masked).  The solver uses it on an order-1 coarsest level. */
+/* Algebraic multigrid of an assembled SPD operator: the coarse solve of
+ * coarseSolver = amg, in the form of the reference's BoomerAMG wrapper
+ * (hypreWrapper.hpp: boomerAMG_t(nrows, nnz, Ai, Aj, Av, ...), solve(b, x);
+ * the settings of coarseLevel.cpp:79-92): classical strength 0.25,
+ * Ruge-Stueben first-pass coarsening, extended+i interpolation (4 entries per
+ * row), Galerkin coarse operators, degree-1 Chebyshev smoothing, dense
+ * coarsest solve.  nrsg_amg_create builds the hierarchy on the host (CSR,
+ * 0-based); nrsg_amg_vcycle runs one V-cycle from x = 0 on the device (FP64
+ * vectors of nrow entries) and synchronises the stream.
+ * nrsg_amg_level_matrix returns level `level`'s operator (which = 0) or its
+ * interpolation from the next level (which = 1); null arrays query the sizes;
+ * lmax is the largest eigenvalue of D^-1 A the smoother uses.  The coarsest
+ * level is level nlevels - 1 (operator only). */
+typedef struct nrsg_amg nrsg_amg;
+int nrsg_amg_create(long long nrow, const long long *h_rowPtr, const long long *h_col, const double *h_val,
+                    nrsg_amg **out);
+int nrsg_amg_destroy(nrsg_amg *a);
+int nrsg_amg_num_levels(const nrsg_amg *a, int *nlevels);
+int nrsg_amg_level_matrix(const nrsg_amg *a, int level, int which, long long *nrow, long long *ncol, long long *nnz,
+                          long long *h_rowPtr, int *h_col, double *h_val, double *lmax);
+int nrsg_amg_vcycle(nrsg_amg *a, const double *d_b, double *d_x, void *stream);
+
 int nrsg_host_assemble_operator(int N, long long E, const long long *h_EToV, const int *h_EToB, const double *h_ggeo,
                                 double lambda0, double lambda1, int poisson, long long *nrow, long long *nnz,
                                 long long *h_rowPtr, long long *h_cols, double *h_vals, long long *h_rowOfNode);

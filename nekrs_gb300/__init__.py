@@ -64,6 +64,12 @@ def lib():
         L.nrsg_host_assemble_galerkin.argtypes = ([ctypes.c_int, LL, vp, vp, vp, ctypes.c_double, ctypes.c_double,
                                                    ctypes.c_int] + [vp] * 6)
         L.nrsg_host_assemble_semfem.argtypes = [ctypes.c_int, LL, vp, vp, vp, ctypes.c_double] + [vp] * 6
+        L.nrsg_amg_create.argtypes = [LL, vp, vp, vp, ctypes.POINTER(vp)]
+        L.nrsg_amg_destroy.argtypes = [vp]
+        L.nrsg_amg_num_levels.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
+        L.nrsg_amg_level_matrix.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(LL), ctypes.POINTER(LL),
+                                            ctypes.POINTER(LL), vp, vp, vp, ctypes.POINTER(ctypes.c_double)]
+        L.nrsg_amg_vcycle.argtypes = [vp, vp, vp, vp]
         L.nrsg_elliptic_create.argtypes = [ctypes.POINTER(MeshDesc), ctypes.c_char_p, ctypes.POINTER(vp)]
         L.nrsg_elliptic_destroy.argtypes = [vp]
         L.nrsg_elliptic_set_stream.argtypes = [vp, vp]
@@ -318,6 +324,48 @@ def host_setup_maps(N, EToV, EToB):
     off = off[: ng.value + 1]
     return {"ids": ids, "maskedIds": masked, "invDegree": inv, "maskIds": mask[: nm.value], "gsOff": off,
             "gsIds": gids[: off[-1]]}
+
+
+class Amg:
+    """Algebraic multigrid of an assembled SPD operator (the coarse solve of coarseSolver = amg): the hierarchy
+    is built on the host at construction (CSR, 0-based), vcycle runs one V-cycle on the device."""
+
+    def __init__(self, rowPtr, cols, vals):
+        rp = np.ascontiguousarray(rowPtr, dtype=np.int64)
+        ci = np.ascontiguousarray(cols, dtype=np.int64)
+        va = np.ascontiguousarray(vals, dtype=np.float64)
+        self.n = len(rp) - 1
+        h = ctypes.c_void_p()
+        check(lib().nrsg_amg_create(self.n, rp.ctypes.data, ci.ctypes.data, va.ctypes.data, ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            lib().nrsg_amg_destroy(self.h)
+            self.h = None
+
+    @property
+    def num_levels(self):
+        n = ctypes.c_int()
+        check(lib().nrsg_amg_num_levels(self.h, ctypes.byref(n)))
+        return n.value
+
+    def level_matrix(self, level, which=0):
+        """(rowPtr, cols, vals, shape, lmax) of level `level`'s operator (which=0) or interpolation (which=1)."""
+        nr, nc, nz = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        lm = ctypes.c_double()
+        check(lib().nrsg_amg_level_matrix(self.h, level, which, ctypes.byref(nr), ctypes.byref(nc), ctypes.byref(nz),
+                                          None, None, None, ctypes.byref(lm)))
+        rp = np.zeros(nr.value + 1, dtype=np.int64)
+        ci = np.zeros(nz.value, dtype=np.int32)
+        va = np.zeros(nz.value)
+        check(lib().nrsg_amg_level_matrix(self.h, level, which, None, None, None, rp.ctypes.data, ci.ctypes.data,
+                                          va.ctypes.data, None))
+        return rp, ci, va, (nr.value, nc.value), lm.value
+
+    def vcycle(self, b, x, stream=None):
+        """One V-cycle from x = 0 on device FP64 vectors (torch tensors or pointers)."""
+        check(lib().nrsg_amg_vcycle(self.h, _ptr(b), _ptr(x), stream))
 
 
 def host_assemble_operator(N, EToV, EToB, ggeo, lambda0=1.0, lambda1=0.0, poisson=True):

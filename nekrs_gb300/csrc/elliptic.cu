@@ -13,6 +13,7 @@
 // host synchronisation per PCG iteration is an 8-byte read of the residual
 // norm for the convergence test.
 
+#include "amg.hpp"
 #include "elliptic.hpp"
 #include "mg_host.hpp"
 
@@ -1277,6 +1278,84 @@ int nrsg_geometric_factors_f64(int N, long long E, const double *VX, double *gge
     dD.upload(D);
     nrsg::launch_geofac(N, E, VX, dz.p, dw.p, dD.p, ggeo, (cudaStream_t)s);
     NRSG_CUDA(cudaStreamSynchronize((cudaStream_t)s));
+  })
+}
+
+} // extern "C"
+
+// ---------------------------------------------------------------------------
+// Algebraic multigrid of an assembled operator (the coarse solve of
+// coarseSolver = amg), in the form of the reference's BoomerAMG wrapper
+// (hypreWrapper.hpp: boomerAMG_t(nrows, nnz, Ai, Aj, Av, ...) and solve(b, x))
+// ---------------------------------------------------------------------------
+struct nrsg_amg {
+  nrsg::AmgHierarchy H;
+  nrsg::AmgDevice<double> D;
+  bool uploaded = false;
+};
+
+extern "C" {
+
+int nrsg_amg_create(long long nrow, const long long *h_rowPtr, const long long *h_col, const double *h_val,
+                    nrsg_amg **out)
+{
+  NRSG_TRY({
+    if (!out || nrow <= 0 || !h_rowPtr || !h_col || !h_val) throw Error(NRSG_ERR_INVALID, "matrix required");
+    auto *a = new nrsg_amg();
+    try {
+      nrsg::amg_build(nrow, h_rowPtr, h_col, h_val, a->H);
+      if (!a->H.invertible) throw Error(NRSG_ERR_INVALID, "algebraic multigrid: singular coarsest operator");
+    } catch (...) {
+      delete a;
+      throw;
+    }
+    *out = a;
+  })
+}
+
+int nrsg_amg_destroy(nrsg_amg *a) { NRSG_TRY(delete a) }
+
+int nrsg_amg_num_levels(const nrsg_amg *a, int *nlevels)
+{
+  NRSG_TRY({
+    if (!a || !nlevels) throw Error(NRSG_ERR_INVALID, "handle required");
+    *nlevels = (int)a->H.levels.size() + 1;
+  })
+}
+
+int nrsg_amg_level_matrix(const nrsg_amg *a, int level, int which, long long *nrow, long long *ncol, long long *nnz,
+                          long long *h_rowPtr, int *h_col, double *h_val, double *lmax)
+{
+  NRSG_TRY({
+    if (!a) throw Error(NRSG_ERR_INVALID, "handle required");
+    const int L = (int)a->H.levels.size();
+    if (level < 0 || level > L || which < 0 || which > 1 || (level == L && which == 1))
+      throw Error(NRSG_ERR_INVALID, "no such level matrix");
+    const nrsg::AmgCsr &M = level == L ? a->H.coarse : (which == 0 ? a->H.levels[level].A : a->H.levels[level].P);
+    if (nrow) *nrow = M.n;
+    if (ncol) *ncol = M.m;
+    if (nnz) *nnz = (long long)M.ci.size();
+    if (h_rowPtr)
+      for (int i = 0; i <= M.n; ++i) h_rowPtr[i] = M.rp[i];
+    if (h_col) std::copy(M.ci.begin(), M.ci.end(), h_col);
+    if (h_val) std::copy(M.v.begin(), M.v.end(), h_val);
+    if (lmax) *lmax = level < L ? a->H.levels[level].lmax : 0.0;
+  })
+}
+
+int nrsg_amg_vcycle(nrsg_amg *a, const double *d_b, double *d_x, void *stream)
+{
+  NRSG_TRY({
+    if (!a || !d_b || !d_x) throw Error(NRSG_ERR_INVALID, "handle and vectors required");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!a->uploaded) {
+      nrsg::amg_upload<double>(a->H, a->D);
+      a->uploaded = true;
+    }
+    const double *x = nrsg::amg_vcycle<double>(a->D, d_b, s);
+    const long long n = a->H.levels.empty() ? a->H.coarse.n : a->H.levels[0].A.n;
+    NRSG_CUDA(cudaMemcpyAsync(d_x, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    NRSG_CUDA(cudaStreamSynchronize(s));
   })
 }
 

@@ -11,6 +11,7 @@
 // runs in the precision T of `mgPrecision` (fp64 or fp32); the coarsest level
 // is solved by Jacobi-PCG in T to `coarseTol` (default 1e-4) or smoothed.
 
+#include "amg.hpp"
 #include "mg_host.hpp"
 
 #include <map>
@@ -78,6 +79,12 @@ template <typename T> struct MGImpl : public MGState {
   DevBuf<PcgScalars> csc;
   // persistent coarse solve (order-1 coarsest level)
   bool persistentCoarse = false;
+  // algebraic multigrid coarse solve (coarseSolver = amg): one V-cycle on the assembled order-1 operator
+  bool amgCoarse = false;
+  AmgDevice<T> amg;
+  DevBuf<int> amgRep, amgRowOf; // row -> representative E-vector node, E-vector node -> row (-1 masked)
+  long long amgRows = 0;
+  std::vector<double> amgInfo;  // rows and nonzeros per level, coarsest last
   static constexpr int kCoarseGridMax = 4096;
   DevBuf<double> cPartials;
   DevBuf<unsigned char> cState;
@@ -159,10 +166,16 @@ template <typename T> struct MGImpl : public MGState {
       cUnknowns = 0;
       for (double w : C.gm.invDegree) cUnknowns += w;
     }
-    persistentCoarse = (C.N == 1) && o.coarse != "smooth" && o.coarsePersistent;
-    if ((o.galerkin || o.semfem) && !persistentCoarse)
+    amgCoarse = o.coarse == "amg";
+    if (amgCoarse && C.N != 1)
+      throw Error(NRSG_ERR_BAD_CONFIG, "coarseSolver = amg needs an order-1 coarsest level");
+    if (amgCoarse && el.allNeumann)
+      throw Error(NRSG_ERR_BAD_CONFIG, "coarseSolver = amg does not take all-Neumann problems (coarseSolver = jpcg)");
+    persistentCoarse = (C.N == 1) && o.coarse != "smooth" && !amgCoarse && o.coarsePersistent;
+    if ((o.galerkin || o.semfem) && !persistentCoarse && !amgCoarse)
       throw Error(NRSG_ERR_BAD_CONFIG, "coarseGridDiscretization FEM+Galerkin / SEMFEM needs an order-1 coarsest level "
-                                       "solved on its assembled operator (coarseSolver = jpcg)");
+                                       "solved on its assembled operator (coarseSolver = jpcg or amg)");
+    if (amgCoarse) build_amg(C);
     if (persistentCoarse) {
       cPartials.alloc(6 * kCoarseGridMax);
       cState.alloc(coarse_state_bytes());
@@ -208,6 +221,63 @@ template <typename T> struct MGImpl : public MGState {
   void build_coarse_matrix(const FieldLevel &C)
   {
     CsrMatrix A;
+    assemble_coarse(C, A);
+    std::vector<int> rep(A.nrow);
+    for (long long r = 0; r < A.nrow; ++r) rep[r] = C.gm.ids[C.gm.off[r]];
+    coarse_matrix_setup<T>(A.nrow, A.rowPtr.data(), A.col.data(), A.val.data(), C.Nlocal, A.rowOfNode.data(),
+                           rep.data(), cA);
+    const long long nv = std::max(A.nrow, 1LL);
+    cx.alloc(nv);
+    cz2.alloc(nv);
+    cz3.alloc(nv);
+  }
+
+  // the algebraic multigrid hierarchy of the assembled coarsest operator and its row maps
+  void build_amg(const FieldLevel &C)
+  {
+    CsrMatrix A;
+    assemble_coarse(C, A);
+    AmgHierarchy H;
+    amg_build(A.nrow, A.rowPtr.data(), A.col.data(), A.val.data(), H);
+    if (!H.invertible) throw Error(NRSG_ERR_INVALID, "algebraic multigrid: singular coarsest operator");
+    amg_upload<T>(H, amg);
+    std::vector<int> rep(A.nrow), rowOf(A.rowOfNode.size());
+    for (long long r = 0; r < A.nrow; ++r) rep[r] = C.gm.ids[C.gm.off[r]];
+    for (size_t i = 0; i < rowOf.size(); ++i) rowOf[i] = (int)A.rowOfNode[i];
+    amgRep.upload(rep);
+    amgRowOf.upload(rowOf);
+    amgRows = A.nrow;
+    amgInfo.clear();
+    for (const auto &L : H.levels) {
+      amgInfo.push_back(L.A.n);
+      amgInfo.push_back((double)L.A.ci.size());
+    }
+    amgInfo.push_back(H.coarse.n);
+    amgInfo.push_back((double)H.coarse.ci.size());
+    if (amgRows > 0) {
+      amgB.alloc(amgRows);
+      amgX.alloc(amgRows);
+      amgR.alloc(amgRows);
+    }
+  }
+  DevBuf<T> amgB;
+
+  // one V-cycle on the assembled unknowns: b (E-vector, assembled) -> rows -> V-cycle -> x (E-vector)
+  void amg_coarse(const T *b, T *x)
+  {
+    launch_rows_gather<T>(amgRows, amgRep.p, b, amgB.p, s);
+    const T *xr = amg_vcycle<T>(amg, amgB.p, s);
+    if (el.opt.amgIterations > 1) {
+      NRSG_CUDA(cudaMemcpyAsync(amgX.p, xr, sizeof(T) * amgRows, cudaMemcpyDeviceToDevice, s));
+      amg_more_cycles<T>(amg, amgB.p, amgX.p, amgR.p, el.opt.amgIterations, s);
+      xr = amgX.p;
+    }
+    launch_rows_scatter<T>((long long)amgRowOf.n, amgRowOf.p, xr, x, s);
+  }
+  DevBuf<T> amgX, amgR;
+
+  void assemble_coarse(const FieldLevel &C, CsrMatrix &A)
+  {
     if (el.opt.galerkin) {
       // B^T A_fine B from the finest level's FP32 operator (ellipticMultiGridSetup.cpp:260-261)
       const std::vector<double> gf = el.fine.d_ggeo64.download();
@@ -224,14 +294,6 @@ template <typename T> struct MGImpl : public MGState {
       const std::vector<double> gg = C.d_ggeo64.download();
       assemble_level(C.N, C.E, C.Dh, gg.data(), el.opt.lambda0, el.opt.lambda1, el.opt.poisson, C.gm, A);
     }
-    std::vector<int> rep(A.nrow);
-    for (long long r = 0; r < A.nrow; ++r) rep[r] = C.gm.ids[C.gm.off[r]];
-    coarse_matrix_setup<T>(A.nrow, A.rowPtr.data(), A.col.data(), A.val.data(), C.Nlocal, A.rowOfNode.data(),
-                           rep.data(), cA);
-    const long long nv = std::max(A.nrow, 1LL);
-    cx.alloc(nv);
-    cz2.alloc(nv);
-    cz3.alloc(nv);
   }
 
   void build_fdm(MGLevelDev<T> &v)
@@ -625,6 +687,8 @@ template <typename T> struct MGImpl : public MGState {
     if (k == base) {
       if (el.opt.coarse == "smooth")
         smooth(v, v.rhs.p, v.x.p, true);
+      else if (amgCoarse)
+        amg_coarse(v.rhs.p, v.x.p);
       else
         coarse_pcg(v, v.rhs.p, v.x.p);
       return;
@@ -704,6 +768,8 @@ template <typename T> struct MGImpl : public MGState {
       for (auto &v : lv)
         if (v.smoothed)
           for (int c = 0; c < kAxVariants; ++c) out.push_back(c < (int)v.axMs.size() ? v.axMs[c] : -1.0);
+    } else if (what == "mg.amgLevels") {
+      out = amgInfo;
     } else if (what == "mg.coarseMatrix") {
       // rows, ELL width, stored nonzeros, row blocks (CTAs), rows per block, matrix in shared memory,
       // thread-block cluster size (0: one CTA or a cooperative launch)
@@ -747,7 +813,7 @@ template <typename T> struct MGImpl : public MGState {
     coarse_pcg(c, c.rhs.p, c.x.p);
   }
   // host-driven coarse iterations read the device between launches: not capturable
-  bool graph_capturable() override { return persistentCoarse || el.opt.coarse == "smooth"; }
+  bool graph_capturable() override { return persistentCoarse || amgCoarse || el.opt.coarse == "smooth"; }
 
   void schwarz(int level, const double *u, double *Su) override
   {

@@ -395,7 +395,15 @@ Options parse_options(const char *text)
       else if (key == "mineigenvalueboundfactor") o.minEigFactor = std::stod(v);
       else if (key == "maxeigenvalueboundfactor") o.maxEigFactor = std::stod(v);
       else if (key == "pmgschedule") o.schedule = v;
-      else if (key == "coarsesolver") o.coarse = v;
+      else if (key == "coarsesolver") {
+        if (v != "jpcg" && v != "smooth" && v != "amg")
+          throw Error(NRSG_ERR_BAD_CONFIG, "coarseSolver must be jpcg, amg or smooth");
+        o.coarse = v;
+      }
+      else if (key == "amgiterations") {
+        o.amgIterations = std::stoi(v);
+        if (o.amgIterations < 1 || o.amgIterations > 16) throw Error(NRSG_ERR_BAD_CONFIG, "amgIterations must be 1..16");
+      }
       else if (key == "coarsegriddiscretization") {
         o.galerkin = (v == "fem+galerkin" || v == "galerkin");
         o.semfem = (v == "semfem");
