@@ -58,4 +58,8 @@ template <typename T> void launch_rows_gather(long long nrow, const int *rep, co
 template <typename T>
 void launch_rows_scatter(long long n, const int *rowOf, const T *rows, T *ev, cudaStream_t s);
 
+// FP64 E-vector -> FP32 rows and back (the SEMFEM preconditioner's pfloat solve)
+void launch_rows_gather_f64_f32(long long nrow, const int *rep, const double *ev, float *rows, cudaStream_t s);
+void launch_rows_scatter_f32_f64(long long n, const int *rowOf, const float *rows, double *ev, cudaStream_t s);
+
 } // namespace nrsg

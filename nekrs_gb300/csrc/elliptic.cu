@@ -197,6 +197,8 @@ Elliptic::Elliptic(const nrsg_mesh_desc *m, const char *options)
     build_jacobi();
   } else if (opt.precon == "multigrid") {
     mg_setup();
+  } else if (opt.precon == "semfem") {
+    semfem_setup();
   }
   if (opt.solver == "pgmres" || opt.solver == "pfgmres") gmres_setup();
   if (opt.projection) {
@@ -381,10 +383,49 @@ void Elliptic::precondition(const double *r, double *zz)
     launch_axmyz<double>(n, r, invDiag.p, zz, stream);
   } else if (opt.precon == "multigrid") {
     mg_apply(r, zz);
+  } else if (opt.precon == "semfem") {
+    // E -> assembled rows (a representative copy), one V-cycle, rows -> every copy (SEMFEMSolver_t::run)
+    launch_rows_gather_f64_f32(sfNrow, sfRep.p, r, sfRows.p, stream);
+    const float *zr = amg_vcycle<float>(*semfem, sfRows.p, stream);
+    launch_rows_scatter_f32_f64(fine.Nlocal, sfRowOf.p, zr, zz, stream);
   } else {
     NRSG_CUDA(cudaMemcpyAsync(zz, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
   }
   if (allNeumann) zero_mean(zz); // ellipticPreconditioner.cpp:82-83
+}
+
+// SEMFEM preconditioner (SEMFEMSolver.cpp:9-158, SEMFEMSolverBuild.cpp): the linear-tetrahedra operator of the
+// fine level's GLL nodes, unmasked nodes as unknowns, solved by one algebraic-multigrid V-cycle in FP32
+void Elliptic::semfem_setup()
+{
+  if (block_mode()) throw Error(NRSG_ERR_BAD_CONFIG, "preconditioner = semfem takes the scalar solve");
+  if (allNeumann)
+    throw Error(NRSG_ERR_BAD_CONFIG, "preconditioner = semfem does not take all-Neumann problems");
+  std::vector<double> X, Y, Z;
+  trilinear_nodes(fine.N, fine.E, fine.VXh.data(), fine.z, X, Y, Z);
+  CsrMatrix A;
+  semfem_assemble(fine.N, fine.E, X.data(), Y.data(), Z.data(), fine.gm, fine.maskIds, opt.lambda0, A);
+  AmgHierarchy H;
+  amg_build(A.nrow, A.rowPtr.data(), A.col.data(), A.val.data(), H);
+  if (!H.invertible) throw Error(NRSG_ERR_INVALID, "algebraic multigrid: singular coarsest operator");
+  semfem.reset(new AmgDevice<float>());
+  amg_upload<float>(H, *semfem);
+  std::vector<int> rep((size_t)A.nrow, -1), rowOf(A.rowOfNode.size());
+  for (size_t i = 0; i < rowOf.size(); ++i) {
+    rowOf[i] = (int)A.rowOfNode[i];
+    if (rowOf[i] >= 0 && rep[(size_t)rowOf[i]] < 0) rep[(size_t)rowOf[i]] = (int)i;
+  }
+  sfRep.upload(rep);
+  sfRowOf.upload(rowOf);
+  sfNrow = A.nrow;
+  sfRows.alloc((size_t)std::max(A.nrow, 1LL));
+  sfInfo.clear();
+  for (const auto &L : H.levels) {
+    sfInfo.push_back(L.A.n);
+    sfInfo.push_back((double)L.A.ci.size());
+  }
+  sfInfo.push_back(H.coarse.n);
+  sfInfo.push_back((double)H.coarse.ci.size());
 }
 
 // ellipticZeroMean (ellipticZeroMean.cpp:31-44): q -= sum(q) / (E Np) over the E-vector
@@ -983,6 +1024,7 @@ int nrsg_elliptic_get(nrsg_elliptic *el, const char *name, void *h_out, long lon
     else if (s == "invDegree") put(L.gm.invDegree);
     else if (s == "D") put(L.Dh);
     else if (s == "history") put(E.history);
+    else if (s == "semfemLevels") put(E.sfInfo);
     else if (s == "deviceBytes") put(std::vector<double>{(double)E.deviceBytes});
     else if (s == "allNeumann") put(std::vector<double>{E.allNeumann ? 1.0 : 0.0});
     else if (s == "proj.vectors") put(std::vector<double>{(double)E.projM, (double)E.projStep});

@@ -1,6 +1,7 @@
 // Solver state of one elliptic problem (the elliptic_t counterpart).
 #pragma once
 
+#include "amg.hpp"
 #include "nrsg_internal.hpp"
 
 #include <memory>
@@ -97,6 +98,14 @@ struct Elliptic {
   bool block_mode() const { return opt.nfields > 1 || coef || opt.stress; }
   void gs_mask_fields(double *v);
   std::vector<FieldMaskPlan> fieldPlans; // empty: every field uses the level's mask
+  // preconditioner = semfem: algebraic multigrid on the low-order (linear tetrahedra) operator of the fine
+  // level's GLL nodes (SEMFEMSolver.cpp), in FP32
+  std::unique_ptr<AmgDevice<float>> semfem;
+  DevBuf<int> sfRep, sfRowOf;
+  DevBuf<float> sfRows;
+  long long sfNrow = 0;
+  std::vector<double> sfInfo; // rows and nonzeros per level
+  void semfem_setup();
   DevBuf<int> znNode;                    // zero-normal entries (empty: none)
   DevBuf<unsigned char> znReps;
   DevBuf<double> znFrame, znMask;

@@ -189,6 +189,34 @@ template <typename T> void amg_more_cycles(AmgDevice<T> &D, const T *b, T *x, T 
   }
 }
 
+template <typename Ti, typename To>
+__global__ void rows_gather_cast_kernel(long long n, const int *rep, const Ti *ev, To *rows)
+{
+  const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (r < n) rows[r] = (To)ev[rep[r]];
+}
+template <typename Ti, typename To>
+__global__ void rows_scatter_cast_kernel(long long n, const int *rowOf, const Ti *rows, To *ev)
+{
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) {
+    const int r = rowOf[i];
+    ev[i] = r >= 0 ? (To)rows[r] : To(0);
+  }
+}
+void launch_rows_gather_f64_f32(long long nrow, const int *rep, const double *ev, float *rows, cudaStream_t s)
+{
+  if (nrow <= 0) return;
+  rows_gather_cast_kernel<double, float><<<amg_grid(nrow), kAmgThreads, 0, s>>>(nrow, rep, ev, rows);
+  NRSG_CHECK_LAUNCH();
+}
+void launch_rows_scatter_f32_f64(long long n, const int *rowOf, const float *rows, double *ev, cudaStream_t s)
+{
+  if (n <= 0) return;
+  rows_scatter_cast_kernel<float, double><<<amg_grid(n), kAmgThreads, 0, s>>>(n, rowOf, rows, ev);
+  NRSG_CHECK_LAUNCH();
+}
+
 template <typename T> void launch_rows_gather(long long nrow, const int *rep, const T *ev, T *rows, cudaStream_t s)
 {
   if (nrow <= 0) return;

@@ -388,7 +388,8 @@ Options parse_options(const char *text)
       } else if (key == "relative") o.relative = std::stoi(v) != 0;
       else if (key == "maxiterations") o.maxIter = std::stoi(v);
       else if (key == "preconditioner") {
-        if (v != "none" && v != "jacobi" && v != "multigrid") throw Error(NRSG_ERR_BAD_CONFIG, "unknown preconditioner '" + v + "'");
+        if (v != "none" && v != "jacobi" && v != "multigrid" && v != "semfem")
+          throw Error(NRSG_ERR_BAD_CONFIG, "unknown preconditioner '" + v + "'");
         o.precon = v;
       } else if (key == "smoothertype") o.smoother = v;
       else if (key == "chebyshevdegree") o.chebyDegree = std::stoi(v);
