@@ -78,3 +78,20 @@ def test_amg_coarse_rejected_for_all_neumann(product_lib, torch_cuda):
     with pytest.raises(G.NrsgError):
         G.Elliptic(3, VX, EToV, EToB, "preconditioner=multigrid;smootherType=cheby+asm;coarseSolver=amg;"
                    "pMGSchedule=p=3+degree=2,p=1,p=3+degree=2")
+
+
+@pytest.mark.parametrize("n", [1, 7, 50])
+def test_amg_dense_only(product_lib, torch_cuda, n):
+    """Operators of at most 50 rows skip coarsening: the V-cycle is the dense coarsest solve alone (exact)."""
+    torch = torch_cuda
+    rng = np.random.default_rng(n)
+    M = rng.standard_normal((n, n))
+    A = sp.csr_matrix(M @ M.T + n * np.eye(n))
+    amg = G.Amg(A.indptr.astype(np.int64), A.indices.astype(np.int64), A.data)
+    assert amg.num_levels == 1
+    b = rng.standard_normal(n)
+    bd = torch.from_numpy(b).cuda()
+    xd = torch.zeros_like(bd)
+    amg.vcycle(bd, xd)
+    want = np.linalg.solve(A.toarray(), b)
+    assert np.abs(xd.cpu().numpy() - want).max() <= 1e-12 * np.abs(want).max()

@@ -51,11 +51,12 @@ def test_fdm_tf32_matches_fp32(product_lib, torch_cuda, N, level, schwarz, eps):
 @pytest.mark.parametrize("eps", [0.3, 1.0])
 def test_fdm_tcgen05_matches_mma_sync(product_lib, torch_cuda, eps):
     """The order-7 RAS FDM on tcgen05.mma (the default for fdmPrecision = tf32) against the mma.sync form of the
-    same TF32 transforms and against the FP32 kernel; E = 5^3 elements, so every persistent CTA (grid = SMs x
-    resident CTAs, larger than E here) takes at most one element, and E = 12^3 below for several per CTA."""
+    same TF32 transforms and against the FP32 kernel; E = 2^3 and 5^3 (every persistent CTA takes at most one
+    element and prefetches no next one: the grid, SMs x resident CTAs, is larger than E) and E = 12^3 (several
+    elements per CTA)."""
     torch = torch_cuda
     N = 7
-    for n in (5, 12):
+    for n in (2, 5, 12):
         VX, EToV, EToB = W.kershaw_box(n, eps=eps)
         base = (f"solver=pfcg;preconditioner=multigrid;smootherType=fourthoptcheby+ras;maxIterations=200;"
                 f"pMGSchedule={SCHED[N]};coarseSolver=jpcg;coarseTol=1e-4;mgPrecision=mixed")
