@@ -256,7 +256,8 @@ __global__ void __launch_bounds__(128, 5)
 // ---------------------------------------------------------------------------
 __constant__ float c_D8[64];
 
-template <bool POISSON>
+// LAM1: lambda0 == 1 (Poisson, the headline), whose multiplies are exact and skipped.
+template <bool POISSON, bool LAM1>
 __global__ void __launch_bounds__(128, 4)
     ax8c_kernel(long long E, const float *__restrict__ ggeo, float lambda0, float lambda1,
                 const float *__restrict__ q, float *__restrict__ Aq)
@@ -320,18 +321,29 @@ __global__ void __launch_bounds__(128, 4)
       qr += Di[m] * qrow[m];
       qs += Dj[m] * qcol[m];
     }
-    s_Gr[el][j][i] = lambda0 * (G00 * qr + G01 * qs + G02 * qt);
-    s_GsT[el][i][j] = lambda0 * (G01 * qr + G11 * qs + G12 * qt);
-    const float Gt = lambda0 * (G02 * qr + G12 * qs + G22 * qt);
+    const float gr = G00 * qr + G01 * qs + G02 * qt;
+    const float gs = G01 * qr + G11 * qs + G12 * qt;
+    const float gt = G02 * qr + G12 * qs + G22 * qt;
+    s_Gr[el][j][i] = LAM1 ? gr : lambda0 * gr;
+    s_GsT[el][i][j] = LAM1 ? gs : lambda0 * gs;
+    const float Gt = LAM1 ? gt : lambda0 * gt;
     float auk = POISSON ? 0.f : GWJ * lambda1 * r_q[k];
     __syncthreads();
     float gsc[NQ], grr[NQ];
     row8(&s_GsT[el][i][0], gsc);
     row8(&s_Gr[el][j][0], grr);
+    // A q update of the 8 planes: independent accumulators, two round-to-nearest fmaf per paired instruction
+    const float2 gt2 = make_float2(Gt, Gt);
+#pragma unroll
+    for (int m = 0; m < NQ; m += 2) {
+      const float2 r = __ffma2_rn(make_float2(c_D8[k * NQ + m], c_D8[k * NQ + m + 1]), gt2,
+                                  make_float2(r_Aq[m], r_Aq[m + 1]));
+      r_Aq[m] = r.x;
+      r_Aq[m + 1] = r.y;
+    }
 #pragma unroll
     for (int m = 0; m < NQ; ++m) {
       auk += DTj[m] * gsc[m];
-      r_Aq[m] += c_D8[k * NQ + m] * Gt;
       auk += DTi[m] * grr[m];
     }
     r_Aq[k] += auk;
@@ -350,10 +362,15 @@ bool launch_ax_const(int N, long long E, const float *ggeo, const float *D, floa
   // D (64 floats, device memory) into the constant bank, ordered on the stream
   NRSG_CUDA(cudaMemcpyToSymbolAsync(c_D8, D, sizeof(float) * 64, 0, cudaMemcpyDeviceToDevice, s));
   const unsigned grid = (unsigned)((E + 1) / 2);
-  if (poisson)
-    ax8c_kernel<true><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, lambda0, lambda1, q, Aq);
+  const bool one = lambda0 == 1.f;
+  if (poisson && one)
+    ax8c_kernel<true, true><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, lambda0, lambda1, q, Aq);
+  else if (poisson)
+    ax8c_kernel<true, false><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, lambda0, lambda1, q, Aq);
+  else if (one)
+    ax8c_kernel<false, true><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, lambda0, lambda1, q, Aq);
   else
-    ax8c_kernel<false><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, lambda0, lambda1, q, Aq);
+    ax8c_kernel<false, false><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, lambda0, lambda1, q, Aq);
   NRSG_CHECK_LAUNCH();
   return true;
 }
