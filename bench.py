@@ -371,15 +371,20 @@ def fdm_roofline(G, el, N, E, peak, ras):
             "fp32_tflops": flops / t / 1e12, "frac_of_hbm": per_el * E / t / 1e9 / peak}
 
 
+COARSE_OPTS = {"jpcg": "coarseSolver=jpcg;coarseTol=1e-4", "amg": "coarseSolver=amg;amgIterations=3"}
+BATCH_COARSE = ["jpcg"]  # set from --coarse-solver
+
+
 def mg_options(N, tol="1e-8"):
     """Mixed-precision pMG-FPCG options for order N (levels N / 3 / 1, or N / 1 for N <= 3), the headline's
-    optimal 4th-kind Chebyshev(5) + RAS, coarse Jacobi-PCG on the assembled order-1 operator."""
+    optimal 4th-kind Chebyshev(5) + RAS, coarse solve on the assembled order-1 operator (Jacobi-PCG to 1e-4 or
+    three algebraic-multigrid V-cycles, --coarse-solver)."""
     mid = {9: 5, 8: 5, 7: 3, 6: 3, 5: 3, 4: 2}.get(N)
     lv = [N] + ([mid] if mid else []) + [1]
     down = [f"p={q}+degree=5" for q in lv[:-1]]
     sched = ",".join(down + ["p=1"] + down[::-1])
     return (f"solver=pfcg;residualTol={tol}+relative;maxIterations=400;preconditioner=multigrid;"
-            f"smootherType=fourthoptcheby+ras;pMGSchedule={sched};coarseSolver=jpcg;coarseTol=1e-4;mgPrecision=mixed")
+            f"smootherType=fourthoptcheby+ras;pMGSchedule={sched};{COARSE_OPTS[BATCH_COARSE[0]]};mgPrecision=mixed")
 
 
 def run_batch(args):
@@ -661,6 +666,8 @@ def main():
     ap.add_argument("--mesh", default=None,
                     help="read the mesh from a Nek5000 .re2 box file (e.g. the reference's kershaw.re2); the "
                          "workload's order, eps and options apply, the right-hand side is the BPS5 one")
+    ap.add_argument("--coarse-solver", default="jpcg", choices=["jpcg", "amg"],
+                    help="coarse solve of the batch and serve workloads' problems")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--oracle-error", action="store_true",
                     help="also solve the same right-hand side with the CPU oracle in FP64 throughout (FP64 "
@@ -670,6 +677,7 @@ def main():
                     help="time the device-resident solves only (no e2e, FP64 comparison or kernel rooflines)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    BATCH_COARSE[0] = args.coarse_solver
     args.workload_name = args.workload
     if args.workload in ("batch", "serve", "velocity", "projection"):
         import torch

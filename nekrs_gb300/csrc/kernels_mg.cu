@@ -189,6 +189,37 @@ __global__ void cheby4_kernel(long long n, T beta, const T *__restrict__ Ad, con
     rout[i] = rin[i] - Ad[i];
   }
 }
+// 4th-kind Chebyshev, x update moved to where each direction is formed:
+// d = c1 Su (first) or fma(c1, Su, c2 d), then x = beta d (xzero) or fma(beta, d, x)
+template <typename T>
+__global__ void cheby4_dx_kernel(long long n, T c1, const T *__restrict__ Su, T c2, T *__restrict__ d, T beta,
+                                 T *__restrict__ x, bool first, bool xzero)
+{
+  MG_LOOP(i, n)
+  {
+    const T dn = first ? mg_mul(c1, Su[i]) : mg_fma(c1, Su[i], mg_mul(c2, d[i]));
+    d[i] = dn;
+    x[i] = xzero ? mg_mul(beta, dn) : mg_fma(beta, dn, x[i]);
+  }
+}
+// rout = rin - Ad (rin may be rout)
+template <typename T> __global__ void cheby4_res_kernel(long long n, const T *__restrict__ Ad, const T *rin, T *rout)
+{
+  MG_LOOP(i, n) rout[i] = rin[i] - Ad[i];
+}
+template <typename T>
+void launch_cheby4_dx(long long n, T c1, const T *Su, T c2, T *d, T beta, T *x, bool first, bool xzero,
+                      cudaStream_t s)
+{
+  cheby4_dx_kernel<T><<<grid_for(n), kT, 0, s>>>(n, c1, Su, c2, d, beta, x, first, xzero);
+  NRSG_CHECK_LAUNCH();
+}
+template <typename T> void launch_cheby4_res(long long n, const T *Ad, const T *rin, T *rout, cudaStream_t s)
+{
+  cheby4_res_kernel<T><<<grid_for(n), kT, 0, s>>>(n, Ad, rin, rout);
+  NRSG_CHECK_LAUNCH();
+}
+
 template <typename T>
 void launch_cheby1_update(long long n, T dc, T rc, const T *SAd, T *d, T *r, T *x, cudaStream_t s)
 {
@@ -1268,6 +1299,8 @@ void launch_random_fill(long long n, unsigned long long seed, double *v, cudaStr
   template void launch_coarsen<T>(int, int, long long, const T *, const T *, T *, cudaStream_t);           \
   template void launch_prolong<T>(int, int, long long, const T *, const T *, T *, cudaStream_t);           \
   template void launch_cheby1_update<T>(long long, T, T, const T *, T *, T *, T *, cudaStream_t);          \
+  template void launch_cheby4_dx<T>(long long, T, const T *, T, T *, T, T *, bool, bool, cudaStream_t);      \
+  template void launch_cheby4_res<T>(long long, const T *, const T *, T *, cudaStream_t);                    \
   template void launch_cheby4_update<T>(long long, T, const T *, const T *, const T *, T *, T *, bool,       \
                                         cudaStream_t);                                                      \
   template void launch_fdm<T>(int, long long, bool, const T *, const int *, const T *, const T *, const T *, \

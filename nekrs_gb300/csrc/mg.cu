@@ -595,28 +595,25 @@ template <typename T> struct MGImpl : public MGState {
     T *res = sRes.p, *Ad = sRes2.p, *d = sUpd.p;
     const double rho = v.lambda1;
     const T *rcur = r;
-    bool xzero = xIsZero;
+    const bool xzero = xIsZero;
     if (!xIsZero) {
       level_op(v, x, res);
       launch_axpby<T>(n, T(1), r, T(-1), res, s);
       rcur = res;
     }
+    // x += beta_k d_k is applied where d_k is formed (the same updates, in the same order, as applying it in
+    // the next step's residual update and once more after the loop)
     apply_S(v, rcur, Ad);
-    launch_scale_copy<T>(n, (T)(4.0 / (3.0 * rho)), Ad, d, s);
+    launch_cheby4_dx<T>(n, (T)(4.0 / (3.0 * rho)), Ad, T(0), d, (T)betas[0], x, true, xzero, s);
     for (int k = 1; k < degree; ++k) {
       level_op(v, d, Ad);
-      launch_cheby4_update<T>(n, (T)betas[k - 1], Ad, d, rcur, res, x, xzero, s);
+      launch_cheby4_res<T>(n, Ad, rcur, res, s);
       rcur = res;
-      xzero = false;
       apply_S(v, res, Ad);
       const T dCoeff = (T)((2.0 * k - 1.0) / (2.0 * k + 3.0));
       const T rCoeff = (T)((8.0 * k + 4.0) / ((2.0 * k + 3.0) * rho));
-      launch_axpby<T>(n, rCoeff, Ad, dCoeff, d, s);
+      launch_cheby4_dx<T>(n, rCoeff, Ad, dCoeff, d, (T)betas[k], x, false, false, s);
     }
-    if (xzero)
-      launch_scale_copy<T>(n, (T)betas.back(), d, x, s);
-    else
-      launch_axpby<T>(n, (T)betas.back(), d, T(1), x, s);
   }
 
   void smooth(MGLevelDev<T> &v, const T *r, T *x, bool xIsZero)

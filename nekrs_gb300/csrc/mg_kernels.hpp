@@ -12,6 +12,12 @@ void launch_cheby1_update(long long n, T dc, T rc, const T *SAd, T *d, T *r, T *
 template <typename T>
 void launch_cheby4_update(long long n, T beta, const T *Ad, const T *d, const T *rin, T *rout, T *x, bool xzero,
                           cudaStream_t s);
+// 4th-kind Chebyshev with the x update where each direction is formed: d = c1 Su (first) or c1 Su + c2 d,
+// x = beta d (xzero) or x + beta d; and the residual update rout = rin - Ad
+template <typename T>
+void launch_cheby4_dx(long long n, T c1, const T *Su, T c2, T *d, T beta, T *x, bool first, bool xzero,
+                      cudaStream_t s);
+template <typename T> void launch_cheby4_res(long long n, const T *Ad, const T *rin, T *rout, cudaStream_t s);
 template <typename T>
 void launch_fdm(int N, long long E, bool ras, const T *u, const int *haloSrc, const T *Sx, const T *Sy, const T *Sz,
                 const T *invL, const T *lam, const T *wts, T *Su, T *haloOut, cudaStream_t s);
