@@ -229,3 +229,29 @@ def test_zero_normal_rejections(product_lib, torch_cuda):
     E3[:, :, 0] = np.where(EToB[:, 0] > 0, 3, 0)  # zero-tangential
     with pytest.raises(G.NrsgError):
         el3.set_field_bcs(E3)
+
+
+def test_zero_normal_stress_block_solve(product_lib, oracle_mod, torch_cuda):
+    """Zero-normal x-planes with the stress (symmetric gradient) block operator: parity with the oracle's
+    restatement (the rotation identity of the test above does not apply: the stress operator's Jacobi diagonal
+    differs per component, and as in the reference the preconditioned vector is not projected)."""
+    torch = torch_cuda
+    N, n = 3, 3
+    R = _rotation()
+    VX, EToV, EToB = W.kershaw_box(n, eps=0.3)
+    opts = BASE + ";lambda1=10.0;residualTol=1e-10+relative;maxIterations=5000;stressFormulation=true"
+    el = G.Elliptic(N, VX @ R.T, EToV, EToB, opts)
+    orc = O.Elliptic(N, VX @ R.T, EToV, EToB, "preconditioner=jacobi")
+    E3 = _zero_normal_x_planes(EToB)
+    el.set_field_bcs(E3)
+    rhs = np.concatenate([W.box_rhs(N, n, n, n, s, orc.get("ggeo")) for s in (31, 32, 33)])
+    r = torch.from_numpy(rhs.copy()).cuda()
+    x = torch.zeros_like(r)
+    ig = el.solve(r, x)
+    torch.cuda.synchronize()
+    xo, io = orc.block_solve(rhs, nf=3, stress=True, poisson=False, l0=1.0, l1=10.0, tol=1e-10, relative=True,
+                             maxit=5000, EToB_fields=E3)
+    assert ig["status"] == 0 and io["status"] == 0
+    assert abs(ig["res0"] - io["res0"]) <= 1e-12 * io["res0"]
+    assert abs(ig["iterations"] - io["iterations"]) <= max(1, io["iterations"] // 100)
+    assert rel(x.cpu().numpy(), xo) < 1e-7
