@@ -31,15 +31,17 @@ sys.path.insert(0, ROOT)
 
 SCHED7 = "p=7+degree=2,p=3+degree=2,p=1,p=3+degree=2,p=7+degree=2"
 PMG = "preconditioner=multigrid;smootherType=cheby+asm;pMGSchedule=" + SCHED7 + ";coarseSolver=jpcg;coarseTol=1e-4"
-# mixed-precision headline: optimal 4th-kind Chebyshev (degree 5) over RAS; at E=48^3 it reaches 1e-8 in 26
-# iterations in 0.73 s, against 32 / 0.81 s for optimal 4th-kind (4) + ASM and 76 / 1.54 s for Chebyshev(2) + ASM
-# (measured on the GB300).  Coarse solve: three V-cycles of the algebraic multigrid (the reference's BoomerAMG
-# configuration) on the assembled order-1 operator: 26 iterations, 0.700 s, against 0.714 s with Jacobi-PCG to
-# 1e-4 and 27 iterations / 0.718 s with one V-cycle
+# mixed-precision headline: optimal 4th-kind Chebyshev over RAS with two algebraic-multigrid V-cycles as
+# the coarse solve; degree 6 at the order-7 and order-3 levels with two V-cycles reaches 1e-8 in 22 iterations
+# (0.663 s) against 26 / 0.681 s for degree 5 with three V-cycles, 23 / 0.677 s for 6 / 5, 22 / 0.674 s for
+# 6 / 7 with one V-cycle, 20 / 0.685 s for 7 / 7 and 31 / 0.705 s for 4 / 5 (GB300, E=48^3); with the Jacobi-PCG
+# coarse solve to 1e-4 and degree 5: 26 iterations, 0.714 s
 SCHED7_5 = "p=7+degree=5,p=3+degree=5,p=1,p=3+degree=5,p=7+degree=5"
+SCHED7_6 = "p=7+degree=6,p=3+degree=6,p=1,p=3+degree=6,p=7+degree=6"
 PMG4_JPCG = ("preconditioner=multigrid;smootherType=fourthoptcheby+ras;pMGSchedule=" + SCHED7_5 +
              ";coarseSolver=jpcg;coarseTol=1e-4")
-PMG4 = PMG4_JPCG.replace("coarseSolver=jpcg;coarseTol=1e-4", "coarseSolver=amg;amgIterations=3")
+PMG4 = ("preconditioner=multigrid;smootherType=fourthoptcheby+ras;pMGSchedule=" + SCHED7_6 +
+        ";coarseSolver=amg;amgIterations=2")
 BPS5 = ("solver=pfgmres+nVector=15;residualTol=1e-8+relative;maxIterations=400;preconditioner=multigrid;"
         "smootherType=fourthoptcheby+ras;pMGSchedule=p=7+degree=3,p=3+degree=3,p=1,p=3+degree=3,p=7+degree=3;"
         "mgPrecision=mixed")
@@ -50,11 +52,12 @@ WORKLOADS = {
     "kershaw48-n7-mixed": (48, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
                            ";mgPrecision=mixed",
                            "Kershaw box E=48^3 N=7 eps=0.3: FP64 flexible PCG, FP32 pMG 7/3/1 (optimal 4th-kind "
-                           "Chebyshev(5)+RAS FDM, coarse solve three algebraic-multigrid V-cycles on the assembled "
+                           "Chebyshev(6)+RAS FDM, coarse solve two algebraic-multigrid V-cycles on the assembled "
                            "order-1 operator), FP64-accurate FP32-pair fine operator, to 1e-8 relative"),
     "kershaw48-n7-mixed-jpcg": (48, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4_JPCG +
                                 ";mgPrecision=mixed",
-                                "the kershaw48-n7-mixed solve with the coarse level solved by Jacobi-PCG to 1e-4"),
+                                "the kershaw48-n7-mixed solve with optimal 4th-kind Chebyshev(5) and the coarse level "
+                                "solved by Jacobi-PCG to 1e-4"),
     "kershaw48-n7-mixed-fp16": (48, 7, 0.3, "solver=pfcg;residualTol=1e-8+relative;maxIterations=400;" + PMG4 +
                                 ";mgPrecision=mixed;fdmPrecision=fp16",
                                 "the kershaw48-n7-mixed solve with the fine-level FDM transforms in FP16 on the tensor "
@@ -345,6 +348,9 @@ def kernel_rooflines(G, el, N, E):
         t = time_kernel(lambda: G.ax_const_f32(N, E, g32, D32, 1.0, 0.0, True, q32, a32, cs), stream)
         out["ax_const_f32"] = {"launch_ms": t * 1e3, "achieved": 32.0 * n / t / 1e9, "unit": "GB/s",
                                "algorithmic_bytes": 32.0 * n}
+        t = time_kernel(lambda: G.ax_const_prefetch_f32(N, E, g32, D32, 1.0, 0.0, True, q32, a32, cs), stream)
+        out["ax_const_prefetch_f32"] = {"launch_ms": t * 1e3, "achieved": 32.0 * n / t / 1e9, "unit": "GB/s",
+                                        "algorithmic_bytes": 32.0 * n}
     for v in out.values():
         v["frac_of_hbm"] = v["achieved"] / peak
     return out, peak, src
@@ -783,9 +789,9 @@ def main():
     peak, psrc = load_peaks()
     tuned = None
     if "multigrid" in opts:
-        names = ["vec", "plain", "epb2", "pipe", "const"]
+        names = ["vec", "plain", "epb2", "pipe", "const", "constpf"]
         ch = el.get("mg.axKernel").astype(int).tolist()
-        tm = el.get("mg.axTimes").reshape(len(ch), 5) if ch else []
+        tm = el.get("mg.axTimes").reshape(len(ch), len(names)) if ch else []
         tuned = [{"level_order": int(o), "chosen": names[c], "ms": {names[k]: (round(float(v), 4) if v > 0 else None)
                                                                     for k, v in enumerate(row)}}
                  for o, c, row in zip(el.get("mg.levels").astype(int).tolist(), ch, tm)]

@@ -358,6 +358,14 @@ int nrsg_ax_pipe_f32(int N, long long E, const float *d_ggeo, const float *d_D, 
  * may overlap must pass the same D.  Other N return NRSG_ERR_INVALID. */
 int nrsg_ax_const_f32(int N, long long E, const float *d_ggeo, const float *d_D, float lambda0, float lambda1,
                       int poisson, const float *d_q, float *d_Aq, void *stream);
+/* nrsg_ax_const_f32 as persistent CTAs (every resident slot of the device)
+ * walking the element pairs; before computing a pair a CTA asks L2 for its
+ * next pair's q and geometric factors (cp.async.bulk.prefetch.L2), so DRAM
+ * reads overlap the contractions.  Bit-identical to nrsg_ax_const_f32; with
+ * d_ggeo or d_q not 16-byte aligned nothing is prefetched.  Other N return
+ * NRSG_ERR_INVALID. */
+int nrsg_ax_const_prefetch_f32(int N, long long E, const float *d_ggeo, const float *d_D, float lambda0,
+                               float lambda1, int poisson, const float *d_q, float *d_Aq, void *stream);
 /* ellipticPartialAxTrilinearHex3D: geometry recomputed from d_VX [E][8][3]. */
 int nrsg_ax_trilinear_f64(int N, long long E, const double *d_VX, const double *d_gllz, const double *d_gllw,
                           const double *d_D, double lambda0, double lambda1, int poisson, const double *d_q,

@@ -102,6 +102,7 @@ def lib():
         L.nrsg_ax_stored_f32.argtypes = [i, LL, vp, vp, f, f, i, vp, vp, vp]
         L.nrsg_ax_pipe_f32.argtypes = [i, LL, vp, vp, f, f, i, vp, vp, vp]
         L.nrsg_ax_const_f32.argtypes = [i, LL, vp, vp, f, f, i, vp, vp, vp]
+        L.nrsg_ax_const_prefetch_f32.argtypes = [i, LL, vp, vp, f, f, i, vp, vp, vp]
         L.nrsg_ax_trilinear_f64.argtypes = [i, LL, vp, vp, vp, vp, d, d, i, vp, vp, vp]
         L.nrsg_ax_trilinear_f32.argtypes = [i, LL, vp, vp, vp, vp, f, f, i, vp, vp, vp]
         L.nrsg_ax_fp32x2.argtypes = [i, LL, vp, vp, d, d, i, vp, vp, vp]
@@ -454,6 +455,11 @@ def ax_pipe_f32(N, E, ggeo, D, lambda0, lambda1, poisson, q, Aq, stream=0):
 
 def ax_const_f32(N, E, ggeo, D, lambda0, lambda1, poisson, q, Aq, stream=0):
     check(lib().nrsg_ax_const_f32(N, E, _ptr(ggeo), _ptr(D), lambda0, lambda1, int(poisson), _ptr(q), _ptr(Aq), stream))
+
+
+def ax_const_prefetch_f32(N, E, ggeo, D, lambda0, lambda1, poisson, q, Aq, stream=0):
+    check(lib().nrsg_ax_const_prefetch_f32(N, E, _ptr(ggeo), _ptr(D), lambda0, lambda1, int(poisson), _ptr(q),
+                                           _ptr(Aq), stream))
 
 
 def ax_trilinear_f64(N, E, VX, z, w, D, lambda0, lambda1, poisson, q, Aq, stream=0):

@@ -1210,6 +1210,12 @@ int nrsg_ax_const_f32(int N, long long E, const float *ggeo, const float *D, flo
   if (N != 7 || E < 1 || !ggeo || !D || !q || !Aq) return NRSG_ERR_INVALID;
   NRSG_TRY(nrsg::launch_ax_const(N, E, ggeo, D, l0, l1, poisson != 0, q, Aq, (cudaStream_t)s))
 }
+int nrsg_ax_const_prefetch_f32(int N, long long E, const float *ggeo, const float *D, float l0, float l1, int poisson,
+                               const float *q, float *Aq, void *s)
+{
+  if (N != 7 || E < 1 || !ggeo || !D || !q || !Aq) return NRSG_ERR_INVALID;
+  NRSG_TRY(nrsg::launch_ax_const(N, E, ggeo, D, l0, l1, poisson != 0, q, Aq, (cudaStream_t)s, true))
+}
 
 int nrsg_elliptic_set_field_bcs(nrsg_elliptic *el, const int *h_EToB)
 {

@@ -257,10 +257,16 @@ __global__ void __launch_bounds__(128, 5)
 __constant__ float c_D8[64];
 
 // LAM1: lambda0 == 1 (Poisson, the headline), whose multiplies are exact and skipped.
-template <bool POISSON, bool LAM1>
+// PF: persistent CTAs walking the element pairs with a stride of the grid; before a pair is
+// computed one thread asks L2 for the next pair of this CTA (cp.async.bulk.prefetch.L2: q and the
+// geometric factors of two elements, two contiguous ranges), so the DRAM reads of the next pair
+// overlap the contractions of this one instead of every resident CTA waiting on DRAM at the same
+// time.  Without PF the grid has one CTA per pair and the loop runs once.  pf: the two ranges are
+// 16-byte aligned (the bulk prefetch's requirement); when not, nothing is prefetched.
+template <bool POISSON, bool LAM1, bool PF>
 __global__ void __launch_bounds__(128, 4)
     ax8c_kernel(long long E, const float *__restrict__ ggeo, float lambda0, float lambda1,
-                const float *__restrict__ q, float *__restrict__ Aq)
+                const float *__restrict__ q, float *__restrict__ Aq, bool pf)
 {
   constexpr int NQ = 8, NP = 512, EPB = 2, RT = 12;
   __shared__ __align__(16) float s_q[EPB][NQ][NQ];
@@ -271,8 +277,6 @@ __global__ void __launch_bounds__(128, 4)
   const int t = threadIdx.x;
   const int i = t % NQ, j = t / NQ;
   const int el = threadIdx.y;
-  const long long e = (long long)blockIdx.x * EPB + el;
-  const bool active = e < E;
   float Di[NQ], Dj[NQ], DTi[NQ], DTj[NQ];
 #pragma unroll
   for (int m = 0; m < NQ; ++m) {
@@ -281,96 +285,143 @@ __global__ void __launch_bounds__(128, 4)
     DTi[m] = c_D8[m * NQ + i];
     DTj[m] = c_D8[m * NQ + j];
   }
-  float r_q[NQ], r_Aq[NQ];
-  const long long base = e * NP + t;
-#pragma unroll
-  for (int k = 0; k < NQ; ++k) {
-    r_q[k] = active ? q[base + k * NQ * NQ] : 0.f;
-    r_Aq[k] = 0;
-  }
   constexpr int NG = POISSON ? 6 : 7;
-  const float *g = ggeo + e * 7 * NP + t;
-  float gpre[NG * NQ];
+  const long long npairs = (E + EPB - 1) / EPB;
+  // one element pair: the whole computation (a lambda, so the single-pass form compiles to straight-line code)
+  auto pair = [&](const long long pr) {
+    if (PF && pf && t == 0 && el == 0 && pr + gridDim.x < npairs) {
+      // the factors this kernel reads (six for Poisson: the seventh, GWJ, is skipped) and q
+      const long long en = (pr + gridDim.x) * EPB;
+      const int cnt = E - en < EPB ? (int)(E - en) : EPB;
+      for (int c = 0; c < cnt; ++c)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(ggeo + (en + c) * 7 * NP),
+                     "r"((unsigned)(NG * NP * sizeof(float)))
+                     : "memory");
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(q + en * NP),
+                   "r"((unsigned)(cnt * NP * sizeof(float)))
+                   : "memory");
+    }
+    const long long e = pr * EPB + el;
+    const bool active = e < E;
+    float r_q[NQ], r_Aq[NQ];
+    const long long base = e * NP + t;
 #pragma unroll
-  for (int k = 0; k < NQ; ++k)
+    for (int k = 0; k < NQ; ++k) {
+      r_q[k] = active ? q[base + k * NQ * NQ] : 0.f;
+      r_Aq[k] = 0;
+    }
+    const float *g = ggeo + e * 7 * NP + t;
+    float gpre[NG * NQ];
 #pragma unroll
-    for (int c = 0; c < NG; ++c) gpre[c * NQ + k] = active ? __ldg(g + c * NP + k * NQ * NQ) : 0.f;
+    for (int k = 0; k < NQ; ++k)
+#pragma unroll
+      for (int c = 0; c < NG; ++c) gpre[c * NQ + k] = active ? __ldg(g + c * NP + k * NQ * NQ) : 0.f;
 
-  auto row8 = [](const float *p, float (&v)[NQ]) {
-    const float4 a = *reinterpret_cast<const float4 *>(p);
-    const float4 b = *reinterpret_cast<const float4 *>(p + 4);
-    v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+    auto row8 = [](const float *p, float (&v)[NQ]) {
+      const float4 a = *reinterpret_cast<const float4 *>(p);
+      const float4 b = *reinterpret_cast<const float4 *>(p + 4);
+      v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+    };
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      const float G00 = gpre[0 * NQ + k], G01 = gpre[1 * NQ + k], G11 = gpre[2 * NQ + k];
+      const float G12 = gpre[3 * NQ + k], G02 = gpre[4 * NQ + k], G22 = gpre[5 * NQ + k];
+      const float GWJ = POISSON ? 0.f : gpre[(NG - 1) * NQ + k];
+      s_q[el][j][i] = r_q[k];
+      s_qT[el][i][j] = r_q[k];
+      float qt = 0;
+#pragma unroll
+      for (int m = 0; m < NQ; ++m) qt += c_D8[k * NQ + m] * r_q[m];
+      __syncthreads();
+      float qrow[NQ], qcol[NQ];
+      row8(&s_q[el][j][0], qrow);
+      row8(&s_qT[el][i][0], qcol);
+      float qr = 0, qs = 0;
+#pragma unroll
+      for (int m = 0; m < NQ; ++m) {
+        qr += Di[m] * qrow[m];
+        qs += Dj[m] * qcol[m];
+      }
+      const float gr = G00 * qr + G01 * qs + G02 * qt;
+      const float gs = G01 * qr + G11 * qs + G12 * qt;
+      const float gt = G02 * qr + G12 * qs + G22 * qt;
+      s_Gr[el][j][i] = LAM1 ? gr : lambda0 * gr;
+      s_GsT[el][i][j] = LAM1 ? gs : lambda0 * gs;
+      const float Gt = LAM1 ? gt : lambda0 * gt;
+      float auk = POISSON ? 0.f : GWJ * lambda1 * r_q[k];
+      __syncthreads();
+      float gsc[NQ], grr[NQ];
+      row8(&s_GsT[el][i][0], gsc);
+      row8(&s_Gr[el][j][0], grr);
+      // A q update of the 8 planes: independent accumulators, two round-to-nearest fmaf per paired instruction
+      const float2 gt2 = make_float2(Gt, Gt);
+#pragma unroll
+      for (int m = 0; m < NQ; m += 2) {
+        const float2 r = __ffma2_rn(make_float2(c_D8[k * NQ + m], c_D8[k * NQ + m + 1]), gt2,
+                                    make_float2(r_Aq[m], r_Aq[m + 1]));
+        r_Aq[m] = r.x;
+        r_Aq[m + 1] = r.y;
+      }
+#pragma unroll
+      for (int m = 0; m < NQ; ++m) {
+        auk += DTj[m] * gsc[m];
+        auk += DTi[m] * grr[m];
+      }
+      r_Aq[k] += auk;
+      __syncthreads();
+    }
+    if (active) {
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) Aq[base + k * NQ * NQ] = r_Aq[k];
+    }
   };
-#pragma unroll
-  for (int k = 0; k < NQ; ++k) {
-    const float G00 = gpre[0 * NQ + k], G01 = gpre[1 * NQ + k], G11 = gpre[2 * NQ + k];
-    const float G12 = gpre[3 * NQ + k], G02 = gpre[4 * NQ + k], G22 = gpre[5 * NQ + k];
-    const float GWJ = POISSON ? 0.f : gpre[(NG - 1) * NQ + k];
-    s_q[el][j][i] = r_q[k];
-    s_qT[el][i][j] = r_q[k];
-    float qt = 0;
-#pragma unroll
-    for (int m = 0; m < NQ; ++m) qt += c_D8[k * NQ + m] * r_q[m];
-    __syncthreads();
-    float qrow[NQ], qcol[NQ];
-    row8(&s_q[el][j][0], qrow);
-    row8(&s_qT[el][i][0], qcol);
-    float qr = 0, qs = 0;
-#pragma unroll
-    for (int m = 0; m < NQ; ++m) {
-      qr += Di[m] * qrow[m];
-      qs += Dj[m] * qcol[m];
-    }
-    const float gr = G00 * qr + G01 * qs + G02 * qt;
-    const float gs = G01 * qr + G11 * qs + G12 * qt;
-    const float gt = G02 * qr + G12 * qs + G22 * qt;
-    s_Gr[el][j][i] = LAM1 ? gr : lambda0 * gr;
-    s_GsT[el][i][j] = LAM1 ? gs : lambda0 * gs;
-    const float Gt = LAM1 ? gt : lambda0 * gt;
-    float auk = POISSON ? 0.f : GWJ * lambda1 * r_q[k];
-    __syncthreads();
-    float gsc[NQ], grr[NQ];
-    row8(&s_GsT[el][i][0], gsc);
-    row8(&s_Gr[el][j][0], grr);
-    // A q update of the 8 planes: independent accumulators, two round-to-nearest fmaf per paired instruction
-    const float2 gt2 = make_float2(Gt, Gt);
-#pragma unroll
-    for (int m = 0; m < NQ; m += 2) {
-      const float2 r = __ffma2_rn(make_float2(c_D8[k * NQ + m], c_D8[k * NQ + m + 1]), gt2,
-                                  make_float2(r_Aq[m], r_Aq[m + 1]));
-      r_Aq[m] = r.x;
-      r_Aq[m + 1] = r.y;
-    }
-#pragma unroll
-    for (int m = 0; m < NQ; ++m) {
-      auk += DTj[m] * gsc[m];
-      auk += DTi[m] * grr[m];
-    }
-    r_Aq[k] += auk;
-    __syncthreads();
-  }
-  if (active) {
-#pragma unroll
-    for (int k = 0; k < NQ; ++k) Aq[base + k * NQ * NQ] = r_Aq[k];
+  if constexpr (PF) {
+    for (long long pr = blockIdx.x; pr < npairs; pr += gridDim.x) pair(pr);
+  } else {
+    pair(blockIdx.x);
   }
 }
 
+template <bool PF>
+static void ax8c_launch(unsigned grid, long long E, const float *ggeo, float lambda0, float lambda1, bool poisson,
+                        const float *q, float *Aq, bool pf, cudaStream_t s)
+{
+  const bool one = lambda0 == 1.f;
+  if (poisson && one)
+    ax8c_kernel<true, true, PF><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, lambda0, lambda1, q, Aq, pf);
+  else if (poisson)
+    ax8c_kernel<true, false, PF><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, lambda0, lambda1, q, Aq, pf);
+  else if (one)
+    ax8c_kernel<false, true, PF><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, lambda0, lambda1, q, Aq, pf);
+  else
+    ax8c_kernel<false, false, PF><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, lambda0, lambda1, q, Aq, pf);
+}
+
 bool launch_ax_const(int N, long long E, const float *ggeo, const float *D, float lambda0, float lambda1,
-                     bool poisson, const float *q, float *Aq, cudaStream_t s)
+                     bool poisson, const float *q, float *Aq, cudaStream_t s, bool prefetch)
 {
   if (N != 7 || E <= 0) return false;
   // D (64 floats, device memory) into the constant bank, ordered on the stream
   NRSG_CUDA(cudaMemcpyToSymbolAsync(c_D8, D, sizeof(float) * 64, 0, cudaMemcpyDeviceToDevice, s));
-  const unsigned grid = (unsigned)((E + 1) / 2);
-  const bool one = lambda0 == 1.f;
-  if (poisson && one)
-    ax8c_kernel<true, true><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, lambda0, lambda1, q, Aq);
-  else if (poisson)
-    ax8c_kernel<true, false><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, lambda0, lambda1, q, Aq);
-  else if (one)
-    ax8c_kernel<false, true><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, lambda0, lambda1, q, Aq);
-  else
-    ax8c_kernel<false, false><<<grid, dim3(64, 2), 0, s>>>(E, ggeo, lambda0, lambda1, q, Aq);
+  const long long npairs = (E + 1) / 2;
+  if (!prefetch) {
+    ax8c_launch<false>((unsigned)npairs, E, ggeo, lambda0, lambda1, poisson, q, Aq, false, s);
+  } else {
+    // persistent: every resident CTA slot of the device (4 per SM at 128 registers a thread)
+    static int slots[64] = {0};
+    int dev = 0;
+    NRSG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return false;
+    if (slots[dev] == 0) {
+      int sms = 0, per = 0;
+      NRSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+      NRSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ax8c_kernel<true, true, true>, 128, 0));
+      slots[dev] = sms * std::max(per, 1);
+    }
+    const unsigned grid = (unsigned)std::min<long long>(npairs, slots[dev]);
+    const bool aligned = ((reinterpret_cast<uintptr_t>(ggeo) | reinterpret_cast<uintptr_t>(q)) & 15) == 0;
+    ax8c_launch<true>(grid, E, ggeo, lambda0, lambda1, poisson, q, Aq, aligned, s);
+  }
   NRSG_CHECK_LAUNCH();
   return true;
 }
@@ -788,6 +839,7 @@ void launch_ax_stored(int N, long long E, const T *ggeo, const T *D, T lambda0, 
 // kAxEpb2  the plain kernel at twice the elements per CTA
 // kAxPipe  the bulk-copy pipelined kernel (order 7 Poisson only)
 // kAxConst D in constant memory and registers (order 7 only)
+// kAxConstPf the same kernel as persistent CTAs prefetching their next element pair into L2
 // Returns false where the variant does not apply.
 bool launch_ax_f32_variant(int variant, int N, long long E, const float *ggeo, const float *D, float lambda0,
                            float lambda1, bool poisson, const float *q, float *Aq, cudaStream_t s)
@@ -797,6 +849,7 @@ bool launch_ax_f32_variant(int variant, int N, long long E, const float *ggeo, c
   case kAxVec: launch_ax_stored<float>(N, E, ggeo, D, lambda0, lambda1, poisson, q, Aq, s); return true;
   case kAxPipe: return launch_ax_pipe(N, E, ggeo, D, lambda0, lambda1, poisson, q, Aq, s);
   case kAxConst: return launch_ax_const(N, E, ggeo, D, lambda0, lambda1, poisson, q, Aq, s);
+  case kAxConstPf: return launch_ax_const(N, E, ggeo, D, lambda0, lambda1, poisson, q, Aq, s, true);
   case kAxPlain:
   case kAxEpb2: break;
   default: return false;

@@ -447,6 +447,7 @@ template <typename T> struct MGImpl : public MGState {
       else if (want == "epb2") v.axVariant = kAxEpb2;
       else if (want == "pipe") v.axVariant = kAxPipe;
       else if (want == "const") v.axVariant = kAxConst;
+      else if (want == "constpf") v.axVariant = kAxConstPf;
       if (want != "auto" || el.opt.axConst || el.opt.axPipeline) return;
       int dev = 0;
       NRSG_CUDA(cudaGetDevice(&dev));

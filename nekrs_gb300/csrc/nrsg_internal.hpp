@@ -108,7 +108,7 @@ struct Options {
   bool graphs = true;               // CUDA graphs of the steady-state PCG iteration (non-legacy streams)
   bool axPipeline = false;          // FP32 order-7 levels: bulk-copy pipelined axhelm
   bool axConst = false;             // FP32 order-7 levels: axhelm with D in constant memory / registers
-  std::string axKernel = "auto";    // FP32 level axhelm: auto (timed at setup) | vec | plain | epb2 | pipe | const
+  std::string axKernel = "auto";    // FP32 level axhelm: auto (timed at setup) | vec | plain | epb2 | pipe | const | constpf
   int nfields = 1;                  // block solver: fields at fieldOffset = Nlocal ("solver = pcg+block" -> 3)
   bool stress = false;              // stressFormulation: symmetric-gradient operator (nfields = 3)
   int projection = 0;               // initialGuess: 0 none, 1 projection (classic), 2 projectionAconj
@@ -208,11 +208,12 @@ bool launch_ax_pipe(int N, long long E, const float *ggeo, const float *D, float
 unsigned ax_pipe_error(cudaStream_t s);
 // FP32 order-7 Poisson / Helmholtz axhelm with D in constant memory and registers (false: not
 // applicable).  D is copied into one constant bank per launch: concurrent launches must pass the same D.
+// prefetch: persistent CTAs that prefetch their next element pair into L2 (same results).
 bool launch_ax_const(int N, long long E, const float *ggeo, const float *D, float lambda0, float lambda1,
-                     bool poisson, const float *q, float *Aq, cudaStream_t s);
+                     bool poisson, const float *q, float *Aq, cudaStream_t s, bool prefetch = false);
 template <typename T> void launch_mask(long long n, const int *ids, T *q, cudaStream_t s);
 // FP32 axhelm variants the multigrid autotuner chooses between (identical results)
-enum AxVariant { kAxVec = 0, kAxPlain = 1, kAxEpb2 = 2, kAxPipe = 3, kAxConst = 4, kAxVariants = 5 };
+enum AxVariant { kAxVec = 0, kAxPlain = 1, kAxEpb2 = 2, kAxPipe = 3, kAxConst = 4, kAxConstPf = 5, kAxVariants = 6 };
 bool launch_ax_f32_variant(int variant, int N, long long E, const float *ggeo, const float *D, float lambda0,
                            float lambda1, bool poisson, const float *q, float *Aq, cudaStream_t s);
 // autotuner helpers: a reproducible [-1, 1) test vector; count entries whose bits differ

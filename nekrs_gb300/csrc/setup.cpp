@@ -436,8 +436,8 @@ Options parse_options(const char *text)
       else if (key == "residualprojectionstart") o.projStart = std::stoi(v);
       else if (key == "mgprecision") o.mgPrecision = v;
       else if (key == "axkernel") {
-        if (v != "auto" && v != "vec" && v != "plain" && v != "epb2" && v != "pipe" && v != "const")
-          throw Error(NRSG_ERR_BAD_CONFIG, "axKernel must be auto, vec, plain, epb2, pipe or const");
+        if (v != "auto" && v != "vec" && v != "plain" && v != "epb2" && v != "pipe" && v != "const" && v != "constpf")
+          throw Error(NRSG_ERR_BAD_CONFIG, "axKernel must be auto, vec, plain, epb2, pipe, const or constpf");
         o.axKernel = v;
       }
       else if (key == "fdmprecision") {

@@ -242,11 +242,13 @@ def test_mg_solve_same_with_and_without_ax_pipeline(product_lib, torch_cuda, var
     assert torch.equal(xa, xb)
 
 
-@pytest.mark.parametrize("E", [1, 2, 7, 1000])
+@pytest.mark.parametrize("E", [1, 2, 7, 1000, 2433])
 @pytest.mark.parametrize("poisson", [True, False])
-def test_ax_const_f32_bit_identical(product_lib, torch_cuda, E, poisson):
+@pytest.mark.parametrize("prefetch", [False, True])
+def test_ax_const_f32_bit_identical(product_lib, torch_cuda, E, poisson, prefetch):
     """The FP32 order-7 axhelm with D in constant memory and registers equals the default kernel bit for bit
-    (same operands, same operation order)."""
+    (same operands, same operation order); so does its persistent form that prefetches each CTA's next
+    element pair into L2 (E = 2433: more pairs than resident CTAs, an odd last pair)."""
     torch = torch_cuda
     N, Np = 7, 512
     gen = torch.Generator(device="cuda").manual_seed(3 * E + poisson)
@@ -257,6 +259,6 @@ def test_ax_const_f32_bit_identical(product_lib, torch_cuda, E, poisson):
     a_c = torch.full_like(q, float("nan"))
     cs = torch.cuda.current_stream().cuda_stream
     G.ax_stored_f32(N, E, g, D, 1.3, 0.7, poisson, q, a_ref, cs)
-    G.ax_const_f32(N, E, g, D, 1.3, 0.7, poisson, q, a_c, cs)
+    (G.ax_const_prefetch_f32 if prefetch else G.ax_const_f32)(N, E, g, D, 1.3, 0.7, poisson, q, a_c, cs)
     torch.cuda.synchronize()
     assert torch.equal(a_ref, a_c)

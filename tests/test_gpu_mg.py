@@ -250,11 +250,11 @@ def test_axhelm_autotuner(product_lib, torch_cuda, N):
     for kern in ("auto", "vec"):
         el = G.Elliptic(N, VX, EToV, EToB, base + f";axKernel={kern}")
         chosen = el.get("mg.axKernel")
-        times = el.get("mg.axTimes").reshape(len(chosen), 5)
+        times = el.get("mg.axTimes").reshape(len(chosen), 6)
         if kern == "auto":
             assert (times[:, 0] > 0).all() and (times[:, 1] > 0).all()  # default and plain always apply
             if N == 7:
-                assert (times[0] > 0).sum() >= 4                          # vec, plain, epb2 and const on order 7
+                assert (times[0] > 0).sum() >= 5                          # vec, plain, epb2, const, constpf
             for lvl, c in enumerate(chosen.astype(int)):
                 ok = times[lvl] > 0
                 assert ok[c] and times[lvl, c] == times[lvl][ok].min()
