@@ -983,7 +983,7 @@ int nrsg_elliptic_gs(nrsg_elliptic *el, double *d_q)
   if (!el || !d_q) return NRSG_ERR_INVALID;
   NRSG_TRY({
     auto &E = *el->impl;
-    nrsg::launch_gs<double>(E.fine.ngroups, E.fine.d_gsOff.p, E.fine.d_gsIds.p, d_q, E.stream);
+    nrsg::launch_gs_mask<double>(E.fine.gsPlan, d_q, false, E.stream);
     NRSG_CUDA(cudaStreamSynchronize(E.stream));
   })
 }

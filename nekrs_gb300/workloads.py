@@ -104,3 +104,46 @@ def box_rhs(N, nx, ny, nz, seed, ggeo):
     E = nx * ny * nz
     JW = np.asarray(ggeo).reshape(E, 7, Np)[:, 6, :].ravel()
     return box_field(N, nx, ny, nz, seed) * JW
+
+
+def axis_fan(nsec=12, layers=2, radius=1.0, z_bc=1, outer_bc=1):
+    """Hexahedra in a fan around the z axis: `nsec` sectors per layer, `layers` layers on [0, layers].
+
+    Sector i of a layer has the corners O (on the axis), A_i, B_i and A_{i+1} (A on the unit circle at
+    angle 2 pi i / nsec, B between two A at a larger radius): a convex quadrilateral extruded in z, with r
+    along O A_i and s along O A_{i+1}, so the Jacobian is positive.  Every axis edge is shared by `nsec`
+    elements and every interior axis vertex by 2 nsec, the conforming case the box meshes do not reach
+    (at most four elements per edge, eight per vertex).  Faces between sectors and layers are interior;
+    the z = 0 / z = layers faces get `z_bc`, the outer faces `outer_bc` (NRSG_BC_* codes).
+    Returns (VX [E,8,3], EToV [E,8] int64, EToB [E,6] int32)."""
+    th = 2.0 * np.pi / nsec
+    rb = radius / np.cos(th / 2.0) * 1.1
+    # vertex ids (1-based): per level z = 0..layers: the axis point, A_0..A_{n-1}, B_0..B_{n-1}
+    per = 1 + 2 * nsec
+
+    def vid(level, kind, i):
+        return 1 + level * per + (0 if kind == "O" else (1 + i % nsec if kind == "A" else 1 + nsec + i % nsec))
+
+    def xyz(kind, i, z):
+        if kind == "O":
+            return (0.0, 0.0, z)
+        if kind == "A":
+            a = th * (i % nsec)
+            return (radius * np.cos(a), radius * np.sin(a), z)
+        a = th * (i % nsec) + th / 2.0
+        return (rb * np.cos(a), rb * np.sin(a), z)
+
+    VX, EToV, EToB = [], [], []
+    for lay in range(layers):
+        for i in range(nsec):
+            quad = [("O", i), ("A", i), ("A", i + 1), ("B", i)]  # (r, s) = (0,0), (1,0), (0,1), (1,1)
+            ids, pts = [], []
+            for c in range(2):
+                for kind, k in quad:
+                    ids.append(vid(lay + c, kind, k))
+                    pts.append(xyz(kind, k, float(lay + c)))
+            VX.append(pts)
+            EToV.append(ids)
+            # nekRS face order: t=0, s=0, r=1, s=1, r=0, t=1
+            EToB.append([z_bc if lay == 0 else 0, 0, outer_bc, outer_bc, 0, z_bc if lay == layers - 1 else 0])
+    return (np.array(VX, dtype=np.float64), np.array(EToV, dtype=np.int64), np.array(EToB, dtype=np.int32))

@@ -129,6 +129,23 @@ def test_gather_scatter_and_mask(product_lib, oracle_mod, torch_cuda):
     assert np.array_equal(qd.cpu().numpy(), el.mask(el.gs(q)))
 
 
+@pytest.mark.parametrize("z_bc", [1, 4])
+def test_gather_scatter_large_groups(product_lib, oracle_mod, torch_cuda, z_bc):
+    """The handle's gather-scatter (the plan kernel: pairs, groups of up to eight members from registers,
+    larger groups member by member) on the twelve-sector fan mesh, whose axis groups have 12 and 24
+    members: equal to the oracle's (same member order)."""
+    torch = torch_cuda
+    N = 4
+    VX, EToV, EToB = W.axis_fan(12, 2, z_bc=z_bc)
+    orc = O.Elliptic(N, VX, EToV, EToB, "preconditioner=jacobi")
+    el = G.Elliptic(N, VX, EToV, EToB, "preconditioner=jacobi")
+    q = np.random.default_rng(7).uniform(-1, 1, orc.Nlocal)
+    qd = dev(torch, q)
+    el.gs(qd)
+    torch.cuda.synchronize()
+    assert np.array_equal(qd.cpu().numpy(), orc.gs(q))
+
+
 def test_fused_pcg_update_and_dot(product_lib, oracle_mod, torch_cuda):
     """r = fma(-alpha, Ap, r), x = fma(alpha, p, x) and (r, r)_w: bit-identical to the oracle; the
     weighted inner product is deterministic and bit-identical too."""

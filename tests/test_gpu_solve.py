@@ -161,6 +161,30 @@ def test_fp32x2_operator_solve_parity(product_lib, oracle_mod, torch_cuda, preco
     assert rel(x.cpu().numpy(), xo) < (1e-10 if precon == "multigrid" else 1e-8)
 
 
+@pytest.mark.parametrize("z_bc", [1, 4])
+def test_jacobi_pcg_parity_axis_fan(product_lib, oracle_mod, torch_cuda, z_bc):
+    """A mesh that is not a box: twelve sectors around an axis in two layers (axis edges in 12 elements,
+    the interior axis vertex in 24), Dirichlet outside, Dirichlet or Neumann ends.  The right-hand side is
+    a smooth function of the node coordinates (continuous across elements) times JW; the GPU's Jacobi-PCG
+    is bit-identical to the oracle's."""
+    torch = torch_cuda
+    N = 5
+    VX, EToV, EToB = W.axis_fan(12, 2, z_bc=z_bc)
+    opts = "preconditioner=jacobi;solver=pcg;residualTol=1e-10+relative;maxIterations=3000"
+    orc = O.Elliptic(N, VX, EToV, EToB, opts)
+    x, y, z = orc.get("x"), orc.get("y"), orc.get("z")
+    JW = orc.get("ggeo").reshape(len(EToV), 7, (N + 1) ** 3)[:, 6, :].ravel()
+    rhs = (np.sin(3.0 * x + 0.5) * np.cos(2.0 * y) + z * z) * JW
+    xo, io = orc.solve(rhs)
+    el = G.Elliptic(N, VX, EToV, EToB, opts)
+    r = torch.from_numpy(rhs.copy()).cuda()
+    xg = torch.zeros_like(r)
+    ig = el.solve(r, xg)
+    torch.cuda.synchronize()
+    assert ig["status"] == 0
+    assert_bit_identical(xo, io, xg.cpu().numpy(), ig, el)
+
+
 def test_jacobi_pcg_parity_tight_tolerance(product_lib, oracle_mod, torch_cuda):
     """At a 1e-12 tolerance: still bit-identical."""
     opts = "preconditioner=jacobi;solver=pcg;residualTol=1e-12+relative;maxIterations=3000"

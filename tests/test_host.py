@@ -48,6 +48,20 @@ def test_setup_maps_bitexact_vs_oracle(product_lib, oracle_mod, N, n, eps):
     assert np.array_equal(m["invDegree"], el.get("invDegree"))
 
 
+@pytest.mark.parametrize("z_bc", [1, 4])
+def test_setup_maps_axis_fan(product_lib, oracle_mod, z_bc):
+    """Twelve sectors around an axis, two layers: axis edges shared by 12 elements and the interior axis
+    vertex by 24 (the box meshes stop at 4 and 8); numbering, gather groups and mask bit-exact."""
+    VX, EToV, EToB = W.axis_fan(12, 2, z_bc=z_bc)
+    N = 4
+    el = O.Elliptic(N, VX, EToV, EToB, "preconditioner=jacobi")
+    m = G.host_setup_maps(N, EToV, EToB)
+    for k in ("ids", "maskedIds", "gsOff", "gsIds", "maskIds"):
+        assert np.array_equal(m[k], el.get(k)), k
+    sizes = np.diff(m["gsOff"])
+    assert sizes.max() == 24 and (sizes == 12).sum() >= 6  # the z = 1 axis vertex; axis edge nodes
+
+
 def test_setup_maps_mixed_boundaries(product_lib, oracle_mod):
     # Neumann faces and an interior-only mask pattern
     VX, EToV, EToB = W.kershaw_box(3, 2, 2, eps=0.3, all_dirichlet=False)
