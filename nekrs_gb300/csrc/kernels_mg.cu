@@ -1223,13 +1223,274 @@ bool launch_fdm8h(long long E, const float *u, const int *haloSrc, const float *
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// Order-3 FP32 FDM (N + 3 = 6 points per direction, the 6^3 extended tile),
+// RECIP form.  Five elements per warp, six lanes per element (lanes 30 and
+// 31 take part in the loads only).  Lane a of an element holds one 6 x 6
+// plane of the tile in registers: the z-plane z = a for the forward x and y
+// transforms, then the y-plane y = a for the forward z transform (scaled by
+// 1/(lx + ly + lz)) and the backward x transform, then the x-plane x = a for
+// the backward y and z transforms.  The planes pass through shared memory
+// three times (warp synchronisation only, no CTA barrier), and each pass
+// reads its 6 x 6 S once per lane (nine 16-byte loads) where the line-per-
+// thread kernel reads one S entry per multiply-add: that kernel was bound
+// by the shared-memory pipe (90% busy, 384 wavefronts per element).  Every
+// output is the same sum in the same order as fdm_kernel<float, 4, RAS, true>
+// (bit-identical).  Tile stride 228 floats: conflict-free 8-byte y-plane
+// accesses, at most two-way conflicts on the z- and x-plane accesses.
+// Requires u, S_x, S_y, S_z and wts 16-byte aligned.
+// ---------------------------------------------------------------------------
+namespace fdm4 {
+constexpr int NL = 6, PL = 36, TS = 228; // points per direction, per plane; tile stride
+constexpr int EPW = 5, WPC = 4;          // elements per warp, warps per CTA
+constexpr int SSZ = 3 * PL;              // S_x, S_y, S_z of an element
+} // namespace fdm4
+
+template <bool RAS>
+__global__ void __launch_bounds__(32 * fdm4::WPC)
+    fdm4_kernel(long long E, const float *__restrict__ u, const int *__restrict__ haloSrc,
+                const float *__restrict__ Sx, const float *__restrict__ Sy, const float *__restrict__ Sz,
+                const float *__restrict__ lam, const float *__restrict__ wts, float *__restrict__ Su,
+                float *__restrict__ haloOut)
+{
+  using namespace fdm4;
+  constexpr int NP = 64, NF = 16, NH = 6 * NF;
+  __shared__ __align__(16) float s_w[WPC][EPW * TS];
+  __shared__ __align__(16) float s_S[WPC][EPW * SSZ];
+  __shared__ float s_l[WPC][EPW * 18];
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const long long e0 = ((long long)blockIdx.x * WPC + wp) * EPW;
+  if (e0 >= E) return; // whole warp; the kernel uses warp-level synchronisation only
+  const int ne = E - e0 < EPW ? (int)(E - e0) : EPW;
+  float *W = s_w[wp], *SS = s_S[wp], *LL = s_l[wp];
+  // tile zero, S, lambda
+  for (int q = lane; q < EPW * TS / 4; q += 32) ((float4 *)W)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float4 *src = (const float4 *)((d == 0 ? Sx : d == 1 ? Sy : Sz) + e0 * PL);
+    for (int q = lane; q < ne * 9; q += 32) *(float4 *)(SS + (q / 9) * SSZ + d * PL + 4 * (q % 9)) = __ldg(src + q);
+  }
+  for (int q = lane; q < ne * 18; q += 32) LL[q] = __ldg(lam + e0 * 18 + q);
+  // halo indices, then own nodes and halo values
+  constexpr int HM = (EPW * NH + 31) / 32;
+  const int *hs = haloSrc + e0 * NH;
+  int hsrc[HM];
+#pragma unroll
+  for (int m = 0; m < HM; ++m) {
+    const int q = lane + 32 * m;
+    hsrc[m] = q < ne * NH ? __ldg(hs + q) : -1;
+  }
+  float hv[HM];
+#pragma unroll
+  for (int m = 0; m < HM; ++m) hv[m] = hsrc[m] >= 0 ? __ldg(u + hsrc[m]) : 0.f;
+  __syncwarp();
+  const float4 *u4 = (const float4 *)(u + e0 * NP);
+  for (int q = lane; q < ne * 16; q += 32) {
+    const float4 v = __ldg(u4 + q);
+    const int r = q % 16;
+    float *dst = W + (q / 16) * TS + 1 + NL * (r % 4 + 1) + PL * (r / 4 + 1);
+    dst[0] = v.x;
+    dst[1] = v.y;
+    dst[2] = v.z;
+    dst[3] = v.w;
+  }
+#pragma unroll
+  for (int m = 0; m < HM; ++m) {
+    const int q = lane + 32 * m;
+    if (q < ne * NH) {
+      const int h = q % NH, f = h / NF, pp = h % NF;
+      W[(q / NH) * TS + halo_ext_index<4>(f, pp % 4, pp / 4)] = hv[m];
+    }
+  }
+  __syncwarp();
+  const int ee = lane / 6, a = lane % 6;
+  const bool act = lane < 30 && ee < ne;
+  float *T = W + (act ? ee : 0) * TS;
+  const float *S = SS + (act ? ee : 0) * SSZ, *L = LL + (act ? ee : 0) * 18;
+  float P[PL], M[PL];
+  auto loadS = [&](int d) {
+#pragma unroll
+    for (int m = 0; m < 9; ++m) {
+      const float4 v = *(const float4 *)(S + d * PL + 4 * m);
+      M[4 * m] = v.x, M[4 * m + 1] = v.y, M[4 * m + 2] = v.z, M[4 * m + 3] = v.w;
+    }
+  };
+  if (act) {
+    // z-plane z = a: P[x + 6 y]
+#pragma unroll
+    for (int m = 0; m < 9; ++m) {
+      const float4 v = *(const float4 *)(T + PL * a + 4 * m);
+      P[4 * m] = v.x, P[4 * m + 1] = v.y, P[4 * m + 2] = v.z, P[4 * m + 3] = v.w;
+    }
+    loadS(0); // forward x: out i of line y = sum_l S_x(l, i) P[l + 6 y]
+#pragma unroll
+    for (int y = 0; y < NL; ++y) {
+      float o[NL];
+#pragma unroll
+      for (int i = 0; i < NL; ++i) {
+        float v = 0;
+#pragma unroll
+        for (int l = 0; l < NL; ++l) v += M[l + NL * i] * P[l + NL * y];
+        o[i] = v;
+      }
+#pragma unroll
+      for (int i = 0; i < NL; ++i) P[i + NL * y] = o[i];
+    }
+    loadS(1); // forward y: out j of line x = sum_l S_y(l, j) P[x + 6 l]
+#pragma unroll
+    for (int x = 0; x < NL; ++x) {
+      float o[NL];
+#pragma unroll
+      for (int j = 0; j < NL; ++j) {
+        float v = 0;
+#pragma unroll
+        for (int l = 0; l < NL; ++l) v += M[l + NL * j] * P[x + NL * l];
+        o[j] = v;
+      }
+#pragma unroll
+      for (int j = 0; j < NL; ++j) P[x + NL * j] = o[j];
+    }
+#pragma unroll
+    for (int m = 0; m < 9; ++m)
+      *(float4 *)(T + PL * a + 4 * m) = make_float4(P[4 * m], P[4 * m + 1], P[4 * m + 2], P[4 * m + 3]);
+  }
+  __syncwarp();
+  if (act) {
+    // y-plane y = a: P[x + 6 z]
+#pragma unroll
+    for (int z = 0; z < NL; ++z)
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        const float2 v = *(const float2 *)(T + NL * a + PL * z + 2 * m);
+        P[2 * m + NL * z] = v.x, P[2 * m + 1 + NL * z] = v.y;
+      }
+    loadS(2); // forward z, scaled: out k of line x = sum_l S_z(l, k) P[x + 6 l] / (lx[x] + ly[a] + lz[k])
+#pragma unroll
+    for (int x = 0; x < NL; ++x) {
+      float o[NL];
+#pragma unroll
+      for (int k = 0; k < NL; ++k) {
+        float v = 0;
+#pragma unroll
+        for (int l = 0; l < NL; ++l) v += M[l + NL * k] * P[x + NL * l];
+        const float d = L[x] + L[NL + a] + L[2 * NL + k];
+        const float sc = d > 1e-5f ? 1.f / d : 0.f;
+        o[k] = v * sc;
+      }
+#pragma unroll
+      for (int k = 0; k < NL; ++k) P[x + NL * k] = o[k];
+    }
+    loadS(0); // backward x: out i of line z = sum_l S_x(i, l) P[l + 6 z]
+#pragma unroll
+    for (int z = 0; z < NL; ++z) {
+      float o[NL];
+#pragma unroll
+      for (int i = 0; i < NL; ++i) {
+        float v = 0;
+#pragma unroll
+        for (int l = 0; l < NL; ++l) v += M[i + NL * l] * P[l + NL * z];
+        o[i] = v;
+      }
+#pragma unroll
+      for (int i = 0; i < NL; ++i) P[i + NL * z] = o[i];
+    }
+#pragma unroll
+    for (int z = 0; z < NL; ++z)
+#pragma unroll
+      for (int m = 0; m < 3; ++m)
+        *(float2 *)(T + NL * a + PL * z + 2 * m) = make_float2(P[2 * m + NL * z], P[2 * m + 1 + NL * z]);
+  }
+  __syncwarp();
+  if (act) {
+    // x-plane x = a: P[y + 6 z]
+#pragma unroll
+    for (int z = 0; z < NL; ++z)
+#pragma unroll
+      for (int y = 0; y < NL; ++y) P[y + NL * z] = T[a + NL * y + PL * z];
+    loadS(1); // backward y: out j of line z = sum_l S_y(j, l) P[l + 6 z]
+#pragma unroll
+    for (int z = 0; z < NL; ++z) {
+      float o[NL];
+#pragma unroll
+      for (int j = 0; j < NL; ++j) {
+        float v = 0;
+#pragma unroll
+        for (int l = 0; l < NL; ++l) v += M[j + NL * l] * P[l + NL * z];
+        o[j] = v;
+      }
+#pragma unroll
+      for (int j = 0; j < NL; ++j) P[j + NL * z] = o[j];
+    }
+    loadS(2); // backward z: out k of line y = sum_l S_z(k, l) P[y + 6 l]
+#pragma unroll
+    for (int y = 0; y < NL; ++y) {
+      float o[NL];
+#pragma unroll
+      for (int k = 0; k < NL; ++k) {
+        float v = 0;
+#pragma unroll
+        for (int l = 0; l < NL; ++l) v += M[k + NL * l] * P[y + NL * l];
+        o[k] = v;
+      }
+#pragma unroll
+      for (int k = 0; k < NL; ++k) P[y + NL * k] = o[k];
+    }
+#pragma unroll
+    for (int z = 0; z < NL; ++z)
+#pragma unroll
+      for (int y = 0; y < NL; ++y) T[a + NL * y + PL * z] = P[y + NL * z];
+  }
+  __syncwarp();
+  // own nodes (RAS: weighted), ASM: the halo results as well
+  float4 *su4 = (float4 *)(Su + e0 * NP);
+  const float4 *wt4 = (const float4 *)(wts + e0 * NP);
+  for (int q = lane; q < ne * 16; q += 32) {
+    const int r = q % 16;
+    const float *src = W + (q / 16) * TS + 1 + NL * (r % 4 + 1) + PL * (r / 4 + 1);
+    float4 v = make_float4(src[0], src[1], src[2], src[3]);
+    if (RAS) {
+      const float4 wt = __ldg(wt4 + q);
+      v.x *= wt.x;
+      v.y *= wt.y;
+      v.z *= wt.z;
+      v.w *= wt.w;
+    }
+    su4[q] = v;
+  }
+  if (!RAS) {
+    float *ho = haloOut + e0 * NH;
+    for (int q = lane; q < ne * NH; q += 32) {
+      const int h = q % NH, f = h / NF, pp = h % NF;
+      ho[q] = W[(q / NH) * TS + halo_ext_index<4>(f, pp % 4, pp / 4)];
+    }
+  }
+}
+
 template <typename T>
 void launch_fdm(int N, long long E, bool ras, const T *u, const int *haloSrc, const T *Sx, const T *Sy, const T *Sz,
-                const T *invL, const T *lam, const T *wts, T *Su, T *haloOut, cudaStream_t s)
+                const T *invL, const T *lam, const T *wts, T *Su, T *haloOut, cudaStream_t s, bool generic)
 {
   if (E <= 0) return;
   const bool recip = (lam != nullptr);
-  if (std::is_same<T, float>::value && N == 7 && recip) {
+  if (std::is_same<T, float>::value && N == 3 && recip && !generic &&
+      ((reinterpret_cast<uintptr_t>(u) | reinterpret_cast<uintptr_t>(Sx) | reinterpret_cast<uintptr_t>(Sy) |
+        reinterpret_cast<uintptr_t>(Sz) | (ras ? reinterpret_cast<uintptr_t>(wts) : 0) |
+        reinterpret_cast<uintptr_t>(Su)) &
+       15) == 0) {
+    constexpr long long per = fdm4::EPW * fdm4::WPC;
+    const unsigned grid = (unsigned)((E + per - 1) / per);
+    const float *uf = (const float *)u, *Sxf = (const float *)Sx, *Syf = (const float *)Sy, *Szf = (const float *)Sz;
+    const float *lf = (const float *)lam, *wf = (const float *)wts;
+    if (ras)
+      fdm4_kernel<true><<<grid, 32 * fdm4::WPC, 0, s>>>(E, uf, haloSrc, Sxf, Syf, Szf, lf, wf, (float *)Su,
+                                                         (float *)haloOut);
+    else
+      fdm4_kernel<false><<<grid, 32 * fdm4::WPC, 0, s>>>(E, uf, haloSrc, Sxf, Syf, Szf, lf, wf, (float *)Su,
+                                                          (float *)haloOut);
+    NRSG_CHECK_LAUNCH();
+    return;
+  }
+  if (std::is_same<T, float>::value && N == 7 && recip && !generic) {
     const unsigned grid = (unsigned)((E + fdm8::EPC - 1) / fdm8::EPC);
     const float *uf = (const float *)u, *Sxf = (const float *)Sx, *Syf = (const float *)Sy, *Szf = (const float *)Sz;
     const float *lf = (const float *)lam, *wf = (const float *)wts;
@@ -1304,7 +1565,7 @@ void launch_random_fill(long long n, unsigned long long seed, double *v, cudaStr
   template void launch_cheby4_update<T>(long long, T, const T *, const T *, const T *, T *, T *, bool,       \
                                         cudaStream_t);                                                      \
   template void launch_fdm<T>(int, long long, bool, const T *, const int *, const T *, const T *, const T *, \
-                              const T *, const T *, const T *, T *, T *, cudaStream_t);                    \
+                              const T *, const T *, const T *, T *, T *, cudaStream_t, bool);              \
   template void launch_asm_combine<T>(int, long long, const int *, const T *, const T *, T *, cudaStream_t);
 NRSG_INST_MG(double)
 NRSG_INST_MG(float)

@@ -520,7 +520,7 @@ template <typename T> struct MGImpl : public MGState {
         return;
     }
     launch_fdm<T>(L.N, L.E, ras, u, v.haloSrc.p, v.Sx.p, v.Sy.p, v.Sz.p, v.invL.p, v.lam.p, v.wts.p, Su, v.haloOut.p,
-                  s);
+                  s, el.opt.fdmGeneric);
   }
 
   // Schwarz: FDM (+ ASM combine) -> gs -> mask; u and Su must not alias

@@ -18,9 +18,10 @@ template <typename T>
 void launch_cheby4_dx(long long n, T c1, const T *Su, T c2, T *d, T beta, T *x, bool first, bool xzero,
                       cudaStream_t s);
 template <typename T> void launch_cheby4_res(long long n, const T *Ad, const T *rin, T *rout, cudaStream_t s);
+// generic: the line-per-thread kernel even where a specialised one applies (FP32 orders 3 and 7)
 template <typename T>
 void launch_fdm(int N, long long E, bool ras, const T *u, const int *haloSrc, const T *Sx, const T *Sy, const T *Sz,
-                const T *invL, const T *lam, const T *wts, T *Su, T *haloOut, cudaStream_t s);
+                const T *invL, const T *lam, const T *wts, T *Su, T *haloOut, cudaStream_t s, bool generic = false);
 // order-7 RAS FDM in FP16 on the tensor cores (per-element max-abs scaling); false if not applicable
 bool launch_fdm8h(long long E, const float *u, const int *haloSrc, const float *Sx, const float *Sy, const float *Sz,
                   const float *lam, const float *wts, float *Su, cudaStream_t s);

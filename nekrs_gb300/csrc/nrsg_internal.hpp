@@ -118,6 +118,8 @@ struct Options {
   bool fdmFp16 = false;             // fdmPrecision = fp16: order-7 RAS FDM transforms in FP16 on the tensor cores
   bool fdmTf32 = false;              // fdmPrecision = tf32: FDM transforms in TF32 on the tensor cores (orders 3, 5, 7)
   bool fdmTcgen05 = true;            // fdmMma = tcgen05 | sync: the TF32 order-7 RAS FDM on tcgen05.mma or mma.sync
+  bool fdmGeneric = false;           // fdmKernel = auto | generic: the FP32 FDM's specialised order-3 / order-7
+                                     // kernels, or the line-per-thread kernel for every order
   int amgIterations = 1;             // V-cycles per coarse solve with coarseSolver = amg (BOOMERAMG ITERATIONS)
   std::string axPrecision = "fp64"; // fine-level operator: fp64 | fp32x2 (FP64-accurate FP32-pair arithmetic)
   bool poisson = true;

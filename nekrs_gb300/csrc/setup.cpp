@@ -450,6 +450,10 @@ Options parse_options(const char *text)
         if (v != "tcgen05" && v != "sync") throw Error(NRSG_ERR_BAD_CONFIG, "fdmMma must be tcgen05 or sync");
         o.fdmTcgen05 = (v == "tcgen05");
       }
+      else if (key == "fdmkernel") {
+        if (v != "auto" && v != "generic") throw Error(NRSG_ERR_BAD_CONFIG, "fdmKernel must be auto or generic");
+        o.fdmGeneric = (v == "generic");
+      }
       else if (key == "axprecision") {
         if (v != "fp64" && v != "fp32x2") throw Error(NRSG_ERR_BAD_CONFIG, "axPrecision must be fp64 or fp32x2");
         o.axPrecision = v;
