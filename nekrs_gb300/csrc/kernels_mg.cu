@@ -1251,7 +1251,7 @@ __global__ void __launch_bounds__(32 * fdm4::WPC)
     fdm4_kernel(long long E, const float *__restrict__ u, const int *__restrict__ haloSrc,
                 const float *__restrict__ Sx, const float *__restrict__ Sy, const float *__restrict__ Sz,
                 const float *__restrict__ lam, const float *__restrict__ wts, float *__restrict__ Su,
-                float *__restrict__ haloOut)
+                float *__restrict__ haloOut, long long pfAhead)
 {
   using namespace fdm4;
   constexpr int NP = 64, NF = 16, NH = 6 * NF;
@@ -1263,6 +1263,22 @@ __global__ void __launch_bounds__(32 * fdm4::WPC)
   if (e0 >= E) return; // whole warp; the kernel uses warp-level synchronisation only
   const int ne = E - e0 < EPW ? (int)(E - e0) : EPW;
   float *W = s_w[wp], *SS = s_S[wp], *LL = s_l[wp];
+  if (pfAhead > 0 && lane == 0 && e0 + pfAhead < E) {
+    // the five elements of the warp one wave of CTAs later into L2: u, halo indices, S, weights
+    // (contiguous), lambda by lines
+    const long long en = e0 + pfAhead;
+    const int nn = E - en < EPW ? (int)(E - en) : EPW;
+    auto bulk = [](const void *p, unsigned bytes) {
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+    };
+    bulk(u + en * NP, nn * NP * 4);
+    bulk(haloSrc + en * NH, nn * NH * 4);
+    bulk(Sx + en * PL, nn * PL * 4);
+    bulk(Sy + en * PL, nn * PL * 4);
+    bulk(Sz + en * PL, nn * PL * 4);
+    if (RAS) bulk(wts + en * NP, nn * NP * 4);
+    for (int c = 0; c < nn * 18; c += 32) asm volatile("prefetch.global.L2 [%0];" ::"l"(lam + en * 18 + c) : "memory");
+  }
   // tile zero, S, lambda
   for (int q = lane; q < EPW * TS / 4; q += 32) ((float4 *)W)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
@@ -1481,12 +1497,27 @@ void launch_fdm(int N, long long E, bool ras, const T *u, const int *haloSrc, co
     const unsigned grid = (unsigned)((E + per - 1) / per);
     const float *uf = (const float *)u, *Sxf = (const float *)Sx, *Syf = (const float *)Sy, *Szf = (const float *)Sz;
     const float *lf = (const float *)lam, *wf = (const float *)wts;
+    // prefetch distance: one wave of resident CTAs (two waves measured slower)
+    long long ahead = 0;
+    if ((reinterpret_cast<uintptr_t>(haloSrc) & 15) == 0) {
+      static int slots[64] = {0};
+      int dev = 0;
+      NRSG_CUDA(cudaGetDevice(&dev));
+      if (dev < 0 || dev >= 64) dev = 0;
+      if (slots[dev] == 0) {
+        int sms = 0, occ = 0;
+        NRSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        NRSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fdm4_kernel<true>, 32 * fdm4::WPC, 0));
+        slots[dev] = sms * std::max(occ, 1);
+      }
+      ahead = (long long)slots[dev] * per;
+    }
     if (ras)
       fdm4_kernel<true><<<grid, 32 * fdm4::WPC, 0, s>>>(E, uf, haloSrc, Sxf, Syf, Szf, lf, wf, (float *)Su,
-                                                         (float *)haloOut);
+                                                         (float *)haloOut, ahead);
     else
       fdm4_kernel<false><<<grid, 32 * fdm4::WPC, 0, s>>>(E, uf, haloSrc, Sxf, Syf, Szf, lf, wf, (float *)Su,
-                                                          (float *)haloOut);
+                                                          (float *)haloOut, ahead);
     NRSG_CHECK_LAUNCH();
     return;
   }
