@@ -356,20 +356,21 @@ def kernel_rooflines(G, el, N, E):
     return out, peak, src
 
 
-def fdm_roofline(G, el, N, E, peak, ras):
-    """Achieved algorithmic GB/s of one fine-level fused FDM launch (the order-7 Schwarz local solve), CUDA
-    events on its stream.  Algorithmic bytes per element follow the reference's extended-element formulation
-    (fusedFDM), 4 B each: read u_ext ((N+3)^3), S_x, S_y, S_z (3 (N+3)^2) and invL ((N+3)^3), then ASM: write
-    Su_ext ((N+3)^3); RAS: read the weights and write Su on the own nodes (2 (N+1)^3)."""
+def fdm_roofline(G, el, N, E, peak, ras, level=0):
+    """Achieved algorithmic GB/s of one fused FDM launch of a multigrid level of order N (level 0: the order-7
+    Schwarz local solve of the fine level), CUDA events on its stream.  Algorithmic bytes per element follow the
+    reference's extended-element formulation (fusedFDM), 4 B each: read u_ext ((N+3)^3), S_x, S_y, S_z
+    (3 (N+3)^2) and invL ((N+3)^3), then ASM: write Su_ext ((N+3)^3); RAS: read the weights and write Su on the
+    own nodes (2 (N+1)^3)."""
     import torch
 
     if el.get("mg.bytes")[0] != 4:
         return None
-    n = el.mg_level_size(0)
+    n = el.mg_level_size(level)
     u = torch.rand(n, dtype=torch.float32, device="cuda")
     su = torch.empty_like(u)
     stream = torch.cuda.current_stream()
-    t = time_kernel(lambda: el.mg_fdm(0, u, su), stream)
+    t = time_kernel(lambda: el.mg_fdm(level, u, su), stream)
     nl = N + 3
     per_el = 4.0 * (2 * nl ** 3 + 3 * nl ** 2 + (2 * (N + 1) ** 3 if ras else nl ** 3))
     flops = float(E) * (12 * nl * nl ** 3 + nl ** 3)
@@ -382,9 +383,9 @@ BATCH_COARSE = ["jpcg"]  # set from --coarse-solver
 
 
 def mg_options(N, tol="1e-8"):
-    """Mixed-precision pMG-FPCG options for order N (levels N / 3 / 1, or N / 1 for N <= 3), the headline's
-    optimal 4th-kind Chebyshev(5) + RAS, coarse solve on the assembled order-1 operator (Jacobi-PCG to 1e-4 or
-    three algebraic-multigrid V-cycles, --coarse-solver)."""
+    """Mixed-precision pMG-FPCG options for order N (levels N / 3 / 1, or N / 1 for N <= 3), optimal 4th-kind
+    Chebyshev(5) + RAS (the degree the E=48^3 solve takes with the Jacobi-PCG coarse solve), coarse solve on the
+    assembled order-1 operator (Jacobi-PCG to 1e-4 or three algebraic-multigrid V-cycles, --coarse-solver)."""
     mid = {9: 5, 8: 5, 7: 3, 6: 3, 5: 3, 4: 2}.get(N)
     lv = [N] + ([mid] if mid else []) + [1]
     down = [f"p={q}+degree=5" for q in lv[:-1]]
@@ -797,6 +798,11 @@ def main():
                  for o, c, row in zip(el.get("mg.levels").astype(int).tolist(), ch, tm)]
     fdm = (fdm_roofline(G, el, N, E, peak, "ras" in opts)
            if "multigrid" in opts and ("asm" in opts or "ras" in opts) else None)
+    fdm3 = None
+    if fdm is not None and "fdmPrecision" not in opts:
+        orders = el.get("mg.levels").astype(int).tolist()
+        if len(orders) > 2 and orders[1] == 3:
+            fdm3 = fdm_roofline(G, el, 3, E, peak, "ras" in opts, level=1)
     extra = {}
     # time-to-tolerance at the other tolerances of the mixed-precision config
     tols = {}
@@ -852,6 +858,8 @@ def main():
                 else "fdm_f32")
     if fdm is not None:
         kr[fdm_name] = fdm
+    if fdm3 is not None:
+        kr["fdm_f32_order3"] = fdm3
     # the dominant kernel of the solve by share of device time (ncu launch list of this workload)
     dominant = fdm_name if fdm is not None else ("ax_fp32x2" if "mixed" in opts else "ax_stored_f64")
     d = kr[dominant]
@@ -859,7 +867,7 @@ def main():
             "frac": d["achieved"] / peak, "traffic": TRAFFIC.get((args.workload, dominant)),
             "peak_source": psrc + " (MEASURED_PEAKS.json hbm_gbs)", "launch_ms": d["launch_ms"], "kernels": kr,
             "note": "fdm_f32: the order-7 FP32 Schwarz local solve, algorithmic bytes of the reference's extended-"
-                    "element form; FP64 axhelm is FP64-pipe bound on GB300 (1.25 TF/s nominal); ax_fp32x2 is its "
+                    "element form (fdm_f32_order3: the order-3 level's); FP64 axhelm is FP64-pipe bound on GB300 (1.25 TF/s nominal); ax_fp32x2 is its "
                     "FP64-accurate FP32-pair form (FP32-pipe bound); ax_stored_f32 is the HBM-bound multigrid operator"}
 
     line = {"metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
