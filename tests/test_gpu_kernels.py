@@ -279,3 +279,23 @@ def test_ax_const_f32_bit_identical(product_lib, torch_cuda, E, poisson, prefetc
     (G.ax_const_prefetch_f32 if prefetch else G.ax_const_f32)(N, E, g, D, 1.3, 0.7, poisson, q, a_c, cs)
     torch.cuda.synchronize()
     assert torch.equal(a_ref, a_c)
+
+
+def test_ax_const_prefetch_unaligned_pointers(product_lib, torch_cuda):
+    """The persistent prefetching axhelm with q and the geometric factors 4 bytes off a 16-byte boundary (the
+    bulk L2 prefetch needs 16-byte alignment, so it is skipped): still bit-identical to the default kernel."""
+    torch = torch_cuda
+    N, Np, E = 7, 512, 1500
+    gen = torch.Generator(device="cuda").manual_seed(41)
+    gbuf = torch.rand(E * 7 * Np + 1, device="cuda", generator=gen, dtype=torch.float32) + 0.5
+    qbuf = torch.rand(E * Np + 1, device="cuda", generator=gen, dtype=torch.float32) - 0.5
+    g, q = gbuf[1:], qbuf[1:]
+    assert g.data_ptr() % 16 == 4 and q.data_ptr() % 16 == 4
+    D = torch.from_numpy(O.dmatrix(N).astype(np.float32).ravel()).cuda()
+    a_ref = torch.full((E * Np,), float("nan"), device="cuda")
+    a_pf = torch.full_like(a_ref, float("nan"))
+    cs = torch.cuda.current_stream().cuda_stream
+    G.ax_stored_f32(N, E, g, D, 1.0, 0.0, True, q, a_ref, cs)
+    G.ax_const_prefetch_f32(N, E, g, D, 1.0, 0.0, True, q, a_pf, cs)
+    torch.cuda.synchronize()
+    assert torch.equal(a_ref, a_pf)
