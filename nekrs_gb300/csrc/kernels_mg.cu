@@ -1225,7 +1225,9 @@ bool launch_fdm8h(long long E, const float *u, const int *haloSrc, const float *
 
 // ---------------------------------------------------------------------------
 // Order-3 FP32 FDM (N + 3 = 6 points per direction, the 6^3 extended tile),
-// RECIP form.  Five elements per warp, six lanes per element (lanes 30 and
+// RECIP form: the reference's preFDM / fusedFDM / postFDM at p_Nq = 4
+// (kernels/elliptic/fusedFDM.okl, ellipticMultiGridSchwarz.cpp:1056-1156) in
+// one launch, the halo read through haloSrc as in fdm_kernel.  Five elements per warp, six lanes per element (lanes 30 and
 // 31 take part in the loads only).  Lane a of an element holds one 6 x 6
 // plane of the tile in registers: the z-plane z = a for the forward x and y
 // transforms, then the y-plane y = a for the forward z transform (scaled by
